@@ -1,0 +1,289 @@
+// Deterministic, nearly correctly rounded double-precision functions for the
+// CA capture geometry, usable from host and device code.
+//
+// Why: the reference evaluates atan2, cos, sin, acos and pow with glibc
+// (VoxelsCA.C:415-424, 548-591; SampleOrientation.C:72-149). glibc is not
+// correctly rounded (about 0.1% of its results differ from the correctly
+// rounded value), and CUDA's own functions differ from it far more often. The
+// GPU path therefore evaluates these functions in double-double arithmetic
+// (relative error below about 2^-80 before the final rounding), which returns
+// the correctly rounded result except when the exact value lies within that
+// error of a rounding boundary. Every routine uses only IEEE +, -, *, /, sqrt
+// and fma with explicit evaluation order, so host and device produce the same
+// bits; compile with FP contraction off (-ffp-contract=off, nvcc --fmad=false).
+//
+// Methods: Dekker/Knuth error-free transformations (two_sum, two_prod via fma);
+// arctangent by table reduction atan(t) = atan(c) + atan((t-c)/(1+tc)) with
+// c = k/64 and a Taylor series; sine/cosine by Cody-Waite reduction by pi/2
+// (four-part constant) and the addition formula around c = j/128 with Taylor
+// series; arccos via atan2(sqrt(1-x^2), x) with the square root refined by one
+// Newton step in double-double. Tables come from gen_crmath_tables.py.
+#ifndef CAFE_CRMATH_H
+#define CAFE_CRMATH_H
+
+#include <math.h>
+
+#if defined(__CUDACC__)
+#define CRM_HD __host__ __device__ __forceinline__
+#ifdef __CUDA_ARCH__
+#define CRM_TAB(name) name##_d
+#else
+#define CRM_TAB(name) name##_h
+#endif
+#else
+#define CRM_HD static inline
+#define CRM_TAB(name) name##_h
+#endif
+
+// Host copies of the tables.
+#define CRM_TABLE_DECL(type, name, dims) static const type name##_h dims
+#include "cafe_crmath_tables.h"
+#undef CRM_TABLE_DECL
+#if defined(__CUDACC__)
+// Device copies (same initialisers; the constant macros are redefined identically).
+#undef CAFE_CRMATH_TABLES_H
+#define CRM_TABLE_DECL(type, name, dims) static __device__ const type name##_d dims
+#include "cafe_crmath_tables.h"
+#undef CRM_TABLE_DECL
+#endif
+
+struct crm_dd {
+  double hi, lo;
+};
+
+CRM_HD crm_dd crm_two_sum(double a, double b) {
+  double s = a + b;
+  double bp = s - a;
+  double e = (a - (s - bp)) + (b - bp);
+  crm_dd r = {s, e};
+  return r;
+}
+CRM_HD crm_dd crm_fast_two_sum(double a, double b) {  // |a| >= |b| or a == 0
+  double s = a + b;
+  double e = b - (s - a);
+  crm_dd r = {s, e};
+  return r;
+}
+CRM_HD crm_dd crm_two_prod(double a, double b) {
+  double p = a * b;
+  double e = fma(a, b, -p);
+  crm_dd r = {p, e};
+  return r;
+}
+CRM_HD crm_dd crm_dd_add(crm_dd a, crm_dd b) {
+  crm_dd s = crm_two_sum(a.hi, b.hi);
+  crm_dd t = crm_two_sum(a.lo, b.lo);
+  double lo = s.lo + t.hi;
+  s = crm_fast_two_sum(s.hi, lo);
+  lo = s.lo + t.lo;
+  return crm_fast_two_sum(s.hi, lo);
+}
+CRM_HD crm_dd crm_dd_neg(crm_dd a) {
+  crm_dd r = {-a.hi, -a.lo};
+  return r;
+}
+CRM_HD crm_dd crm_dd_mul(crm_dd a, crm_dd b) {
+  crm_dd p = crm_two_prod(a.hi, b.hi);
+  double lo = p.lo + (a.hi * b.lo + a.lo * b.hi);
+  return crm_fast_two_sum(p.hi, lo);
+}
+CRM_HD crm_dd crm_dd_mul_d(crm_dd a, double b) {
+  crm_dd p = crm_two_prod(a.hi, b);
+  double lo = p.lo + a.lo * b;
+  return crm_fast_two_sum(p.hi, lo);
+}
+CRM_HD crm_dd crm_dd_div(crm_dd a, crm_dd b) {
+  double q1 = a.hi / b.hi;
+  crm_dd r = crm_dd_add(a, crm_dd_neg(crm_dd_mul_d(b, q1)));
+  double q2 = r.hi / b.hi;
+  r = crm_dd_add(r, crm_dd_neg(crm_dd_mul_d(b, q2)));
+  double q3 = r.hi / b.hi;
+  crm_dd q = crm_fast_two_sum(q1, q2);
+  return crm_dd_add(q, crm_dd{q3, 0.0});
+}
+CRM_HD double crm_dd_round(crm_dd a) { return a.hi + a.lo; }
+
+// atan(t) for t = num/den with 0 <= t <= 1, num and den double-double.
+CRM_HD crm_dd crm_atan_unit(crm_dd num, crm_dd den) {
+  crm_dd t = crm_dd_div(num, den);
+  int k = (int)(t.hi * (double)CRM_ATAN_STEPS + 0.5);
+  if (k > CRM_ATAN_STEPS) k = CRM_ATAN_STEPS;
+  if (k < 0) k = 0;
+  double c = (double)k * (1.0 / CRM_ATAN_STEPS);
+  // u = (t - c) / (1 + t c); t.hi - c is exact (Sterbenz) for k >= 1 and trivially for k = 0
+  crm_dd un = crm_two_sum(t.hi - c, t.lo);
+  crm_dd tc = crm_dd_mul_d(t, c);
+  crm_dd ud = crm_dd_add(crm_dd{1.0, 0.0}, tc);
+  crm_dd u = crm_dd_div(un, ud);
+  // atan(u) = u (1 - w/3 + w^2/5 - w^3/7 + ... ), w = u^2 <= 2^-14
+  crm_dd w = crm_dd_mul(u, u);
+  double wh = w.hi;
+  double tail = wh * wh * (1.0 / 5 - wh * (1.0 / 7 - wh * (1.0 / 9 - wh * (1.0 / 11 - wh * (1.0 / 13)))));
+  crm_dd w3 = crm_dd_div(w, crm_dd{3.0, 0.0});
+  crm_dd q = crm_dd_add(crm_dd{1.0, 0.0}, crm_dd_neg(w3));
+  q = crm_dd_add(q, crm_dd{tail, 0.0});
+  crm_dd au = crm_dd_mul(u, q);
+  crm_dd base = {CRM_TAB(crm_atan_tab)[k][0], CRM_TAB(crm_atan_tab)[k][1]};
+  return crm_dd_add(base, au);
+}
+
+// atan2 on double-double magnitudes ay, ax >= 0 (not both zero), then sign
+// handling for the original signs.
+CRM_HD double crm_atan2_dd(crm_dd ay, crm_dd ax, int y_neg, int x_neg) {
+  const crm_dd pio2 = {CRM_PIO2_1, CRM_PIO2_2};
+  const crm_dd pi = {CRM_PI_HI, CRM_PI_LO};
+  crm_dd r;
+  if (ay.hi <= ax.hi) {
+    r = crm_atan_unit(ay, ax);
+  } else {
+    r = crm_dd_add(pio2, crm_dd_neg(crm_atan_unit(ax, ay)));
+  }
+  if (x_neg) r = crm_dd_add(pi, crm_dd_neg(r));
+  double v = crm_dd_round(r);
+  return y_neg ? -v : v;
+}
+
+CRM_HD double crm_atan2(double y, double x) {
+  if (y != y || x != x) return y + x;
+  int yn = signbit(y) ? 1 : 0, xn = signbit(x) ? 1 : 0;
+  double ay = fabs(y), ax = fabs(x);
+  const double pio2 = CRM_PIO2_1, pi = CRM_PI_HI;
+  if (ay == 0.0) {
+    double v = xn ? pi : 0.0;
+    return yn ? -v : v;
+  }
+  if (ax == INFINITY || ay == INFINITY) {
+    double v;
+    if (ax == INFINITY && ay == INFINITY)
+      v = xn ? 3.0 * (pi / 4.0) : pi / 4.0;
+    else if (ax == INFINITY)
+      v = xn ? pi : 0.0;
+    else
+      v = pio2;
+    return yn ? -v : v;
+  }
+  if (ax == 0.0) return yn ? -pio2 : pio2;
+  return crm_atan2_dd(crm_dd{ay, 0.0}, crm_dd{ax, 0.0}, yn, xn);
+}
+
+// Cody-Waite reduction x = k pi/2 + r for |x| < 2^20, r in double-double.
+CRM_HD crm_dd crm_reduce_pio2(double x, int *quadrant) {
+  double kd = x * CRM_TWO_OVER_PI;
+  kd = (kd >= 0.0) ? (double)(long long)(kd + 0.5) : -(double)(long long)(-kd + 0.5);
+  crm_dd a = crm_two_prod(kd, CRM_PIO2_1);  // exact
+  crm_dd s = crm_two_sum(x, -a.hi);         // exact
+  crm_dd r = crm_fast_two_sum(s.hi, s.lo - a.lo);
+  crm_dd b = crm_two_prod(kd, CRM_PIO2_2);
+  r = crm_dd_add(r, crm_dd_neg(b));
+  crm_dd c = crm_two_prod(kd, CRM_PIO2_3);
+  r = crm_dd_add(r, crm_dd_neg(c));
+  r = crm_dd_add(r, crm_dd{-kd * CRM_PIO2_4, 0.0});
+  long long k = (long long)kd;
+  *quadrant = (int)(k & 3);
+  return r;
+}
+
+// sin and cos of a double-double r with |r| <= pi/4 + 2^-20.
+CRM_HD void crm_sincos_small(crm_dd r, crm_dd *sn, crm_dd *cs) {
+  int neg = r.hi < 0.0;
+  if (neg) r = crm_dd_neg(r);
+  int j = (int)(r.hi * (double)CRM_SC_STEPS + 0.5);
+  if (j > 103) j = 103;
+  double c = (double)j * (1.0 / CRM_SC_STEPS);
+  crm_dd s = crm_two_sum(r.hi - c, r.lo);  // |s| <= 2^-8
+  crm_dd w = crm_dd_mul(s, s);
+  double wh = w.hi;
+  // sin s = s (1 - w/6 + w^2/120 - w^3/5040 + w^4/362880 - w^5/39916800)
+  double st = wh * wh * (1.0 / 120 - wh * (1.0 / 5040 - wh * (1.0 / 362880 - wh * (1.0 / 39916800))));
+  crm_dd sq = crm_dd_add(crm_dd{1.0, 0.0}, crm_dd_neg(crm_dd_div(w, crm_dd{6.0, 0.0})));
+  sq = crm_dd_add(sq, crm_dd{st, 0.0});
+  crm_dd ss = crm_dd_mul(s, sq);
+  // cos s = 1 - w/2 + w^2/24 - w^3/720 + w^4/40320 - w^5/3628800
+  double ct = wh * wh * (1.0 / 24 - wh * (1.0 / 720 - wh * (1.0 / 40320 - wh * (1.0 / 3628800))));
+  crm_dd cq = crm_dd_add(crm_dd{1.0, 0.0}, crm_dd{-0.5 * w.hi, -0.5 * w.lo});
+  crm_dd csv = crm_dd_add(cq, crm_dd{ct, 0.0});
+  crm_dd sc = {CRM_TAB(crm_sincos_tab)[j][0], CRM_TAB(crm_sincos_tab)[j][1]};
+  crm_dd cc = {CRM_TAB(crm_sincos_tab)[j][2], CRM_TAB(crm_sincos_tab)[j][3]};
+  crm_dd sv = crm_dd_add(crm_dd_mul(sc, csv), crm_dd_mul(cc, ss));
+  crm_dd cv = crm_dd_add(crm_dd_mul(cc, csv), crm_dd_neg(crm_dd_mul(sc, ss)));
+  *sn = neg ? crm_dd_neg(sv) : sv;
+  *cs = cv;
+}
+
+// Supported domain |x| < 2^20 (the CA evaluates arguments in [-2 pi, 2 pi]);
+// outside it the result is NaN.
+CRM_HD double crm_sin(double x) {
+  if (!(fabs(x) < 1048576.0)) return NAN;
+  if (x == 0.0) return x;
+  int q;
+  crm_dd r = crm_reduce_pio2(x, &q);
+  crm_dd s, c;
+  crm_sincos_small(r, &s, &c);
+  switch (q) {
+    case 0: return crm_dd_round(s);
+    case 1: return crm_dd_round(c);
+    case 2: return -crm_dd_round(s);
+    default: return -crm_dd_round(c);
+  }
+}
+CRM_HD double crm_cos(double x) {
+  if (!(fabs(x) < 1048576.0)) return NAN;
+  int q;
+  crm_dd r = crm_reduce_pio2(x, &q);
+  crm_dd s, c;
+  crm_sincos_small(r, &s, &c);
+  switch (q) {
+    case 0: return crm_dd_round(c);
+    case 1: return -crm_dd_round(s);
+    case 2: return -crm_dd_round(c);
+    default: return crm_dd_round(s);
+  }
+}
+
+CRM_HD double crm_acos(double x) {
+  if (x != x) return x;
+  if (fabs(x) > 1.0) return (x - x) / (x - x);
+  if (x == 1.0) return 0.0;
+  if (x == -1.0) return CRM_PI_HI;
+  // d = 1 - x^2 in double-double, then sqrt(d) refined by one Newton step
+  crm_dd p = crm_two_prod(x, x);
+  crm_dd s = crm_two_sum(1.0, -p.hi);
+  crm_dd d = crm_fast_two_sum(s.hi, s.lo - p.lo);
+  double s0 = sqrt(d.hi);
+  crm_dd s0sq = crm_two_prod(s0, s0);
+  double rem = ((d.hi - s0sq.hi) - s0sq.lo) + d.lo;
+  crm_dd sq = crm_fast_two_sum(s0, rem / (2.0 * s0));
+  int xn = signbit(x) ? 1 : 0;
+  return crm_atan2_dd(sq, crm_dd{fabs(x), 0.0}, 0, xn);
+}
+
+// pow(x, 0.5) as glibc's pow defines it; the correctly rounded value is sqrt
+// except for the sign of zero and -inf.
+CRM_HD double crm_pow_half(double x) {
+  if (x == 0.0) return 0.0;
+  if (x == -INFINITY) return INFINITY;
+  return sqrt(x);
+}
+
+// x^e for integer e >= 1, evaluated in double-double by binary powering.
+CRM_HD double crm_pow_int(double x, int e) {
+  if (x != x) return x;
+  if (x == 0.0 || fabs(x) == INFINITY || e == 1) {
+    double r = x;
+    for (int i = 1; i < e; ++i) r = r * x;
+    return r;
+  }
+  crm_dd base = {x, 0.0}, acc = {1.0, 0.0};
+  int first = 1;
+  while (e > 0) {
+    if (e & 1) {
+      acc = first ? base : crm_dd_mul(acc, base);
+      first = 0;
+    }
+    e >>= 1;
+    if (e) base = crm_dd_mul(base, base);
+  }
+  return crm_dd_round(acc);
+}
+
+#endif

@@ -1,0 +1,370 @@
+// Device-side data structures and per-cell physics of the CA step.
+//
+// Layout in HBM (one realisation, N = nx*ny*nz cells, x fastest):
+//   state  u8[N]   vState (0 powder/empty, 1 liquid, 2 mushy, 3 solid)
+//   gid    i32[N]  grain ID (0 = none)
+//   ext    f64[N]  octahedron half-diagonal ("extents")
+//   cx,cy,cz f64[N] octahedron centre ("centroidOct"), structure of arrays
+//   buildj u8[N]   TempField::BuildjID (sticky "was above liquidus")
+//   pos_of i32[N]  position of a cell in this step's active list, -1 otherwise
+// Grain table: cth f64[4*G] (axis-angle, cTheta) and rot f64[9*G] (loadRotMat).
+// Active list (sorted cell indices, the reference's vI) and per-position
+// copies (vS, G, T class, ExtA, CentroidA, ruq, neighbour positions) are sized
+// by the active capacity.
+#ifndef CAFE_DEVICE_CUH
+#define CAFE_DEVICE_CUH
+#include <stdint.h>
+
+#include "cafe_crmath.h"
+#include "cafe_rng.h"
+
+#define CAFE_NSLOT 26
+
+// Error bits written to CafeDev::err by device code.
+enum {
+  CAFE_ERR_ACTIVE_CAP = 1,
+  CAFE_ERR_ROW_CAP = 2,
+  CAFE_ERR_GRAIN_CAP = 4,
+  CAFE_ERR_MUSHY_CAP = 8,
+  CAFE_ERR_ITER_CAP = 16,
+};
+
+// Scalars that change every step (computed on the host from Grid/TempField).
+struct CafeStepParams {
+  double lx, ly, lz;  // laser x, y (scan frame) and the laser plane height
+  double cg, sg;      // cos(gth), sin(gth) (host libm, as TempField.C:163-166)
+  double dirp;        // scan direction sign source (TempField.C:167-171)
+  int lo[3], hi[3];   // cell box outside which T cannot reach the liquidus
+  int ilaserLoc;
+  int tInd;           // Grid::tInd (seeds of VoxelsCA.C:338-340)
+  int any_hot_full;   // 1: evaluate T exactly everywhere below the plane
+};
+
+// Scalars fixed for a run.
+struct CafeConsts {
+  int nx, ny, nz, nxy;
+  long long N;
+  double dx[3];
+  double hLX0, hLX1;  // LX/2
+  double a1[6];       // TempField::a1 (TempField.C:69-76)
+  double bmDX0;       // DelT * bmV
+  double tL, tS, T0, xi;
+  double Tcls[3];     // temperature per class: 0 = T0 (above laser plane), 1 = tS, 2 = xi
+  double vhat_cls[3]; // growth velocity per class (VoxelsCA.C:405), host libm pow
+  int hot_cls[3];     // T >= tL
+  int gt_cls[3];      // T > tL (BuildjID)
+  double rX;          // rNmax * pow(dx*1e6, 3)
+  double DelT;
+  double ruq_dx;      // dX[0]
+  unsigned int seed0, seed1;
+  // SampleOrientation constants (SampleOrientation.C:15-22)
+  double so_R1, so_a, so_aprime, so_beta, so_s2, so_s2q, so_s6pi, so_spi, so_s24, so_coeffA[7];
+  double s3, s23;     // pow(3,.5), pow(2/3,.5) (VoxelsCA.C:583-585)
+};
+
+struct CafeDev {
+  // dense fields
+  uint8_t *state;
+  int32_t *gid;
+  double *ext, *cx, *cy, *cz;
+  uint8_t *buildj;
+  int32_t *pos_of;
+  // grains
+  double *cth, *rot;
+  int grain_cap;
+  // active list and per-position copies
+  int32_t *act;
+  long long act_cap;
+  uint8_t *a_state, *a_cls, *a_nn, *a_cold;
+  int32_t *a_gid, *a_liq, *a_frow, *a_nbr;
+  double *a_ext, *a_cx, *a_cy, *a_cz, *a_ruq;
+  // mushy list (vs2ind) and frontier rows
+  int32_t *vs2;
+  long long vs2_cap;
+  int32_t *row_pos, *row_j;
+  uint8_t *row_alive, *row_ord;
+  uint32_t *row_live;
+  double *row_g;
+  long long row_cap;
+  // scan scratch
+  int32_t *blk;       // per-block counts / offsets
+  long long blk_cap;
+  // device scalars
+  int *ctr;           // see CTR_* below
+  int *err;
+  unsigned long long *stat;  // event statistics
+};
+
+enum {
+  CTR_NA = 0,      // active-list length
+  CTR_NVS2,        // mushy-list length at step start
+  CTR_NROWS,       // frontier rows at step start
+  CTR_NGRAIN,      // grains in the table
+  CTR_HOT,         // any T >= tL this step
+  CTR_NEV,         // events this step
+  CTR_NNUC,        // nucleations this step
+  CTR_NVS2_END,    // mushy-list length after the event loop
+  CTR_COUNT
+};
+enum { STAT_EVENTS = 0, STAT_NUC, STAT_MAXNA, STAT_MAXROWS, STAT_STEPS, STAT_NEGDT, STAT_COUNT };
+
+// --------------------------------------------------------------- temperature
+// TempField::AnalyticTempCurr (TempField.C:155-190) for one cell; returns the
+// class 0 (T0, above the laser plane), 1 (tS) or 2 (xi = tL(1+eps)).
+__device__ __forceinline__ int cafe_temp_class(const CafeConsts &K, const CafeStepParams &P, int i,
+                                               int j, int k) {
+  double zp = ((double)k + .5) * K.dx[2];
+  if (zp > P.lz) return 0;
+  if (!P.any_hot_full &&
+      (i < P.lo[0] || i >= P.hi[0] || j < P.lo[1] || j >= P.hi[1] || k < P.lo[2] || k >= P.hi[2]))
+    return 1;
+  double x0 = ((double)i + .5) * K.dx[0];
+  double y0 = ((double)j + .5) * K.dx[1];
+  double xp = P.cg * (x0 - K.hLX0) + P.sg * (y0 - K.hLX1) + K.hLX0;
+  double yp = -P.sg * (x0 - K.hLX0) + P.cg * (y0 - K.hLX1) + K.hLX1;
+  double r0 = xp - P.lx, r1 = yp - P.ly, r2 = zp - P.lz;
+  bool in;
+  if (P.dirp * r0 > 0) {
+    double q1 = r1 / K.a1[1], q2 = r2 / K.a1[2];
+    double dsq = q1 * q1 + q2 * q2;
+    in = (dsq < 1.0) && (fabs(r0) < K.bmDX0);
+  } else {
+    double q0 = r0 / K.a1[3], q1 = r1 / K.a1[4], q2 = r2 / K.a1[5];
+    double dsq = q0 * q0 + q1 * q1 + q2 * q2;
+    in = dsq < 1.0;
+  }
+  return in ? 2 : 1;
+}
+
+__device__ __forceinline__ void cafe_cell_xyz(const CafeConsts &K, long long idx, int &i, int &j,
+                                              int &k) {
+  k = (int)(idx / K.nxy);
+  long long r = idx - (long long)K.nxy * k;
+  j = (int)(r / K.nx);
+  i = (int)(r - (long long)K.nx * j);
+}
+
+// --------------------------------------------------------------- geometry
+// loadRotMat (VoxelsCA.h:94-107), row-major R[3*a+b].
+__device__ __forceinline__ void cafe_rot_from_cth(const double *c, double *R) {
+  double omega = c[0], a0 = c[1], a1 = c[2], a2 = c[3];
+  double co = crm_cos(omega), so = crm_sin(omega);
+  R[0] = co + (a0 * a0) * (1 - co);
+  R[1] = a0 * a1 * (1 - co) - a2 * so;
+  R[2] = a0 * a2 * (1 - co) + a1 * so;
+  R[3] = a0 * a1 * (1 - co) + a2 * so;
+  R[4] = co + (a1 * a1) * (1 - co);
+  R[5] = a1 * a2 * (1 - co) - a0 * so;
+  R[6] = a2 * a0 * (1 - co) - a1 * so;
+  R[7] = a2 * a1 * (1 - co) + a0 * so;
+  R[8] = co + (a2 * a2) * (1 - co);
+}
+
+// Capture-time numerator pow(cos th sin ph,.5)*|R^T dn|_1 for the octahedron
+// at (c0,c1,c2) with rotation R and the neighbour cell at (i,j,k)
+// (VoxelsCA.C:409-424, without "- ExtA").
+__device__ __forceinline__ double cafe_candidate_g(const CafeConsts &K, double c0, double c1,
+                                                   double c2, const double *R, int i, int j, int k) {
+  double d0 = ((double)i + .5) * K.dx[0] - c0;
+  double d1 = ((double)j + .5) * K.dx[1] - c1;
+  double d2 = ((double)k + .5) * K.dx[2] - c2;
+  const double pi4 = 3.14159265358979323846 / 4.0, pi2 = 3.14159265358979323846 / 2.0;
+  double th = crm_atan2(fabs(d1), fabs(d0));
+  th = th > pi4 ? pi2 - th : th;
+  double ph = crm_atan2(crm_pow_half(d0 * d0 + d1 * d1), fabs(d2));
+  ph = ph < pi4 ? pi2 - ph : ph;
+  double l0 = fabs(R[0] * d0 + R[3] * d1 + R[6] * d2);
+  double l1 = fabs(R[1] * d0 + R[4] * d1 + R[7] * d2);
+  double l2 = fabs(R[2] * d0 + R[5] * d1 + R[8] * d2);
+  return crm_pow_half(crm_cos(th) * crm_sin(ph)) * (l0 + l1 + l2);
+}
+
+// projectPointLine (VoxelsCA.h:78-93)
+__device__ __forceinline__ void cafe_project(const double *A, const double *x0, const double *x1,
+                                             double *xp) {
+  double e0 = x1[0] - x0[0], e1 = x1[1] - x0[1], e2 = x1[2] - x0[2];
+  double snorm = crm_pow_half(e0 * e0 + e1 * e1 + e2 * e2);
+  double n0 = e0 / snorm, n1 = e1 / snorm, n2 = e2 / snorm;
+  double d = -(n0 * A[0] + n1 * A[1] + n2 * A[2]);
+  double t = (-d - n0 * x0[0] - n1 * x0[1] - n2 * x0[2]) / (n0 * e0 + n1 * e1 + n2 * e2);
+  xp[0] = x0[0] + e0 * t;
+  xp[1] = x0[1] + e1 * t;
+  xp[2] = x0[2] + e2 * t;
+}
+
+// Decentered-octahedron capture (VoxelsCA.C:528-605): captured cell (ci,cj,ck),
+// capturing cell (si,sj,sk) with centre cs and rotation R.
+__device__ __noinline__ void cafe_capture_geometry(const CafeConsts &K, int ci, int cj, int ck,
+                                                   int si, int sj, int sk, const double *cs,
+                                                   const double *R, double *ext_out,
+                                                   double *cen_out) {
+  const double pi4 = 3.14159265358979323846 / 4.0, pi2 = 3.14159265358979323846 / 2.0;
+  double q0 = (ci - si) * K.dx[0], q1 = (cj - sj) * K.dx[1], q2 = (ck - sk) * K.dx[2];
+  double l = crm_pow_half(q0 * q0 + q1 * q1 + q2 * q2);
+  double dn[3];
+  dn[0] = ((double)ci + .5) * K.dx[0] - cs[0];
+  dn[1] = ((double)cj + .5) * K.dx[1] - cs[1];
+  dn[2] = ((double)ck + .5) * K.dx[2] - cs[2];
+  double loc[3];
+  loc[0] = R[0] * dn[0] + R[3] * dn[1] + R[6] * dn[2];
+  loc[1] = R[1] * dn[0] + R[4] * dn[1] + R[7] * dn[2];
+  loc[2] = R[2] * dn[0] + R[5] * dn[1] + R[8] * dn[2];
+  double th = crm_atan2(fabs(dn[1]), fabs(dn[0]));
+  th = th > pi4 ? pi2 - th : th;
+  double ph = crm_atan2(crm_pow_half(dn[0] * dn[0] + dn[1] * dn[1]), fabs(dn[2]));
+  ph = ph < pi4 ? pi2 - ph : ph;
+  double dr = fabs(loc[0]) + fabs(loc[1]) + fabs(loc[2]);
+  // octahedron corners S0*dr and the corner triple of the octant (loadS, VoxelsCA.h:56-77)
+  const signed char S0[6][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}, {-1, 0, 0}, {0, -1, 0}, {0, 0, -1}};
+  const unsigned char SI[8][3] = {{0, 1, 2}, {1, 2, 3}, {0, 2, 4}, {2, 3, 4},
+                                  {0, 1, 5}, {1, 3, 5}, {0, 4, 5}, {3, 4, 5}};
+  int jInd = 4 * (signbit(loc[2]) ? 1 : 0) + 2 * (signbit(loc[1]) ? 1 : 0) + (signbit(loc[0]) ? 1 : 0);
+  double corner[3][3];
+  for (int a = 0; a < 3; ++a)
+    for (int b = 0; b < 3; ++b) corner[a][b] = (double)S0[SI[jInd][a]][b] * dr;
+  double dnorm[3];
+  for (int a = 0; a < 3; ++a) {
+    double e0 = loc[0] - corner[a][0], e1 = loc[1] - corner[a][1], e2 = loc[2] - corner[a][2];
+    dnorm[a] = e0 * e0 + e1 * e1 + e2 * e2;
+  }
+  int imin = 0, imax = 0;
+  for (int a = 1; a < 3; ++a) {
+    if (dnorm[a] < dnorm[imin]) imin = a;
+    if (dnorm[imax] < dnorm[a]) imax = a;
+  }
+  int k0, k1, k2;
+  if (imin == imax) {
+    k0 = 0;
+    k1 = 1;
+    k2 = 2;
+  } else {
+    k0 = imin;
+    k2 = imax;
+    k1 = 3 - imin - imax;
+  }
+  const double *p0 = corner[k0], *p1 = corner[k1], *p2 = corner[k2];
+  double xI[3], xJ[3];
+  cafe_project(loc, p0, p1, xI);
+  cafe_project(loc, p0, p2, xJ);
+  double e0, e1, e2;
+  e0 = p0[0] - xI[0]; e1 = p0[1] - xI[1]; e2 = p0[2] - xI[2];
+  double d1I = crm_pow_half(e0 * e0 + e1 * e1 + e2 * e2);
+  e0 = p1[0] - xI[0]; e1 = p1[1] - xI[1]; e2 = p1[2] - xI[2];
+  double dI2 = crm_pow_half(e0 * e0 + e1 * e1 + e2 * e2);
+  e0 = p0[0] - xJ[0]; e1 = p0[1] - xJ[1]; e2 = p0[2] - xJ[2];
+  double d1J = crm_pow_half(e0 * e0 + e1 * e1 + e2 * e2);
+  e0 = p2[0] - xJ[0]; e1 = p2[1] - xJ[1]; e2 = p2[2] - xJ[2];
+  double dJ3 = crm_pow_half(e0 * e0 + e1 * e1 + e2 * e2);
+  double s3l = K.s3 * l;
+  // std::min(a,b) = (b < a) ? b : a ; std::max(a,b) = (a < b) ? b : a
+  double L12 = .5 * (((s3l < d1I) ? s3l : d1I) + ((s3l < dI2) ? s3l : dI2));
+  double L13 = .5 * (((s3l < d1J) ? s3l : d1J) + ((s3l < dJ3) ? s3l : dJ3));
+  double Lmud = K.s3 * (K.s23 * ((L12 < L13) ? L13 : L12));
+  *ext_out = crm_pow_half(crm_cos(th) * crm_sin(ph)) * Lmud * 1.0;
+  const signed char *s0 = S0[SI[jInd][k0]];
+  double m0 = p0[0] - Lmud * (double)s0[0];
+  double m1 = p0[1] - Lmud * (double)s0[1];
+  double m2 = p0[2] - Lmud * (double)s0[2];
+  double g0 = R[0] * m0 + R[1] * m1 + R[2] * m2;
+  double g1 = R[3] * m0 + R[4] * m1 + R[5] * m2;
+  double g2 = R[6] * m0 + R[7] * m1 + R[8] * m2;
+  cen_out[0] = cs[0] + g0;
+  cen_out[1] = cs[1] + g1;
+  cen_out[2] = cs[2] + g2;
+}
+
+// One orientation of SampleOrientation::GenerateSamples (SampleOrientation.C:
+// 124-161) for a single sample with engine seed `seed`.
+__device__ __noinline__ void cafe_sample_orientation(const CafeConsts &K, unsigned int seed,
+                                                     double *out) {
+  cafe_uniform_stream st;
+  st.x = cafe_minstd_seed(seed);
+  double u0 = cafe_uniform_next(&st), u1 = cafe_uniform_next(&st), u2 = cafe_uniform_next(&st);
+  double xyz0[3] = {u0 - .5, u1 - .5, u2 - .5};
+  double xyz[3] = {K.so_aprime * xyz0[0], K.so_aprime * xyz0[1], K.so_aprime * xyz0[2]};
+  int P[3] = {1, 2, 3};
+  {
+    double x = xyz[0], y = xyz[1], z = xyz[2];
+    if ((fabs(x) <= z) && (fabs(y) <= z)) { P[0] = 1; P[1] = 2; P[2] = 3; }
+    if ((z <= -fabs(x)) && (z <= -fabs(y))) { P[0] = -1; P[1] = 2; P[2] = -3; }
+    if ((fabs(x) <= y) && (fabs(z) <= y)) { P[0] = 1; P[1] = -3; P[2] = 2; }
+    if ((y <= -fabs(x)) && (y <= -fabs(z))) { P[0] = 1; P[1] = 3; P[2] = -2; }
+    if ((fabs(z) < x) && (fabs(y) <= x)) { P[0] = -3; P[1] = 2; P[2] = 1; }
+    if ((x <= -fabs(z)) && (x <= -fabs(y))) { P[0] = 3; P[1] = 2; P[2] = -1; }
+  }
+  double xyz2[3];
+  for (int j = 0; j < 3; ++j) {
+    int a = P[j] < 0 ? -P[j] : P[j];
+    xyz2[j] = (double)(P[j] / a) * xyz[a - 1];
+  }
+  double m1[3];
+  for (int j = 0; j < 3; ++j) m1[j] = K.so_a / K.so_aprime * xyz2[j];
+  const double PI = 3.14159265358979323846;
+  double m2[3];
+  {
+    double x = m1[0], y = m1[1], z = m1[2], T1 = 0, T2 = 0;
+    if (fabs(y) <= fabs(x)) {
+      if (fabs(x) < 1e-10) {
+        T1 = 0.0;
+        T2 = 0.0;
+      } else {
+        double ang = y * PI / 12 / x;
+        double cang = crm_cos(ang);
+        T1 = K.so_s2 * cang - 1;
+        T2 = K.so_s2 * crm_sin(ang);
+        double f = K.so_s2q * x / (K.so_beta * crm_pow_half(K.so_s2 - cang));
+        T1 *= f;
+        T2 *= f;
+      }
+    }
+    if (fabs(x) <= fabs(y)) {
+      if (fabs(y) < 1e-10) {
+        T1 = 0.0;
+        T2 = 0.0;
+      } else {
+        double ang = x * PI / 12 / y;
+        double cang = crm_cos(ang);
+        T1 = K.so_s2 * crm_sin(ang);
+        T2 = K.so_s2 * cang - 1;
+        double f = K.so_s2q * y / (K.so_beta * crm_pow_half(K.so_s2 - cang));
+        T1 *= f;
+        T2 *= f;
+      }
+    }
+    m2[0] = T1;
+    m2[1] = T2;
+    m2[2] = z;
+  }
+  double m3[3];
+  {
+    double x = m2[0], y = m2[1], z = m2[2];
+    if (fabs(z) < 1e-10) {
+      m3[0] = m3[1] = m3[2] = 0;
+    } else {
+      double q = 1 - (x * x + y * y) * PI / (24 * (z * z));
+      double sq = crm_pow_half(q);
+      m3[0] = sq * x;
+      m3[1] = sq * y;
+      m3[2] = K.so_s6pi * z - (x * x + y * y) * K.so_spi / (K.so_s24 * z);
+    }
+  }
+  double xyzb[3];
+  for (int j = 0; j < 3; ++j) {
+    int a = P[j] < 0 ? -P[j] : P[j];
+    xyzb[a - 1] = (double)(P[j] / a) * m3[j];
+  }
+  double ax0 = fabs(xyz0[0]), ax1 = fabs(xyz0[1]), ax2 = fabs(xyz0[2]);
+  double pmax = (ax0 < ax1) ? ax1 : ax0;
+  pmax = (pmax < ax2) ? ax2 : pmax;
+  double rhoP = K.so_R1 * pmax / .5;
+  double t = 1;
+  for (int j = 1; j < 8; ++j) t += K.so_coeffA[j - 1] * crm_pow_int(rhoP, 2 * j);
+  double omega = 2.0 * crm_acos(t);
+  double tnorm = crm_pow_half(xyzb[0] * xyzb[0] + xyzb[1] * xyzb[1] + xyzb[2] * xyzb[2]);
+  out[0] = omega;
+  out[1] = xyzb[0] / tnorm;
+  out[2] = xyzb[1] / tnorm;
+  out[3] = xyzb[2] / tnorm;
+}
+
+#endif

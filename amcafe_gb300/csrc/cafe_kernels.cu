@@ -1,0 +1,939 @@
+// CUDA kernels of the CA step (VoxelsCA::UpdateVoxels and TempField::
+// AnalyticTempCurr, AMCAFE src/src-mpi/VoxelsCA.C:232-655, TempField.C:139-217)
+// and of the per-layer operations (CleanLayer, AddLayer1 Voronoi assignment).
+//
+// Step pipeline (one realisation, launched by cafe_host.cu on one stream):
+//   k_melt          pool box only: SetLiquid3 + BuildjID + "any cell at the
+//                   liquidus" flag (VoxelsCA.C:1098-1116, TempField.C:191-206)
+//   k_solid2mushy   ConvertSolid1(1) (VoxelsCA.C:780-797), in place
+//   k_active_count  \ order-preserving compaction of the active set
+//   k_scan_blocks    > (VoxelsCA.C:262-275): mushy, undercooled liquid and
+//   k_active_scatter/  their neighbours at/above the liquidus, in index order
+//   k_gather        per-position copies, neighbour positions (VoxelsCA.C:
+//                   283-335), ruq offsets (VoxelsCA.C:380) by RNG jump-ahead
+//   k_lists_*       vs2ind (mushy positions in order) and frontier rows
+//   k_rows_init     capture-time numerators per (frontier cell, liquid
+//                   neighbour), sorted per cell
+//   k_event_loop    the sequential capture/nucleation loop (VoxelsCA.C:
+//                   381-610), one thread block
+//   k_writeback     VoxelsCA.C:633-643
+//   k_mushy2solid   ConvertSolid1(0) (VoxelsCA.C:739-758), in place
+// All FP64 arithmetic follows the reference's expression order; the file is
+// compiled with --fmad=false so no product is fused into an add.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "cafe_device.cuh"
+
+#define CAFE_DENSE_THREADS 256
+#define CAFE_CELLS_PER_THREAD 8
+#define CAFE_CELLS_PER_BLOCK (CAFE_DENSE_THREADS * CAFE_CELLS_PER_THREAD)
+#define CAFE_LOOP_THREADS 512
+
+// ------------------------------------------------------------------ helpers
+__device__ __forceinline__ int cafe_hot(const CafeConsts &K, const CafeStepParams &P, int i, int j,
+                                        int k) {
+  return K.hot_cls[cafe_temp_class(K, P, i, j, k)];
+}
+
+// Moore neighbours in ascending linear-index order (Grid.C:399-414 + sort at
+// Grid.C:375); writes cell indices, returns the count.
+__device__ __forceinline__ int cafe_moore(const CafeConsts &K, int i, int j, int k, long long *nb) {
+  int n = 0;
+  for (int dz = -1; dz <= 1; ++dz) {
+    int z = k + dz;
+    if (z < 0 || z >= K.nz) continue;
+    for (int dy = -1; dy <= 1; ++dy) {
+      int y = j + dy;
+      if (y < 0 || y >= K.ny) continue;
+      for (int dx = -1; dx <= 1; ++dx) {
+        int x = i + dx;
+        if (x < 0 || x >= K.nx) continue;
+        if (dx == 0 && dy == 0 && dz == 0) continue;
+        nb[n++] = (long long)K.nxy * z + (long long)K.nx * y + x;
+      }
+    }
+  }
+  return n;
+}
+
+// ------------------------------------------------------------------ K: melt
+// Over the box where T may reach the liquidus: SetLiquid3 and BuildjID.
+__global__ void k_melt(CafeDev D, CafeConsts K, CafeStepParams P) {
+  int bx = P.hi[0] - P.lo[0], by = P.hi[1] - P.lo[1], bz = P.hi[2] - P.lo[2];
+  long long nbox = (long long)bx * by * bz;
+  long long iz1 = (long long)P.ilaserLoc * K.nxy;
+  int any = 0;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < nbox;
+       t += (long long)gridDim.x * blockDim.x) {
+    int i = P.lo[0] + (int)(t % bx);
+    long long r = t / bx;
+    int j = P.lo[1] + (int)(r % by);
+    int k = P.lo[2] + (int)(r / by);
+    int c = cafe_temp_class(K, P, i, j, k);
+    long long idx = (long long)K.nxy * k + (long long)K.nx * j + i;
+    if (K.gt_cls[c]) D.buildj[idx] = 1;
+    if (K.hot_cls[c]) {
+      any = 1;
+      if (idx < K.nxy) {
+        D.state[idx] = 2;
+      } else if (idx < iz1) {
+        D.state[idx] = 1;
+        D.gid[idx] = 0;
+      }
+      D.ext[idx] = 0.0;
+    }
+  }
+  if (__syncthreads_or(any) && threadIdx.x == 0) atomicOr(&D.ctr[CTR_HOT], 1);
+}
+
+// ------------------------------------------------------------------ K: solid -> mushy
+// ConvertSolid1(1): solid cells with a liquid neighbour become mushy. In place
+// is equivalent to the reference's collect-then-apply: the test reads only
+// "neighbour == liquid", which this pass never changes.
+__global__ void k_solid2mushy(CafeDev D, CafeConsts K) {
+  long long base = ((long long)blockIdx.x * blockDim.x + threadIdx.x) * CAFE_CELLS_PER_THREAD;
+  for (int c = 0; c < CAFE_CELLS_PER_THREAD; ++c) {
+    long long idx = base + c;
+    if (idx >= K.N) return;
+    if (D.state[idx] != 3) continue;
+    int i, j, k;
+    cafe_cell_xyz(K, idx, i, j, k);
+    long long nb[26];
+    int n = cafe_moore(K, i, j, k, nb);
+    bool liq = false;
+    for (int a = 0; a < n && !liq; ++a) liq = (D.state[nb[a]] == 1);
+    if (liq) D.state[idx] = 2;
+  }
+}
+
+// ------------------------------------------------------------------ active set
+__device__ __forceinline__ bool cafe_is_active(const CafeDev &D, const CafeConsts &K,
+                                               const CafeStepParams &P, long long idx) {
+  uint8_t s = D.state[idx];
+  int i, j, k;
+  cafe_cell_xyz(K, idx, i, j, k);
+  int hot = cafe_hot(K, P, i, j, k);
+  if (s == 2 || (s == 1 && !hot)) return true;
+  if (!hot) return false;
+  long long nb[26];
+  int n = cafe_moore(K, i, j, k, nb);
+  for (int a = 0; a < n; ++a) {
+    uint8_t t = D.state[nb[a]];
+    if (t == 2) return true;
+    if (t == 1) {
+      int ni, nj, nk;
+      cafe_cell_xyz(K, nb[a], ni, nj, nk);
+      if (!cafe_hot(K, P, ni, nj, nk)) return true;
+    }
+  }
+  return false;
+}
+
+__global__ void k_active_count(CafeDev D, CafeConsts K, CafeStepParams P) {
+  __shared__ int wsum[CAFE_DENSE_THREADS / 32];
+  long long base = ((long long)blockIdx.x * blockDim.x + threadIdx.x) * CAFE_CELLS_PER_THREAD;
+  int cnt = 0;
+  for (int c = 0; c < CAFE_CELLS_PER_THREAD; ++c) {
+    long long idx = base + c;
+    if (idx < K.N && cafe_is_active(D, K, P, idx)) ++cnt;
+  }
+  for (int o = 16; o > 0; o >>= 1) cnt += __shfl_down_sync(0xffffffffu, cnt, o);
+  if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = cnt;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int s = 0;
+    for (int w = 0; w < CAFE_DENSE_THREADS / 32; ++w) s += wsum[w];
+    D.blk[blockIdx.x] = s;
+  }
+}
+
+// Exclusive scan of n block counts in place; writes the total to *total.
+__global__ void k_scan_blocks(int32_t *blk, long long n, int *total) {
+  __shared__ long long part[1024];
+  long long per = (n + blockDim.x - 1) / blockDim.x;
+  long long b0 = threadIdx.x * per, b1 = b0 + per < n ? b0 + per : n;
+  long long s = 0;
+  for (long long b = b0; b < b1; ++b) s += blk[b];
+  part[threadIdx.x] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    long long acc = 0;
+    for (int t = 0; t < (int)blockDim.x; ++t) {
+      long long v = part[t];
+      part[t] = acc;
+      acc += v;
+    }
+    *total = (int)acc;
+  }
+  __syncthreads();
+  long long acc = part[threadIdx.x];
+  for (long long b = b0; b < b1; ++b) {
+    long long v = blk[b];
+    blk[b] = (int32_t)acc;
+    acc += v;
+  }
+}
+
+__global__ void k_active_scatter(CafeDev D, CafeConsts K, CafeStepParams P) {
+  __shared__ int wsum[CAFE_DENSE_THREADS / 32];
+  long long base = ((long long)blockIdx.x * blockDim.x + threadIdx.x) * CAFE_CELLS_PER_THREAD;
+  uint32_t flags = 0;
+  int cnt = 0;
+  for (int c = 0; c < CAFE_CELLS_PER_THREAD; ++c) {
+    long long idx = base + c;
+    if (idx < K.N && cafe_is_active(D, K, P, idx)) {
+      flags |= 1u << c;
+      ++cnt;
+    }
+  }
+  // block-exclusive scan of per-thread counts
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  int incl = cnt;
+  for (int o = 1; o < 32; o <<= 1) {
+    int v = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += v;
+  }
+  if (lane == 31) wsum[w] = incl;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    int v = threadIdx.x < CAFE_DENSE_THREADS / 32 ? wsum[threadIdx.x] : 0;
+    int inc = v;
+    for (int o = 1; o < 32; o <<= 1) {
+      int u = __shfl_up_sync(0xffffffffu, inc, o);
+      if (threadIdx.x >= o) inc += u;
+    }
+    if (threadIdx.x < CAFE_DENSE_THREADS / 32) wsum[threadIdx.x] = inc - v;
+  }
+  __syncthreads();
+  long long pos = (long long)D.blk[blockIdx.x] + wsum[w] + (incl - cnt);
+  for (int c = 0; c < CAFE_CELLS_PER_THREAD; ++c) {
+    if (!(flags >> c & 1u)) continue;
+    long long idx = base + c;
+    if (pos < D.act_cap) {
+      D.act[pos] = (int32_t)idx;
+      D.pos_of[idx] = (int32_t)pos;
+    } else {
+      atomicOr(D.err, CAFE_ERR_ACTIVE_CAP);
+    }
+    ++pos;
+  }
+}
+
+// ------------------------------------------------------------------ gather
+// Per active position: copies of the cell data, temperature class, neighbour
+// positions in ascending index order (-1 = not active), liquid-neighbour count,
+// all-neighbours-below-liquidus flag and the ruq offset (VoxelsCA.C:380:
+// ruq[p] = (U_p - .5) dX / 100, U_p the p-th uniform of minstd(30 tInd + seed1)).
+__global__ void k_gather(CafeDev D, CafeConsts K, CafeStepParams P) {
+  int na = D.ctr[CTR_NA];
+  if (na > D.act_cap) na = (int)D.act_cap;
+  uint32_t seed = cafe_minstd_seed((uint64_t)(uint32_t)(30 * P.tInd + (int)K.seed1));
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < na; p += gridDim.x * blockDim.x) {
+    long long idx = D.act[p];
+    int i, j, k;
+    cafe_cell_xyz(K, idx, i, j, k);
+    D.a_state[p] = D.state[idx];
+    D.a_gid[p] = D.gid[idx];
+    D.a_ext[p] = D.ext[idx];
+    D.a_cx[p] = D.cx[idx];
+    D.a_cy[p] = D.cy[idx];
+    D.a_cz[p] = D.cz[idx];
+    D.a_cls[p] = (uint8_t)cafe_temp_class(K, P, i, j, k);
+    long long nb[26];
+    int n = cafe_moore(K, i, j, k, nb);
+    int m = 0, liq = 0, cold = 1;
+    for (int a = 0; a < n; ++a) {
+      int q = D.pos_of[nb[a]];
+      if (q < 0) continue;
+      D.a_nbr[(long long)p * CAFE_NSLOT + m] = q;
+      ++m;
+      if (D.state[nb[a]] == 1) ++liq;
+      int ni, nj, nk;
+      cafe_cell_xyz(K, nb[a], ni, nj, nk);
+      if (cafe_hot(K, P, ni, nj, nk)) cold = 0;
+    }
+    D.a_nn[p] = (uint8_t)m;
+    D.a_liq[p] = liq;
+    D.a_cold[p] = (uint8_t)cold;
+    D.a_frow[p] = -1;
+    double U = cafe_uniform_at(seed, (uint64_t)p);
+    D.a_ruq[p] = (U - .5) * K.ruq_dx / 100.;
+  }
+}
+
+// ------------------------------------------------------------------ vs2ind + frontier rows
+// Two order-preserving compactions over positions: mushy positions (vs2ind,
+// VoxelsCA.C:346-353) and, among them, those with a liquid neighbour and no
+// neighbour at the liquidus (the cells that can capture, VoxelsCA.C:396-397).
+__global__ void k_lists_count(CafeDev D) {
+  __shared__ int ws[2][CAFE_DENSE_THREADS / 32];
+  int na = D.ctr[CTR_NA];
+  long long base = ((long long)blockIdx.x * blockDim.x + threadIdx.x) * CAFE_CELLS_PER_THREAD;
+  int c2 = 0, cf = 0;
+  for (int c = 0; c < CAFE_CELLS_PER_THREAD; ++c) {
+    long long p = base + c;
+    if (p >= na) break;
+    if (D.a_state[p] == 2) {
+      ++c2;
+      if (D.a_liq[p] > 0 && D.a_cold[p]) ++cf;
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    c2 += __shfl_down_sync(0xffffffffu, c2, o);
+    cf += __shfl_down_sync(0xffffffffu, cf, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    ws[0][threadIdx.x >> 5] = c2;
+    ws[1][threadIdx.x >> 5] = cf;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int s2 = 0, sf = 0;
+    for (int w = 0; w < CAFE_DENSE_THREADS / 32; ++w) {
+      s2 += ws[0][w];
+      sf += ws[1][w];
+    }
+    D.blk[2 * blockIdx.x] = s2;
+    D.blk[2 * blockIdx.x + 1] = sf;
+  }
+}
+
+// Exclusive scan of interleaved pairs (blk[2b], blk[2b+1]).
+__global__ void k_scan_pairs(int32_t *blk, long long n, int *tot0, int *tot1) {
+  if (threadIdx.x != 0) return;
+  long long a0 = 0, a1 = 0;
+  for (long long b = 0; b < n; ++b) {
+    long long v0 = blk[2 * b], v1 = blk[2 * b + 1];
+    blk[2 * b] = (int32_t)a0;
+    blk[2 * b + 1] = (int32_t)a1;
+    a0 += v0;
+    a1 += v1;
+  }
+  *tot0 = (int)a0;
+  *tot1 = (int)a1;
+}
+
+__global__ void k_lists_scatter(CafeDev D) {
+  __shared__ int ws[2][CAFE_DENSE_THREADS / 32];
+  int na = D.ctr[CTR_NA];
+  long long base = ((long long)blockIdx.x * blockDim.x + threadIdx.x) * CAFE_CELLS_PER_THREAD;
+  int c2 = 0, cf = 0;
+  for (int c = 0; c < CAFE_CELLS_PER_THREAD; ++c) {
+    long long p = base + c;
+    if (p >= na) break;
+    if (D.a_state[p] == 2) {
+      ++c2;
+      if (D.a_liq[p] > 0 && D.a_cold[p]) ++cf;
+    }
+  }
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  int i2 = c2, i_f = cf;
+  for (int o = 1; o < 32; o <<= 1) {
+    int v2 = __shfl_up_sync(0xffffffffu, i2, o), vf = __shfl_up_sync(0xffffffffu, i_f, o);
+    if (lane >= o) {
+      i2 += v2;
+      i_f += vf;
+    }
+  }
+  if (lane == 31) {
+    ws[0][w] = i2;
+    ws[1][w] = i_f;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int a2 = 0, af = 0;
+    for (int q = 0; q < CAFE_DENSE_THREADS / 32; ++q) {
+      int v2 = ws[0][q], vf = ws[1][q];
+      ws[0][q] = a2;
+      ws[1][q] = af;
+      a2 += v2;
+      af += vf;
+    }
+  }
+  __syncthreads();
+  long long j2 = (long long)D.blk[2 * blockIdx.x] + ws[0][w] + (i2 - c2);
+  long long jf = (long long)D.blk[2 * blockIdx.x + 1] + ws[1][w] + (i_f - cf);
+  for (int c = 0; c < CAFE_CELLS_PER_THREAD; ++c) {
+    long long p = base + c;
+    if (p >= na) break;
+    if (D.a_state[p] != 2) continue;
+    if (j2 < D.vs2_cap)
+      D.vs2[j2] = (int32_t)p;
+    else
+      atomicOr(D.err, CAFE_ERR_MUSHY_CAP);
+    if (D.a_liq[p] > 0 && D.a_cold[p]) {
+      if (jf < D.row_cap) {
+        D.row_pos[jf] = (int32_t)p;
+        D.row_j[jf] = (int32_t)j2;
+        D.row_alive[jf] = 1;
+        D.a_frow[p] = (int32_t)jf;
+      } else {
+        atomicOr(D.err, CAFE_ERR_ROW_CAP);
+      }
+      ++jf;
+    }
+    ++j2;
+  }
+}
+
+// ------------------------------------------------------------------ frontier rows
+// Candidate order inside a row: by g, NaN last, ties by slot.
+__device__ __forceinline__ bool cafe_g_before(double ga, int sa, double gb, int sb) {
+  bool na = ga != ga, nb = gb != gb;
+  if (na || nb) return nb && !na ? true : (na && nb ? sa < sb : false);
+  return ga < gb || (ga == gb && sa < sb);
+}
+
+// Fills row r for position p cooperatively within one warp: lane s computes
+// the numerator of slot s, lane 0 orders the live slots.
+__device__ void cafe_row_fill_warp(const CafeDev &D, const CafeConsts &K, long long r, int p) {
+  int lane = threadIdx.x & 31;
+  int nn = D.a_nn[p];
+  double *g = D.row_g + r * CAFE_NSLOT;
+  bool liv = false;
+  if (lane < nn) {
+    int q = D.a_nbr[(long long)p * CAFE_NSLOT + lane];
+    if (D.a_state[q] == 1) {
+      const double *R = D.rot + 9LL * (D.a_gid[p] - 1);
+      double Rm[9];
+      for (int a = 0; a < 9; ++a) Rm[a] = R[a];
+      int i, j, k;
+      cafe_cell_xyz(K, D.act[q], i, j, k);
+      g[lane] = cafe_candidate_g(K, D.a_cx[p], D.a_cy[p], D.a_cz[p], Rm, i, j, k);
+      liv = true;
+    }
+  }
+  uint32_t live = __ballot_sync(0xffffffffu, liv);
+  __syncwarp();
+  if (lane == 0) {
+    uint8_t *ord = D.row_ord + r * CAFE_NSLOT;
+    int no = 0;
+    for (int s = 0; s < nn; ++s) {
+      if (!(live >> s & 1u)) continue;
+      double gv = g[s];
+      int at = no;
+      while (at > 0 && cafe_g_before(gv, s, g[ord[at - 1]], ord[at - 1])) {
+        ord[at] = ord[at - 1];
+        --at;
+      }
+      ord[at] = (uint8_t)s;
+      ++no;
+    }
+    // slots that are not candidates follow, so ord is a permutation of 0..nn-1
+    for (int s = 0; s < nn; ++s)
+      if (!(live >> s & 1u)) ord[no++] = (uint8_t)s;
+    D.row_live[r] = live;
+  }
+  __syncwarp();
+}
+
+// One warp per row at step start.
+__global__ void k_rows_init(CafeDev D, CafeConsts K) {
+  int nrows = D.ctr[CTR_NROWS];
+  if (nrows > D.row_cap) nrows = (int)D.row_cap;
+  int warps = (gridDim.x * blockDim.x) >> 5;
+  int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  for (int r = w; r < nrows; r += warps) cafe_row_fill_warp(D, K, r, D.row_pos[r]);
+}
+
+// ------------------------------------------------------------------ event loop
+struct CafeCand {
+  double t, ruqs;
+  int j, s;  // vs2 index and neighbour slot of the capturing cell; j < 0 = none
+};
+__device__ __forceinline__ bool cafe_cand_better(const CafeCand &a, const CafeCand &b) {
+  // lexicographic (t, ruqs, scan position): VoxelsCA.C:427-440 keeps the first
+  // scanned candidate among full ties
+  if (a.j < 0) return false;
+  if (b.j < 0) return true;
+  if (a.t < b.t) return true;
+  if (b.t < a.t) return false;
+  if (a.ruqs < b.ruqs) return true;
+  if (b.ruqs < a.ruqs) return false;
+  if (a.j != b.j) return a.j < b.j;
+  return a.s < b.s;
+}
+__device__ __forceinline__ CafeCand cafe_shfl_cand(const CafeCand &c, int o) {
+  CafeCand r;
+  r.t = __shfl_down_sync(0xffffffffu, c.t, o);
+  r.ruqs = __shfl_down_sync(0xffffffffu, c.ruqs, o);
+  r.j = __shfl_down_sync(0xffffffffu, c.j, o);
+  r.s = __shfl_down_sync(0xffffffffu, c.s, o);
+  return r;
+}
+
+// Best candidate of frontier row r. For a positive finite growth velocity the
+// capture time fl(fl(g - E)/v) is non-decreasing in g, so the live slots are
+// visited in g order and the visit stops at the first time above the row's
+// minimum; otherwise every live slot is evaluated (VoxelsCA.C:406-442).
+__device__ __forceinline__ void cafe_row_best(const CafeDev &D, const CafeConsts &K, long long r,
+                                              CafeCand &best) {
+  int p = D.row_pos[r];
+  uint32_t live = D.row_live[r];
+  if (!live) return;
+  double E = D.a_ext[p];
+  double v = K.vhat_cls[D.a_cls[p]];
+  bool mono = (v > 0.0) && (v < INFINITY);
+  const double *g = D.row_g + r * CAFE_NSLOT;
+  const uint8_t *ord = D.row_ord + r * CAFE_NSLOT;
+  int nn = D.a_nn[p];
+  int jrow = D.row_j[r];
+  double ruq_p = D.a_ruq[p];
+  bool have = false;
+  double tfirst = 0.0;
+  for (int k = 0; k < nn; ++k) {
+    int s = mono ? ord[k] : k;
+    if (!(live >> s & 1u)) continue;
+    double dr = g[s] - E;
+    double t = dr / v;
+    if (!(t <= 1e6)) {
+      if (mono && t > 1e6) break;
+      continue;
+    }
+    if (mono && have && t > tfirst) break;
+    int q = D.a_nbr[(long long)p * CAFE_NSLOT + s];
+    CafeCand c;
+    c.t = t;
+    c.ruqs = .5 * (ruq_p + D.a_ruq[q]);
+    c.j = jrow;
+    c.s = s;
+    if (cafe_cand_better(c, best)) best = c;
+    if (!have) {
+      have = true;
+      tfirst = t;
+    }
+  }
+}
+
+__device__ __forceinline__ int cafe_find_slot(const CafeDev &D, int q, int target) {
+  int nn = D.a_nn[q];
+  const int32_t *nb = D.a_nbr + (long long)q * CAFE_NSLOT;
+  for (int s = 0; s < nn; ++s)
+    if (nb[s] == target) return s;
+  return -1;
+}
+
+// The capture/nucleation loop of one step (VoxelsCA.C:381-610), one block.
+__global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
+    k_event_loop(CafeDev D, CafeConsts K, CafeStepParams P, long long max_events) {
+  __shared__ CafeCand red[CAFE_LOOP_THREADS / 32];
+  __shared__ CafeCand s_best;
+  __shared__ double s_tinc, s_dt;
+  __shared__ int s_nvs2, s_countS, s_nrows, s_ngrain, s_done, s_nuc, s_icap, s_jspos, s_na;
+  __shared__ uint32_t s_rng;
+  __shared__ unsigned int s_sdloc;
+  __shared__ long long s_nev, s_nnuc, s_negdt;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (tid == 0) {
+    s_na = D.ctr[CTR_NA];
+    s_nvs2 = D.ctr[CTR_NVS2];
+    s_nrows = D.ctr[CTR_NROWS];
+    s_ngrain = D.ctr[CTR_NGRAIN];
+    uint32_t seed = cafe_minstd_seed((uint64_t)(uint32_t)(30 * P.tInd + (int)K.seed1));
+    s_rng = cafe_minstd_skip(seed, 2ULL * (uint64_t)s_na);
+    s_sdloc = K.seed0 + 32u * (unsigned int)P.tInd + 64u * (unsigned int)s_ngrain;
+    s_tinc = 0.0;
+    s_countS = s_na;
+    s_nev = 0;
+    s_nnuc = 0;
+    s_negdt = 0;
+    s_done = (*D.err != 0) || (s_na > D.act_cap) || (s_nvs2 > D.vs2_cap) || (s_nrows > D.row_cap);
+  }
+  __syncthreads();
+  while (true) {
+    if (tid == 0) {
+      // while (vSind2 != countS && tinc < DelT)
+      if (!(s_nvs2 != s_countS && s_tinc < K.DelT)) s_done = 1;
+      s_countS = s_nvs2;
+    }
+    __syncthreads();
+    if (s_done) break;
+    // ---- candidate scan and block argmin
+    CafeCand best;
+    best.j = -1;
+    best.t = 0;
+    best.ruqs = 0;
+    best.s = 0;
+    for (int r = tid; r < s_nrows; r += blockDim.x)
+      if (D.row_alive[r]) cafe_row_best(D, K, r, best);
+    for (int o = 16; o > 0; o >>= 1) {
+      CafeCand c = cafe_shfl_cand(best, o);
+      if (cafe_cand_better(c, best)) best = c;
+    }
+    if (lane == 0) red[warp] = best;
+    __syncthreads();
+    if (tid == 0) {
+      CafeCand b = red[0];
+      for (int w = 1; w < (int)(blockDim.x >> 5); ++w)
+        if (cafe_cand_better(red[w], b)) b = red[w];
+      if (b.j < 0 || !(b.t < 1e6) || s_nev >= max_events) {
+        if (b.j >= 0 && b.t < 1e6) atomicOr(D.err, CAFE_ERR_ITER_CAP);
+        s_done = 1;
+      } else {
+        cafe_uniform_stream st;
+        st.x = s_rng;
+        double U = cafe_uniform_next(&st);
+        s_rng = st.x;
+        int jspos = D.vs2[b.j];
+        s_jspos = jspos;
+        s_icap = D.a_nbr[(long long)jspos * CAFE_NSLOT + b.s];
+        s_nuc = U < K.rX;
+        s_dt = s_nuc ? 0.0 : b.t;
+        s_best = b;
+        if (s_dt < 0.0) s_negdt++;
+      }
+    }
+    __syncthreads();
+    if (s_done) break;
+    // ---- growth of every mushy cell of the list (VoxelsCA.C:511-516)
+    if (!s_nuc) {
+      double d = s_dt;
+      if (isfinite(d)) {
+        for (int r = tid; r < s_nrows; r += blockDim.x) {
+          if (!D.row_alive[r]) continue;
+          int p = D.row_pos[r];
+          double e = D.a_ext[p] + K.vhat_cls[D.a_cls[p]] * d;
+          D.a_ext[p] = (e < 0.0) ? 0.0 : e;
+        }
+      } else {
+        for (int j = tid; j < s_countS; j += blockDim.x) {
+          int p = D.vs2[j];
+          int r = D.a_frow[p];
+          double v = (r >= 0 && D.row_alive[r]) ? K.vhat_cls[D.a_cls[p]] : 0.0;
+          double e = D.a_ext[p] + v * d;
+          D.a_ext[p] = (e < 0.0) ? 0.0 : e;
+        }
+      }
+    }
+    __syncthreads();
+    // ---- the captured cell (VoxelsCA.C:483-505 and 518-605)
+    if (tid == 0) {
+      int icap = s_icap, js = s_jspos;
+      D.a_state[icap] = 2;
+      if (s_nvs2 < D.vs2_cap) {
+        D.vs2[s_nvs2] = icap;
+      } else {
+        atomicOr(D.err, CAFE_ERR_MUSHY_CAP);
+        s_done = 1;
+      }
+      s_nvs2 += 1;
+      int ci, cj, ck;
+      cafe_cell_xyz(K, D.act[icap], ci, cj, ck);
+      if (s_nuc) {
+        if (s_ngrain < D.grain_cap) {
+          double q4[4];
+          cafe_sample_orientation(K, s_sdloc, q4);
+          double *c = D.cth + 4LL * s_ngrain;
+          for (int a = 0; a < 4; ++a) c[a] = q4[a];
+          cafe_rot_from_cth(c, D.rot + 9LL * s_ngrain);
+        } else {
+          atomicOr(D.err, CAFE_ERR_GRAIN_CAP);
+          s_done = 1;
+        }
+        s_ngrain += 1;
+        D.a_gid[icap] = s_ngrain;
+        D.a_cx[icap] = ((double)ci + .5) * K.dx[0];
+        D.a_cy[icap] = ((double)cj + .5) * K.dx[1];
+        D.a_cz[icap] = ((double)ck + .5) * K.dx[2];
+        s_sdloc += 10u;
+        D.a_ext[icap] = 0.0;
+        s_nnuc++;
+      } else {
+        int g = D.a_gid[js];
+        D.a_gid[icap] = g;
+        int si, sj, sk;
+        cafe_cell_xyz(K, D.act[js], si, sj, sk);
+        double cs[3] = {D.a_cx[js], D.a_cy[js], D.a_cz[js]};
+        double e, cn[3];
+        cafe_capture_geometry(K, ci, cj, ck, si, sj, sk, cs, D.rot + 9LL * (g - 1), &e, cn);
+        D.a_ext[icap] = e;
+        D.a_cx[icap] = cn[0];
+        D.a_cy[icap] = cn[1];
+        D.a_cz[icap] = cn[2];
+      }
+      s_tinc += s_dt;
+      s_nev++;
+    }
+    __syncthreads();
+    // ---- neighbours of the captured cell lose one liquid neighbour
+    if (warp == 0) {
+      int icap = s_icap;
+      int nn = D.a_nn[icap];
+      if (lane < nn) {
+        int q = D.a_nbr[(long long)icap * CAFE_NSLOT + lane];
+        int left = --D.a_liq[q];
+        int r = D.a_frow[q];
+        if (r >= 0 && D.row_alive[r]) {
+          int s = cafe_find_slot(D, q, icap);
+          if (s >= 0) D.row_live[r] &= ~(1u << s);
+          if (left <= 0) D.row_alive[r] = 0;
+        }
+      }
+      __syncwarp();
+      // ---- the captured cell becomes a capturing cell if it qualifies
+      if (D.a_liq[icap] > 0 && D.a_cold[icap] && !s_done) {
+        int r = s_nrows;
+        if (r < D.row_cap) {
+          if (lane == 0) {
+            D.row_pos[r] = icap;
+            D.row_j[r] = s_nvs2 - 1;
+            D.row_alive[r] = 1;
+            D.a_frow[icap] = r;
+          }
+          __syncwarp();
+          cafe_row_fill_warp(D, K, r, icap);
+          if (lane == 0) s_nrows = r + 1;
+        } else if (lane == 0) {
+          atomicOr(D.err, CAFE_ERR_ROW_CAP);
+          s_done = 1;
+        }
+      }
+    }
+    __syncthreads();
+  }
+  if (tid == 0) {
+    D.ctr[CTR_NGRAIN] = s_ngrain;
+    D.ctr[CTR_NVS2_END] = s_nvs2;
+    D.ctr[CTR_NEV] = (int)s_nev;
+    D.ctr[CTR_NNUC] = (int)s_nnuc;
+    atomicAdd(&D.stat[STAT_EVENTS], (unsigned long long)s_nev);
+    atomicAdd(&D.stat[STAT_NUC], (unsigned long long)s_nnuc);
+    atomicAdd(&D.stat[STAT_NEGDT], (unsigned long long)s_negdt);
+    atomicMax(&D.stat[STAT_MAXNA], (unsigned long long)s_na);
+    atomicMax(&D.stat[STAT_MAXROWS], (unsigned long long)s_nrows);
+    atomicAdd(&D.stat[STAT_STEPS], 1ULL);
+  }
+}
+
+// ------------------------------------------------------------------ write back
+__global__ void k_writeback(CafeDev D) {
+  int na = D.ctr[CTR_NA];
+  if (na > D.act_cap) na = (int)D.act_cap;
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < na; p += gridDim.x * blockDim.x) {
+    long long idx = D.act[p];
+    D.state[idx] = D.a_state[p];
+    D.gid[idx] = D.a_gid[p];
+    D.ext[idx] = D.a_ext[p];
+    D.cx[idx] = D.a_cx[p];
+    D.cy[idx] = D.a_cy[p];
+    D.cz[idx] = D.a_cz[p];
+    D.pos_of[idx] = -1;
+  }
+}
+
+// ConvertSolid1(0): mushy cells whose neighbours are all mushy or solid become
+// solid with zero extent. Every mushy cell is in this step's active list. In
+// place is equivalent to collect-then-apply: 2 -> 3 keeps "neighbour >= 2".
+__global__ void k_mushy2solid(CafeDev D, CafeConsts K) {
+  int na = D.ctr[CTR_NA];
+  if (na > D.act_cap) na = (int)D.act_cap;
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < na; p += gridDim.x * blockDim.x) {
+    if (D.a_state[p] != 2) continue;
+    long long idx = D.act[p];
+    int i, j, k;
+    cafe_cell_xyz(K, idx, i, j, k);
+    long long nb[26];
+    int n = cafe_moore(K, i, j, k, nb);
+    bool all = true;
+    for (int a = 0; a < n && all; ++a) all = D.state[nb[a]] >= 2;
+    if (all) {
+      D.state[idx] = 3;
+      D.ext[idx] = 0.0;
+    }
+  }
+}
+
+// ------------------------------------------------------------------ grains
+__global__ void k_rot_range(CafeDev D, int g0, int g1) {
+  for (int g = g0 + blockIdx.x * blockDim.x + threadIdx.x; g < g1; g += gridDim.x * blockDim.x)
+    cafe_rot_from_cth(D.cth + 4LL * g, D.rot + 9LL * g);
+}
+
+// CleanLayer (VoxelsCA.C:800-839): grain volumes, renumbering, compaction.
+__global__ void k_grain_count(CafeDev D, CafeConsts K, int32_t *cnt) {
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < K.N;
+       idx += (long long)gridDim.x * blockDim.x) {
+    int g = D.gid[idx];
+    if (g > 0) atomicAdd(&cnt[g - 1], 1);
+  }
+}
+// Single block: newid[g] (1-based, 0 = dropped) and compacted grain tables.
+__global__ void k_grain_renumber(CafeDev D, const int32_t *cnt, int32_t *newid, double *cth2,
+                                 double *rot2) {
+  __shared__ int part[1024];
+  int ng = D.ctr[CTR_NGRAIN];
+  int per = (ng + blockDim.x - 1) / blockDim.x;
+  int b0 = threadIdx.x * per, b1 = min(b0 + per, ng);
+  int s = 0;
+  for (int g = b0; g < b1; ++g) s += cnt[g] > 0;
+  part[threadIdx.x] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int acc = 0;
+    for (int t = 0; t < (int)blockDim.x; ++t) {
+      int v = part[t];
+      part[t] = acc;
+      acc += v;
+    }
+    D.ctr[CTR_NVS2_END] = acc;  // scratch: new grain count
+  }
+  __syncthreads();
+  int k = part[threadIdx.x];
+  for (int g = b0; g < b1; ++g) {
+    if (cnt[g] > 0) {
+      newid[g] = k + 1;
+      for (int a = 0; a < 4; ++a) cth2[4LL * k + a] = D.cth[4LL * g + a];
+      for (int a = 0; a < 9; ++a) rot2[9LL * k + a] = D.rot[9LL * g + a];
+      ++k;
+    } else {
+      newid[g] = 0;
+    }
+  }
+}
+__global__ void k_gid_remap(CafeDev D, CafeConsts K, const int32_t *newid) {
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < K.N;
+       idx += (long long)gridDim.x * blockDim.x) {
+    int g = D.gid[idx];
+    if (g != 0) D.gid[idx] = newid[g - 1];
+  }
+}
+
+// ------------------------------------------------------------------ Voronoi
+// Nearest site with the reference's distance (dx^2 + dy^2) + dz^2 and its
+// first-minimum rule (BasePlate.C:269-272, VoxelsCA.C:925-930). Sites are
+// bucketed on a uniform grid; rings of buckets are searched until no unvisited
+// bucket can hold a site whose rounded distance could reach the best found.
+struct CafeSiteGrid {
+  const double *xyz;      // 3 per site
+  const int32_t *start;   // bucket CSR
+  const int32_t *idx;     // site indices, ascending inside a bucket
+  double lo[3], h;
+  int nb[3];
+};
+
+__device__ int cafe_nearest_site(const CafeSiteGrid &G, double q0, double q1, double q2) {
+  double q[3] = {q0, q1, q2};
+  int qb[3];
+  for (int a = 0; a < 3; ++a) {
+    double f = floor((q[a] - G.lo[a]) / G.h);
+    int b = f < 0 ? 0 : (f > G.nb[a] - 1 ? G.nb[a] - 1 : (int)f);
+    qb[a] = b;
+  }
+  double best = INFINITY;
+  int besti = -1;
+  int rmax = max(G.nb[0], max(G.nb[1], G.nb[2]));
+  for (int r = 0; r <= rmax; ++r) {
+    for (int dz = -r; dz <= r; ++dz) {
+      int bz = qb[2] + dz;
+      if (bz < 0 || bz >= G.nb[2]) continue;
+      for (int dy = -r; dy <= r; ++dy) {
+        int by = qb[1] + dy;
+        if (by < 0 || by >= G.nb[1]) continue;
+        bool edge = (abs(dz) == r || abs(dy) == r);
+        for (int dxx = -r; dxx <= r; dxx += (edge ? 1 : (2 * r > 0 ? 2 * r : 1))) {
+          int bx = qb[0] + dxx;
+          if (bx < 0 || bx >= G.nb[0]) continue;
+          int b = (bz * G.nb[1] + by) * G.nb[0] + bx;
+          for (int t = G.start[b]; t < G.start[b + 1]; ++t) {
+            int i = G.idx[t];
+            double a = q0 - G.xyz[3LL * i], bb = q1 - G.xyz[3LL * i + 1], c = q2 - G.xyz[3LL * i + 2];
+            double d = a * a + bb * bb + c * c;
+            if (d < best || (d == best && i < besti)) {
+              best = d;
+              besti = i;
+            }
+          }
+          if (r == 0) break;
+        }
+      }
+    }
+    // lower bound on the distance to any bucket outside rings 0..r
+    double gap = INFINITY;
+    bool more = false;
+    for (int a = 0; a < 3; ++a) {
+      if (qb[a] - r - 1 >= 0) {
+        more = true;
+        double g = q[a] - (G.lo[a] + (qb[a] - r) * G.h);
+        gap = g < gap ? g : gap;
+      }
+      if (qb[a] + r + 1 < G.nb[a]) {
+        more = true;
+        double g = (G.lo[a] + (qb[a] + r + 1) * G.h) - q[a];
+        gap = g < gap ? g : gap;
+      }
+    }
+    if (!more) break;
+    gap -= 1e-9 * G.h;
+    if (besti >= 0 && gap > 0 && gap * gap > best * (1.0 + 1e-9)) break;
+  }
+  return besti;
+}
+
+// Baseplate (BasePlate.C:262-273 + VoxelsCA.C:133-141, 148-156): cell centres,
+// cells below z = Nzh-1 solid, the top baseplate plane mushy.
+__global__ void k_baseplate(CafeDev D, CafeConsts K, CafeSiteGrid G, int Nzh) {
+  long long nbp = (long long)Nzh * K.nxy;
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < nbp;
+       idx += (long long)gridDim.x * blockDim.x) {
+    int i, j, k;
+    cafe_cell_xyz(K, idx, i, j, k);
+    double x = (i + .5) * K.dx[0], y = (j + .5) * K.dx[1], z = (k + .5) * K.dx[2];
+    int s = cafe_nearest_site(G, x, y, z);
+    D.gid[idx] = s + 1;
+    D.state[idx] = idx < (long long)(Nzh - 1) * K.nxy ? 3 : 2;
+    D.cx[idx] = ((double)i + .5) * K.dx[0];
+    D.cy[idx] = ((double)j + .5) * K.dx[1];
+    D.cz[idx] = ((double)k + .5) * K.dx[2];
+  }
+}
+
+// AddLayer1 part 1 (VoxelsCA.C:922-936): nearest site (corner coordinates) for
+// every cell of the layer slab [iz1, ilaserLoc) (also beyond the box top, as
+// the reference does), and the used-site flags.
+__global__ void k_layer_voronoi(CafeConsts K, CafeSiteGrid G, int iz1, int ilaser, int32_t *gtmp,
+                                int32_t *used) {
+  long long nslab = (long long)K.nxy * (ilaser - iz1);
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < nslab;
+       t += (long long)gridDim.x * blockDim.x) {
+    int k = iz1 + (int)(t / K.nxy);
+    long long r = t % K.nxy;
+    int j = (int)(r / K.nx), i = (int)(r % K.nx);
+    double x = i * K.dx[0], y = j * K.dx[1], z = k * K.dx[2];
+    int s = cafe_nearest_site(G, x, y, z);
+    gtmp[t] = s;
+    used[s] = 1;
+  }
+}
+// AddLayer1 part 2 (VoxelsCA.C:952-981): new grain IDs, solid state, cell
+// centres inside the slab; empty state above the laser plane.
+__global__ void k_layer_apply(CafeDev D, CafeConsts K, int iz1, int ilaser, const int32_t *gtmp,
+                              const int32_t *map, int ngrain0) {
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < K.N;
+       idx += (long long)gridDim.x * blockDim.x) {
+    int i, j, k;
+    cafe_cell_xyz(K, idx, i, j, k);
+    if (k >= iz1 && k < ilaser) {
+      long long t = (long long)(k - iz1) * K.nxy + (long long)j * K.nx + i;
+      D.gid[idx] = ngrain0 + map[gtmp[t]] + 1;
+      D.state[idx] = 3;
+      D.cx[idx] = ((double)i + .5) * K.dx[0];
+      D.cy[idx] = ((double)j + .5) * K.dx[1];
+      D.cz[idx] = ((double)k + .5) * K.dx[2];
+    }
+    if (idx >= (long long)K.nxy * ilaser) {
+      D.state[idx] = 0;
+      D.gid[idx] = 0;
+    }
+  }
+}
+
+// TempField::TempCurr for output (the step computes it on the fly).
+__global__ void k_temperature(CafeConsts K, CafeStepParams P, double *T) {
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < K.N;
+       idx += (long long)gridDim.x * blockDim.x) {
+    int i, j, k;
+    cafe_cell_xyz(K, idx, i, j, k);
+    T[idx] = K.Tcls[cafe_temp_class(K, P, i, j, k)];
+  }
+}
