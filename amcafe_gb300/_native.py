@@ -1,0 +1,95 @@
+"""ctypes binding of libcafe_gpu.so (the C ABI declared in include/cafe_gpu.h).
+
+The library is built in-tree by amcafe_gb300.build (nvcc, sm_103a). Loading
+fails with an ImportError when it has not been built: there is no fallback
+implementation of the GPU path.
+"""
+import ctypes
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "libcafe_gpu.so")
+
+# Every symbol declared in include/cafe_gpu.h.
+EXPORTS = (
+    "cafe_sim_create", "cafe_sim_destroy", "cafe_sim_initialize_voxels", "cafe_sim_add_layer",
+    "cafe_sim_update_laser", "cafe_sim_temperature", "cafe_sim_update_voxels",
+    "cafe_sim_clean_layer", "cafe_sim_update_time", "cafe_sim_begin", "cafe_sim_step",
+    "cafe_sim_run", "cafe_sim_synchronize", "cafe_sim_info", "cafe_sim_stats",
+    "cafe_sim_download_state", "cafe_sim_download_temperature", "cafe_sim_download_ctheta",
+    "cafe_sim_upload_state", "cafe_last_error",
+)
+
+
+class CafeOptions(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int), ("active_capacity", ctypes.c_longlong),
+                ("grain_capacity", ctypes.c_longlong)]
+
+
+class CafeInfo(ctypes.Structure):
+    _fields_ = [("nx", ctypes.c_int), ("ny", ctypes.c_int), ("nz", ctypes.c_int),
+                ("dx", ctypes.c_double), ("tInd", ctypes.c_int), ("time", ctypes.c_double),
+                ("isp", ctypes.c_int), ("indlayer", ctypes.c_int), ("inewlayerflg", ctypes.c_int),
+                ("inewscanflg", ctypes.c_int), ("ilaserLoc", ctypes.c_int), ("nGrain", ctypes.c_int),
+                ("nlayerTot", ctypes.c_int), ("Nzh", ctypes.c_int), ("done", ctypes.c_int),
+                ("steps", ctypes.c_longlong)]
+
+
+class CafeStats(ctypes.Structure):
+    _fields_ = [("events", ctypes.c_ulonglong), ("nucleations", ctypes.c_ulonglong),
+                ("max_active", ctypes.c_ulonglong), ("max_rows", ctypes.c_ulonglong),
+                ("steps", ctypes.c_ulonglong), ("negative_dt", ctypes.c_ulonglong)]
+
+
+_lib = None
+
+
+def load():
+    """Returns the loaded library; raises ImportError if it is missing."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError("libcafe_gpu.so is not built (%s); run amcafe_gb300.build.build()" % LIB_PATH)
+    lib = ctypes.CDLL(LIB_PATH)
+    P, I, LL, D = ctypes.c_void_p, ctypes.c_int, ctypes.c_longlong, ctypes.c_double
+    i32p = ctypes.POINTER(ctypes.c_int32)
+    f64p = ctypes.POINTER(ctypes.c_double)
+    sig = {
+        "cafe_sim_create": (I, [ctypes.c_char_p, ctypes.POINTER(CafeOptions), ctypes.POINTER(P)]),
+        "cafe_sim_destroy": (None, [P]),
+        "cafe_sim_initialize_voxels": (I, [P]),
+        "cafe_sim_add_layer": (I, [P]),
+        "cafe_sim_update_laser": (I, [P]),
+        "cafe_sim_temperature": (I, [P]),
+        "cafe_sim_update_voxels": (I, [P]),
+        "cafe_sim_clean_layer": (I, [P]),
+        "cafe_sim_update_time": (I, [P]),
+        "cafe_sim_begin": (I, [P]),
+        "cafe_sim_step": (I, [P, ctypes.POINTER(I)]),
+        "cafe_sim_run": (I, [P, LL, ctypes.POINTER(LL)]),
+        "cafe_sim_synchronize": (I, [P]),
+        "cafe_sim_info": (I, [P, ctypes.POINTER(CafeInfo)]),
+        "cafe_sim_stats": (I, [P, ctypes.POINTER(CafeStats)]),
+        "cafe_sim_download_state": (I, [P, i32p, i32p, f64p, f64p, i32p]),
+        "cafe_sim_download_temperature": (I, [P, f64p]),
+        "cafe_sim_download_ctheta": (I, [P, f64p, LL, ctypes.POINTER(I)]),
+        "cafe_sim_upload_state": (I, [P, i32p, i32p, f64p, f64p, f64p, I]),
+        "cafe_last_error": (ctypes.c_char_p, []),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+class CafeError(RuntimeError):
+    pass
+
+
+def check(rc):
+    if rc != 0:
+        msg = load().cafe_last_error()
+        raise CafeError("cafe error %d: %s" % (rc, msg.decode() if msg else ""))

@@ -1,0 +1,151 @@
+"""Python face of libcafe_gpu.so, mirroring AMCAFE's class interface.
+
+The reference's time loop (main1.C:18-101) reads
+
+    Grid g(file); Partition part(g); part.PartitionGraph2(); BasePlate bp(g, part);
+    TempField TempF(g, part, bp, ut); TempF.InitializeAnalytic();
+    VoxelsCA vox(g, TempF, part); vox.InitializeVoxels(bp);
+    vox.AddLayer1(); g.UpdateLaser();
+    while (!bcheck) { TempF.AnalyticTempCurr(...); vox.UpdateVoxels(); g.UpdateLaser();
+                      bcheck = g.indlayer > nlayerTot; if (g.inewlayerflg) vox.CleanLayer();
+                      g.UpdateTime2(TempF.DelT); if (g.inewlayerflg) vox.AddLayer1(); }
+    vox.CleanLayer();
+
+`Simulation(deck)` performs the constructors; the same calls exist as methods
+with the reference's names (InitializeVoxels, AddLayer1, UpdateLaser,
+AnalyticTempCurr, UpdateVoxels, CleanLayer, UpdateTime2) and as `step()` /
+`run()` for the loop body and the whole loop. The public fields (gID, vState,
+extents, centroidOct, TempCurr, BuildjID, cTheta, nGrain) are read with
+`state()`, `temperature()` and `ctheta()`.
+"""
+import ctypes
+
+import numpy as np
+
+from ._native import CafeInfo, CafeOptions, CafeStats, check, load
+
+
+def _ptr(a, ct):
+    return a.ctypes.data_as(ctypes.POINTER(ct)) if a is not None else None
+
+
+class Simulation:
+    def __init__(self, deck, device=0, active_capacity=0, grain_capacity=0):
+        self._lib = load()
+        self._h = ctypes.c_void_p()
+        opt = CafeOptions(device, active_capacity, grain_capacity)
+        check(self._lib.cafe_sim_create(str(deck).encode(), ctypes.byref(opt), ctypes.byref(self._h)))
+        inf = self.info()
+        self.shape = (inf["nz"], inf["ny"], inf["nx"])
+        self.ncell = inf["nx"] * inf["ny"] * inf["nz"]
+
+    # -- reference calls -------------------------------------------------
+    def InitializeVoxels(self):
+        check(self._lib.cafe_sim_initialize_voxels(self._h))
+
+    def AddLayer1(self):
+        check(self._lib.cafe_sim_add_layer(self._h))
+
+    def UpdateLaser(self):
+        check(self._lib.cafe_sim_update_laser(self._h))
+
+    def AnalyticTempCurr(self):
+        check(self._lib.cafe_sim_temperature(self._h))
+
+    def UpdateVoxels(self):
+        check(self._lib.cafe_sim_update_voxels(self._h))
+
+    def CleanLayer(self):
+        check(self._lib.cafe_sim_clean_layer(self._h))
+
+    def UpdateTime2(self):
+        check(self._lib.cafe_sim_update_time(self._h))
+
+    # -- loop helpers ----------------------------------------------------
+    def begin(self):
+        """InitializeVoxels() was called; AddLayer1() + first UpdateLaser() (main1.C:60-61)."""
+        check(self._lib.cafe_sim_begin(self._h))
+
+    def step(self):
+        done = ctypes.c_int(0)
+        check(self._lib.cafe_sim_step(self._h, ctypes.byref(done)))
+        return bool(done.value)
+
+    def run(self, max_steps=0):
+        n = ctypes.c_longlong(0)
+        check(self._lib.cafe_sim_run(self._h, int(max_steps), ctypes.byref(n)))
+        return n.value
+
+    def synchronize(self):
+        check(self._lib.cafe_sim_synchronize(self._h))
+
+    # -- state -------------------------------------------------------------
+    def info(self):
+        i = CafeInfo()
+        check(self._lib.cafe_sim_info(self._h, ctypes.byref(i)))
+        return {f: getattr(i, f) for f, _ in CafeInfo._fields_}
+
+    def stats(self):
+        s = CafeStats()
+        check(self._lib.cafe_sim_stats(self._h, ctypes.byref(s)))
+        return {f: getattr(s, f) for f, _ in CafeStats._fields_}
+
+    def state(self):
+        n = self.ncell
+        gid = np.empty(n, np.int32)
+        vs = np.empty(n, np.int32)
+        ext = np.empty(n, np.float64)
+        cen = np.empty(3 * n, np.float64)
+        bj = np.empty(n, np.int32)
+        check(self._lib.cafe_sim_download_state(self._h, _ptr(gid, ctypes.c_int32), _ptr(vs, ctypes.c_int32),
+                                                _ptr(ext, ctypes.c_double), _ptr(cen, ctypes.c_double),
+                                                _ptr(bj, ctypes.c_int32)))
+        return dict(gID=gid, vState=vs, extents=ext, centroid=cen, buildj=bj)
+
+    def temperature(self):
+        t = np.empty(self.ncell, np.float64)
+        check(self._lib.cafe_sim_download_temperature(self._h, _ptr(t, ctypes.c_double)))
+        return t
+
+    def ctheta(self):
+        ng = ctypes.c_int(0)
+        check(self._lib.cafe_sim_download_ctheta(self._h, None, 0, ctypes.byref(ng)))
+        out = np.empty(4 * max(ng.value, 1), np.float64)
+        check(self._lib.cafe_sim_download_ctheta(self._h, _ptr(out, ctypes.c_double), out.size, ctypes.byref(ng)))
+        return out[:4 * ng.value]
+
+    def upload_state(self, gID, vState, extents, centroid, ctheta):
+        gID = np.ascontiguousarray(gID, np.int32)
+        vState = np.ascontiguousarray(vState, np.int32)
+        extents = np.ascontiguousarray(extents, np.float64)
+        centroid = np.ascontiguousarray(centroid, np.float64)
+        ctheta = np.ascontiguousarray(ctheta, np.float64)
+        check(self._lib.cafe_sim_upload_state(self._h, _ptr(gID, ctypes.c_int32), _ptr(vState, ctypes.c_int32),
+                                              _ptr(extents, ctypes.c_double), _ptr(centroid, ctypes.c_double),
+                                              _ptr(ctheta, ctypes.c_double), len(ctheta) // 4))
+
+    def close(self):
+        if self._h:
+            self._lib.cafe_sim_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
+def run_deck(deck, max_steps=0, device=0, **kw):
+    """The whole main1.C time loop on one deck; returns the Simulation."""
+    sim = Simulation(deck, device=device, **kw)
+    sim.InitializeVoxels()
+    sim.begin()
+    sim.run(max_steps)
+    return sim

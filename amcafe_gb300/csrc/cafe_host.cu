@@ -1,0 +1,1109 @@
+// Host side of libcafe_gpu.so: the reference's Grid / BasePlate / TempField /
+// VoxelsCA objects for one realisation, with the voxel state on the device,
+// behind the C ABI of include/cafe_gpu.h.
+//
+// What stays on the host (cheap scalar state machines and the reference's
+// host-side random draws, which use libstdc++ <random> exactly as AMCAFE does):
+//   * the .in deck parser and derived values (Grid.C:15-109, 165-318),
+//   * the laser path and scan/layer state machine (Grid.C:110-164),
+//   * TempField scan order and ellipsoid parameters (TempField.C:16-77),
+//   * Poisson grain counts, Voronoi sites and orientations of the baseplate
+//     and of each powder layer (BasePlate.C:31-97, VoxelsCA.C:887-982).
+// Everything per voxel runs on the device (cafe_kernels.cu).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <limits>
+#include <numeric>
+#include <random>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "../../include/cafe_gpu.h"
+#include "cafe_kernels.cu"
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return code;
+}
+
+#define CUDA_TRY(call)                                                                      \
+  do {                                                                                      \
+    cudaError_t e_ = (call);                                                                \
+    if (e_ != cudaSuccess)                                                                  \
+      return fail(CAFE_E_CUDA, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), \
+                  __FILE__, __LINE__);                                                      \
+  } while (0)
+
+const int kSeed0 = 2132512, kSeed1 = 2912351;  // VoxelsCA.C:47-48
+
+// ------------------------------------------------------------------ Grid
+struct GridH {
+  int nX[3] = {128, 128, 64};
+  double dX[3] = {1e-6, 1e-6, 1e-6};
+  int outint = 1, patternID = 1, outNL = 0;
+  double tL = 1620, tS = 1531.5, T0 = 300, layerT = 25e-6, bpH = 0.0, mu = .01, lrate = 0;
+  double meltparam[4] = {75e-6, 162.75e-6, 75e-6, 75e-6};
+  double bhatch = 0, bmDelT = 0, bmV = 500e-3, bmP = 0, rNmax = .002;
+  double offset[3] = {0, 0, 0};
+  double gth0 = 0, gth = 0, Avel = 0, nvel = 0, gsize[2] = {0, 0};
+  bool set_bmdelt = false, set_lrate = false;
+  double LX[3];
+  int nZlayer = 0, Nzhg = 0, Ntd = 0, Nsd = 0, NpT = 0;
+  std::vector<double> lcoor, lcoor2;
+  double gbox[4];
+  int isp = 0, inewscanflg = 1, inewlayerflg = 1, indlayer = 1, ilaserLoc = 0, tInd = 0;
+  double time = 0.0;
+};
+
+// Grid::readInputFile (Grid.C:165-318): whitespace-separated keywords,
+// case-insensitive, '#' to end of line is a comment, the last character of
+// the file is read twice (so the file must end in whitespace).
+int parse_deck(const char *path, GridH &g) {
+  std::ifstream f(path);
+  if (!f) return fail(CAFE_E_IO, "cannot open deck '%s'", path);
+  std::string data;
+  char c = 0;
+  while (!f.eof()) {
+    f.get(c);
+    if (c == '#')
+      while (f && c != '\n') f.get(c);
+    data.push_back(c);
+  }
+  g.bhatch = 1.53 * g.meltparam[2];
+  std::istringstream in(data);
+  std::string kw;
+  auto num = [&](double &v) -> bool {
+    if (!(in >> kw)) return false;
+    char *end = nullptr;
+    v = std::strtod(kw.c_str(), &end);
+    return end != kw.c_str();
+  };
+  auto inum = [&](int &v) -> bool {
+    if (!(in >> kw)) return false;
+    char *end = nullptr;
+    long x = std::strtol(kw.c_str(), &end, 10);
+    v = (int)x;
+    return end != kw.c_str();
+  };
+  in >> kw;
+  while (in) {
+    std::string key = kw;
+    std::transform(key.begin(), key.end(), key.begin(), [](unsigned char s) { return (char)std::tolower(s); });
+    bool ok = true;
+    if (key == "dx") {
+      ok = num(g.dX[0]);
+      g.dX[1] = g.dX[2] = g.dX[0];
+    } else if (key == "bmv") ok = num(g.bmV);
+    else if (key == "bmp") ok = num(g.bmP);
+    else if (key == "bmdelt") { ok = num(g.bmDelT); g.set_bmdelt = true; }
+    else if (key == "nx") ok = inum(g.nX[0]) && inum(g.nX[1]) && inum(g.nX[2]);
+    else if (key == "r") ok = num(g.rNmax);
+    else if (key == "lt") ok = num(g.layerT);
+    else if (key == "tl") ok = num(g.tL);
+    else if (key == "ts") ok = num(g.tS);
+    else if (key == "bhatch") ok = num(g.bhatch);
+    else if (key == "mu") ok = num(g.mu);
+    else if (key == "bph") ok = num(g.bpH);
+    else if (key == "lrate") { ok = num(g.lrate); g.set_lrate = true; }
+    else if (key == "outnl") ok = inum(g.outNL);
+    else if (key == "ntsd") { int dummy; ok = inum(dummy); }
+    else if (key == "offset") ok = num(g.offset[0]) && num(g.offset[1]) && num(g.offset[2]);
+    else if (key == "meltparam")
+      ok = num(g.meltparam[0]) && num(g.meltparam[1]) && num(g.meltparam[2]) && num(g.meltparam[3]);
+    else if (key == "patternid") ok = inum(g.patternID);
+    else if (key == "outint") ok = inum(g.outint);
+    else if (key == "gridsize") ok = num(g.gsize[0]) && num(g.gsize[1]);
+    else if (key == "gridtheta") ok = num(g.gth0);
+    else if (key == "dendritegrowth2") ok = num(g.Avel) && num(g.nvel);
+    if (!ok) return fail(CAFE_E_ARG, "deck '%s': bad value after keyword '%s'", path, key.c_str());
+    in >> kw;
+  }
+  // Grid.C:57-58 reads an uninitialised bmV for the bmDelT default and lrate
+  // has no default: both must come from the deck.
+  if (!g.set_bmdelt) return fail(CAFE_E_ARG, "deck '%s' must set bmDelT", path);
+  if (!g.set_lrate) return fail(CAFE_E_ARG, "deck '%s' must set lrate", path);
+  for (int k = 0; k < 3; ++k)
+    if (g.nX[k] < 1) return fail(CAFE_E_ARG, "deck '%s': nX must be positive", path);
+  if (!(g.dX[0] > 0) || !(g.bmDelT > 0) || !(g.bmV > 0) || !(g.bhatch > 0))
+    return fail(CAFE_E_ARG, "deck '%s': dx, bmDelT, bmV and bhatch must be positive", path);
+  if ((long long)g.nX[0] * g.nX[1] * g.nX[2] > 2000000000LL)
+    return fail(CAFE_E_ARG, "deck '%s': more than 2e9 voxels", path);
+  return CAFE_OK;
+}
+
+void grid_laser_grid(GridH &g, bool init) {
+  double gmid0 = g.LX[0] / 2., gmid1 = g.LX[1] / 2.;
+  double xlmin = (g.LX[0] - g.gsize[0]) / 2., ylmin = (g.LX[1] - g.gsize[1]) / 2.;
+  g.gth += g.gth0;
+  for (int j2 = 0; j2 < g.Ntd; ++j2)
+    for (int j1 = 0; j1 < g.Nsd; ++j1) {
+      int k = g.Nsd * j2 + j1;
+      if (init) {
+        g.lcoor[2 * k] = j1 * g.bmDelT * g.bmV + xlmin;
+        g.lcoor[2 * k + 1] = j2 * g.bhatch + ylmin;
+      }
+      g.lcoor2[2 * k] = std::cos(g.gth) * (g.lcoor[2 * k] - gmid0) -
+                        std::sin(g.gth) * (g.lcoor[2 * k + 1] - gmid1) + gmid0;
+      g.lcoor2[2 * k + 1] = std::sin(g.gth) * (g.lcoor[2 * k] - gmid0) +
+                            std::cos(g.gth) * (g.lcoor[2 * k + 1] - gmid1) + gmid1;
+    }
+}
+
+// Grid constructor tail (Grid.C:69-108).
+int grid_derive(GridH &g) {
+  for (int k = 0; k < 3; ++k) g.LX[k] = g.nX[k] * g.dX[k];
+  if (g.bpH < std::numeric_limits<double>::epsilon()) g.bpH = g.layerT;
+  g.nZlayer = (int)std::round(g.layerT / g.dX[2]);
+  if (g.nZlayer < 1) return fail(CAFE_E_ARG, "layer thickness below one voxel");
+  g.Nzhg = std::min(g.nX[2], int(std::ceil(g.bpH * .9999 / g.dX[2])));
+  g.indlayer = 1;
+  g.ilaserLoc = g.Nzhg + g.indlayer * g.nZlayer;
+  double ntd = std::ceil(g.gsize[1] / g.bhatch) + 1, nsd = std::ceil(g.gsize[0] / (g.bmV * g.bmDelT)) + 1;
+  if (!(ntd * nsd < 2e9) || ntd < 1 || nsd < 1) return fail(CAFE_E_ARG, "laser grid too large");
+  g.Ntd = (int)ntd;
+  g.Nsd = (int)nsd;
+  g.NpT = g.Nsd * g.Ntd;
+  if (g.NpT < 2) return fail(CAFE_E_ARG, "laser grid has fewer than two points (set gridsize)");
+  g.lcoor.assign(2 * (size_t)g.NpT, 0.);
+  g.lcoor2.assign(2 * (size_t)g.NpT, 0.);
+  grid_laser_grid(g, true);
+  g.gbox[0] = -g.bhatch / 2.;
+  g.gbox[1] = g.LX[0] + g.bhatch / 2.;
+  g.gbox[2] = -g.bhatch / 2.;
+  g.gbox[3] = g.LX[1] + g.bhatch / 2.;
+  return CAFE_OK;
+}
+
+// Grid::UpdateLaser (Grid.C:110-164).
+void grid_update_laser(GridH &g) {
+  int itmp, iflg = 0, irep = 0;
+  if (std::fmod(g.isp + 1, g.Nsd) == 0) g.inewscanflg = 1;
+  if (g.isp == g.NpT - 1) {
+    g.inewscanflg = 1;
+    g.inewlayerflg = 1;
+    g.isp = 0;
+    g.indlayer += 1;
+  }
+  while (irep == 0 || g.isp == 0) {
+    irep += 1;
+    itmp = g.isp;
+    if (g.inewscanflg == 0 && itmp < g.NpT - 1) {
+      g.isp += 1;
+    } else {
+      while (itmp < g.NpT - 1 && iflg == 0) {
+        itmp += 1;
+        double x = g.lcoor2[2 * itmp], y = g.lcoor2[2 * itmp + 1];
+        if (x > g.gbox[0] && x < g.gbox[1] && y > g.gbox[2] && y < g.gbox[3]) iflg = 1;
+      }
+      if (itmp < g.NpT - 1) {
+        g.isp = itmp;
+        g.inewscanflg = 0;
+      } else {
+        g.inewlayerflg = 1;
+        g.inewscanflg = 1;
+        g.indlayer += 1;
+        g.ilaserLoc = g.Nzhg + g.indlayer * g.nZlayer;
+        g.isp = 0;
+        grid_laser_grid(g, false);
+      }
+    }
+  }
+  if (irep == 1) g.inewlayerflg = 0;
+}
+
+// ------------------------------------------------------------------ orientations (host)
+struct OrientConsts {
+  double R1, a, aprime, beta, s2, s2q, s6pi, spi, s24, coeffA[7];
+};
+OrientConsts orient_consts() {
+  // SampleOrientation::SampleOrientation (SampleOrientation.C:10-23) and the
+  // constant factors of ComputeMap2/3 (SampleOrientation.C:72-103).
+  OrientConsts k;
+  double r = 1;
+  k.R1 = std::pow(3.0 * M_PI / 4.0, 1.0 / 3.0) * r;
+  k.a = std::pow(2.0 * M_PI / 3.0, 1.0 / 2.0) * k.R1;
+  k.aprime = std::pow(4.0 * M_PI / 3.0, 1.0 / 3.0) * k.R1;
+  const double cA[7] = {-0.500009615, -0.024866061, -0.004549382, 0.000511867,
+                        -0.001650083, 0.000759335,  -0.000204042};
+  for (int j = 0; j < 7; ++j) k.coeffA[j] = cA[j];
+  k.beta = std::pow(M_PI / 6.0, 1.0 / 2.0);
+  k.s2 = std::pow(2.0, 1.0 / 2.0);
+  k.s2q = std::pow(2.0, 1.0 / 4.0);
+  k.s6pi = std::pow(6 / M_PI, 1.0 / 2.0);
+  k.spi = std::pow(M_PI, 1.0 / 2.0);
+  k.s24 = std::pow(24, 1.0 / 2.0);
+  return k;
+}
+
+// SampleOrientation::GenerateSamples (SampleOrientation.C:124-161) with the
+// host libm, for baseplate and powder-layer grains. As compiled, the
+// reference evaluates ComputeMap3's pair pow(q, 1/2) as a square root.
+void host_generate_samples(int n, unsigned int seedL, std::vector<double> &out) {
+  static const OrientConsts K = orient_consts();
+  std::uniform_real_distribution<double> xrand(0.0, 1.0);
+  std::default_random_engine g1(seedL);
+  out.assign(4 * (size_t)n, 0.0);
+  for (int jn = 0; jn < n; ++jn) {
+    double u0 = xrand(g1), u1 = xrand(g1), u2 = xrand(g1);
+    double xyz0[3] = {u0 - .5, u1 - .5, u2 - .5};
+    double xyz[3] = {K.aprime * xyz0[0], K.aprime * xyz0[1], K.aprime * xyz0[2]};
+    int P[3] = {1, 2, 3};
+    double x = xyz[0], y = xyz[1], z = xyz[2];
+    if ((std::fabs(x) <= z) && (std::fabs(y) <= z)) { P[0] = 1; P[1] = 2; P[2] = 3; }
+    if ((z <= -std::fabs(x)) && (z <= -std::fabs(y))) { P[0] = -1; P[1] = 2; P[2] = -3; }
+    if ((std::fabs(x) <= y) && (std::fabs(z) <= y)) { P[0] = 1; P[1] = -3; P[2] = 2; }
+    if ((y <= -std::fabs(x)) && (y <= -std::fabs(z))) { P[0] = 1; P[1] = 3; P[2] = -2; }
+    if ((std::fabs(z) < x) && (std::fabs(y) <= x)) { P[0] = -3; P[1] = 2; P[2] = 1; }
+    if ((x <= -std::fabs(z)) && (x <= -std::fabs(y))) { P[0] = 3; P[1] = 2; P[2] = -1; }
+    double xyz2[3], m1[3], m2[3], m3[3], xyzb[3];
+    for (int j = 0; j < 3; ++j) xyz2[j] = P[j] / std::abs(P[j]) * xyz[std::abs(P[j]) - 1];
+    for (int j = 0; j < 3; ++j) m1[j] = K.a / K.aprime * xyz2[j];
+    {
+      double x1 = m1[0], y1 = m1[1], T1 = 0, T2 = 0;
+      if (std::fabs(y1) <= std::fabs(x1)) {
+        if (std::fabs(x1) >= 1e-10) {
+          double cang = std::cos(y1 * M_PI / 12 / x1);
+          T1 = K.s2 * cang - 1;
+          T2 = K.s2 * std::sin(y1 * M_PI / 12 / x1);
+          double f = K.s2q * x1 / (K.beta * std::pow(K.s2 - cang, 1.0 / 2.0));
+          T1 *= f;
+          T2 *= f;
+        }
+      }
+      if (std::fabs(x1) <= std::fabs(y1)) {
+        if (std::fabs(y1) < 1e-10) {
+          T1 = 0.0;
+          T2 = 0.0;
+        } else {
+          double cang = std::cos(x1 * M_PI / 12 / y1);
+          T1 = K.s2 * std::sin(x1 * M_PI / 12 / y1);
+          T2 = K.s2 * cang - 1;
+          double f = K.s2q * y1 / (K.beta * std::pow(K.s2 - cang, 1.0 / 2.0));
+          T1 *= f;
+          T2 *= f;
+        }
+      }
+      m2[0] = T1;
+      m2[1] = T2;
+      m2[2] = m1[2];
+    }
+    {
+      double x2 = m2[0], y2 = m2[1], z2 = m2[2];
+      if (std::fabs(z2) < 1e-10) {
+        m3[0] = m3[1] = m3[2] = 0;
+      } else {
+        double q = 1 - (x2 * x2 + y2 * y2) * M_PI / (24 * (z2 * z2));
+        double sq = std::sqrt(q);
+        m3[0] = sq * x2;
+        m3[1] = sq * y2;
+        m3[2] = K.s6pi * z2 - (x2 * x2 + y2 * y2) * K.spi / (K.s24 * z2);
+      }
+    }
+    for (int j = 0; j < 3; ++j) xyzb[std::abs(P[j]) - 1] = P[j] / std::abs(P[j]) * m3[j];
+    double ax0 = std::fabs(xyz0[0]), ax1 = std::fabs(xyz0[1]), ax2 = std::fabs(xyz0[2]);
+    double pmax = (ax0 < ax1) ? ax1 : ax0;
+    pmax = (pmax < ax2) ? ax2 : pmax;
+    double rhoP = K.R1 * pmax / .5;
+    double t = 1;
+    for (int j = 1; j < 8; ++j) t += K.coeffA[j - 1] * std::pow(rhoP, 2.0 * j);
+    double omega = 2.0 * std::acos(t);
+    double tnorm = std::pow(xyzb[0] * xyzb[0] + xyzb[1] * xyzb[1] + xyzb[2] * xyzb[2], .5);
+    out[4 * (size_t)jn] = omega;
+    out[4 * (size_t)jn + 1] = xyzb[0] / tnorm;
+    out[4 * (size_t)jn + 2] = xyzb[1] / tnorm;
+    out[4 * (size_t)jn + 3] = xyzb[2] / tnorm;
+  }
+}
+
+// ------------------------------------------------------------------ device buffers
+template <class T>
+int dalloc(T **p, size_t n, std::vector<void *> &owned) {
+  *p = nullptr;
+  if (n == 0) n = 1;
+  CUDA_TRY(cudaMalloc((void **)p, n * sizeof(T)));
+  owned.push_back((void *)*p);
+  return CAFE_OK;
+}
+
+}  // namespace
+
+struct cafe_sim {
+  GridH g;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  // TempField
+  std::vector<int> ispvec;
+  double DelT = 0;
+  int tf_tInd = 0;
+  // BasePlate / VoxelsCA host state
+  int Nzh = 0, nlayerTot = 0, nGrain = 0;
+  std::default_random_engine bp_generator;  // BasePlate.h:28 (default seed)
+  std::default_random_engine genlayer;      // VoxelsCA.h:129
+  bool initialized = false, begun = false, done = false;
+  long long steps = 0;
+  // device
+  CafeConsts K;
+  CafeDev D;
+  CafeStepParams P;      // last temperature parameters
+  bool have_P = false;
+  std::vector<void *> owned;
+  int *h_pinned = nullptr;  // pinned host mirror of ctr + err
+  long long nblk = 0;       // dense compaction blocks
+  long long nblk_pos = 0;   // position compaction blocks
+  int nsm = 1;
+};
+
+namespace {
+
+int sim_sync(cafe_sim *s) {
+  CUDA_TRY(cudaStreamSynchronize(s->stream));
+  CUDA_TRY(cudaMemcpy(s->h_pinned, s->D.err, sizeof(int), cudaMemcpyDeviceToHost));
+  int err = s->h_pinned[0];
+  if (err) {
+    return fail(CAFE_E_CAPACITY,
+                "device capacity exceeded (flags 0x%x: 1 active list, 2 frontier rows, 4 grain "
+                "table, 8 mushy list, 16 event cap); recreate with larger capacities",
+                err);
+  }
+  return CAFE_OK;
+}
+
+int read_ctr(cafe_sim *s, int which, int *out) {
+  CUDA_TRY(cudaMemcpyAsync(s->h_pinned + 1, s->D.ctr + which, sizeof(int), cudaMemcpyDeviceToHost,
+                           s->stream));
+  CUDA_TRY(cudaStreamSynchronize(s->stream));
+  *out = s->h_pinned[1];
+  return CAFE_OK;
+}
+
+int grow_grains(cafe_sim *s, long long need) {
+  if (need <= s->D.grain_cap) return CAFE_OK;
+  long long cap = std::max<long long>(need * 2, (long long)s->D.grain_cap * 2);
+  double *cth = nullptr, *rot = nullptr;
+  CUDA_TRY(cudaMalloc((void **)&cth, cap * 4 * sizeof(double)));
+  CUDA_TRY(cudaMalloc((void **)&rot, cap * 9 * sizeof(double)));
+  CUDA_TRY(cudaMemcpyAsync(cth, s->D.cth, (size_t)s->D.grain_cap * 4 * sizeof(double),
+                           cudaMemcpyDeviceToDevice, s->stream));
+  CUDA_TRY(cudaMemcpyAsync(rot, s->D.rot, (size_t)s->D.grain_cap * 9 * sizeof(double),
+                           cudaMemcpyDeviceToDevice, s->stream));
+  CUDA_TRY(cudaStreamSynchronize(s->stream));
+  for (auto &p : s->owned) {
+    if (p == (void *)s->D.cth) { cudaFree(p); p = (void *)cth; }
+    else if (p == (void *)s->D.rot) { cudaFree(p); p = (void *)rot; }
+  }
+  s->D.cth = cth;
+  s->D.rot = rot;
+  s->D.grain_cap = (int)std::min<long long>(cap, 2000000000LL);
+  return CAFE_OK;
+}
+
+// Bucket grid over Voronoi sites (CSR, ascending site index in each bucket).
+struct HostSiteGrid {
+  std::vector<int32_t> start, idx;
+  double lo[3], h;
+  int nb[3];
+};
+void build_site_grid(HostSiteGrid &G, const std::vector<double> &xyz, const double lo[3],
+                     const double hi[3]) {
+  int n = (int)(xyz.size() / 3);
+  double vol = 1.0;
+  for (int a = 0; a < 3; ++a) vol *= std::max(hi[a] - lo[a], 1e-300);
+  G.h = std::cbrt(vol / std::max(1, n)) * 1.5;
+  for (int a = 0; a < 3; ++a) {
+    G.lo[a] = lo[a];
+    G.nb[a] = std::max(1, std::min(512, (int)std::ceil((hi[a] - lo[a]) / G.h)));
+  }
+  // enlarge h if the bucket count per axis was clipped
+  for (int a = 0; a < 3; ++a) G.h = std::max(G.h, (hi[a] - lo[a]) / G.nb[a] * (1 + 1e-12));
+  size_t nbt = (size_t)G.nb[0] * G.nb[1] * G.nb[2];
+  std::vector<int32_t> cnt(nbt + 1, 0), cell(n);
+  for (int i = 0; i < n; ++i) {
+    int b[3];
+    for (int a = 0; a < 3; ++a) {
+      double f = std::floor((xyz[3 * (size_t)i + a] - G.lo[a]) / G.h);
+      b[a] = f < 0 ? 0 : (f > G.nb[a] - 1 ? G.nb[a] - 1 : (int)f);
+    }
+    cell[i] = (b[2] * G.nb[1] + b[1]) * G.nb[0] + b[0];
+    cnt[cell[i] + 1]++;
+  }
+  for (size_t b = 0; b < nbt; ++b) cnt[b + 1] += cnt[b];
+  G.start = cnt;
+  G.idx.assign(n, 0);
+  std::vector<int32_t> fill(cnt.begin(), cnt.end() - 1);
+  for (int i = 0; i < n; ++i) G.idx[fill[cell[i]]++] = i;
+}
+
+// Uploads sites + grid; returns the device view. Buffers are freed by the caller.
+int upload_site_grid(cafe_sim *s, const std::vector<double> &xyz, const HostSiteGrid &G,
+                     CafeSiteGrid &dv, std::vector<void *> &tmp) {
+  double *dxyz;
+  int32_t *dstart, *didx;
+  CUDA_TRY(cudaMalloc((void **)&dxyz, std::max<size_t>(1, xyz.size()) * sizeof(double)));
+  tmp.push_back(dxyz);
+  CUDA_TRY(cudaMalloc((void **)&dstart, G.start.size() * sizeof(int32_t)));
+  tmp.push_back(dstart);
+  CUDA_TRY(cudaMalloc((void **)&didx, std::max<size_t>(1, G.idx.size()) * sizeof(int32_t)));
+  tmp.push_back(didx);
+  CUDA_TRY(cudaMemcpyAsync(dxyz, xyz.data(), xyz.size() * sizeof(double), cudaMemcpyHostToDevice, s->stream));
+  CUDA_TRY(cudaMemcpyAsync(dstart, G.start.data(), G.start.size() * sizeof(int32_t), cudaMemcpyHostToDevice, s->stream));
+  CUDA_TRY(cudaMemcpyAsync(didx, G.idx.data(), G.idx.size() * sizeof(int32_t), cudaMemcpyHostToDevice, s->stream));
+  dv.xyz = dxyz;
+  dv.start = dstart;
+  dv.idx = didx;
+  for (int a = 0; a < 3; ++a) {
+    dv.lo[a] = G.lo[a];
+    dv.nb[a] = G.nb[a];
+  }
+  dv.h = G.h;
+  return CAFE_OK;
+}
+
+void free_tmp(cafe_sim *s, std::vector<void *> &tmp) {
+  cudaStreamSynchronize(s->stream);
+  for (void *p : tmp) cudaFree(p);
+  tmp.clear();
+}
+
+int grid_blocks(long long work, int threads, cafe_sim *s) {
+  long long b = (work + threads - 1) / threads;
+  long long cap = (long long)s->nsm * 16;
+  if (b > cap) b = cap;
+  if (b < 1) b = 1;
+  return (int)b;
+}
+
+// Per-step temperature parameters (TempField.C:145-171) and the cell box
+// outside which no cell can reach the liquidus.
+void make_step_params(cafe_sim *s, CafeStepParams &P) {
+  GridH &g = s->g;
+  const int *isv = s->ispvec.data();
+  P.lx = g.lcoor[2 * isv[g.isp]] - g.offset[0];
+  P.ly = g.lcoor[2 * isv[g.isp] + 1] - g.offset[1];
+  P.lz = g.ilaserLoc * g.dX[2] - g.offset[2];
+  P.cg = std::cos(g.gth);
+  P.sg = std::sin(g.gth);
+  if (std::fmod(g.isp, g.Nsd) == 0)
+    P.dirp = (g.lcoor[2 * isv[g.isp + 1]] - g.lcoor[2 * isv[g.isp]]);
+  else
+    P.dirp = (g.lcoor[2 * isv[g.isp]] - g.lcoor[2 * isv[g.isp - 1]]);
+  P.ilaserLoc = g.ilaserLoc;
+  P.tInd = g.tInd;
+  const CafeConsts &K = s->K;
+  P.any_hot_full = !(K.tS < K.tL) || !(K.T0 < K.tL);
+  // half extents of the hot region in the laser frame, with a relative margin
+  double A = std::max(K.bmDX0, K.a1[3]) * (1 + 1e-9);
+  double B = std::max(K.a1[1], K.a1[4]) * (1 + 1e-9);
+  double C = std::max(K.a1[2], K.a1[5]) * (1 + 1e-9);
+  double c = std::fabs(P.cg), sn = std::fabs(P.sg);
+  double hx = c * A + sn * B, hy = sn * A + c * B;
+  // pool centre in the voxel frame: inverse rotation of the laser position
+  double u = P.lx - K.hLX0, w = P.ly - K.hLX1;
+  double X = P.cg * u - P.sg * w + K.hLX0, Y = P.sg * u + P.cg * w + K.hLX1;
+  double lo[3] = {X - hx, Y - hy, P.lz - C}, hi[3] = {X + hx, Y + hy, P.lz + C};
+  int nmax[3] = {g.nX[0], g.nX[1], g.nX[2]};
+  for (int a = 0; a < 3; ++a) {
+    double l = std::floor(lo[a] / g.dX[a] - 0.5) - 2, h = std::ceil(hi[a] / g.dX[a] - 0.5) + 3;
+    if (!(l == l) || !(h == h)) { l = 0; h = nmax[a]; }
+    l = std::max(0.0, std::min((double)nmax[a], l));
+    h = std::max(0.0, std::min((double)nmax[a], h));
+    P.lo[a] = (int)l;
+    P.hi[a] = std::max((int)h, (int)l);
+  }
+  if (P.any_hot_full) {
+    for (int a = 0; a < 3; ++a) {
+      P.lo[a] = 0;
+      P.hi[a] = nmax[a];
+    }
+  }
+}
+
+}  // namespace
+
+// ====================================================================== C ABI
+extern "C" {
+
+const char *cafe_last_error(void) { return g_last_error.c_str(); }
+
+int cafe_sim_create(const char *deck_path, const cafe_options *opt, cafe_sim **out) {
+  if (!deck_path || !out) return fail(CAFE_E_ARG, "null argument");
+  *out = nullptr;
+  cafe_sim *s = new cafe_sim();
+  int rc = parse_deck(deck_path, s->g);
+  if (!rc) rc = grid_derive(s->g);
+  if (rc) {
+    delete s;
+    return rc;
+  }
+  GridH &g = s->g;
+  s->device = opt ? opt->device : 0;
+  cudaError_t ce = cudaSetDevice(s->device);
+  if (ce != cudaSuccess) {
+    delete s;
+    return fail(CAFE_E_CUDA, "cudaSetDevice(%d): %s", opt ? opt->device : 0, cudaGetErrorString(ce));
+  }
+  cudaDeviceGetAttribute(&s->nsm, cudaDevAttrMultiProcessorCount, s->device);
+  if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete s;
+    return fail(CAFE_E_CUDA, "cudaStreamCreate failed");
+  }
+  // TempField (TempField.C:26-50)
+  s->DelT = g.bmDelT;
+  s->ispvec.assign(g.NpT, 0);
+  if (g.patternID == 1 || g.patternID == 3) std::iota(s->ispvec.begin(), s->ispvec.end(), 0);
+  if (g.patternID == 2 || g.patternID == 4) {
+    for (int j = 0; j < g.Ntd; ++j) {
+      int k = g.Nsd * j;
+      if (std::fmod(j, 2) == 0)
+        std::iota(s->ispvec.begin() + k, s->ispvec.begin() + k + g.Nsd, k);
+      else
+        for (int j1 = 0; j1 < g.Nsd; ++j1) s->ispvec[k + j1] = k + g.Nsd - 1 - j1;
+    }
+  }
+  // BasePlate (BasePlate.C:20-30), main1.C:59
+  s->Nzh = std::min(g.nX[2], int(std::ceil(g.bpH * .9999 / g.dX[2])));
+  s->nlayerTot = int(std::ceil((double)(g.nX[2] - s->Nzh) / (double)g.nZlayer));
+  s->genlayer.seed(kSeed1);
+  // constants
+  CafeConsts &K = s->K;
+  K.nx = g.nX[0];
+  K.ny = g.nX[1];
+  K.nz = g.nX[2];
+  K.nxy = K.nx * K.ny;
+  K.N = (long long)K.nxy * K.nz;
+  for (int a = 0; a < 3; ++a) K.dx[a] = g.dX[a];
+  K.hLX0 = g.LX[0] / 2.;
+  K.hLX1 = g.LX[1] / 2.;
+  K.a1[0] = g.meltparam[0];
+  K.a1[1] = g.meltparam[2];
+  K.a1[2] = g.meltparam[3];
+  K.a1[3] = g.meltparam[1];
+  K.a1[4] = K.a1[1];
+  K.a1[5] = K.a1[2];
+  K.bmDX0 = s->DelT * g.bmV;
+  K.tL = g.tL;
+  K.tS = g.tS;
+  K.T0 = g.T0;
+  K.xi = g.tL * (1 + std::numeric_limits<double>::epsilon());
+  K.Tcls[0] = g.T0;
+  K.Tcls[1] = g.tS;
+  K.Tcls[2] = K.xi;
+  for (int c = 0; c < 3; ++c) {
+    double T = K.Tcls[c];
+    K.hot_cls[c] = T >= g.tL;
+    K.gt_cls[c] = T > g.tL;
+    K.vhat_cls[c] = T >= g.tL ? 0.0 : g.Avel * std::pow(g.tL - T, g.nvel);
+  }
+  K.rX = g.rNmax * std::pow(g.dX[0] * 1e6, 3.);
+  K.DelT = s->DelT;
+  K.ruq_dx = g.dX[0];
+  K.seed0 = (unsigned int)kSeed0;
+  K.seed1 = (unsigned int)kSeed1;
+  OrientConsts oc = orient_consts();
+  K.so_R1 = oc.R1;
+  K.so_a = oc.a;
+  K.so_aprime = oc.aprime;
+  K.so_beta = oc.beta;
+  K.so_s2 = oc.s2;
+  K.so_s2q = oc.s2q;
+  K.so_s6pi = oc.s6pi;
+  K.so_spi = oc.spi;
+  K.so_s24 = oc.s24;
+  for (int j = 0; j < 7; ++j) K.so_coeffA[j] = oc.coeffA[j];
+  K.s3 = std::pow(3.0, .5);
+  K.s23 = std::pow(2.0 / 3.0, .5);
+  // device buffers
+  CafeDev &D = s->D;
+  std::memset(&D, 0, sizeof D);
+  long long N = K.N;
+  long long acap = opt && opt->active_capacity > 0 ? opt->active_capacity
+                                                   : std::min<long long>(N, std::max<long long>(1 << 20, N / 4));
+  acap = std::min<long long>(acap, N);
+  D.act_cap = acap;
+  D.vs2_cap = acap;
+  D.row_cap = acap;
+  double est = g.mu * (g.dX[0] * 1e6) * (g.dX[1] * 1e6) * g.nX[0] * g.nX[1] * (s->Nzh * g.dX[2] * 1e6) +
+               (s->nlayerTot + 1) * g.lrate * (g.dX[0] * 1e6) * (g.dX[1] * 1e6) * g.nX[0] * g.nX[1] * (g.layerT * 1e6);
+  long long gcap = opt && opt->grain_capacity > 0 ? opt->grain_capacity : (long long)(2 * est) + (1 << 16);
+  D.grain_cap = (int)std::min<long long>(gcap, 2000000000LL);
+  s->nblk = (N + CAFE_CELLS_PER_BLOCK - 1) / CAFE_CELLS_PER_BLOCK;
+  s->nblk_pos = (acap + CAFE_CELLS_PER_BLOCK - 1) / CAFE_CELLS_PER_BLOCK;
+  D.blk_cap = std::max(s->nblk, 2 * s->nblk_pos);
+  auto &o = s->owned;
+  if ((rc = dalloc(&D.state, N, o)) || (rc = dalloc(&D.gid, N, o)) || (rc = dalloc(&D.ext, N, o)) ||
+      (rc = dalloc(&D.cx, N, o)) || (rc = dalloc(&D.cy, N, o)) || (rc = dalloc(&D.cz, N, o)) ||
+      (rc = dalloc(&D.buildj, N, o)) || (rc = dalloc(&D.pos_of, N, o)) ||
+      (rc = dalloc(&D.cth, 4 * (size_t)D.grain_cap, o)) || (rc = dalloc(&D.rot, 9 * (size_t)D.grain_cap, o)) ||
+      (rc = dalloc(&D.act, acap, o)) || (rc = dalloc(&D.a_state, acap, o)) || (rc = dalloc(&D.a_cls, acap, o)) ||
+      (rc = dalloc(&D.a_nn, acap, o)) || (rc = dalloc(&D.a_cold, acap, o)) || (rc = dalloc(&D.a_gid, acap, o)) ||
+      (rc = dalloc(&D.a_liq, acap, o)) || (rc = dalloc(&D.a_frow, acap, o)) ||
+      (rc = dalloc(&D.a_nbr, (size_t)acap * CAFE_NSLOT, o)) || (rc = dalloc(&D.a_ext, acap, o)) ||
+      (rc = dalloc(&D.a_cx, acap, o)) || (rc = dalloc(&D.a_cy, acap, o)) || (rc = dalloc(&D.a_cz, acap, o)) ||
+      (rc = dalloc(&D.a_ruq, acap, o)) || (rc = dalloc(&D.vs2, acap, o)) || (rc = dalloc(&D.row_pos, acap, o)) ||
+      (rc = dalloc(&D.row_j, acap, o)) || (rc = dalloc(&D.row_alive, acap, o)) ||
+      (rc = dalloc(&D.row_ord, (size_t)acap * CAFE_NSLOT, o)) || (rc = dalloc(&D.row_live, acap, o)) ||
+      (rc = dalloc(&D.row_g, (size_t)acap * CAFE_NSLOT, o)) || (rc = dalloc(&D.blk, D.blk_cap, o)) ||
+      (rc = dalloc(&D.ctr, CTR_COUNT, o)) || (rc = dalloc(&D.err, 1, o)) || (rc = dalloc(&D.stat, STAT_COUNT, o))) {
+    cafe_sim_destroy(s);
+    return rc;
+  }
+  if (cudaMallocHost((void **)&s->h_pinned, 16 * sizeof(int)) != cudaSuccess) {
+    cafe_sim_destroy(s);
+    return fail(CAFE_E_CUDA, "cudaMallocHost failed");
+  }
+  cudaMemsetAsync(D.state, 0, N, s->stream);
+  cudaMemsetAsync(D.gid, 0, N * sizeof(int32_t), s->stream);
+  cudaMemsetAsync(D.ext, 0, N * sizeof(double), s->stream);
+  cudaMemsetAsync(D.cx, 0, N * sizeof(double), s->stream);
+  cudaMemsetAsync(D.cy, 0, N * sizeof(double), s->stream);
+  cudaMemsetAsync(D.cz, 0, N * sizeof(double), s->stream);
+  cudaMemsetAsync(D.buildj, 0, N, s->stream);
+  cudaMemsetAsync(D.pos_of, 0xff, N * sizeof(int32_t), s->stream);
+  cudaMemsetAsync(D.ctr, 0, CTR_COUNT * sizeof(int), s->stream);
+  cudaMemsetAsync(D.err, 0, sizeof(int), s->stream);
+  cudaMemsetAsync(D.stat, 0, STAT_COUNT * sizeof(unsigned long long), s->stream);
+  ce = cudaStreamSynchronize(s->stream);
+  if (ce != cudaSuccess) {
+    cafe_sim_destroy(s);
+    return fail(CAFE_E_CUDA, "device initialisation: %s", cudaGetErrorString(ce));
+  }
+  *out = s;
+  return CAFE_OK;
+}
+
+void cafe_sim_destroy(cafe_sim *s) {
+  if (!s) return;
+  cudaSetDevice(s->device);
+  if (s->stream) cudaStreamSynchronize(s->stream);
+  for (void *p : s->owned) cudaFree(p);
+  if (s->h_pinned) cudaFreeHost(s->h_pinned);
+  if (s->stream) cudaStreamDestroy(s->stream);
+  delete s;
+}
+
+int cafe_sim_initialize_voxels(cafe_sim *s) {
+  if (!s) return fail(CAFE_E_ARG, "null handle");
+  if (s->initialized) return fail(CAFE_E_STATE, "initialize_voxels called twice");
+  CUDA_TRY(cudaSetDevice(s->device));
+  GridH &g = s->g;
+  const CafeConsts &K = s->K;
+  // BasePlate::GenerateNgrain / GenerateVoxel (BasePlate.C:31-53)
+  double height = s->Nzh * (g.dX[2]);
+  double rate = g.mu * (g.dX[0] * 1e6) * (g.dX[1] * 1e6) * g.nX[0] * g.nX[1] * (height * 1e6);
+  if (!(rate > 0)) return fail(CAFE_E_ARG, "baseplate grain rate must be positive (mu, bpH)");
+  std::poisson_distribution<int> ng(rate);
+  int Ngrain = 0;
+  while (Ngrain == 0) Ngrain = ng(s->bp_generator);
+  std::vector<double> xs(3 * (size_t)Ngrain);
+  std::uniform_real_distribution<double> xrand(0.0, 1.0);
+  double Lx = g.dX[0] * g.nX[0], Ly = g.dX[1] * g.nX[1];
+  for (int j = 0; j < Ngrain; ++j) {
+    xs[3 * (size_t)j] = xrand(s->bp_generator) * Lx;
+    xs[3 * (size_t)j + 1] = xrand(s->bp_generator) * Ly;
+    xs[3 * (size_t)j + 2] = xrand(s->bp_generator) * height;
+  }
+  int rc = grow_grains(s, (long long)Ngrain + 1);
+  if (rc) return rc;
+  HostSiteGrid G;
+  double lo[3] = {0, 0, 0}, hi[3] = {Lx, Ly, std::max(height, g.dX[2])};
+  build_site_grid(G, xs, lo, hi);
+  std::vector<void *> tmp;
+  CafeSiteGrid dv;
+  if ((rc = upload_site_grid(s, xs, G, dv, tmp))) return rc;
+  long long nbp = (long long)s->Nzh * K.nxy;
+  if (nbp > 0) k_baseplate<<<grid_blocks(nbp, 256, s), 256, 0, s->stream>>>(s->D, K, dv, s->Nzh);
+  CUDA_TRY(cudaGetLastError());
+  // orientations (BasePlate.C:83-96)
+  std::default_random_engine g1(531231);
+  unsigned int sdloc = unsigned(double(g1()) / double(g1.max()) * std::pow(2.0, 32.0));
+  std::vector<double> aa;
+  host_generate_samples(Ngrain, sdloc, aa);
+  CUDA_TRY(cudaMemcpyAsync(s->D.cth, aa.data(), aa.size() * sizeof(double), cudaMemcpyHostToDevice, s->stream));
+  k_rot_range<<<grid_blocks(Ngrain, 128, s), 128, 0, s->stream>>>(s->D, 0, Ngrain);
+  CUDA_TRY(cudaGetLastError());
+  s->nGrain = Ngrain;
+  s->h_pinned[2] = Ngrain;
+  CUDA_TRY(cudaMemcpyAsync(s->D.ctr + CTR_NGRAIN, s->h_pinned + 2, sizeof(int), cudaMemcpyHostToDevice, s->stream));
+  free_tmp(s, tmp);
+  s->initialized = true;
+  return sim_sync(s);
+}
+
+int cafe_sim_add_layer(cafe_sim *s) {
+  if (!s || !s->initialized) return fail(CAFE_E_STATE, "add_layer before initialize_voxels");
+  CUDA_TRY(cudaSetDevice(s->device));
+  GridH &g = s->g;
+  const CafeConsts &K = s->K;
+  int rc = read_ctr(s, CTR_NGRAIN, &s->nGrain);
+  if (rc) return rc;
+  // VoxelsCA.C:898-917
+  unsigned int sdloc = unsigned(double(s->genlayer()) / double(s->genlayer.max()) * std::pow(2.0, 32.0));
+  double rate = g.lrate * (g.dX[0] * 1e6) * (g.dX[1] * 1e6) * g.nX[0] * g.nX[1] * (g.layerT * 1e6);
+  if (!(rate > 0)) return fail(CAFE_E_ARG, "layer grain rate must be positive (lrate, lT)");
+  std::poisson_distribution<int> ng(rate);
+  int ng2 = 0;
+  while (ng2 == 0) ng2 = ng(s->genlayer);
+  int iz1 = g.ilaserLoc - g.nZlayer;
+  double zloc0 = iz1 * g.dX[2];
+  std::vector<double> xs(3 * (size_t)ng2);
+  std::uniform_real_distribution<double> xrand(0.0, 1.0);
+  double Lx = g.nX[0] * g.dX[0], Ly = g.nX[1] * g.dX[1];
+  for (int j = 0; j < ng2; ++j) {
+    xs[3 * (size_t)j] = xrand(s->genlayer) * Lx;
+    xs[3 * (size_t)j + 1] = xrand(s->genlayer) * Ly;
+    xs[3 * (size_t)j + 2] = xrand(s->genlayer) * g.layerT + zloc0;
+  }
+  HostSiteGrid G;
+  double lo[3] = {0, 0, zloc0}, hi[3] = {Lx, Ly, zloc0 + std::max(g.layerT, g.dX[2])};
+  build_site_grid(G, xs, lo, hi);
+  std::vector<void *> tmp;
+  CafeSiteGrid dv;
+  if ((rc = upload_site_grid(s, xs, G, dv, tmp))) return rc;
+  long long nslab = (long long)K.nxy * g.nZlayer;
+  int32_t *gtmp, *used, *map;
+  CUDA_TRY(cudaMalloc((void **)&gtmp, std::max<long long>(1, nslab) * sizeof(int32_t)));
+  tmp.push_back(gtmp);
+  CUDA_TRY(cudaMalloc((void **)&used, ng2 * sizeof(int32_t)));
+  tmp.push_back(used);
+  CUDA_TRY(cudaMalloc((void **)&map, ng2 * sizeof(int32_t)));
+  tmp.push_back(map);
+  CUDA_TRY(cudaMemsetAsync(used, 0, ng2 * sizeof(int32_t), s->stream));
+  if (nslab > 0)
+    k_layer_voronoi<<<grid_blocks(nslab, 256, s), 256, 0, s->stream>>>(K, dv, iz1, g.ilaserLoc, gtmp, used);
+  CUDA_TRY(cudaGetLastError());
+  std::vector<int32_t> hu(ng2), hm(ng2, 0);
+  CUDA_TRY(cudaMemcpyAsync(hu.data(), used, ng2 * sizeof(int32_t), cudaMemcpyDeviceToHost, s->stream));
+  CUDA_TRY(cudaStreamSynchronize(s->stream));
+  // contiguous renumbering of the used sites (VoxelsCA.C:938-951)
+  int i2 = 0;
+  for (int j = 0; j < ng2; ++j)
+    if (hu[j]) hm[j] = i2++;
+  if (i2 == ng2)
+    for (int j = 0; j < ng2; ++j) hm[j] = j;
+  CUDA_TRY(cudaMemcpyAsync(map, hm.data(), ng2 * sizeof(int32_t), cudaMemcpyHostToDevice, s->stream));
+  k_layer_apply<<<grid_blocks(K.N, 256, s), 256, 0, s->stream>>>(s->D, K, iz1, g.ilaserLoc, gtmp, map, s->nGrain);
+  CUDA_TRY(cudaGetLastError());
+  int n0 = s->nGrain;
+  s->nGrain += i2 + 1;
+  if ((rc = grow_grains(s, s->nGrain + 1))) return rc;
+  std::vector<double> aa;
+  host_generate_samples(i2 + 1, sdloc, aa);
+  CUDA_TRY(cudaMemcpyAsync(s->D.cth + 4LL * n0, aa.data(), aa.size() * sizeof(double), cudaMemcpyHostToDevice, s->stream));
+  k_rot_range<<<grid_blocks(i2 + 1, 128, s), 128, 0, s->stream>>>(s->D, n0, s->nGrain);
+  CUDA_TRY(cudaGetLastError());
+  s->h_pinned[2] = s->nGrain;
+  CUDA_TRY(cudaMemcpyAsync(s->D.ctr + CTR_NGRAIN, s->h_pinned + 2, sizeof(int), cudaMemcpyHostToDevice, s->stream));
+  free_tmp(s, tmp);
+  return sim_sync(s);
+}
+
+int cafe_sim_update_laser(cafe_sim *s) {
+  if (!s) return fail(CAFE_E_ARG, "null handle");
+  grid_update_laser(s->g);
+  return CAFE_OK;
+}
+
+int cafe_sim_temperature(cafe_sim *s) {
+  if (!s || !s->initialized) return fail(CAFE_E_STATE, "temperature before initialize_voxels");
+  CUDA_TRY(cudaSetDevice(s->device));
+  GridH &g = s->g;
+  s->tf_tInd = int(std::round(g.time / s->DelT));
+  if (g.isp < 0 || g.isp >= g.NpT || (std::fmod(g.isp, g.Nsd) == 0 && g.isp + 1 >= g.NpT) ||
+      (std::fmod(g.isp, g.Nsd) != 0 && g.isp < 1))
+    return fail(CAFE_E_STATE, "laser index %d outside the scan grid", g.isp);
+  make_step_params(s, s->P);
+  s->have_P = true;
+  const CafeStepParams &P = s->P;
+  CUDA_TRY(cudaMemsetAsync(s->D.ctr + CTR_HOT, 0, sizeof(int), s->stream));
+  long long nbox = (long long)(P.hi[0] - P.lo[0]) * (P.hi[1] - P.lo[1]) * (P.hi[2] - P.lo[2]);
+  if (nbox > 0) k_melt<<<grid_blocks(nbox, 256, s), 256, 0, s->stream>>>(s->D, s->K, P);
+  CUDA_TRY(cudaGetLastError());
+  // end-of-scan check (TempField.C:199-216), only when the laser is outside the grid box
+  const int *isv = s->ispvec.data();
+  double x = g.lcoor2[2 * isv[g.isp]] - g.offset[0];
+  double y = g.lcoor2[2 * isv[g.isp] + 1] - g.offset[1];
+  if (x < g.gbox[0] || x > g.gbox[1] || y < g.gbox[2] || y > g.gbox[3]) {
+    int hot = 0;
+    int rc = read_ctr(s, CTR_HOT, &hot);
+    if (rc) return rc;
+    if (hot == 0 || std::fmod(g.isp + 1, g.Nsd) == 0) g.inewscanflg = 1;
+    if (g.isp == g.NpT - 1) {
+      g.inewscanflg = 1;
+      g.inewlayerflg = 1;
+      g.isp = 0;
+      g.indlayer += 1;
+    }
+  }
+  return CAFE_OK;
+}
+
+int cafe_sim_update_voxels(cafe_sim *s) {
+  if (!s || !s->have_P) return fail(CAFE_E_STATE, "update_voxels before temperature");
+  CUDA_TRY(cudaSetDevice(s->device));
+  CafeDev &D = s->D;
+  const CafeConsts &K = s->K;
+  const CafeStepParams &P = s->P;
+  cudaStream_t st = s->stream;
+  int nb = (int)s->nblk;
+  k_solid2mushy<<<nb, CAFE_DENSE_THREADS, 0, st>>>(D, K);
+  k_active_count<<<nb, CAFE_DENSE_THREADS, 0, st>>>(D, K, P);
+  k_scan_blocks<<<1, 1024, 0, st>>>(D.blk, s->nblk, D.ctr + CTR_NA);
+  k_active_scatter<<<nb, CAFE_DENSE_THREADS, 0, st>>>(D, K, P);
+  int gb = s->nsm * 8;
+  k_gather<<<gb, 256, 0, st>>>(D, K, P);
+  int nbp = (int)s->nblk_pos;
+  k_lists_count<<<nbp, CAFE_DENSE_THREADS, 0, st>>>(D);
+  k_scan_pairs<<<1, 1024, 0, st>>>(D.blk, s->nblk_pos, D.ctr + CTR_NVS2, D.ctr + CTR_NROWS);
+  k_lists_scatter<<<nbp, CAFE_DENSE_THREADS, 0, st>>>(D);
+  k_rows_init<<<s->nsm * 4, 256, 0, st>>>(D, K);
+  k_event_loop<<<1, CAFE_LOOP_THREADS, 0, st>>>(D, K, P, D.act_cap + 1);
+  k_writeback<<<gb, 256, 0, st>>>(D);
+  k_mushy2solid<<<gb, 256, 0, st>>>(D, K);
+  CUDA_TRY(cudaGetLastError());
+  return CAFE_OK;
+}
+
+int cafe_sim_clean_layer(cafe_sim *s) {
+  if (!s || !s->initialized) return fail(CAFE_E_STATE, "clean_layer before initialize_voxels");
+  CUDA_TRY(cudaSetDevice(s->device));
+  int rc = read_ctr(s, CTR_NGRAIN, &s->nGrain);
+  if (rc) return rc;
+  int ng = s->nGrain;
+  int32_t *cnt, *newid;
+  double *cth2, *rot2;
+  std::vector<void *> tmp;
+  CUDA_TRY(cudaMalloc((void **)&cnt, std::max(1, ng) * sizeof(int32_t)));
+  tmp.push_back(cnt);
+  CUDA_TRY(cudaMalloc((void **)&newid, std::max(1, ng) * sizeof(int32_t)));
+  tmp.push_back(newid);
+  CUDA_TRY(cudaMalloc((void **)&cth2, (size_t)s->D.grain_cap * 4 * sizeof(double)));
+  CUDA_TRY(cudaMalloc((void **)&rot2, (size_t)s->D.grain_cap * 9 * sizeof(double)));
+  CUDA_TRY(cudaMemsetAsync(cnt, 0, std::max(1, ng) * sizeof(int32_t), s->stream));
+  k_grain_count<<<grid_blocks(s->K.N, 256, s), 256, 0, s->stream>>>(s->D, s->K, cnt);
+  k_grain_renumber<<<1, 1024, 0, s->stream>>>(s->D, cnt, newid, cth2, rot2);
+  k_gid_remap<<<grid_blocks(s->K.N, 256, s), 256, 0, s->stream>>>(s->D, s->K, newid);
+  CUDA_TRY(cudaGetLastError());
+  int nnew = 0;
+  if ((rc = read_ctr(s, CTR_NVS2_END, &nnew))) return rc;
+  for (auto &p : s->owned) {
+    if (p == (void *)s->D.cth) { cudaFree(p); p = (void *)cth2; }
+    else if (p == (void *)s->D.rot) { cudaFree(p); p = (void *)rot2; }
+  }
+  s->D.cth = cth2;
+  s->D.rot = rot2;
+  s->nGrain = nnew;
+  s->h_pinned[2] = nnew;
+  CUDA_TRY(cudaMemcpyAsync(s->D.ctr + CTR_NGRAIN, s->h_pinned + 2, sizeof(int), cudaMemcpyHostToDevice, s->stream));
+  free_tmp(s, tmp);
+  return sim_sync(s);
+}
+
+int cafe_sim_update_time(cafe_sim *s) {
+  if (!s) return fail(CAFE_E_ARG, "null handle");
+  s->g.time += s->DelT;
+  s->g.tInd += 1;
+  return CAFE_OK;
+}
+
+int cafe_sim_begin(cafe_sim *s) {
+  if (!s || !s->initialized) return fail(CAFE_E_STATE, "begin before initialize_voxels");
+  if (s->begun) return fail(CAFE_E_STATE, "begin called twice");
+  int rc = cafe_sim_add_layer(s);
+  if (rc) return rc;
+  grid_update_laser(s->g);
+  s->begun = true;
+  return CAFE_OK;
+}
+
+int cafe_sim_step(cafe_sim *s, int *done) {
+  if (!s || !s->begun) return fail(CAFE_E_STATE, "step before begin");
+  if (s->done) {
+    if (done) *done = 1;
+    return CAFE_OK;
+  }
+  int rc;
+  if ((rc = cafe_sim_temperature(s))) return rc;
+  if ((rc = cafe_sim_update_voxels(s))) return rc;
+  grid_update_laser(s->g);
+  bool bcheck = s->g.indlayer > s->nlayerTot;
+  if (s->g.inewlayerflg == 1 && (rc = cafe_sim_clean_layer(s))) return rc;
+  cafe_sim_update_time(s);
+  if (s->g.inewlayerflg == 1 && (rc = cafe_sim_add_layer(s))) return rc;
+  s->steps++;
+  if (bcheck) s->done = true;
+  if (done) *done = s->done ? 1 : 0;
+  return CAFE_OK;
+}
+
+int cafe_sim_run(cafe_sim *s, long long max_steps, long long *steps_done) {
+  if (!s || !s->begun) return fail(CAFE_E_STATE, "run before begin");
+  long long n = 0;
+  int done = s->done ? 1 : 0, rc;
+  while (!done && (max_steps <= 0 || n < max_steps)) {
+    if ((rc = cafe_sim_step(s, &done))) return rc;
+    ++n;
+  }
+  if (done && (rc = cafe_sim_clean_layer(s))) return rc;
+  if (steps_done) *steps_done = n;
+  return sim_sync(s);
+}
+
+int cafe_sim_synchronize(cafe_sim *s) {
+  if (!s) return fail(CAFE_E_ARG, "null handle");
+  CUDA_TRY(cudaSetDevice(s->device));
+  return sim_sync(s);
+}
+
+int cafe_sim_info(cafe_sim *s, cafe_info *info) {
+  if (!s || !info) return fail(CAFE_E_ARG, "null argument");
+  int rc = read_ctr(s, CTR_NGRAIN, &s->nGrain);
+  if (rc) return rc;
+  const GridH &g = s->g;
+  info->nx = g.nX[0];
+  info->ny = g.nX[1];
+  info->nz = g.nX[2];
+  info->dx = g.dX[0];
+  info->tInd = g.tInd;
+  info->time = g.time;
+  info->isp = g.isp;
+  info->indlayer = g.indlayer;
+  info->inewlayerflg = g.inewlayerflg;
+  info->inewscanflg = g.inewscanflg;
+  info->ilaserLoc = g.ilaserLoc;
+  info->nGrain = s->nGrain;
+  info->nlayerTot = s->nlayerTot;
+  info->Nzh = s->Nzh;
+  info->done = s->done ? 1 : 0;
+  info->steps = s->steps;
+  return CAFE_OK;
+}
+
+int cafe_sim_stats(cafe_sim *s, cafe_stats *st) {
+  if (!s || !st) return fail(CAFE_E_ARG, "null argument");
+  unsigned long long v[STAT_COUNT];
+  CUDA_TRY(cudaStreamSynchronize(s->stream));
+  CUDA_TRY(cudaMemcpy(v, s->D.stat, sizeof v, cudaMemcpyDeviceToHost));
+  st->events = v[STAT_EVENTS];
+  st->nucleations = v[STAT_NUC];
+  st->max_active = v[STAT_MAXNA];
+  st->max_rows = v[STAT_MAXROWS];
+  st->steps = v[STAT_STEPS];
+  st->negative_dt = v[STAT_NEGDT];
+  return CAFE_OK;
+}
+
+int cafe_sim_download_state(cafe_sim *s, int32_t *gID, int32_t *vState, double *extents,
+                            double *centroid, int32_t *buildjID) {
+  if (!s) return fail(CAFE_E_ARG, "null handle");
+  CUDA_TRY(cudaSetDevice(s->device));
+  int rc = sim_sync(s);
+  if (rc) return rc;
+  long long N = s->K.N;
+  if (gID) CUDA_TRY(cudaMemcpy(gID, s->D.gid, N * sizeof(int32_t), cudaMemcpyDeviceToHost));
+  if (extents) CUDA_TRY(cudaMemcpy(extents, s->D.ext, N * sizeof(double), cudaMemcpyDeviceToHost));
+  if (vState || buildjID) {
+    std::vector<uint8_t> b(N);
+    if (vState) {
+      CUDA_TRY(cudaMemcpy(b.data(), s->D.state, N, cudaMemcpyDeviceToHost));
+      for (long long i = 0; i < N; ++i) vState[i] = b[i];
+    }
+    if (buildjID) {
+      CUDA_TRY(cudaMemcpy(b.data(), s->D.buildj, N, cudaMemcpyDeviceToHost));
+      for (long long i = 0; i < N; ++i) buildjID[i] = b[i];
+    }
+  }
+  if (centroid) {
+    std::vector<double> c(N);
+    double *src[3] = {s->D.cx, s->D.cy, s->D.cz};
+    for (int a = 0; a < 3; ++a) {
+      CUDA_TRY(cudaMemcpy(c.data(), src[a], N * sizeof(double), cudaMemcpyDeviceToHost));
+      for (long long i = 0; i < N; ++i) centroid[3 * i + a] = c[i];
+    }
+  }
+  return CAFE_OK;
+}
+
+int cafe_sim_download_temperature(cafe_sim *s, double *temp) {
+  if (!s || !temp) return fail(CAFE_E_ARG, "null argument");
+  CUDA_TRY(cudaSetDevice(s->device));
+  long long N = s->K.N;
+  if (!s->have_P) {
+    for (long long i = 0; i < N; ++i) temp[i] = 0.0;
+    return CAFE_OK;
+  }
+  double *d;
+  CUDA_TRY(cudaMalloc((void **)&d, N * sizeof(double)));
+  k_temperature<<<grid_blocks(N, 256, s), 256, 0, s->stream>>>(s->K, s->P, d);
+  cudaError_t e1 = cudaGetLastError();
+  cudaError_t e2 = cudaMemcpyAsync(temp, d, N * sizeof(double), cudaMemcpyDeviceToHost, s->stream);
+  cudaError_t e3 = cudaStreamSynchronize(s->stream);
+  cudaFree(d);
+  if (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess)
+    return fail(CAFE_E_CUDA, "temperature download failed");
+  return CAFE_OK;
+}
+
+int cafe_sim_download_ctheta(cafe_sim *s, double *ctheta, long long cap, int *ngrain) {
+  if (!s) return fail(CAFE_E_ARG, "null handle");
+  CUDA_TRY(cudaSetDevice(s->device));
+  int rc = read_ctr(s, CTR_NGRAIN, &s->nGrain);
+  if (rc) return rc;
+  if (ngrain) *ngrain = s->nGrain;
+  if (ctheta) {
+    if (cap < 4LL * s->nGrain) return fail(CAFE_E_ARG, "ctheta buffer too small (%lld < %lld)", cap, 4LL * s->nGrain);
+    CUDA_TRY(cudaMemcpy(ctheta, s->D.cth, 4LL * s->nGrain * sizeof(double), cudaMemcpyDeviceToHost));
+  }
+  return CAFE_OK;
+}
+
+int cafe_sim_upload_state(cafe_sim *s, const int32_t *gID, const int32_t *vState, const double *extents,
+                          const double *centroid, const double *ctheta, int ngrain) {
+  if (!s || !gID || !vState || !extents || !centroid || !ctheta || ngrain < 0)
+    return fail(CAFE_E_ARG, "null or negative argument");
+  CUDA_TRY(cudaSetDevice(s->device));
+  long long N = s->K.N;
+  for (long long i = 0; i < N; ++i) {
+    if (vState[i] < 0 || vState[i] > 3) return fail(CAFE_E_ARG, "vState[%lld] = %d outside 0..3", i, vState[i]);
+    if (gID[i] < 0 || gID[i] > ngrain) return fail(CAFE_E_ARG, "gID[%lld] = %d outside 0..nGrain", i, gID[i]);
+  }
+  int rc = grow_grains(s, (long long)ngrain + 1);
+  if (rc) return rc;
+  std::vector<uint8_t> b(N);
+  for (long long i = 0; i < N; ++i) b[i] = (uint8_t)vState[i];
+  CUDA_TRY(cudaMemcpy(s->D.state, b.data(), N, cudaMemcpyHostToDevice));
+  CUDA_TRY(cudaMemcpy(s->D.gid, gID, N * sizeof(int32_t), cudaMemcpyHostToDevice));
+  CUDA_TRY(cudaMemcpy(s->D.ext, extents, N * sizeof(double), cudaMemcpyHostToDevice));
+  std::vector<double> c(N);
+  double *dst[3] = {s->D.cx, s->D.cy, s->D.cz};
+  for (int a = 0; a < 3; ++a) {
+    for (long long i = 0; i < N; ++i) c[i] = centroid[3 * i + a];
+    CUDA_TRY(cudaMemcpy(dst[a], c.data(), N * sizeof(double), cudaMemcpyHostToDevice));
+  }
+  if (ngrain > 0) {
+    CUDA_TRY(cudaMemcpy(s->D.cth, ctheta, 4LL * ngrain * sizeof(double), cudaMemcpyHostToDevice));
+    k_rot_range<<<grid_blocks(ngrain, 128, s), 128, 0, s->stream>>>(s->D, 0, ngrain);
+    CUDA_TRY(cudaGetLastError());
+  }
+  s->nGrain = ngrain;
+  s->h_pinned[2] = ngrain;
+  CUDA_TRY(cudaMemcpyAsync(s->D.ctr + CTR_NGRAIN, s->h_pinned + 2, sizeof(int), cudaMemcpyHostToDevice, s->stream));
+  s->initialized = true;
+  return sim_sync(s);
+}
+
+}  // extern "C"

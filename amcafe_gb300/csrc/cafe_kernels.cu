@@ -269,6 +269,7 @@ __global__ void k_gather(CafeDev D, CafeConsts K, CafeStepParams P) {
 __global__ void k_lists_count(CafeDev D) {
   __shared__ int ws[2][CAFE_DENSE_THREADS / 32];
   int na = D.ctr[CTR_NA];
+  if (na > D.act_cap) na = (int)D.act_cap;
   long long base = ((long long)blockIdx.x * blockDim.x + threadIdx.x) * CAFE_CELLS_PER_THREAD;
   int c2 = 0, cf = 0;
   for (int c = 0; c < CAFE_CELLS_PER_THREAD; ++c) {
@@ -299,24 +300,46 @@ __global__ void k_lists_count(CafeDev D) {
   }
 }
 
-// Exclusive scan of interleaved pairs (blk[2b], blk[2b+1]).
+// Exclusive scan of interleaved pairs (blk[2b], blk[2b+1]), b < n, one block.
 __global__ void k_scan_pairs(int32_t *blk, long long n, int *tot0, int *tot1) {
-  if (threadIdx.x != 0) return;
-  long long a0 = 0, a1 = 0;
-  for (long long b = 0; b < n; ++b) {
+  __shared__ long long part[2][1024];
+  long long per = (n + blockDim.x - 1) / blockDim.x;
+  long long b0 = threadIdx.x * per, b1 = b0 + per < n ? b0 + per : n;
+  long long s0 = 0, s1 = 0;
+  for (long long b = b0; b < b1; ++b) {
+    s0 += blk[2 * b];
+    s1 += blk[2 * b + 1];
+  }
+  part[0][threadIdx.x] = s0;
+  part[1][threadIdx.x] = s1;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    long long a0 = 0, a1 = 0;
+    for (int t = 0; t < (int)blockDim.x; ++t) {
+      long long v0 = part[0][t], v1 = part[1][t];
+      part[0][t] = a0;
+      part[1][t] = a1;
+      a0 += v0;
+      a1 += v1;
+    }
+    *tot0 = (int)a0;
+    *tot1 = (int)a1;
+  }
+  __syncthreads();
+  long long a0 = part[0][threadIdx.x], a1 = part[1][threadIdx.x];
+  for (long long b = b0; b < b1; ++b) {
     long long v0 = blk[2 * b], v1 = blk[2 * b + 1];
     blk[2 * b] = (int32_t)a0;
     blk[2 * b + 1] = (int32_t)a1;
     a0 += v0;
     a1 += v1;
   }
-  *tot0 = (int)a0;
-  *tot1 = (int)a1;
 }
 
 __global__ void k_lists_scatter(CafeDev D) {
   __shared__ int ws[2][CAFE_DENSE_THREADS / 32];
   int na = D.ctr[CTR_NA];
+  if (na > D.act_cap) na = (int)D.act_cap;
   long long base = ((long long)blockIdx.x * blockDim.x + threadIdx.x) * CAFE_CELLS_PER_THREAD;
   int c2 = 0, cf = 0;
   for (int c = 0; c < CAFE_CELLS_PER_THREAD; ++c) {
@@ -392,10 +415,15 @@ __device__ void cafe_row_fill_warp(const CafeDev &D, const CafeConsts &K, long l
   int nn = D.a_nn[p];
   double *g = D.row_g + r * CAFE_NSLOT;
   bool liv = false;
+  int gp = D.a_gid[p];
+  bool grain_ok = gp >= 1 && gp <= D.grain_cap;
   if (lane < nn) {
     int q = D.a_nbr[(long long)p * CAFE_NSLOT + lane];
-    if (D.a_state[q] == 1) {
-      const double *R = D.rot + 9LL * (D.a_gid[p] - 1);
+    if (D.a_state[q] == 1 && !grain_ok) {
+      g[lane] = NAN;  // a capturing cell without a grain never captures
+      liv = true;
+    } else if (D.a_state[q] == 1) {
+      const double *R = D.rot + 9LL * (gp - 1);
       double Rm[9];
       for (int a = 0; a < 9; ++a) Rm[a] = R[a];
       int i, j, k;
@@ -518,7 +546,6 @@ __device__ __forceinline__ int cafe_find_slot(const CafeDev &D, int q, int targe
 __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
     k_event_loop(CafeDev D, CafeConsts K, CafeStepParams P, long long max_events) {
   __shared__ CafeCand red[CAFE_LOOP_THREADS / 32];
-  __shared__ CafeCand s_best;
   __shared__ double s_tinc, s_dt;
   __shared__ int s_nvs2, s_countS, s_nrows, s_ngrain, s_done, s_nuc, s_icap, s_jspos, s_na;
   __shared__ uint32_t s_rng;
@@ -580,7 +607,6 @@ __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
         s_icap = D.a_nbr[(long long)jspos * CAFE_NSLOT + b.s];
         s_nuc = U < K.rX;
         s_dt = s_nuc ? 0.0 : b.t;
-        s_best = b;
         if (s_dt < 0.0) s_negdt++;
       }
     }
@@ -641,7 +667,8 @@ __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
         s_nnuc++;
       } else {
         int g = D.a_gid[js];
-        D.a_gid[icap] = g;
+        if (g < 1 || g > D.grain_cap) g = 1;  // unreachable: rows of grainless cells hold no finite time
+        D.a_gid[icap] = D.a_gid[js];
         int si, sj, sk;
         cafe_cell_xyz(K, D.act[js], si, sj, sk);
         double cs[3] = {D.a_cx[js], D.a_cy[js], D.a_cz[js]};

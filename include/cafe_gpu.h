@@ -1,0 +1,121 @@
+/* C ABI of the GB300 CA engine (libcafe_gpu.so).
+ *
+ * One cafe_sim is one realisation of AMCAFE's model on one GPU: the state of
+ * its Grid, Partition (world size 1), BasePlate, TempField and VoxelsCA
+ * objects (AMCAFE src/src-mpi/main1.C:29-42) with the voxel fields resident in
+ * device memory. The entry points below replace, one for one, the member
+ * functions that the reference's time loop (main1.C:60-96) calls; each cites
+ * the reference function it stands in for. All functions return 0 on success
+ * and a nonzero CAFE_E_* code otherwise (never abort); cafe_last_error()
+ * returns a message for the calling thread. Calls on one handle must be
+ * serialised by the caller (one host thread per handle); different handles
+ * are independent.
+ */
+#ifndef CAFE_GPU_H
+#define CAFE_GPU_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct cafe_sim cafe_sim;
+
+enum {
+  CAFE_OK = 0,
+  CAFE_E_ARG = 1,      /* bad argument or deck value */
+  CAFE_E_CUDA = 2,     /* CUDA runtime error (message has the CUDA error string) */
+  CAFE_E_CAPACITY = 3, /* an active-list, frontier or grain table capacity was exceeded */
+  CAFE_E_STATE = 4,    /* call out of order (e.g. step before initialize) */
+  CAFE_E_IO = 5        /* deck file could not be read */
+};
+
+typedef struct {
+  int device;                  /* CUDA device ordinal */
+  long long active_capacity;   /* max active-list length per step; 0 = automatic */
+  long long grain_capacity;    /* initial grain-table capacity; 0 = automatic */
+} cafe_options;
+
+typedef struct {
+  int nx, ny, nz;
+  double dx;
+  int tInd;        /* Grid::tInd */
+  double time;     /* Grid::time */
+  int isp, indlayer, inewlayerflg, inewscanflg, ilaserLoc;
+  int nGrain;      /* VoxelsCA::nGrain */
+  int nlayerTot;   /* main1.C:59 */
+  int Nzh;         /* BasePlate::Nzh */
+  int done;        /* main1.C loop condition reached (indlayer > nlayerTot) */
+  long long steps; /* loop iterations executed */
+} cafe_info;
+
+typedef struct {
+  unsigned long long events;       /* captures + nucleations */
+  unsigned long long nucleations;
+  unsigned long long max_active;   /* largest active list */
+  unsigned long long max_rows;     /* largest frontier (capturing cells) */
+  unsigned long long steps;        /* UpdateVoxels calls */
+  unsigned long long negative_dt;  /* events with a negative capture time */
+} cafe_stats;
+
+/* Grid::Grid (Grid.C:15-109, deck parse Grid.C:165-318) + Partition::
+ * PartitionGraph2 at world size 1 (Partition.C:260-412) + BasePlate::BasePlate
+ * (BasePlate.C:18-30) + TempField::TempField/InitializeAnalytic
+ * (TempField.C:16-77) + VoxelsCA::VoxelsCA (VoxelsCA.C:34-74). Allocates the
+ * device state. opt may be NULL. */
+int cafe_sim_create(const char *deck_path, const cafe_options *opt, cafe_sim **out);
+void cafe_sim_destroy(cafe_sim *sim);
+
+/* VoxelsCA::InitializeVoxels(BasePlate&) (VoxelsCA.C:125-161, BasePlate::
+ * GenerateVoxel BasePlate.C:41-97). */
+int cafe_sim_initialize_voxels(cafe_sim *sim);
+/* VoxelsCA::AddLayer1 (VoxelsCA.C:887-982). */
+int cafe_sim_add_layer(cafe_sim *sim);
+/* Grid::UpdateLaser (Grid.C:110-164). */
+int cafe_sim_update_laser(cafe_sim *sim);
+/* TempField::AnalyticTempCurr (TempField.C:139-217), including the
+ * end-of-scan check that may set Grid::inewscanflg / inewlayerflg. Sets
+ * TempField::tInd = round(time/DelT) first (main1.C:64). */
+int cafe_sim_temperature(cafe_sim *sim);
+/* VoxelsCA::UpdateVoxels (VoxelsCA.C:232-655). */
+int cafe_sim_update_voxels(cafe_sim *sim);
+/* VoxelsCA::CleanLayer (VoxelsCA.C:800-839). */
+int cafe_sim_clean_layer(cafe_sim *sim);
+/* Grid::UpdateTime2(TempField::DelT) (Grid.C:334-339). */
+int cafe_sim_update_time(cafe_sim *sim);
+
+/* main1.C:60-61: AddLayer1 then the first UpdateLaser (after
+ * initialize_voxels). */
+int cafe_sim_begin(cafe_sim *sim);
+/* One iteration of the main1.C:62-93 loop body (without HDF5 output);
+ * *done = 1 when the loop condition ends the run. */
+int cafe_sim_step(cafe_sim *sim, int *done);
+/* Runs loop iterations until done or max_steps (> 0) iterations; then, when
+ * done, the closing CleanLayer (main1.C:95). */
+int cafe_sim_run(cafe_sim *sim, long long max_steps, long long *steps_done);
+/* Waits for all queued device work; reports device-side errors. */
+int cafe_sim_synchronize(cafe_sim *sim);
+
+int cafe_sim_info(cafe_sim *sim, cafe_info *info);
+int cafe_sim_stats(cafe_sim *sim, cafe_stats *stats);
+
+/* VoxelsCA public fields gID, vState, extents, centroidOct (x,y,z interleaved,
+ * 3 per cell) and TempField::BuildjID, N = nx*ny*nz entries each; any pointer
+ * may be NULL. */
+int cafe_sim_download_state(cafe_sim *sim, int32_t *gID, int32_t *vState, double *extents,
+                            double *centroid, int32_t *buildjID);
+/* TempField::TempCurr of the last cafe_sim_temperature call. */
+int cafe_sim_download_temperature(cafe_sim *sim, double *temp);
+/* VoxelsCA::cTheta, 4 per grain; cap = capacity of out in doubles; *ngrain gets nGrain. */
+int cafe_sim_download_ctheta(cafe_sim *sim, double *ctheta, long long cap, int *ngrain);
+/* Replaces the voxel state and grain table (same layouts as the downloads). */
+int cafe_sim_upload_state(cafe_sim *sim, const int32_t *gID, const int32_t *vState,
+                          const double *extents, const double *centroid, const double *ctheta,
+                          int ngrain);
+
+const char *cafe_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
