@@ -17,8 +17,11 @@ EXPORTS = (
     "cafe_sim_clean_layer", "cafe_sim_update_time", "cafe_sim_begin", "cafe_sim_step",
     "cafe_sim_run", "cafe_sim_synchronize", "cafe_sim_info", "cafe_sim_stats",
     "cafe_sim_download_state", "cafe_sim_download_temperature", "cafe_sim_download_ctheta",
-    "cafe_sim_upload_state", "cafe_last_error",
+    "cafe_sim_upload_state", "cafe_last_error", "cafe_sim_set_timing", "cafe_sim_phase_times",
+    "cafe_sim_stream", "cafe_sim_mark", "cafe_sim_elapsed",
 )
+PHASES = ("melt", "classify", "gather", "events", "writeback", "layer")
+NPHASE = 8
 
 
 class CafeOptions(ctypes.Structure):
@@ -32,13 +35,15 @@ class CafeInfo(ctypes.Structure):
                 ("isp", ctypes.c_int), ("indlayer", ctypes.c_int), ("inewlayerflg", ctypes.c_int),
                 ("inewscanflg", ctypes.c_int), ("ilaserLoc", ctypes.c_int), ("nGrain", ctypes.c_int),
                 ("nlayerTot", ctypes.c_int), ("Nzh", ctypes.c_int), ("done", ctypes.c_int),
-                ("steps", ctypes.c_longlong)]
+                ("steps", ctypes.c_longlong), ("gth", ctypes.c_double), ("genlayer_state", ctypes.c_uint)]
 
 
 class CafeStats(ctypes.Structure):
     _fields_ = [("events", ctypes.c_ulonglong), ("nucleations", ctypes.c_ulonglong),
                 ("max_active", ctypes.c_ulonglong), ("max_rows", ctypes.c_ulonglong),
-                ("steps", ctypes.c_ulonglong), ("negative_dt", ctypes.c_ulonglong)]
+                ("steps", ctypes.c_ulonglong), ("negative_dt", ctypes.c_ulonglong),
+                ("sum_active", ctypes.c_ulonglong), ("sum_rows", ctypes.c_ulonglong),
+                ("launches", ctypes.c_ulonglong)]
 
 
 _lib = None
@@ -76,6 +81,11 @@ def load():
         "cafe_sim_download_ctheta": (I, [P, f64p, LL, ctypes.POINTER(I)]),
         "cafe_sim_upload_state": (I, [P, i32p, i32p, f64p, f64p, f64p, I]),
         "cafe_last_error": (ctypes.c_char_p, []),
+        "cafe_sim_set_timing": (I, [P, I]),
+        "cafe_sim_phase_times": (I, [P, f64p, ctypes.POINTER(LL), I, I]),
+        "cafe_sim_stream": (I, [P, ctypes.POINTER(P)]),
+        "cafe_sim_mark": (I, [P, I]),
+        "cafe_sim_elapsed": (I, [P, I, I, ctypes.POINTER(D)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

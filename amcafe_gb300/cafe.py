@@ -22,7 +22,7 @@ import ctypes
 
 import numpy as np
 
-from ._native import CafeInfo, CafeOptions, CafeStats, check, load
+from ._native import NPHASE, PHASES, CafeInfo, CafeOptions, CafeStats, check, load
 
 
 def _ptr(a, ct):
@@ -123,6 +123,31 @@ class Simulation:
         check(self._lib.cafe_sim_upload_state(self._h, _ptr(gID, ctypes.c_int32), _ptr(vState, ctypes.c_int32),
                                               _ptr(extents, ctypes.c_double), _ptr(centroid, ctypes.c_double),
                                               _ptr(ctheta, ctypes.c_double), len(ctheta) // 4))
+
+    # -- profiling ---------------------------------------------------------
+    def set_timing(self, on=True):
+        check(self._lib.cafe_sim_set_timing(self._h, 1 if on else 0))
+
+    def phase_times(self, reset=False):
+        """{phase: (milliseconds, kernel launches)} accumulated while timing was on."""
+        ms = (ctypes.c_double * NPHASE)()
+        nl = (ctypes.c_longlong * NPHASE)()
+        check(self._lib.cafe_sim_phase_times(self._h, ms, nl, NPHASE, 1 if reset else 0))
+        return {name: (ms[i], nl[i]) for i, name in enumerate(PHASES)}
+
+    def mark(self, slot):
+        check(self._lib.cafe_sim_mark(self._h, slot))
+
+    def elapsed_ms(self, a, b):
+        ms = ctypes.c_double(0)
+        check(self._lib.cafe_sim_elapsed(self._h, a, b, ctypes.byref(ms)))
+        return ms.value
+
+    def stream(self):
+        """The cudaStream_t (as an int) that this simulation's work runs on."""
+        p = ctypes.c_void_p()
+        check(self._lib.cafe_sim_stream(self._h, ctypes.byref(p)))
+        return p.value or 0
 
     def close(self):
         if self._h:

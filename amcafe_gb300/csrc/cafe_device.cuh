@@ -34,7 +34,9 @@ struct CafeStepParams {
   double lx, ly, lz;  // laser x, y (scan frame) and the laser plane height
   double cg, sg;      // cos(gth), sin(gth) (host libm, as TempField.C:163-166)
   double dirp;        // scan direction sign source (TempField.C:167-171)
-  int lo[3], hi[3];   // cell box outside which T cannot reach the liquidus
+  int lo[3], hi[3];   // cell box ("pool box") outside which T cannot reach the liquidus
+  int plo[3], phi[3]; // pool box of the previous step (liquid cells may remain there)
+  int kabove;         // first z index with cell centre above the laser plane (T = T0)
   int ilaserLoc;
   int tInd;           // Grid::tInd (seeds of VoxelsCA.C:338-340)
   int any_hot_full;   // 1: evaluate T exactly everywhere below the plane
@@ -69,6 +71,11 @@ struct CafeDev {
   double *ext, *cx, *cy, *cz;
   uint8_t *buildj;
   int32_t *pos_of;
+  // temperature class of every cell of the pool box, written by k_melt
+  uint8_t *tcls;
+  long long tcls_cap;
+  // liquid cells left by the previous step (cell indices)
+  int32_t *liq;
   // grains
   double *cth, *rot;
   int grain_cap;
@@ -104,14 +111,15 @@ enum {
   CTR_NEV,         // events this step
   CTR_NNUC,        // nucleations this step
   CTR_NVS2_END,    // mushy-list length after the event loop
+  CTR_NLIQ,        // liquid cells listed by the last write-back
   CTR_COUNT
 };
-enum { STAT_EVENTS = 0, STAT_NUC, STAT_MAXNA, STAT_MAXROWS, STAT_STEPS, STAT_NEGDT, STAT_COUNT };
+enum { STAT_EVENTS = 0, STAT_NUC, STAT_MAXNA, STAT_MAXROWS, STAT_STEPS, STAT_NEGDT, STAT_SUMNA, STAT_SUMROWS, STAT_COUNT };
 
 // --------------------------------------------------------------- temperature
 // TempField::AnalyticTempCurr (TempField.C:155-190) for one cell; returns the
 // class 0 (T0, above the laser plane), 1 (tS) or 2 (xi = tL(1+eps)).
-__device__ __forceinline__ int cafe_temp_class(const CafeConsts &K, const CafeStepParams &P, int i,
+__device__ __forceinline__ int cafe_temp_class_exact(const CafeConsts &K, const CafeStepParams &P, int i,
                                                int j, int k) {
   double zp = ((double)k + .5) * K.dx[2];
   if (zp > P.lz) return 0;
@@ -138,10 +146,22 @@ __device__ __forceinline__ int cafe_temp_class(const CafeConsts &K, const CafeSt
 
 __device__ __forceinline__ void cafe_cell_xyz(const CafeConsts &K, long long idx, int &i, int &j,
                                               int &k) {
-  k = (int)(idx / K.nxy);
-  long long r = idx - (long long)K.nxy * k;
-  j = (int)(r / K.nx);
-  i = (int)(r - (long long)K.nx * j);
+  // N < 2^31 (checked on the host), so 32-bit unsigned division suffices
+  unsigned int u = (unsigned int)idx, nxy = (unsigned int)K.nxy, nx = (unsigned int)K.nx;
+  unsigned int kk = u / nxy, r = u - kk * nxy, jj = r / nx;
+  k = (int)kk;
+  j = (int)jj;
+  i = (int)(r - jj * nx);
+}
+
+// Temperature class of a cell from the per-step class map (integer work only):
+// above the laser plane T0, outside the pool box tS, inside it the class that
+// k_melt computed with cafe_temp_class_exact.
+__device__ __forceinline__ int cafe_cls(const CafeDev &D, const CafeStepParams &P, int i, int j, int k) {
+  if (k >= P.kabove) return 0;
+  if (i < P.lo[0] || i >= P.hi[0] || j < P.lo[1] || j >= P.hi[1] || k < P.lo[2] || k >= P.hi[2]) return 1;
+  long long bx = P.hi[0] - P.lo[0], by = P.hi[1] - P.lo[1];
+  return D.tcls[((long long)(k - P.lo[2]) * by + (j - P.lo[1])) * bx + (i - P.lo[0])];
 }
 
 // --------------------------------------------------------------- geometry

@@ -362,14 +362,72 @@ struct cafe_sim {
   CafeDev D;
   CafeStepParams P;      // last temperature parameters
   bool have_P = false;
+  bool have_prev_box = false;
+  int prev_lo[3] = {0, 0, 0}, prev_hi[3] = {0, 0, 0};
+  bool full_k2 = false;   // next solid->mushy pass must scan the whole box
   std::vector<void *> owned;
   int *h_pinned = nullptr;  // pinned host mirror of ctr + err
+  // per-phase device timing (CUDA events on `stream`) and kernel-launch counts
+  bool timing = false;
+  cudaEvent_t marks[8] = {nullptr};
+  std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> pend;
+  std::vector<cudaEvent_t> ev_pool;
+  double phase_ms[CAFE_NPHASE] = {0};
+  long long phase_launch[CAFE_NPHASE] = {0};
+  long long launches = 0;
   long long nblk = 0;       // dense compaction blocks
   long long nblk_pos = 0;   // position compaction blocks
   int nsm = 1;
 };
 
 namespace {
+
+cudaEvent_t ev_get(cafe_sim *s) {
+  if (!s->ev_pool.empty()) {
+    cudaEvent_t e = s->ev_pool.back();
+    s->ev_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e;
+  cudaEventCreate(&e);
+  return e;
+}
+void resolve_phases(cafe_sim *s) {
+  for (auto &p : s->pend) {
+    float ms = 0.f;
+    cudaEventSynchronize(p.second.second);
+    cudaEventElapsedTime(&ms, p.second.first, p.second.second);
+    s->phase_ms[p.first] += ms;
+    s->ev_pool.push_back(p.second.first);
+    s->ev_pool.push_back(p.second.second);
+  }
+  s->pend.clear();
+}
+// Brackets a group of launches of phase `ph`.
+struct PhaseScope {
+  cafe_sim *s;
+  int ph;
+  cudaEvent_t a = nullptr;
+  PhaseScope(cafe_sim *s_, int ph_) : s(s_), ph(ph_) {
+    if (s->timing) {
+      a = ev_get(s);
+      cudaEventRecord(a, s->stream);
+    }
+  }
+  ~PhaseScope() {
+    if (s->timing) {
+      cudaEvent_t b = ev_get(s);
+      cudaEventRecord(b, s->stream);
+      s->pend.push_back({ph, {a, b}});
+      if (s->pend.size() > 4096) resolve_phases(s);
+    }
+  }
+};
+#define LAUNCHED(ph, n)          \
+  do {                            \
+    s->launches += (n);           \
+    s->phase_launch[ph] += (n);   \
+  } while (0)
 
 int sim_sync(cafe_sim *s) {
   CUDA_TRY(cudaStreamSynchronize(s->stream));
@@ -531,6 +589,14 @@ void make_step_params(cafe_sim *s, CafeStepParams &P) {
       P.hi[a] = nmax[a];
     }
   }
+  // first z index whose cell centre lies above the laser plane (TempField.C:162)
+  int kab = 0;
+  while (kab < g.nX[2] && !(((double)kab + .5) * g.dX[2] > P.lz)) ++kab;
+  P.kabove = kab;
+  for (int a = 0; a < 3; ++a) {
+    P.plo[a] = s->have_prev_box ? s->prev_lo[a] : 0;
+    P.phi[a] = s->have_prev_box ? s->prev_hi[a] : 0;
+  }
 }
 
 }  // namespace
@@ -636,7 +702,7 @@ int cafe_sim_create(const char *deck_path, const cafe_options *opt, cafe_sim **o
   acap = std::min<long long>(acap, N);
   D.act_cap = acap;
   D.vs2_cap = acap;
-  D.row_cap = acap;
+  D.row_cap = std::min<long long>(acap, 1LL << 22);
   double est = g.mu * (g.dX[0] * 1e6) * (g.dX[1] * 1e6) * g.nX[0] * g.nX[1] * (s->Nzh * g.dX[2] * 1e6) +
                (s->nlayerTot + 1) * g.lrate * (g.dX[0] * 1e6) * (g.dX[1] * 1e6) * g.nX[0] * g.nX[1] * (g.layerT * 1e6);
   long long gcap = opt && opt->grain_capacity > 0 ? opt->grain_capacity : (long long)(2 * est) + (1 << 16);
@@ -647,7 +713,7 @@ int cafe_sim_create(const char *deck_path, const cafe_options *opt, cafe_sim **o
   auto &o = s->owned;
   if ((rc = dalloc(&D.state, N, o)) || (rc = dalloc(&D.gid, N, o)) || (rc = dalloc(&D.ext, N, o)) ||
       (rc = dalloc(&D.cx, N, o)) || (rc = dalloc(&D.cy, N, o)) || (rc = dalloc(&D.cz, N, o)) ||
-      (rc = dalloc(&D.buildj, N, o)) || (rc = dalloc(&D.pos_of, N, o)) ||
+      (rc = dalloc(&D.buildj, N, o)) || (rc = dalloc(&D.pos_of, N, o)) || (rc = dalloc(&D.liq, acap, o)) ||
       (rc = dalloc(&D.cth, 4 * (size_t)D.grain_cap, o)) || (rc = dalloc(&D.rot, 9 * (size_t)D.grain_cap, o)) ||
       (rc = dalloc(&D.act, acap, o)) || (rc = dalloc(&D.a_state, acap, o)) || (rc = dalloc(&D.a_cls, acap, o)) ||
       (rc = dalloc(&D.a_nn, acap, o)) || (rc = dalloc(&D.a_cold, acap, o)) || (rc = dalloc(&D.a_gid, acap, o)) ||
@@ -690,6 +756,10 @@ void cafe_sim_destroy(cafe_sim *s) {
   if (!s) return;
   cudaSetDevice(s->device);
   if (s->stream) cudaStreamSynchronize(s->stream);
+  resolve_phases(s);
+  for (cudaEvent_t e : s->ev_pool) cudaEventDestroy(e);
+  for (cudaEvent_t e : s->marks)
+    if (e) cudaEventDestroy(e);
   for (void *p : s->owned) cudaFree(p);
   if (s->h_pinned) cudaFreeHost(s->h_pinned);
   if (s->stream) cudaStreamDestroy(s->stream);
@@ -797,6 +867,7 @@ int cafe_sim_add_layer(cafe_sim *s) {
     for (int j = 0; j < ng2; ++j) hm[j] = j;
   CUDA_TRY(cudaMemcpyAsync(map, hm.data(), ng2 * sizeof(int32_t), cudaMemcpyHostToDevice, s->stream));
   k_layer_apply<<<grid_blocks(K.N, 256, s), 256, 0, s->stream>>>(s->D, K, iz1, g.ilaserLoc, gtmp, map, s->nGrain);
+  LAUNCHED(CAFE_PH_LAYER, 3);
   CUDA_TRY(cudaGetLastError());
   int n0 = s->nGrain;
   s->nGrain += i2 + 1;
@@ -831,6 +902,19 @@ int cafe_sim_temperature(cafe_sim *s) {
   const CafeStepParams &P = s->P;
   CUDA_TRY(cudaMemsetAsync(s->D.ctr + CTR_HOT, 0, sizeof(int), s->stream));
   long long nbox = (long long)(P.hi[0] - P.lo[0]) * (P.hi[1] - P.lo[1]) * (P.hi[2] - P.lo[2]);
+  if (nbox > s->D.tcls_cap) {
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    for (auto &p : s->owned)
+      if (p == (void *)s->D.tcls) {
+        cudaFree(p);
+        p = nullptr;
+      }
+    long long cap = std::max<long long>(nbox, 2 * s->D.tcls_cap);
+    cap = std::min<long long>(cap, s->K.N);
+    CUDA_TRY(cudaMalloc((void **)&s->D.tcls, cap));
+    s->owned.push_back(s->D.tcls);
+    s->D.tcls_cap = cap;
+  }
   if (nbox > 0) k_melt<<<grid_blocks(nbox, 256, s), 256, 0, s->stream>>>(s->D, s->K, P);
   CUDA_TRY(cudaGetLastError());
   // end-of-scan check (TempField.C:199-216), only when the laser is outside the grid box
@@ -860,21 +944,58 @@ int cafe_sim_update_voxels(cafe_sim *s) {
   const CafeStepParams &P = s->P;
   cudaStream_t st = s->stream;
   int nb = (int)s->nblk;
-  k_solid2mushy<<<nb, CAFE_DENSE_THREADS, 0, st>>>(D, K);
-  k_active_count<<<nb, CAFE_DENSE_THREADS, 0, st>>>(D, K, P);
-  k_scan_blocks<<<1, 1024, 0, st>>>(D.blk, s->nblk, D.ctr + CTR_NA);
-  k_active_scatter<<<nb, CAFE_DENSE_THREADS, 0, st>>>(D, K, P);
+  {
+    PhaseScope ps(s, CAFE_PH_CLASSIFY);
+    if (s->full_k2) {
+      k_solid2mushy_dense<<<nb, CAFE_DENSE_THREADS, 0, st>>>(D, K);
+      LAUNCHED(CAFE_PH_CLASSIFY, 1);
+      s->full_k2 = false;
+    } else {
+      long long vb = (long long)(P.hi[0] - P.lo[0] + 2) * (P.hi[1] - P.lo[1] + 2) * (P.hi[2] - P.lo[2] + 2);
+      k_solid2mushy_box<<<grid_blocks(vb, 256, s), 256, 0, st>>>(D, K, P.lo[0], P.hi[0], P.lo[1], P.hi[1], P.lo[2], P.hi[2]);
+      LAUNCHED(CAFE_PH_CLASSIFY, 1);
+      long long pb = (long long)(P.phi[0] - P.plo[0] + 2) * (P.phi[1] - P.plo[1] + 2) * (P.phi[2] - P.plo[2] + 2);
+      if (P.phi[0] > P.plo[0] && P.phi[1] > P.plo[1] && P.phi[2] > P.plo[2]) {
+        k_solid2mushy_box<<<grid_blocks(pb, 256, s), 256, 0, st>>>(D, K, P.plo[0], P.phi[0], P.plo[1], P.phi[1], P.plo[2], P.phi[2]);
+        LAUNCHED(CAFE_PH_CLASSIFY, 1);
+      }
+      k_solid2mushy_list<<<s->nsm * 4, 256, 0, st>>>(D, K);
+      LAUNCHED(CAFE_PH_CLASSIFY, 1);
+    }
+    CUDA_TRY(cudaMemsetAsync(D.ctr + CTR_NLIQ, 0, sizeof(int), st));
+    k_active_count<<<nb, CAFE_DENSE_THREADS, 0, st>>>(D, K, P);
+    k_scan_blocks<<<1, 1024, 0, st>>>(D.blk, s->nblk, D.ctr + CTR_NA);
+    k_active_scatter<<<nb, CAFE_DENSE_THREADS, 0, st>>>(D, K, P);
+    LAUNCHED(CAFE_PH_CLASSIFY, 3);
+  }
   int gb = s->nsm * 8;
-  k_gather<<<gb, 256, 0, st>>>(D, K, P);
-  int nbp = (int)s->nblk_pos;
-  k_lists_count<<<nbp, CAFE_DENSE_THREADS, 0, st>>>(D);
-  k_scan_pairs<<<1, 1024, 0, st>>>(D.blk, s->nblk_pos, D.ctr + CTR_NVS2, D.ctr + CTR_NROWS);
-  k_lists_scatter<<<nbp, CAFE_DENSE_THREADS, 0, st>>>(D);
-  k_rows_init<<<s->nsm * 4, 256, 0, st>>>(D, K);
-  k_event_loop<<<1, CAFE_LOOP_THREADS, 0, st>>>(D, K, P, D.act_cap + 1);
-  k_writeback<<<gb, 256, 0, st>>>(D);
-  k_mushy2solid<<<gb, 256, 0, st>>>(D, K);
+  {
+    PhaseScope ps(s, CAFE_PH_GATHER);
+    k_gather<<<gb, 256, 0, st>>>(D, K, P);
+    int nbp = (int)s->nblk_pos;
+    k_lists_count<<<nbp, CAFE_DENSE_THREADS, 0, st>>>(D);
+    k_scan_pairs<<<1, 1024, 0, st>>>(D.blk, s->nblk_pos, D.ctr + CTR_NVS2, D.ctr + CTR_NROWS);
+    k_lists_scatter<<<nbp, CAFE_DENSE_THREADS, 0, st>>>(D);
+    k_rows_init<<<s->nsm * 4, 256, 0, st>>>(D, K);
+    LAUNCHED(CAFE_PH_GATHER, 5);
+  }
+  {
+    PhaseScope ps(s, CAFE_PH_EVENTS);
+    k_event_loop<<<1, CAFE_LOOP_THREADS, 0, st>>>(D, K, P, D.act_cap + 1);
+    LAUNCHED(CAFE_PH_EVENTS, 1);
+  }
+  {
+    PhaseScope ps(s, CAFE_PH_WRITEBACK);
+    k_writeback<<<gb, 256, 0, st>>>(D);
+    k_mushy2solid<<<gb, 256, 0, st>>>(D, K);
+    LAUNCHED(CAFE_PH_WRITEBACK, 2);
+  }
   CUDA_TRY(cudaGetLastError());
+  for (int a = 0; a < 3; ++a) {
+    s->prev_lo[a] = P.lo[a];
+    s->prev_hi[a] = P.hi[a];
+  }
+  s->have_prev_box = true;
   return CAFE_OK;
 }
 
@@ -894,6 +1015,7 @@ int cafe_sim_clean_layer(cafe_sim *s) {
   CUDA_TRY(cudaMalloc((void **)&cth2, (size_t)s->D.grain_cap * 4 * sizeof(double)));
   CUDA_TRY(cudaMalloc((void **)&rot2, (size_t)s->D.grain_cap * 9 * sizeof(double)));
   CUDA_TRY(cudaMemsetAsync(cnt, 0, std::max(1, ng) * sizeof(int32_t), s->stream));
+  LAUNCHED(CAFE_PH_LAYER, 3);
   k_grain_count<<<grid_blocks(s->K.N, 256, s), 256, 0, s->stream>>>(s->D, s->K, cnt);
   k_grain_renumber<<<1, 1024, 0, s->stream>>>(s->D, cnt, newid, cth2, rot2);
   k_gid_remap<<<grid_blocks(s->K.N, 256, s), 256, 0, s->stream>>>(s->D, s->K, newid);
@@ -990,6 +1112,12 @@ int cafe_sim_info(cafe_sim *s, cafe_info *info) {
   info->Nzh = s->Nzh;
   info->done = s->done ? 1 : 0;
   info->steps = s->steps;
+  info->gth = g.gth;
+  {
+    std::ostringstream os;
+    os << s->genlayer;
+    info->genlayer_state = (unsigned int)std::stoul(os.str());
+  }
   return CAFE_OK;
 }
 
@@ -1004,6 +1132,61 @@ int cafe_sim_stats(cafe_sim *s, cafe_stats *st) {
   st->max_rows = v[STAT_MAXROWS];
   st->steps = v[STAT_STEPS];
   st->negative_dt = v[STAT_NEGDT];
+  st->sum_active = v[STAT_SUMNA];
+  st->sum_rows = v[STAT_SUMROWS];
+  st->launches = (unsigned long long)s->launches;
+  return CAFE_OK;
+}
+
+int cafe_sim_set_timing(cafe_sim *s, int on) {
+  if (!s) return fail(CAFE_E_ARG, "null handle");
+  CUDA_TRY(cudaSetDevice(s->device));
+  CUDA_TRY(cudaStreamSynchronize(s->stream));
+  resolve_phases(s);
+  s->timing = on != 0;
+  return CAFE_OK;
+}
+
+int cafe_sim_phase_times(cafe_sim *s, double *ms, long long *launches, int nphase, int reset) {
+  if (!s) return fail(CAFE_E_ARG, "null handle");
+  CUDA_TRY(cudaSetDevice(s->device));
+  CUDA_TRY(cudaStreamSynchronize(s->stream));
+  resolve_phases(s);
+  for (int p = 0; p < nphase && p < CAFE_NPHASE; ++p) {
+    if (ms) ms[p] = s->phase_ms[p];
+    if (launches) launches[p] = s->phase_launch[p];
+  }
+  if (reset) {
+    for (int p = 0; p < CAFE_NPHASE; ++p) {
+      s->phase_ms[p] = 0;
+      s->phase_launch[p] = 0;
+    }
+    s->launches = 0;
+  }
+  return CAFE_OK;
+}
+
+int cafe_sim_mark(cafe_sim *s, int slot) {
+  if (!s || slot < 0 || slot >= 8) return fail(CAFE_E_ARG, "bad mark slot");
+  CUDA_TRY(cudaSetDevice(s->device));
+  if (!s->marks[slot]) CUDA_TRY(cudaEventCreate(&s->marks[slot]));
+  CUDA_TRY(cudaEventRecord(s->marks[slot], s->stream));
+  return CAFE_OK;
+}
+
+int cafe_sim_elapsed(cafe_sim *s, int a, int b, double *ms) {
+  if (!s || !ms || a < 0 || a >= 8 || b < 0 || b >= 8 || !s->marks[a] || !s->marks[b])
+    return fail(CAFE_E_ARG, "bad mark slots");
+  CUDA_TRY(cudaEventSynchronize(s->marks[b]));
+  float f = 0.f;
+  CUDA_TRY(cudaEventElapsedTime(&f, s->marks[a], s->marks[b]));
+  *ms = f;
+  return CAFE_OK;
+}
+
+int cafe_sim_stream(cafe_sim *s, void **stream) {
+  if (!s || !stream) return fail(CAFE_E_ARG, "null argument");
+  *stream = (void *)s->stream;
   return CAFE_OK;
 }
 
@@ -1102,6 +1285,9 @@ int cafe_sim_upload_state(cafe_sim *s, const int32_t *gID, const int32_t *vState
   s->nGrain = ngrain;
   s->h_pinned[2] = ngrain;
   CUDA_TRY(cudaMemcpyAsync(s->D.ctr + CTR_NGRAIN, s->h_pinned + 2, sizeof(int), cudaMemcpyHostToDevice, s->stream));
+  CUDA_TRY(cudaMemsetAsync(s->D.ctr + CTR_NLIQ, 0, sizeof(int), s->stream));
+  s->full_k2 = true;
+  s->have_prev_box = false;
   s->initialized = true;
   return sim_sync(s);
 }

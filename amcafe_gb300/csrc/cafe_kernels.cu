@@ -31,9 +31,9 @@
 #define CAFE_LOOP_THREADS 512
 
 // ------------------------------------------------------------------ helpers
-__device__ __forceinline__ int cafe_hot(const CafeConsts &K, const CafeStepParams &P, int i, int j,
-                                        int k) {
-  return K.hot_cls[cafe_temp_class(K, P, i, j, k)];
+__device__ __forceinline__ int cafe_hot(const CafeDev &D, const CafeConsts &K, const CafeStepParams &P,
+                                        int i, int j, int k) {
+  return K.hot_cls[cafe_cls(D, P, i, j, k)];
 }
 
 // Moore neighbours in ascending linear-index order (Grid.C:399-414 + sort at
@@ -70,7 +70,8 @@ __global__ void k_melt(CafeDev D, CafeConsts K, CafeStepParams P) {
     long long r = t / bx;
     int j = P.lo[1] + (int)(r % by);
     int k = P.lo[2] + (int)(r / by);
-    int c = cafe_temp_class(K, P, i, j, k);
+    int c = cafe_temp_class_exact(K, P, i, j, k);
+    D.tcls[t] = (uint8_t)c;
     long long idx = (long long)K.nxy * k + (long long)K.nx * j + i;
     if (K.gt_cls[c]) D.buildj[idx] = 1;
     if (K.hot_cls[c]) {
@@ -90,8 +91,11 @@ __global__ void k_melt(CafeDev D, CafeConsts K, CafeStepParams P) {
 // ------------------------------------------------------------------ K: solid -> mushy
 // ConvertSolid1(1): solid cells with a liquid neighbour become mushy. In place
 // is equivalent to the reference's collect-then-apply: the test reads only
-// "neighbour == liquid", which this pass never changes.
-__global__ void k_solid2mushy(CafeDev D, CafeConsts K) {
+// "neighbour == liquid", which this pass never changes. Liquid cells can only
+// be (a) cells listed by the previous step's write-back, (b) cells of the
+// previous step's pool box, (c) cells of this step's pool box; the box kernel
+// covers (b) and (c) dilated by one cell, the list kernel (a).
+__global__ void k_solid2mushy_dense(CafeDev D, CafeConsts K) {
   long long base = ((long long)blockIdx.x * blockDim.x + threadIdx.x) * CAFE_CELLS_PER_THREAD;
   for (int c = 0; c < CAFE_CELLS_PER_THREAD; ++c) {
     long long idx = base + c;
@@ -107,24 +111,63 @@ __global__ void k_solid2mushy(CafeDev D, CafeConsts K) {
   }
 }
 
+__global__ void k_solid2mushy_box(CafeDev D, CafeConsts K, int x0, int x1, int y0, int y1, int z0, int z1) {
+  x0 = max(x0 - 1, 0); y0 = max(y0 - 1, 0); z0 = max(z0 - 1, 0);
+  x1 = min(x1 + 1, K.nx); y1 = min(y1 + 1, K.ny); z1 = min(z1 + 1, K.nz);
+  if (x1 <= x0 || y1 <= y0 || z1 <= z0) return;
+  long long bx = x1 - x0, by = y1 - y0, nbox = bx * by * (z1 - z0);
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < nbox;
+       t += (long long)gridDim.x * blockDim.x) {
+    int i = x0 + (int)(t % bx);
+    long long r = t / bx;
+    int j = y0 + (int)(r % by), k = z0 + (int)(r / by);
+    long long idx = (long long)K.nxy * k + (long long)K.nx * j + i;
+    if (D.state[idx] != 3) continue;
+    long long nb[26];
+    int n = cafe_moore(K, i, j, k, nb);
+    bool liq = false;
+    for (int a = 0; a < n && !liq; ++a) liq = (D.state[nb[a]] == 1);
+    if (liq) D.state[idx] = 2;
+  }
+}
+
+__global__ void k_solid2mushy_list(CafeDev D, CafeConsts K) {
+  int n = D.ctr[CTR_NLIQ];
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+    long long idx = D.liq[t];
+    if (D.state[idx] != 1) continue;
+    int i, j, k;
+    cafe_cell_xyz(K, idx, i, j, k);
+    long long nb[26];
+    int m = cafe_moore(K, i, j, k, nb);
+    for (int a = 0; a < m; ++a)
+      if (D.state[nb[a]] == 3) D.state[nb[a]] = 2;
+  }
+}
+
 // ------------------------------------------------------------------ active set
 __device__ __forceinline__ bool cafe_is_active(const CafeDev &D, const CafeConsts &K,
                                                const CafeStepParams &P, long long idx) {
   uint8_t s = D.state[idx];
+  if (s == 2) return true;
   int i, j, k;
   cafe_cell_xyz(K, idx, i, j, k);
-  int hot = cafe_hot(K, P, i, j, k);
-  if (s == 2 || (s == 1 && !hot)) return true;
+  int hot = cafe_hot(D, K, P, i, j, k);
+  if (s == 1) return !hot;
   if (!hot) return false;
-  long long nb[26];
-  int n = cafe_moore(K, i, j, k, nb);
-  for (int a = 0; a < n; ++a) {
-    uint8_t t = D.state[nb[a]];
-    if (t == 2) return true;
-    if (t == 1) {
-      int ni, nj, nk;
-      cafe_cell_xyz(K, nb[a], ni, nj, nk);
-      if (!cafe_hot(K, P, ni, nj, nk)) return true;
+  for (int dz = -1; dz <= 1; ++dz) {
+    int z = k + dz;
+    if (z < 0 || z >= K.nz) continue;
+    for (int dy = -1; dy <= 1; ++dy) {
+      int y = j + dy;
+      if (y < 0 || y >= K.ny) continue;
+      for (int dx = -1; dx <= 1; ++dx) {
+        int x = i + dx;
+        if (x < 0 || x >= K.nx || (dx == 0 && dy == 0 && dz == 0)) continue;
+        uint8_t t = D.state[(long long)K.nxy * z + (long long)K.nx * y + x];
+        if (t == 2) return true;
+        if (t == 1 && !cafe_hot(D, K, P, x, y, z)) return true;
+      }
     }
   }
   return false;
@@ -239,7 +282,7 @@ __global__ void k_gather(CafeDev D, CafeConsts K, CafeStepParams P) {
     D.a_cx[p] = D.cx[idx];
     D.a_cy[p] = D.cy[idx];
     D.a_cz[p] = D.cz[idx];
-    D.a_cls[p] = (uint8_t)cafe_temp_class(K, P, i, j, k);
+    D.a_cls[p] = (uint8_t)cafe_cls(D, P, i, j, k);
     long long nb[26];
     int n = cafe_moore(K, i, j, k, nb);
     int m = 0, liq = 0, cold = 1;
@@ -251,7 +294,7 @@ __global__ void k_gather(CafeDev D, CafeConsts K, CafeStepParams P) {
       if (D.state[nb[a]] == 1) ++liq;
       int ni, nj, nk;
       cafe_cell_xyz(K, nb[a], ni, nj, nk);
-      if (cafe_hot(K, P, ni, nj, nk)) cold = 0;
+      if (cafe_hot(D, K, P, ni, nj, nk)) cold = 0;
     }
     D.a_nn[p] = (uint8_t)m;
     D.a_liq[p] = liq;
@@ -730,6 +773,8 @@ __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
     atomicMax(&D.stat[STAT_MAXNA], (unsigned long long)s_na);
     atomicMax(&D.stat[STAT_MAXROWS], (unsigned long long)s_nrows);
     atomicAdd(&D.stat[STAT_STEPS], 1ULL);
+    atomicAdd(&D.stat[STAT_SUMNA], (unsigned long long)s_na);
+    atomicAdd(&D.stat[STAT_SUMROWS], (unsigned long long)s_nrows);
   }
 }
 
@@ -746,6 +791,10 @@ __global__ void k_writeback(CafeDev D) {
     D.cy[idx] = D.a_cy[p];
     D.cz[idx] = D.a_cz[p];
     D.pos_of[idx] = -1;
+    if (D.a_state[p] == 1) {
+      int t = atomicAdd(&D.ctr[CTR_NLIQ], 1);
+      D.liq[t] = (int32_t)idx;  // t < na <= act_cap = liq capacity
+    }
   }
 }
 
@@ -961,6 +1010,6 @@ __global__ void k_temperature(CafeConsts K, CafeStepParams P, double *T) {
        idx += (long long)gridDim.x * blockDim.x) {
     int i, j, k;
     cafe_cell_xyz(K, idx, i, j, k);
-    T[idx] = K.Tcls[cafe_temp_class(K, P, i, j, k)];
+    T[idx] = K.Tcls[cafe_temp_class_exact(K, P, i, j, k)];
   }
 }

@@ -1,0 +1,374 @@
+#!/usr/bin/env python3
+"""Throughput of AMCAFE's CA time step on GB300: voxel-updates per second.
+
+One step is one iteration of the reference's time loop (main1.C:62-93:
+AnalyticTempCurr + UpdateVoxels + UpdateLaser + layer bookkeeping) over the
+whole voxel box; one voxel-update is one box voxel advanced one step, so
+value = N_voxels * steps / time. The default workload is config 1
+(512x256x128 voxels at 2.5 um, four layers, bidirectional hatching;
+amcafe_gb300/decks/c1.in). Before timing, the run is advanced by --spinup
+steps (part of setup, untimed) so that the melt pool, its liquid trail and the
+solidification front are developed; then --warmup untimed steps; then --steps
+timed steps. The voxel state (about 700 MB for config 1) is larger than L2.
+
+Printed keys beyond the common contract:
+  e2e        the same metric through the C ABI with host buffers: the state is
+             uploaded from host memory before the steps and downloaded after,
+             and every step reads its summary (nGrain, flags) back to the host;
+  roofline   for the phase with the largest device time in the timed region,
+             its algorithmic bytes per launch over its mean launch time
+             (CUDA events on the engine's stream), against the measured HBM
+             copy bandwidth;
+  cpu_baseline  the CPU oracle (a single-threaded restatement of the
+             reference) resumed from the GPU state at the start of the timed
+             window, for a bounded wall-clock sample.
+`--impl reference` times the CPU restatement of the reference from the deck's
+initial state (the reference's own CPU code path; no GPU work).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    # name: (deck, default spin-up steps, description)
+    "c1": ("amcafe_gb300/decks/c1.in", 2000, "config 1: 512x256x128 voxels @2.5um, 4 layers, hatching 100um"),
+    "c2": ("amcafe_gb300/decks/c2.in", 1200, "config 2: 1024x1024x256 voxels @2.5um, 10 layers, 67 deg rotation"),
+    "c0": ("amcafe_gb300/decks/c0.in", 300, "config 0: 128x64x32 voxels @2.5um, single track"),
+}
+FALLBACK_HBM_GBS = 6800.0
+BYTES_DENSE_PER_VOXEL = 2   # read + write of the uint8 cell state per voxel-update
+BYTES_PER_FRONT_CELL = 74   # gID 4, extents 8, centroid 24, state 1; read and written
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def init_dist(ws):
+    if ws <= 1:
+        return None
+    import torch.distributed as dist
+
+    dist.init_process_group("gloo")
+    return dist
+
+
+def reduce_max(dist, v):
+    if dist is None:
+        return v
+    import torch
+
+    t = torch.tensor([float(v)])
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples every 200 ms while active."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.fh, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.fh.close()
+        sm, smax, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, f[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def hbm_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        d = json.load(open(path))
+        for k in ("hbm_gbs", "hbm_GBs", "hbm"):
+            if k in d:
+                v = d[k]
+                return float(v["value"] if isinstance(v, dict) else v), "measured"
+    except Exception:
+        pass
+    return FALLBACK_HBM_GBS, "fallback"
+
+
+def committed_traffic(workload, phase):
+    """DRAM bytes per launch of `phase` from a committed ncu summary, or None."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        d = json.load(open(path))
+        return d.get(workload, {}).get(phase)
+    except Exception:
+        return None
+
+
+def cpu_baseline(deck, info, state, ctheta, nvox, seconds):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import cafe_oracle as orc
+
+    orc.set_budget(seconds)
+    _, sec, st = orc.run_window(deck, info, state, ctheta, 1 << 30, libm=orc.LIBM_GLIBC)
+    orc.set_budget(0)
+    steps = st["steps"]
+    return {"value": nvox * steps / sec if sec > 0 else None, "unit": "voxel-updates/s", "cores": 1,
+            "kind": "port",
+            "sample": "%d steps from step %d of the same run (GPU state handed over), one thread, "
+                      "glibc libm, %.1f s" % (steps, info["steps"], sec)}
+
+
+def run_reference(args, ws, rank):
+    if rank != 0:
+        return 0
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import cafe_oracle as orc
+
+    deck_rel, _, desc = WORKLOADS[args.workload]
+    deck = os.path.join(ROOT, deck_rel)
+    budget = args.ref_seconds
+    vals = []
+    steps_total, sec_total = 0, 0.0
+    t_wall0 = time.time()
+    # each step of this arm is a bounded sample: the loop from the deck's start
+    orc.set_budget(budget)
+    st = orc.run(deck, "", max_steps=max(1, args.warmup + args.steps), dump_stride=0, libm=orc.LIBM_GLIBC)
+    orc.set_budget(0)
+    sec = st["loop_ns"] * 1e-9
+    nvox = st["ncell"]
+    steps_total, sec_total = st["steps"], sec
+    value = nvox * steps_total / sec_total if sec_total > 0 else None
+    out = {
+        "impl": "reference",
+        "metric": "voxel-updates/s",
+        "value": value,
+        "unit": "voxel-updates/s",
+        "n_gpus": ws,
+        "steps": steps_total,
+        "warmup": 0,
+        "ms_per_step": 1e3 * sec_total / max(1, steps_total),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic (seeded Voronoi microstructure and laser path from the deck)",
+        "config": {"workload": args.workload, "deck": deck_rel, "description": desc,
+                   "window": "first %d steps from the deck's initial state" % steps_total},
+        "cpu_baseline": {"value": value, "unit": "voxel-updates/s", "cores": 1, "kind": "port",
+                         "sample": "steps 1..%d of %s from its initial state, one thread, glibc libm, "
+                                   "%.1f s loop time (init excluded)" % (steps_total, args.workload, sec_total)},
+        "e2e": {"value": value, "unit": "voxel-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "wall_s": time.time() - t_wall0,
+    }
+    print(json.dumps(out))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="c1", choices=sorted(WORKLOADS))
+    ap.add_argument("--spinup", type=int, default=None)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--ref-seconds", type=float, default=60.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+    ws, rank, local = dist_env()
+    if args.impl == "reference":
+        return run_reference(args, ws, rank)
+    dist = init_dist(ws)
+    from amcafe_gb300 import Simulation
+
+    deck_rel, spin_default, desc = WORKLOADS[args.workload]
+    deck = os.path.join(ROOT, deck_rel)
+    spinup = spin_default if args.spinup is None else args.spinup
+    t_setup = time.time()
+    sim = Simulation(deck, device=local)
+    sim.InitializeVoxels()
+    sim.begin()
+    if spinup > 0:
+        sim.run(spinup)
+    for _ in range(args.warmup):
+        sim.step()
+    sim.synchronize()
+    setup_s = time.time() - t_setup
+    info0 = sim.info()
+    nvox = info0["nx"] * info0["ny"] * info0["nz"]
+    snapshot = None
+    if rank == 0 and not args.no_cpu:
+        snapshot = (sim.info(), sim.state(), sim.ctheta())
+
+    # ---- timed region: device time between two events on the engine's stream
+    stats0 = sim.stats()
+    sim.set_timing(True)
+    sim.phase_times(reset=True)
+    clocks = ClockSampler(local)
+    barrier(dist)
+    sim.synchronize()
+    clocks.start()
+    sim.mark(0)
+    t0 = time.time()
+    done = False
+    k = 0
+    while k < args.steps and not done:
+        done = sim.step()
+        k += 1
+    sim.mark(1)
+    ms = sim.elapsed_ms(0, 1)
+    sim.synchronize()
+    wall = time.time() - t0
+    clk = clocks.stop()
+    phases = sim.phase_times()
+    stats1 = sim.stats()
+    sim.set_timing(False)
+    ms = reduce_max(dist, ms)
+    barrier(dist)
+    value = ws * nvox * k / (ms * 1e-3)
+
+    # ---- roofline of the dominant phase
+    peak, peak_src = hbm_peak()
+    dom = max(phases, key=lambda p: phases[p][0])
+    dom_ms, dom_launches = phases[dom]
+    steps_done = max(1, stats1["steps"] - stats0["steps"])
+    avg_na = (stats1["sum_active"] - stats0["sum_active"]) / steps_done
+    if dom in ("events", "writeback", "gather"):
+        bytes_per_launch = BYTES_PER_FRONT_CELL * avg_na
+    else:
+        bytes_per_launch = BYTES_DENSE_PER_VOXEL * nvox
+    launches_dom = max(1, dom_launches)
+    per_launch_ms = dom_ms / launches_dom if dom != "events" else dom_ms / steps_done
+    achieved = bytes_per_launch / (per_launch_ms * 1e-3) / 1e9
+    step_bytes = BYTES_DENSE_PER_VOXEL * nvox + BYTES_PER_FRONT_CELL * avg_na
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": committed_traffic(args.workload, dom),
+                "kernel": {"events": "k_event_loop", "classify": "k_active_count/k_active_scatter",
+                           "gather": "k_gather", "melt": "k_melt", "writeback": "k_writeback"}.get(dom, dom),
+                "phase": dom, "peak_source": peak_src,
+                "step_achieved_GBs": step_bytes * k / (ms * 1e-3) / 1e9}
+
+    # ---- end to end through the C ABI with host buffers
+    e2e = None
+    if not args.no_e2e and not done:
+        st_host = sim.state()
+        cth_host = sim.ctheta()
+        h2d = sum(a.nbytes for a in (st_host["gID"], st_host["vState"], st_host["extents"], st_host["centroid"])) \
+            + cth_host.nbytes
+        d2h = h2d - cth_host.nbytes + st_host["buildj"].nbytes
+        ke = args.steps
+        sim.synchronize()
+        barrier(dist)
+        te0 = time.time()
+        sim.upload_state(st_host["gID"], st_host["vState"], st_host["extents"], st_host["centroid"], cth_host)
+        n_e, done_e = 0, False
+        per_step_d2h = 0
+        while n_e < ke and not done_e:
+            done_e = sim.step()
+            inf = sim.info()  # per-step result read back to the host
+            per_step_d2h += 8
+            n_e += 1
+        out_state = sim.state()
+        te = time.time() - te0
+        te = reduce_max(dist, te)
+        e2e = {"value": ws * nvox * n_e / te, "unit": "voxel-updates/s",
+               "h2d_bytes_per_step": int(h2d / max(1, n_e)),
+               "d2h_bytes_per_step": int(d2h / max(1, n_e) + per_step_d2h / max(1, n_e)),
+               "steps": n_e}
+        del out_state, inf
+
+    cpu = None
+    if snapshot is not None:
+        cpu = cpu_baseline(deck, snapshot[0], snapshot[1], snapshot[2], nvox, args.cpu_seconds)
+    if rank == 0:
+        ev = stats1["events"] - stats0["events"]
+        out = {
+            "metric": "voxel-updates/s",
+            "value": value,
+            "unit": "voxel-updates/s",
+            "n_gpus": ws,
+            "steps": k,
+            "warmup": args.warmup,
+            "ms_per_step": ms / k,
+            "higher_is_better": True,
+            "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": "f64",
+            "data": "synthetic (seeded Voronoi microstructure and laser path from the deck)",
+            "config": {"workload": args.workload, "deck": deck_rel, "description": desc,
+                       "voxels": nvox, "spinup_steps": spinup, "window_start_step": info0["steps"],
+                       "l2": "state larger than L2 (inputs > 129 MB)",
+                       "parallelism": "replicas%d" % ws},
+            "e2e": e2e,
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+            "clocks": clk,
+            "gpu_launches": int(stats1["launches"]),
+            "events_per_step": ev / max(1, k),
+            "phase_ms": {p: round(v[0], 3) for p, v in phases.items()},
+            "wall_s_timed": wall,
+            "setup_s": setup_s,
+        }
+        print(json.dumps(out))
+    sim.close()
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

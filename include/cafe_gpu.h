@@ -47,6 +47,8 @@ typedef struct {
   int Nzh;         /* BasePlate::Nzh */
   int done;        /* main1.C loop condition reached (indlayer > nlayerTot) */
   long long steps; /* loop iterations executed */
+  double gth;      /* Grid::gth, current rotation of the laser grid */
+  unsigned int genlayer_state; /* VoxelsCA::genlayer engine state (minstd_rand0) */
 } cafe_info;
 
 typedef struct {
@@ -56,6 +58,9 @@ typedef struct {
   unsigned long long max_rows;     /* largest frontier (capturing cells) */
   unsigned long long steps;        /* UpdateVoxels calls */
   unsigned long long negative_dt;  /* events with a negative capture time */
+  unsigned long long sum_active;   /* sum over steps of the active-list length */
+  unsigned long long sum_rows;     /* sum over steps of the frontier size */
+  unsigned long long launches;     /* kernels launched by this handle since the last phase reset */
 } cafe_stats;
 
 /* Grid::Grid (Grid.C:15-109, deck parse Grid.C:165-318) + Partition::
@@ -97,6 +102,27 @@ int cafe_sim_run(cafe_sim *sim, long long max_steps, long long *steps_done);
 int cafe_sim_synchronize(cafe_sim *sim);
 
 int cafe_sim_info(cafe_sim *sim, cafe_info *info);
+
+/* Device-time accounting, for profiling: phases of one step, each bracketed
+ * by CUDA events on the handle's stream when timing is on. */
+enum {
+  CAFE_PH_MELT = 0,      /* TempField::AnalyticTempCurr + SetLiquid3 on the pool box */
+  CAFE_PH_CLASSIFY = 1,  /* ConvertSolid1(1) + active-set compaction */
+  CAFE_PH_GATHER = 2,    /* active copies, neighbour lists, frontier numerators */
+  CAFE_PH_EVENTS = 3,    /* the capture/nucleation event loop */
+  CAFE_PH_WRITEBACK = 4, /* write-back + ConvertSolid1(0) */
+  CAFE_PH_LAYER = 5,     /* CleanLayer / AddLayer1 device work */
+  CAFE_NPHASE = 8
+};
+int cafe_sim_set_timing(cafe_sim *sim, int on);
+/* Accumulated milliseconds and kernel launches per phase (nphase entries). */
+int cafe_sim_phase_times(cafe_sim *sim, double *ms, long long *launches, int nphase, int reset);
+/* The CUDA stream (cudaStream_t) all work of this handle is queued on. */
+int cafe_sim_stream(cafe_sim *sim, void **stream);
+/* Records CUDA event `slot` (0..7) on the handle's stream; cafe_sim_elapsed
+ * waits for slot b and returns the device time between slots a and b. */
+int cafe_sim_mark(cafe_sim *sim, int slot);
+int cafe_sim_elapsed(cafe_sim *sim, int a, int b, double *ms);
 int cafe_sim_stats(cafe_sim *sim, cafe_stats *stats);
 
 /* VoxelsCA public fields gID, vState, extents, centroidOct (x,y,z interleaved,

@@ -45,6 +45,7 @@
 #include <sstream>
 #include <string>
 #include <vector>
+#include <time.h>
 
 #include "../amcafe_gb300/csrc/cafe_crmath.h"
 
@@ -1189,7 +1190,12 @@ static int setup(State &S, const char *deck) {
 
 using namespace orc;
 
+// Wall-clock budget for the loops below (0 = none); set by cafe_oracle_set_budget.
+static double g_max_seconds = 0.0;
+
 extern "C" {
+
+void cafe_oracle_set_budget(double seconds) { g_max_seconds = seconds; }
 
 // Runs the whole main1.C time loop on deck `deck`. dump_stride: 0 = write only
 // the initial and final records, k > 0 = also every k-th step. max_steps > 0
@@ -1211,6 +1217,8 @@ int cafe_oracle_run(const char *deck, const char *dump_path, long max_steps, int
   update_laser(g);
   dump_state(fp, 0, S);
   long nstep = 0;
+  struct timespec t0, t1;
+  clock_gettime(CLOCK_MONOTONIC, &t0);
   while (!bcheck) {
     S.tf_tInd = int(std::round(g.time / S.DelT));
     analytic_temp(S);
@@ -1226,7 +1234,12 @@ int cafe_oracle_run(const char *deck, const char *dump_path, long max_steps, int
     S.n_steps = nstep;
     if (dump_stride > 0 && nstep % dump_stride == 0) dump_state(fp, 1, S);
     if (max_steps > 0 && nstep >= max_steps) break;
+    if (g_max_seconds > 0) {
+      clock_gettime(CLOCK_MONOTONIC, &t1);
+      if ((t1.tv_sec - t0.tv_sec) + 1e-9 * (t1.tv_nsec - t0.tv_nsec) > g_max_seconds) break;
+    }
   }
+  clock_gettime(CLOCK_MONOTONIC, &t1);
   if (bcheck) {
     clean_layer(S);
     dump_state(fp, 2, S);
@@ -1242,7 +1255,104 @@ int cafe_oracle_run(const char *deck, const char *dump_path, long max_steps, int
     stats[4] = S.max_front;
     stats[5] = S.nGrain;
     stats[6] = S.N;
+    stats[7] = (long long)((t1.tv_sec - t0.tv_sec) * 1000000000LL + (t1.tv_nsec - t0.tv_nsec));
   }
+  return 0;
+}
+
+// Grid/TempField/VoxelsCA scalars of a running simulation (for resuming).
+struct cafe_oracle_window {
+  int isp, inewscanflg, inewlayerflg, indlayer, ilaserLoc, tInd;
+  double time, gth;
+  unsigned int genlayer_state;
+  int ngrain;
+};
+
+// Runs `nsteps` loop iterations of `deck` starting from the given state (the
+// arrays have N = nx*ny*nz entries; centroid holds x,y,z per cell), without
+// the initial baseplate/layer construction. Wall seconds of the loop go to
+// *seconds. The final state is written back into the arrays (if non-NULL).
+int cafe_oracle_run_window(const char *deck, const cafe_oracle_window *w, int32_t *gID, int32_t *vState,
+                           double *ext, double *cen, int32_t *buildj, double *cth, long nsteps,
+                           int libm_mode, double *seconds, long long *stats, int *ngrain_out) {
+  g_libm.mode = libm_mode;
+  State S;
+  std::string err;
+  if (!read_deck(deck, S.g, err)) {
+    std::fprintf(stderr, "oracle: %s: %s\n", deck, err.c_str());
+    return 1;
+  }
+  grid_derive(S.g);
+  S.nx = S.g.nX[0];
+  S.ny = S.g.nX[1];
+  S.nz = S.g.nX[2];
+  S.nxy = S.nx * S.ny;
+  S.N = S.nxy * S.nz;
+  S.Nzh = std::min(S.g.nX[2], int(std::ceil(S.g.bpH * .9999 / S.g.dX[2])));
+  init_tempfield(S);
+  Grid &g = S.g;
+  g.isp = w->isp;
+  g.inewscanflg = w->inewscanflg;
+  g.inewlayerflg = w->inewlayerflg;
+  g.indlayer = w->indlayer;
+  g.ilaserLoc = w->ilaserLoc;
+  g.tInd = w->tInd;
+  g.time = w->time;
+  g.gth = w->gth;
+  {
+    double gmid0 = g.LX[0] / 2., gmid1 = g.LX[1] / 2.;
+    for (int k = 0; k < g.NpT; ++k) {
+      g.lcoor2[2 * k] = std::cos(g.gth) * (g.lcoor[2 * k] - gmid0) - std::sin(g.gth) * (g.lcoor[2 * k + 1] - gmid1) + gmid0;
+      g.lcoor2[2 * k + 1] = std::sin(g.gth) * (g.lcoor[2 * k] - gmid0) + std::cos(g.gth) * (g.lcoor[2 * k + 1] - gmid1) + gmid1;
+    }
+  }
+  S.genlayer.seed(w->genlayer_state);
+  S.nGrain = w->ngrain;
+  S.gID.assign(gID, gID + S.N);
+  S.vState.assign(vState, vState + S.N);
+  S.buildj.assign(buildj, buildj + S.N);
+  S.extents.assign(ext, ext + S.N);
+  S.cen.assign(cen, cen + 3 * (size_t)S.N);
+  S.temp.assign(S.N, 0.0);
+  S.cTheta.assign(cth, cth + 4 * (size_t)w->ngrain);
+  int nlayerTot = int(std::ceil((double)(g.nX[2] - S.Nzh) / (double)g.nZlayer));
+  struct timespec t0, t1;
+  clock_gettime(CLOCK_MONOTONIC, &t0);
+  long n = 0;
+  bool bcheck = false;
+  while (!bcheck && n < nsteps) {
+    if (g_max_seconds > 0) {
+      clock_gettime(CLOCK_MONOTONIC, &t1);
+      if ((t1.tv_sec - t0.tv_sec) + 1e-9 * (t1.tv_nsec - t0.tv_nsec) > g_max_seconds) break;
+    }
+    S.tf_tInd = int(std::round(g.time / S.DelT));
+    analytic_temp(S);
+    update_voxels(S);
+    update_laser(g);
+    bcheck = g.indlayer > nlayerTot;
+    if (g.inewlayerflg == 1) clean_layer(S);
+    g.time += S.DelT;
+    g.tInd += 1;
+    if (g.inewlayerflg == 1) add_layer(S);
+    ++n;
+  }
+  clock_gettime(CLOCK_MONOTONIC, &t1);
+  if (seconds) *seconds = (t1.tv_sec - t0.tv_sec) + 1e-9 * (t1.tv_nsec - t0.tv_nsec);
+  if (stats) {
+    stats[0] = n;
+    stats[1] = S.n_events;
+    stats[2] = S.n_nuc;
+    stats[3] = S.max_na;
+    stats[4] = S.max_front;
+    stats[5] = S.nGrain;
+    stats[6] = S.N;
+  }
+  if (ngrain_out) *ngrain_out = S.nGrain;
+  std::memcpy(gID, S.gID.data(), S.N * sizeof(int32_t));
+  std::memcpy(vState, S.vState.data(), S.N * sizeof(int32_t));
+  std::memcpy(buildj, S.buildj.data(), S.N * sizeof(int32_t));
+  std::memcpy(ext, S.extents.data(), S.N * sizeof(double));
+  std::memcpy(cen, S.cen.data(), 3 * (size_t)S.N * sizeof(double));
   return 0;
 }
 

@@ -35,6 +35,40 @@ def load():
     return _lib
 
 
+class Window(ctypes.Structure):
+    _fields_ = [("isp", ctypes.c_int), ("inewscanflg", ctypes.c_int), ("inewlayerflg", ctypes.c_int),
+                ("indlayer", ctypes.c_int), ("ilaserLoc", ctypes.c_int), ("tInd", ctypes.c_int),
+                ("time", ctypes.c_double), ("gth", ctypes.c_double), ("genlayer_state", ctypes.c_uint),
+                ("ngrain", ctypes.c_int)]
+
+
+def run_window(deck, info, state, ctheta, nsteps, libm=LIBM_CR):
+    """Resumes the loop from a GPU state (info from Simulation.info(), state
+    from Simulation.state()); returns (new_state, seconds, stats). The arrays
+    in `state` are copied, not modified."""
+    import numpy as np
+
+    lib = load()
+    f = lib.cafe_oracle_run_window
+    i32p, f64p = ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_double)
+    f.argtypes = [ctypes.c_char_p, ctypes.POINTER(Window), i32p, i32p, f64p, f64p, i32p, f64p, ctypes.c_long,
+                  ctypes.c_int, f64p, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_int)]
+    w = Window(info["isp"], info["inewscanflg"], info["inewlayerflg"], info["indlayer"], info["ilaserLoc"],
+               info["tInd"], info["time"], info["gth"], info["genlayer_state"], info["nGrain"])
+    st = {k: np.array(v, copy=True) for k, v in state.items()}
+    cth = np.ascontiguousarray(ctheta, np.float64)
+    sec = ctypes.c_double(0)
+    stats = (ctypes.c_longlong * 8)()
+    ng = ctypes.c_int(0)
+    rc = f(str(deck).encode(), ctypes.byref(w), st["gID"].ctypes.data_as(i32p), st["vState"].ctypes.data_as(i32p),
+           st["extents"].ctypes.data_as(f64p), st["centroid"].ctypes.data_as(f64p), st["buildj"].ctypes.data_as(i32p),
+           cth.ctypes.data_as(f64p), int(nsteps), libm, ctypes.byref(sec), stats, ctypes.byref(ng))
+    if rc != 0:
+        raise RuntimeError("oracle window run failed")
+    keys = ("steps", "events", "nucleations", "max_active", "max_front", "nGrain", "ncell")
+    return st, sec.value, dict(zip(keys, list(stats)[:7]))
+
+
 def run(deck, dump_path="", max_steps=-1, dump_stride=1, libm=LIBM_GLIBC, perturb_p=0.0, perturb_seed=0):
     """Runs the main1.C loop on `deck`; returns a stats dict."""
     st = (ctypes.c_longlong * 8)()
@@ -42,5 +76,12 @@ def run(deck, dump_path="", max_steps=-1, dump_stride=1, libm=LIBM_GLIBC, pertur
                                 perturb_p, perturb_seed, st)
     if rc != 0:
         raise RuntimeError("oracle run failed on %s" % deck)
-    keys = ("steps", "events", "nucleations", "max_active", "max_front", "nGrain", "ncell")
-    return dict(zip(keys, list(st)[:7]))
+    keys = ("steps", "events", "nucleations", "max_active", "max_front", "nGrain", "ncell", "loop_ns")
+    return dict(zip(keys, list(st)[:8]))
+
+
+def set_budget(seconds):
+    """Wall-clock limit (s) for the oracle's loops; 0 = none."""
+    lib = load()
+    lib.cafe_oracle_set_budget.argtypes = [ctypes.c_double]
+    lib.cafe_oracle_set_budget(float(seconds))
