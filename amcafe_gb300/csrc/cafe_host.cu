@@ -915,7 +915,11 @@ int cafe_sim_temperature(cafe_sim *s) {
     s->owned.push_back(s->D.tcls);
     s->D.tcls_cap = cap;
   }
-  if (nbox > 0) k_melt<<<grid_blocks(nbox, 256, s), 256, 0, s->stream>>>(s->D, s->K, P);
+  if (nbox > 0) {
+    PhaseScope ps(s, CAFE_PH_MELT);
+    k_melt<<<grid_blocks(nbox, 256, s), 256, 0, s->stream>>>(s->D, s->K, P);
+    LAUNCHED(CAFE_PH_MELT, 1);
+  }
   CUDA_TRY(cudaGetLastError());
   // end-of-scan check (TempField.C:199-216), only when the laser is outside the grid box
   const int *isv = s->ispvec.data();

@@ -153,8 +153,8 @@ __device__ __forceinline__ bool cafe_is_active(const CafeDev &D, const CafeConst
   int i, j, k;
   cafe_cell_xyz(K, idx, i, j, k);
   int hot = cafe_hot(D, K, P, i, j, k);
-  if (s == 1) return !hot;
-  if (!hot) return false;
+  if (!hot) return s == 1;  // undercooled liquid; a cell below the liquidus is active only as such
+  // a cell at/above the liquidus is active when a neighbour is mushy or undercooled liquid
   for (int dz = -1; dz <= 1; ++dz) {
     int z = k + dz;
     if (z < 0 || z >= K.nz) continue;
