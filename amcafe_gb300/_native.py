@@ -18,7 +18,7 @@ EXPORTS = (
     "cafe_sim_run", "cafe_sim_synchronize", "cafe_sim_info", "cafe_sim_stats",
     "cafe_sim_download_state", "cafe_sim_download_temperature", "cafe_sim_download_ctheta",
     "cafe_sim_upload_state", "cafe_last_error", "cafe_sim_set_timing", "cafe_sim_phase_times",
-    "cafe_sim_stream", "cafe_sim_mark", "cafe_sim_elapsed",
+    "cafe_sim_stream", "cafe_sim_mark", "cafe_sim_elapsed", "cafe_clean_layer_noalloc",
 )
 PHASES = ("melt", "classify", "gather", "events", "writeback", "layer")
 NPHASE = 8
@@ -86,6 +86,7 @@ def load():
         "cafe_sim_stream": (I, [P, ctypes.POINTER(P)]),
         "cafe_sim_mark": (I, [P, I]),
         "cafe_sim_elapsed": (I, [P, I, I, ctypes.POINTER(D)]),
+        "cafe_clean_layer_noalloc": (I, [P, LL, P, I, ctypes.POINTER(I), P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

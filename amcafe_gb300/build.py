@@ -49,7 +49,8 @@ def build_engine(force=False, verbose=False):
     os.makedirs(LIB_DIR, exist_ok=True)
     if not force and not _stale(LIB, _sources()):
         return LIB
-    cmd = [_nvcc()] + NVCC_FLAGS + [os.path.join(CSRC, "cafe_host.cu"), "-o", LIB + ".tmp"]
+    cmd = [_nvcc()] + NVCC_FLAGS + [os.path.join(CSRC, "cafe_host.cu"), os.path.join(CSRC, "cafe_noalloc.cu"),
+                                    "-o", LIB + ".tmp"]
     if verbose:
         print(" ".join(cmd))
     subprocess.run(cmd, check=True)

@@ -343,6 +343,9 @@ int dalloc(T **p, size_t n, std::vector<void *> &owned) {
 
 }  // namespace
 
+// Lets the other translation unit of the library (cafe_noalloc.cu) report errors.
+void cafe_internal_set_error(const char *msg) { g_last_error = msg ? msg : ""; }
+
 struct cafe_sim {
   GridH g;
   int device = 0;

@@ -139,6 +139,25 @@ int cafe_sim_upload_state(cafe_sim *sim, const int32_t *gID, const int32_t *vSta
                           const double *extents, const double *centroid, const double *ctheta,
                           int ngrain);
 
+/* Allocation-free CleanLayer renumbering on caller-owned device arrays. No
+ * counterpart in the reference: it serves callers that cannot go to the CUDA
+ * allocator mid-run (device memory owned by their own pool, or no tolerance
+ * for the device-wide synchronisation of cudaFree). Same result as
+ * cafe_sim_clean_layer: grains with no cells are dropped, the rest renumbered
+ * 1..k in their old order, gid[] remapped in place and ctheta[] (4 doubles per
+ * grain) packed in place; *ngrain_out receives k. gid and ctheta are device
+ * pointers; stream is a cudaStream_t (NULL = legacy default stream). It calls
+ * no cudaMalloc/cudaFree: its scratch is one file-scope device array sized for
+ * CAFE_NOALLOC_MAX_GRAINS grains (about 10.5 MB, held by every GPU that loads
+ * the library until exit); larger ngrain is rejected with CAFE_E_CAPACITY. The
+ * first call on a device looks up that array's device address, so make the
+ * first call outside any stream capture. All calls share the scratch: calls
+ * whose GPU work overlaps race and must be serialised by the caller. The call
+ * waits for its own work before returning. */
+#define CAFE_NOALLOC_MAX_GRAINS (1 << 18)
+int cafe_clean_layer_noalloc(int32_t *gid, long long ncell, double *ctheta, int ngrain,
+                             int *ngrain_out, void *stream);
+
 const char *cafe_last_error(void);
 
 #ifdef __cplusplus
