@@ -1,0 +1,66 @@
+"""Generates tests/golden/*.npz from the reference itself.
+
+Runs oracle/_ref/cafe_ref_dump (AMCAFE's own sources built with single-rank
+shims; see oracle/Makefile) on each deck in tests/golden/decks and stores, per
+dumped record, SHA-256 digests of the integer fields and sums of the float
+fields, plus the complete arrays of the last record. Needs the reference
+checkout (to build oracle/_ref); run from the repository root:
+    make -C oracle ref && python tests/golden/make_golden.py
+"""
+import hashlib
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+from cafe_dump import read_dump  # noqa: E402
+
+REF = os.path.join(ROOT, "oracle", "_ref", "cafe_ref_dump")
+# deck, max steps (-1 = whole run), keep every k-th record
+DECKS = [("track_r0", -1, 1), ("track_nuc", -1, 1), ("layers_rot", -1, 5), ("c0_small", 160, 10)]
+
+
+def digest(a):
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def summarize(recs, stride):
+    keep = [i for i in range(len(recs)) if i == 0 or i == len(recs) - 1 or i % stride == 0]
+    out = {"index": np.array(keep)}
+    for f in ("tag", "tInd", "nGrain", "isp", "indlayer", "inewlayerflg", "inewscanflg"):
+        out[f] = np.array([recs[i][f] for i in keep])
+    for f in ("gID", "vState", "buildj"):
+        out["sha_" + f] = np.array([digest(recs[i][f]) for i in keep])
+    for f in ("extents", "centroid", "temp", "cTheta"):
+        out["sum_" + f] = np.array([np.nansum(recs[i][f]) for i in keep])
+    last = recs[-1]
+    for f in ("gID", "vState", "buildj", "extents", "centroid", "temp", "cTheta"):
+        out["last_" + f] = last[f]
+    return out
+
+
+def main():
+    if not os.path.exists(REF):
+        sys.exit("build the reference first: make -C oracle ref")
+    for name, nsteps, stride in DECKS:
+        deck = os.path.join(HERE, "decks", name + ".in")
+        with tempfile.TemporaryDirectory() as td:
+            dump = os.path.join(td, "ref.bin")
+            cmd = [REF, deck, dump] + ([str(nsteps)] if nsteps > 0 else [])
+            subprocess.run(cmd, check=True, stdout=subprocess.DEVNULL)
+            recs = read_dump(dump)
+        data = summarize(recs, stride)
+        data["nsteps"] = np.array(nsteps)
+        data["stride"] = np.array(stride)
+        data["nrec"] = np.array(len(recs))
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **data)
+        print(name, len(recs), "records")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,68 @@
+"""The CPU oracle against the reference itself.
+
+tests/golden/*.npz were produced by the reference's own sources (oracle/_ref,
+built from AMCAFE src/src-mpi with single-rank shims; tests/golden/
+make_golden.py). The oracle restatement with glibc libm must reproduce every
+dumped record: integer fields bit for bit (SHA-256), float fields to 1e-12
+relative (bit-exact on the machine that made the fixtures).
+The correctly-rounded-libm mode (the arithmetic the GPU uses) must reproduce
+the integer fields too on these decks.
+"""
+import hashlib
+import os
+
+import numpy as np
+import pytest
+
+import cafe_oracle as orc
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+DECKS = ["track_r0", "track_nuc", "layers_rot", "c0_small"]
+
+
+def _digest(a):
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def _rel(a, b):
+    a, b = float(a), float(b)
+    return 0.0 if a == b else abs(a - b) / max(abs(b), 1e-300)
+
+
+def _check(name, libm, tmp_path, check_floats):
+    g = np.load(os.path.join(HERE, "golden", name + ".npz"))
+    nsteps, stride = int(g["nsteps"]), int(g["stride"])
+    dump = str(tmp_path / (name + ".bin"))
+    orc.run(os.path.join(HERE, "golden", "decks", name + ".in"), dump, max_steps=nsteps, dump_stride=stride,
+            libm=libm)
+    recs = orc.read_dump(dump)
+    assert len(recs) == len(g["index"]), "%s: %d records vs %d in the fixture" % (name, len(recs), len(g["index"]))
+    for j, r in enumerate(recs):
+        where = "%s record %d" % (name, int(g["index"][j]))
+        for f in ("tag", "tInd", "nGrain", "isp", "indlayer", "inewlayerflg", "inewscanflg"):
+            assert r[f] == int(g[f][j]), "%s: %s %s vs %s" % (where, f, r[f], g[f][j])
+        for f in ("gID", "vState", "buildj"):
+            assert _digest(r[f]) == str(g["sha_" + f][j]), "%s: %s differs from the reference" % (where, f)
+        if check_floats:
+            for f in ("extents", "centroid", "temp", "cTheta"):
+                assert _rel(np.nansum(r[f]), g["sum_" + f][j]) <= 1e-12, "%s: sum of %s" % (where, f)
+    last = recs[-1]
+    for f in ("gID", "vState", "buildj"):
+        assert np.array_equal(last[f], g["last_" + f]), name
+    if check_floats:
+        for f in ("extents", "centroid", "temp", "cTheta"):
+            a, b = last[f], g["last_" + f]
+            same = (a == b) | (np.isnan(a) & np.isnan(b))
+            if not same.all():
+                d = np.abs(a - b)[~same] / np.maximum(np.abs(b)[~same], 1e-300)
+                assert d.max() <= 1e-12, "%s: %s rel diff %g" % (name, f, d.max())
+
+
+@pytest.mark.parametrize("name", DECKS)
+def test_oracle_glibc_reproduces_reference(name, tmp_path):
+    _check(name, orc.LIBM_GLIBC, tmp_path, check_floats=True)
+
+
+@pytest.mark.parametrize("name", DECKS)
+def test_oracle_correctly_rounded_libm_keeps_reference_integers(name, tmp_path):
+    _check(name, orc.LIBM_CR, tmp_path, check_floats=False)
