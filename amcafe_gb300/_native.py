@@ -26,7 +26,7 @@ NPHASE = 8
 
 class CafeOptions(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int), ("active_capacity", ctypes.c_longlong),
-                ("grain_capacity", ctypes.c_longlong)]
+                ("grain_capacity", ctypes.c_longlong), ("event_scan", ctypes.c_int)]
 
 
 class CafeInfo(ctypes.Structure):
@@ -43,7 +43,8 @@ class CafeStats(ctypes.Structure):
                 ("max_active", ctypes.c_ulonglong), ("max_rows", ctypes.c_ulonglong),
                 ("steps", ctypes.c_ulonglong), ("negative_dt", ctypes.c_ulonglong),
                 ("sum_active", ctypes.c_ulonglong), ("sum_rows", ctypes.c_ulonglong),
-                ("launches", ctypes.c_ulonglong)]
+                ("launches", ctypes.c_ulonglong), ("exact_scan_steps", ctypes.c_ulonglong),
+                ("row_evaluations", ctypes.c_ulonglong)]
 
 
 _lib = None

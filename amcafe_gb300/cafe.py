@@ -30,10 +30,10 @@ def _ptr(a, ct):
 
 
 class Simulation:
-    def __init__(self, deck, device=0, active_capacity=0, grain_capacity=0):
+    def __init__(self, deck, device=0, active_capacity=0, grain_capacity=0, event_scan=0):
         self._lib = load()
         self._h = ctypes.c_void_p()
-        opt = CafeOptions(device, active_capacity, grain_capacity)
+        opt = CafeOptions(device, active_capacity, grain_capacity, event_scan)
         check(self._lib.cafe_sim_create(str(deck).encode(), ctypes.byref(opt), ctypes.byref(self._h)))
         inf = self.info()
         self.shape = (inf["nz"], inf["ny"], inf["nx"])

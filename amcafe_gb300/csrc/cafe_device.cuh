@@ -93,6 +93,18 @@ struct CafeDev {
   uint32_t *row_live;
   double *row_g;
   long long row_cap;
+  // lazily grown rows: a_ext of the row's cell includes the growth of events
+  // 1..row_m; the row grows at events (birth, row_death]; row_key orders the
+  // rows by estimated absolute capture time; row_b* hold the exact best
+  // candidate of the iteration row_stamp
+  int32_t *row_m, *row_death, *row_stamp, *row_bslot;
+  unsigned long long *row_key;
+  double *row_bt, *row_bruq;
+  // per-event growth log: ev_vd[e] = fl(v * DtMin_e) for captures (ev_grew[e] = 1),
+  // ev_vs[e] = running sum of ev_vd
+  double *ev_vd, *ev_vs;
+  uint8_t *ev_grew;
+  long long ev_cap;
   // scan scratch
   int32_t *blk;       // per-block counts / offsets
   long long blk_cap;
@@ -112,9 +124,12 @@ enum {
   CTR_NNUC,        // nucleations this step
   CTR_NVS2_END,    // mushy-list length after the event loop
   CTR_NLIQ,        // liquid cells listed by the last write-back
+  CTR_SLOW,        // 1: this step's rows do not share one growth velocity
+  CTR_NROWS_END,   // frontier rows after the event loop
   CTR_COUNT
 };
-enum { STAT_EVENTS = 0, STAT_NUC, STAT_MAXNA, STAT_MAXROWS, STAT_STEPS, STAT_NEGDT, STAT_SUMNA, STAT_SUMROWS, STAT_COUNT };
+enum { STAT_EVENTS = 0, STAT_NUC, STAT_MAXNA, STAT_MAXROWS, STAT_STEPS, STAT_NEGDT, STAT_SUMNA, STAT_SUMROWS,
+       STAT_SLOWSTEPS, STAT_EVALS, STAT_COUNT };
 
 // --------------------------------------------------------------- temperature
 // TempField::AnalyticTempCurr (TempField.C:155-190) for one cell; returns the

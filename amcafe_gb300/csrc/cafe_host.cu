@@ -368,6 +368,7 @@ struct cafe_sim {
   bool have_prev_box = false;
   int prev_lo[3] = {0, 0, 0}, prev_hi[3] = {0, 0, 0};
   bool full_k2 = false;   // next solid->mushy pass must scan the whole box
+  int event_scan = 0;     // 1: evaluate every frontier row at every event
   std::vector<void *> owned;
   int *h_pinned = nullptr;  // pinned host mirror of ctr + err
   // per-phase device timing (CUDA events on `stream`) and kernel-launch counts
@@ -621,6 +622,7 @@ int cafe_sim_create(const char *deck_path, const cafe_options *opt, cafe_sim **o
   }
   GridH &g = s->g;
   s->device = opt ? opt->device : 0;
+  s->event_scan = opt ? opt->event_scan : 0;
   cudaError_t ce = cudaSetDevice(s->device);
   if (ce != cudaSuccess) {
     delete s;
@@ -706,6 +708,7 @@ int cafe_sim_create(const char *deck_path, const cafe_options *opt, cafe_sim **o
   D.act_cap = acap;
   D.vs2_cap = acap;
   D.row_cap = std::min<long long>(acap, 1LL << 22);
+  D.ev_cap = acap + 2;
   double est = g.mu * (g.dX[0] * 1e6) * (g.dX[1] * 1e6) * g.nX[0] * g.nX[1] * (s->Nzh * g.dX[2] * 1e6) +
                (s->nlayerTot + 1) * g.lrate * (g.dX[0] * 1e6) * (g.dX[1] * 1e6) * g.nX[0] * g.nX[1] * (g.layerT * 1e6);
   long long gcap = opt && opt->grain_capacity > 0 ? opt->grain_capacity : (long long)(2 * est) + (1 << 16);
@@ -727,6 +730,11 @@ int cafe_sim_create(const char *deck_path, const cafe_options *opt, cafe_sim **o
       (rc = dalloc(&D.row_j, acap, o)) || (rc = dalloc(&D.row_alive, acap, o)) ||
       (rc = dalloc(&D.row_ord, (size_t)acap * CAFE_NSLOT, o)) || (rc = dalloc(&D.row_live, acap, o)) ||
       (rc = dalloc(&D.row_g, (size_t)acap * CAFE_NSLOT, o)) || (rc = dalloc(&D.blk, D.blk_cap, o)) ||
+      (rc = dalloc(&D.row_m, D.row_cap, o)) || (rc = dalloc(&D.row_death, D.row_cap, o)) ||
+      (rc = dalloc(&D.row_stamp, D.row_cap, o)) || (rc = dalloc(&D.row_bslot, D.row_cap, o)) ||
+      (rc = dalloc(&D.row_key, D.row_cap, o)) || (rc = dalloc(&D.row_bt, D.row_cap, o)) ||
+      (rc = dalloc(&D.row_bruq, D.row_cap, o)) || (rc = dalloc(&D.ev_vd, D.ev_cap, o)) ||
+      (rc = dalloc(&D.ev_vs, D.ev_cap, o)) || (rc = dalloc(&D.ev_grew, D.ev_cap, o)) ||
       (rc = dalloc(&D.ctr, CTR_COUNT, o)) || (rc = dalloc(&D.err, 1, o)) || (rc = dalloc(&D.stat, STAT_COUNT, o))) {
     cafe_sim_destroy(s);
     return rc;
@@ -983,13 +991,15 @@ int cafe_sim_update_voxels(cafe_sim *s) {
     k_lists_count<<<nbp, CAFE_DENSE_THREADS, 0, st>>>(D);
     k_scan_pairs<<<1, 1024, 0, st>>>(D.blk, s->nblk_pos, D.ctr + CTR_NVS2, D.ctr + CTR_NROWS);
     k_lists_scatter<<<nbp, CAFE_DENSE_THREADS, 0, st>>>(D);
+    CUDA_TRY(cudaMemsetAsync(D.ctr + CTR_SLOW, 0, sizeof(int), st));
     k_rows_init<<<s->nsm * 4, 256, 0, st>>>(D, K);
     LAUNCHED(CAFE_PH_GATHER, 5);
   }
   {
     PhaseScope ps(s, CAFE_PH_EVENTS);
-    k_event_loop<<<1, CAFE_LOOP_THREADS, 0, st>>>(D, K, P, D.act_cap + 1);
-    LAUNCHED(CAFE_PH_EVENTS, 1);
+    k_event_loop<<<1, CAFE_LOOP_THREADS, 0, st>>>(D, K, P, D.act_cap + 1, s->event_scan ? 0 : 1);
+    k_rows_finalize<<<s->nsm * 4, 256, 0, st>>>(D);
+    LAUNCHED(CAFE_PH_EVENTS, 2);
   }
   {
     PhaseScope ps(s, CAFE_PH_WRITEBACK);
@@ -1142,6 +1152,8 @@ int cafe_sim_stats(cafe_sim *s, cafe_stats *st) {
   st->sum_active = v[STAT_SUMNA];
   st->sum_rows = v[STAT_SUMROWS];
   st->launches = (unsigned long long)s->launches;
+  st->exact_scan_steps = v[STAT_SLOWSTEPS];
+  st->row_evaluations = v[STAT_EVALS];
   return CAFE_OK;
 }
 

@@ -499,14 +499,6 @@ __device__ void cafe_row_fill_warp(const CafeDev &D, const CafeConsts &K, long l
   __syncwarp();
 }
 
-// One warp per row at step start.
-__global__ void k_rows_init(CafeDev D, CafeConsts K) {
-  int nrows = D.ctr[CTR_NROWS];
-  if (nrows > D.row_cap) nrows = (int)D.row_cap;
-  int warps = (gridDim.x * blockDim.x) >> 5;
-  int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  for (int r = w; r < nrows; r += warps) cafe_row_fill_warp(D, K, r, D.row_pos[r]);
-}
 
 // ------------------------------------------------------------------ event loop
 struct CafeCand {
@@ -534,12 +526,14 @@ __device__ __forceinline__ CafeCand cafe_shfl_cand(const CafeCand &c, int o) {
   return r;
 }
 
-// Best candidate of frontier row r. For a positive finite growth velocity the
+// Best candidate of frontier row r (VoxelsCA.C:386-445 restricted to one cell)
+// with the row cell's current extent. For a positive finite growth velocity the
 // capture time fl(fl(g - E)/v) is non-decreasing in g, so the live slots are
 // visited in g order and the visit stops at the first time above the row's
-// minimum; otherwise every live slot is evaluated (VoxelsCA.C:406-442).
+// minimum; otherwise every live slot is evaluated. `bounded` applies the
+// reference's acceptance limit t <= 1e6 (VoxelsCA.C:383, 427).
 __device__ __forceinline__ void cafe_row_best(const CafeDev &D, const CafeConsts &K, long long r,
-                                              CafeCand &best) {
+                                              CafeCand &best, bool bounded = true) {
   int p = D.row_pos[r];
   uint32_t live = D.row_live[r];
   if (!live) return;
@@ -558,8 +552,9 @@ __device__ __forceinline__ void cafe_row_best(const CafeDev &D, const CafeConsts
     if (!(live >> s & 1u)) continue;
     double dr = g[s] - E;
     double t = dr / v;
-    if (!(t <= 1e6)) {
-      if (mono && t > 1e6) break;
+    if (t != t) continue;
+    if (bounded && !(t <= 1e6)) {
+      if (mono) break;
       continue;
     }
     if (mono && have && t > tfirst) break;
@@ -585,16 +580,102 @@ __device__ __forceinline__ int cafe_find_slot(const CafeDev &D, int q, int targe
   return -1;
 }
 
+// ---- lazily grown rows ------------------------------------------------------
+// Every frontier cell of a step grows by the same fl(v * DtMin) at every capture
+// event while it has a liquid neighbour (VoxelsCA.C:511-516), and a row's
+// candidate times all fall by about DtMin per event. A row therefore carries a
+// key: the absolute time T + t_best of its best candidate when it was last
+// evaluated exactly. Between evaluations the key is within a small rounding
+// bound of the row's exact current value (or below it once a candidate was
+// captured by someone else), so the event needs exact times only for the rows
+// whose key lies within twice that bound of the smallest key. The growth itself
+// is logged once per event and replayed per row when the row is evaluated, and
+// for every row at the end of the step (k_rows_finalize, across the GPU).
+#define CAFE_KEY_NONE 0xffffffffffffffffULL
+#define CAFE_M_DONE 0x7fffffff  // row extent needs no further replay
+
+__device__ __forceinline__ unsigned long long cafe_key(double x) {
+  unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  return (b >> 63) ? ~b : (b | 0x8000000000000000ULL);
+}
+__device__ __forceinline__ double cafe_unkey(unsigned long long k) {
+  unsigned long long b = (k >> 63) ? (k & 0x7fffffffffffffffULL) : ~k;
+  return __longlong_as_double((long long)b);
+}
+
+// Applies the logged growth of events row_m+1 .. min(upto, row_death).
+__device__ __forceinline__ void cafe_row_replay(const CafeDev &D, int r, int upto) {
+  int m = D.row_m[r];
+  int stop = min(upto, D.row_death[r]);
+  if (stop <= m) return;
+  int p = D.row_pos[r];
+  double E = D.a_ext[p];
+  for (int k = m + 1; k <= stop; ++k) {
+    if (D.ev_grew[k]) {
+      E = E + D.ev_vd[k];
+      E = (E < 0.0) ? 0.0 : E;
+    }
+  }
+  D.a_ext[p] = E;
+  D.row_m[r] = stop;
+}
+
+// Exact evaluation of row r for the iteration after `ev` events at time T.
+__device__ __forceinline__ void cafe_row_eval(const CafeDev &D, const CafeConsts &K, int r, int ev,
+                                              double T) {
+  cafe_row_replay(D, r, ev);
+  CafeCand b;
+  b.j = -1;
+  b.t = b.ruqs = 0;
+  b.s = 0;
+  cafe_row_best(D, K, r, b, false);
+  D.row_stamp[r] = ev + 1;
+  if (b.j < 0) {
+    D.row_key[r] = CAFE_KEY_NONE;
+    return;
+  }
+  D.row_bt[r] = b.t;
+  D.row_bruq[r] = b.ruqs;
+  D.row_bslot[r] = b.s;
+  D.row_key[r] = cafe_key(T + b.t);
+}
+
+// Frontier rows of the step: numerators, order, and (when every row grows
+// with the same velocity) the initial exact evaluation and keys.
+__global__ void k_rows_init(CafeDev D, CafeConsts K) {
+  int nrows = D.ctr[CTR_NROWS];
+  if (nrows > D.row_cap) nrows = (int)D.row_cap;
+  int warps = (gridDim.x * blockDim.x) >> 5;
+  int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
+  const double V = K.vhat_cls[1];
+  for (int r = w; r < nrows; r += warps) {
+    int p = D.row_pos[r];
+    cafe_row_fill_warp(D, K, r, p);
+    if (lane == 0) {
+      D.row_m[r] = 0;
+      D.row_death[r] = CAFE_M_DONE;
+      if (D.a_cls[p] != 1 || !(V > 0.0 && V < INFINITY)) atomicOr(&D.ctr[CTR_SLOW], 1);
+      cafe_row_eval(D, K, r, 0, 0.0);
+    }
+  }
+}
+
 // The capture/nucleation loop of one step (VoxelsCA.C:381-610), one block.
 __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
-    k_event_loop(CafeDev D, CafeConsts K, CafeStepParams P, long long max_events) {
+    k_event_loop(CafeDev D, CafeConsts K, CafeStepParams P, long long max_events, int allow_fast) {
   __shared__ CafeCand red[CAFE_LOOP_THREADS / 32];
-  __shared__ double s_tinc, s_dt;
-  __shared__ int s_nvs2, s_countS, s_nrows, s_ngrain, s_done, s_nuc, s_icap, s_jspos, s_na;
+  __shared__ unsigned long long redk[CAFE_LOOP_THREADS / 32];
+  __shared__ double s_tinc, s_dt, s_dsum, s_gmax, s_emax, s_vs;
+  __shared__ int s_nvs2, s_countS, s_nrows, s_ngrain, s_done, s_nuc, s_icap, s_jspos, s_na, s_slow,
+      s_ev, s_switch;
+  __shared__ unsigned long long s_kthr;
   __shared__ uint32_t s_rng;
   __shared__ unsigned int s_sdloc;
-  __shared__ long long s_nev, s_nnuc, s_negdt;
+  __shared__ long long s_nnuc, s_negdt, s_evals;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int nthr = blockDim.x, nwarp = blockDim.x >> 5;
+  const double V = K.vhat_cls[1];
   if (tid == 0) {
     s_na = D.ctr[CTR_NA];
     s_nvs2 = D.ctr[CTR_NVS2];
@@ -604,13 +685,63 @@ __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
     s_rng = cafe_minstd_skip(seed, 2ULL * (uint64_t)s_na);
     s_sdloc = K.seed0 + 32u * (unsigned int)P.tInd + 64u * (unsigned int)s_ngrain;
     s_tinc = 0.0;
+    s_dsum = 0.0;
+    s_vs = 0.0;
     s_countS = s_na;
-    s_nev = 0;
     s_nnuc = 0;
     s_negdt = 0;
+    s_evals = 0;
+    s_ev = 0;
+    s_switch = 0;
+    D.ev_vs[0] = 0.0;
+    D.ev_vd[0] = 0.0;
+    D.ev_grew[0] = 0;
+    s_slow = !allow_fast || D.ctr[CTR_SLOW] != 0;
     s_done = (*D.err != 0) || (s_na > D.act_cap) || (s_nvs2 > D.vs2_cap) || (s_nrows > D.row_cap);
+    if (!s_done && s_slow) {
+      // exact per-event scan with eager growth; row extents are kept current
+      for (int r = 0; r < s_nrows; ++r) D.row_m[r] = CAFE_M_DONE;
+    }
+    if (s_na + 2 > D.ev_cap) {
+      atomicOr(D.err, CAFE_ERR_ITER_CAP);
+      s_done = 1;
+    }
   }
   __syncthreads();
+  // magnitudes for the key rounding bound: largest numerator and extent
+  if (!s_slow && !s_done) {
+    unsigned long long gk = 0, ek = 0;
+    for (int r = tid; r < s_nrows; r += nthr) {
+      int p = D.row_pos[r];
+      uint32_t live = D.row_live[r];
+      int nn = D.a_nn[p];
+      for (int k = 0; k < nn; ++k)
+        if (live >> k & 1u) {
+          double gv = fabs(D.row_g[(long long)r * CAFE_NSLOT + k]);
+          if (gv == gv) gk = max(gk, cafe_key(gv));
+        }
+      ek = max(ek, cafe_key(fabs(D.a_ext[p])));
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      gk = max(gk, __shfl_down_sync(0xffffffffu, gk, o));
+      ek = max(ek, __shfl_down_sync(0xffffffffu, ek, o));
+    }
+    if (lane == 0) {
+      red[warp].t = cafe_unkey(gk);
+      red[warp].ruqs = cafe_unkey(ek);
+    }
+    __syncthreads();
+    if (tid == 0) {
+      double gm = 0, em = 0;
+      for (int w = 0; w < nwarp; ++w) {
+        gm = fmax(gm, red[w].t);
+        em = fmax(em, red[w].ruqs);
+      }
+      s_gmax = gm;
+      s_emax = em;
+    }
+    __syncthreads();
+  }
   while (true) {
     if (tid == 0) {
       // while (vSind2 != countS && tinc < DelT)
@@ -619,14 +750,67 @@ __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
     }
     __syncthreads();
     if (s_done) break;
-    // ---- candidate scan and block argmin
     CafeCand best;
     best.j = -1;
     best.t = 0;
     best.ruqs = 0;
     best.s = 0;
-    for (int r = tid; r < s_nrows; r += blockDim.x)
-      if (D.row_alive[r]) cafe_row_best(D, K, r, best);
+    if (s_slow) {
+      // ---- exact scan of every row (VoxelsCA.C:386-445)
+      for (int r = tid; r < s_nrows; r += nthr)
+        if (D.row_alive[r]) cafe_row_best(D, K, r, best);
+    } else {
+      // ---- keyed selection: exact evaluation only near the smallest key
+      const int ev = s_ev;
+      while (true) {
+        unsigned long long km = CAFE_KEY_NONE;
+        for (int r = tid; r < s_nrows; r += nthr)
+          if (D.row_alive[r]) km = min(km, D.row_key[r]);
+        for (int o = 16; o > 0; o >>= 1) km = min(km, __shfl_down_sync(0xffffffffu, km, o));
+        if (lane == 0) redk[warp] = km;
+        __syncthreads();
+        if (tid == 0) {
+          unsigned long long k0 = redk[0];
+          for (int w = 1; w < nwarp; ++w) k0 = min(k0, redk[w]);
+          if (k0 == CAFE_KEY_NONE) {
+            s_kthr = CAFE_KEY_NONE;
+          } else {
+            double kd = cafe_unkey(k0);
+            double mag = fabs(kd) + fabs(s_tinc) + (s_gmax + s_emax) / V + 2.0 * s_dsum + 1e-300;
+            double delta = (double)(ev + 16) * 0x1p-48 * mag;
+            double thr = kd + 2.0 * delta;
+            s_kthr = (thr == thr) ? cafe_key(thr) : CAFE_KEY_NONE;
+          }
+        }
+        __syncthreads();
+        const unsigned long long kthr = s_kthr;
+        int again = 0;
+        if (kthr != CAFE_KEY_NONE) {
+          for (int r = tid; r < s_nrows; r += nthr) {
+            if (!D.row_alive[r]) continue;
+            int stamp = D.row_stamp[r];
+            if (stamp == ev + 1 || (D.row_key[r] > kthr && stamp != -1)) continue;
+            cafe_row_eval(D, K, r, ev, s_tinc);  // stamp -1: forced after a possible clamp
+            again = 1;
+          }
+        }
+        again = __syncthreads_or(again);
+        if (tid == 0 && again) s_evals++;
+        if (!again) break;
+      }
+      const unsigned long long kthr = s_kthr;
+      if (kthr != CAFE_KEY_NONE) {
+        for (int r = tid; r < s_nrows; r += nthr) {
+          if (!D.row_alive[r] || D.row_key[r] > kthr) continue;
+          CafeCand c;
+          c.t = D.row_bt[r];
+          c.ruqs = D.row_bruq[r];
+          c.j = D.row_j[r];
+          c.s = D.row_bslot[r];
+          if (cafe_cand_better(c, best)) best = c;
+        }
+      }
+    }
     for (int o = 16; o > 0; o >>= 1) {
       CafeCand c = cafe_shfl_cand(best, o);
       if (cafe_cand_better(c, best)) best = c;
@@ -635,9 +819,9 @@ __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
     __syncthreads();
     if (tid == 0) {
       CafeCand b = red[0];
-      for (int w = 1; w < (int)(blockDim.x >> 5); ++w)
+      for (int w = 1; w < nwarp; ++w)
         if (cafe_cand_better(red[w], b)) b = red[w];
-      if (b.j < 0 || !(b.t < 1e6) || s_nev >= max_events) {
+      if (b.j < 0 || !(b.t < 1e6) || s_ev >= max_events) {
         if (b.j >= 0 && b.t < 1e6) atomicOr(D.err, CAFE_ERR_ITER_CAP);
         s_done = 1;
       } else {
@@ -651,22 +835,32 @@ __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
         s_nuc = U < K.rX;
         s_dt = s_nuc ? 0.0 : b.t;
         if (s_dt < 0.0) s_negdt++;
+        s_ev += 1;
+        if (!s_slow) {
+          // log this event's growth (VoxelsCA.C:514) for the rows alive now
+          double vd = s_nuc ? 0.0 : V * s_dt;
+          D.ev_vd[s_ev] = vd;
+          D.ev_grew[s_ev] = s_nuc ? 0 : 1;
+          s_vs = s_vs + (s_nuc ? 0.0 : vd);
+          D.ev_vs[s_ev] = s_vs;
+          s_dsum += fabs(s_dt);
+        }
       }
     }
     __syncthreads();
     if (s_done) break;
-    // ---- growth of every mushy cell of the list (VoxelsCA.C:511-516)
-    if (!s_nuc) {
+    // ---- growth of every mushy cell of the list (VoxelsCA.C:511-516), slow path
+    if (s_slow && !s_nuc) {
       double d = s_dt;
       if (isfinite(d)) {
-        for (int r = tid; r < s_nrows; r += blockDim.x) {
+        for (int r = tid; r < s_nrows; r += nthr) {
           if (!D.row_alive[r]) continue;
           int p = D.row_pos[r];
           double e = D.a_ext[p] + K.vhat_cls[D.a_cls[p]] * d;
           D.a_ext[p] = (e < 0.0) ? 0.0 : e;
         }
       } else {
-        for (int j = tid; j < s_countS; j += blockDim.x) {
+        for (int j = tid; j < s_countS; j += nthr) {
           int p = D.vs2[j];
           int r = D.a_frow[p];
           double v = (r >= 0 && D.row_alive[r]) ? K.vhat_cls[D.a_cls[p]] : 0.0;
@@ -723,7 +917,6 @@ __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
         D.a_cz[icap] = cn[2];
       }
       s_tinc += s_dt;
-      s_nev++;
     }
     __syncthreads();
     // ---- neighbours of the captured cell lose one liquid neighbour
@@ -737,7 +930,11 @@ __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
         if (r >= 0 && D.row_alive[r]) {
           int s = cafe_find_slot(D, q, icap);
           if (s >= 0) D.row_live[r] &= ~(1u << s);
-          if (left <= 0) D.row_alive[r] = 0;
+          if (left <= 0) {
+            D.row_alive[r] = 0;
+            if (!s_slow) D.row_death[r] = s_ev;  // it grew at this event too
+            D.row_key[r] = CAFE_KEY_NONE;
+          }
         }
       }
       __syncwarp();
@@ -750,13 +947,61 @@ __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
             D.row_j[r] = s_nvs2 - 1;
             D.row_alive[r] = 1;
             D.a_frow[icap] = r;
+            D.row_death[r] = CAFE_M_DONE;
+            D.row_m[r] = s_slow ? CAFE_M_DONE : s_ev;
           }
           __syncwarp();
           cafe_row_fill_warp(D, K, r, icap);
-          if (lane == 0) s_nrows = r + 1;
+          if (lane == 0) {
+            if (!s_slow) {
+              if (D.a_cls[icap] != 1) {
+                s_switch = 1;
+              } else {
+                cafe_row_eval(D, K, r, s_ev, s_tinc);
+                int nn2 = D.a_nn[icap];
+                uint32_t live = D.row_live[r];
+                for (int k = 0; k < nn2; ++k)
+                  if (live >> k & 1u) {
+                    double gv = fabs(D.row_g[(long long)r * CAFE_NSLOT + k]);
+                    if (gv > s_gmax) s_gmax = gv;
+                  }
+                double ea = fabs(D.a_ext[icap]);
+                if (ea > s_emax) s_emax = ea;
+              }
+            }
+            s_nrows = r + 1;
+          }
         } else if (lane == 0) {
           atomicOr(D.err, CAFE_ERR_ROW_CAP);
           s_done = 1;
+        }
+      }
+    }
+    __syncthreads();
+    if (!s_slow && !s_done) {
+      if (s_switch) {
+        // a capturing cell with another growth velocity: bring every row up to
+        // date and continue with the exact per-event scan
+        for (int r = tid; r < s_nrows; r += nthr) {
+          cafe_row_replay(D, r, s_ev);
+          D.row_m[r] = CAFE_M_DONE;
+        }
+        __syncthreads();
+        if (tid == 0) {
+          s_slow = 1;
+          s_switch = 0;
+        }
+      } else if (!s_nuc && s_dt < 0.0) {
+        // a negative event may clamp a small extent at zero (VoxelsCA.C:515),
+        // which breaks the key bound of that row: re-evaluate such rows
+        const double vd = D.ev_vd[s_ev];
+        const double margin = (double)(s_ev + 16) * 0x1p-48 * (s_emax + s_gmax + V * s_dsum + 1e-300);
+        for (int r = tid; r < s_nrows; r += nthr) {
+          if (!D.row_alive[r]) continue;
+          int m = D.row_m[r];
+          if (m >= s_ev) continue;
+          double elb = D.a_ext[D.row_pos[r]] + (D.ev_vs[s_ev - 1] - D.ev_vs[m]);
+          if (elb + vd < margin) D.row_stamp[r] = -1;
         }
       }
     }
@@ -765,9 +1010,10 @@ __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
   if (tid == 0) {
     D.ctr[CTR_NGRAIN] = s_ngrain;
     D.ctr[CTR_NVS2_END] = s_nvs2;
-    D.ctr[CTR_NEV] = (int)s_nev;
+    D.ctr[CTR_NROWS_END] = s_nrows;
+    D.ctr[CTR_NEV] = s_ev;
     D.ctr[CTR_NNUC] = (int)s_nnuc;
-    atomicAdd(&D.stat[STAT_EVENTS], (unsigned long long)s_nev);
+    atomicAdd(&D.stat[STAT_EVENTS], (unsigned long long)s_ev);
     atomicAdd(&D.stat[STAT_NUC], (unsigned long long)s_nnuc);
     atomicAdd(&D.stat[STAT_NEGDT], (unsigned long long)s_negdt);
     atomicMax(&D.stat[STAT_MAXNA], (unsigned long long)s_na);
@@ -775,7 +1021,19 @@ __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
     atomicAdd(&D.stat[STAT_STEPS], 1ULL);
     atomicAdd(&D.stat[STAT_SUMNA], (unsigned long long)s_na);
     atomicAdd(&D.stat[STAT_SUMROWS], (unsigned long long)s_nrows);
+    atomicAdd(&D.stat[STAT_EVALS], (unsigned long long)s_evals);
+    if (s_slow) atomicAdd(&D.stat[STAT_SLOWSTEPS], 1ULL);
   }
+}
+
+// Brings every row's extent up to the end of the step (the lazily applied
+// growth of VoxelsCA.C:511-516), spread over the whole GPU.
+__global__ void k_rows_finalize(CafeDev D) {
+  int nrows = D.ctr[CTR_NROWS_END];
+  int nev = D.ctr[CTR_NEV];
+  if (nrows > D.row_cap) nrows = (int)D.row_cap;
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < nrows; r += gridDim.x * blockDim.x)
+    cafe_row_replay(D, r, nev);
 }
 
 // ------------------------------------------------------------------ write back

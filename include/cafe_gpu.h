@@ -34,6 +34,8 @@ typedef struct {
   int device;                  /* CUDA device ordinal */
   long long active_capacity;   /* max active-list length per step; 0 = automatic */
   long long grain_capacity;    /* initial grain-table capacity; 0 = automatic */
+  int event_scan;              /* 0: keyed event selection (default); 1: evaluate every
+                                  frontier cell at every event (the reference's scan) */
 } cafe_options;
 
 typedef struct {
@@ -61,6 +63,8 @@ typedef struct {
   unsigned long long sum_active;   /* sum over steps of the active-list length */
   unsigned long long sum_rows;     /* sum over steps of the frontier size */
   unsigned long long launches;     /* kernels launched by this handle since the last phase reset */
+  unsigned long long exact_scan_steps; /* steps run with the full per-event scan */
+  unsigned long long row_evaluations;  /* keyed-selection rounds that evaluated rows exactly */
 } cafe_stats;
 
 /* Grid::Grid (Grid.C:15-109, deck parse Grid.C:165-318) + Partition::

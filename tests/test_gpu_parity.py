@@ -17,14 +17,14 @@ pytestmark = pytest.mark.gpu
 DECKS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "decks")
 
 
-def run_and_compare(deck, nsteps, stride, tmp_path):
+def run_and_compare(deck, nsteps, stride, tmp_path, event_scan=0):
     from amcafe_gb300 import Simulation
 
     path = os.path.join(DECKS, deck)
     dump = str(tmp_path / "o.bin")
     ostats = orc.run(path, dump, max_steps=nsteps if nsteps > 0 else -1, dump_stride=stride, libm=orc.LIBM_CR)
     recs = orc.read_dump(dump)
-    sim = Simulation(path, device=0)
+    sim = Simulation(path, device=0, event_scan=event_scan)
     sim.InitializeVoxels()
     sim.begin()
     worst = 0.0
@@ -67,7 +67,17 @@ def run_and_compare(deck, nsteps, stride, tmp_path):
 
 
 @pytest.mark.parametrize("deck,nsteps,stride", [
-    ("track_r0.in", 0, 1), ("track_nuc.in", 0, 1), ("layers_rot.in", 0, 20), ("c0_small.in", 120, 20)])
+    ("track_r0.in", 0, 1), ("track_nuc.in", 0, 1), ("layers_rot.in", 0, 20), ("c0_small.in", 400, 40)])
 def test_gpu_matches_oracle(tmp_path, deck, nsteps, stride):
+    """Default keyed event selection with lazily replayed growth."""
     worst, stats = run_and_compare(deck, nsteps, stride, tmp_path)
+    assert stats["exact_scan_steps"] == 0, "steps fell back to the full scan: %s" % stats
     print("%s: max float rel diff %g, %s" % (deck, worst, stats))
+
+
+@pytest.mark.parametrize("deck,nsteps,stride", [("track_nuc.in", 0, 1), ("layers_rot.in", 0, 20)])
+def test_gpu_full_scan_matches_oracle(tmp_path, deck, nsteps, stride):
+    """The reference's per-event scan of every frontier cell (event_scan=1)."""
+    worst, stats = run_and_compare(deck, nsteps, stride, tmp_path, event_scan=1)
+    assert stats["exact_scan_steps"] == stats["steps"]
+    print("%s full scan: max float rel diff %g, %s" % (deck, worst, stats))
