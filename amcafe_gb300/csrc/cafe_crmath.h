@@ -12,6 +12,12 @@
 // and fma with explicit evaluation order, so host and device produce the same
 // bits; compile with FP contraction off (-ffp-contract=off, nvcc --fmad=false).
 //
+// Each of atan2, sin and cos first runs a short evaluation whose result is a
+// double plus a correction with relative error below 2^-63, and returns it when
+// rounding the result plus or minus that bound gives the same double (Ziv's
+// rounding test; about one call in 500 fails it); otherwise the accurate
+// double-double evaluation below decides.
+//
 // Methods: Dekker/Knuth error-free transformations (two_sum, two_prod via fma);
 // arctangent by table reduction atan(t) = atan(c) + atan((t-c)/(1+tc)) with
 // c = k/64 and a Taylor series; sine/cosine by Cody-Waite reduction by pi/2
@@ -143,7 +149,7 @@ CRM_HD double crm_atan2_dd(crm_dd ay, crm_dd ax, int y_neg, int x_neg) {
   return y_neg ? -v : v;
 }
 
-CRM_HD double crm_atan2(double y, double x) {
+CRM_HD double crm_atan2_acc(double y, double x) {
   if (y != y || x != x) return y + x;
   int yn = signbit(y) ? 1 : 0, xn = signbit(x) ? 1 : 0;
   double ay = fabs(y), ax = fabs(x);
@@ -212,7 +218,7 @@ CRM_HD void crm_sincos_small(crm_dd r, crm_dd *sn, crm_dd *cs) {
 
 // Supported domain |x| < 2^20 (the CA evaluates arguments in [-2 pi, 2 pi]);
 // outside it the result is NaN.
-CRM_HD double crm_sin(double x) {
+CRM_HD double crm_sin_acc(double x) {
   if (!(fabs(x) < 1048576.0)) return NAN;
   if (x == 0.0) return x;
   int q;
@@ -226,7 +232,7 @@ CRM_HD double crm_sin(double x) {
     default: return -crm_dd_round(c);
   }
 }
-CRM_HD double crm_cos(double x) {
+CRM_HD double crm_cos_acc(double x) {
   if (!(fabs(x) < 1048576.0)) return NAN;
   int q;
   crm_dd r = crm_reduce_pio2(x, &q);
@@ -255,6 +261,131 @@ CRM_HD double crm_acos(double x) {
   crm_dd sq = crm_fast_two_sum(s0, rem / (2.0 * s0));
   int xn = signbit(x) ? 1 : 0;
   return crm_atan2_dd(sq, crm_dd{fabs(x), 0.0}, 0, xn);
+}
+
+// ---------------------------------------------------------------- fast paths
+// Returns 1 and the rounded value when s + lo is within err of the exact
+// result and both s + lo - err and s + lo + err round to the same double.
+CRM_HD int crm_round_test(double s, double lo, double err, double *out) {
+  double a = s + (lo - err), b = s + (lo + err);
+  if (a == b) {
+    *out = s + lo;
+    return 1;
+  }
+  return 0;
+}
+
+// atan(num/den), 0 <= num <= den, den > 0, as hi + lo.
+CRM_HD void crm_atan_unit_fast(double num, double den, double *hi, double *lo) {
+  double t = num / den;
+  double tl = fma(-t, den, num) / den;
+  int k = (int)(t * (double)CRM_ATAN_STEPS + 0.5);
+  if (k > CRM_ATAN_STEPS) k = CRM_ATAN_STEPS;
+  double c = (double)k * (1.0 / CRM_ATAN_STEPS);
+  double dn = t - c;  // exact (Sterbenz)
+  double p = t * c;
+  double pe = fma(t, c, -p);
+  crm_dd d1 = crm_two_sum(1.0, p);
+  double den2 = d1.hi;
+  double den2l = d1.lo + pe + tl * c;
+  double uh = (dn + tl) / den2;
+  double r = fma(-uh, den2, dn) + tl - uh * den2l;
+  double ul = r / den2;
+  double w = uh * uh;
+  double poly = uh * w * (-1.0 / 3 + w * (1.0 / 5 + w * (-1.0 / 7 + w * (1.0 / 9 + w * (-1.0 / 11)))));
+  double th = CRM_TAB(crm_atan_tab)[k][0], tlo = CRM_TAB(crm_atan_tab)[k][1];
+  crm_dd sm = crm_two_sum(th, uh);
+  *hi = sm.hi;
+  *lo = sm.lo + (tlo + (ul + poly));
+}
+
+CRM_HD double crm_atan2(double y, double x) {
+  if (y != y || x != x || y == 0.0 || x == 0.0 || fabs(y) == INFINITY || fabs(x) == INFINITY)
+    return crm_atan2_acc(y, x);
+  double ay = fabs(y), ax = fabs(x);
+  double h, l;
+  if (ay <= ax) {
+    crm_atan_unit_fast(ay, ax, &h, &l);
+  } else {
+    double h0, l0;
+    crm_atan_unit_fast(ax, ay, &h0, &l0);
+    crm_dd d = crm_two_sum(CRM_PIO2_1, -h0);
+    h = d.hi;
+    l = d.lo + (CRM_PIO2_2 - l0);
+  }
+  if (signbit(x)) {
+    crm_dd d = crm_two_sum(CRM_PI_HI, -h);
+    h = d.hi;
+    l = d.lo + (CRM_PI_LO - l);
+  }
+  double v;
+  if (crm_round_test(h, l, fabs(h) * 0x1p-63, &v)) return signbit(y) ? -v : v;
+  return crm_atan2_acc(y, x);
+}
+
+// sin and cos of x, |x| < 2^20, as hi + lo pairs (quadrant applied).
+CRM_HD void crm_sincos_fast(double x, double *sh, double *sl, double *ch, double *cl) {
+  double rh, rl;
+  int q;
+  if (fabs(x) <= 0.78) {
+    rh = x;
+    rl = 0.0;
+    q = 0;
+  } else {
+    crm_dd r = crm_reduce_pio2(x, &q);
+    rh = r.hi;
+    rl = r.lo;
+  }
+  int neg = rh < 0.0;
+  if (neg) {
+    rh = -rh;
+    rl = -rl;
+  }
+  int j = (int)(rh * (double)CRM_SC_STEPS + 0.5);
+  if (j > 103) j = 103;
+  double c = (double)j * (1.0 / CRM_SC_STEPS);
+  double sh0 = rh - c;  // exact (Sterbenz)
+  double slo = rl;
+  double w = sh0 * sh0;
+  double sm = sh0 * w * (-1.0 / 6 + w * (1.0 / 120 + w * (-1.0 / 5040)));            // sin s - s
+  double cm = w * (-0.5 + w * (1.0 / 24 + w * (-1.0 / 720 + w * (1.0 / 40320)))) - sh0 * slo;  // cos s - 1
+  double sc = CRM_TAB(crm_sincos_tab)[j][0], scl = CRM_TAB(crm_sincos_tab)[j][1];
+  double cc = CRM_TAB(crm_sincos_tab)[j][2], ccl = CRM_TAB(crm_sincos_tab)[j][3];
+  // sin(c+s) = sin c + cos c * s + cos c (sin s - s) + sin c (cos s - 1)
+  crm_dd p = crm_two_prod(cc, sh0);
+  crm_dd t = crm_two_sum(sc, p.hi);
+  double sinh = t.hi;
+  double sinl = t.lo + (scl + (p.lo + (cc * slo + (ccl * sh0 + (cc * sm + sc * cm)))));
+  // cos(c+s) = cos c - sin c * s - sin c (sin s - s) + cos c (cos s - 1)
+  crm_dd p2 = crm_two_prod(sc, sh0);
+  crm_dd t2 = crm_two_sum(cc, -p2.hi);
+  double cosh = t2.hi;
+  double cosl = t2.lo + (ccl + (-p2.lo + (-sc * slo + (-scl * sh0 + (-sc * sm + cc * cm)))));
+  if (neg) {
+    sinh = -sinh;
+    sinl = -sinl;
+  }
+  switch (q & 3) {
+    case 0: *sh = sinh; *sl = sinl; *ch = cosh; *cl = cosl; break;
+    case 1: *sh = cosh; *sl = cosl; *ch = -sinh; *cl = -sinl; break;
+    case 2: *sh = -sinh; *sl = -sinl; *ch = -cosh; *cl = -cosl; break;
+    default: *sh = -cosh; *sl = -cosl; *ch = sinh; *cl = sinl; break;
+  }
+}
+
+CRM_HD double crm_sin(double x) {
+  if (!(fabs(x) < 1048576.0) || x == 0.0) return crm_sin_acc(x);
+  double sh, sl, ch, cl, v;
+  crm_sincos_fast(x, &sh, &sl, &ch, &cl);
+  if (crm_round_test(sh, sl, fabs(sh) * 0x1p-63 + 0x1p-1000, &v)) return v;
+  return crm_sin_acc(x);
+}
+CRM_HD double crm_cos(double x) {
+  if (!(fabs(x) < 1048576.0)) return crm_cos_acc(x);
+  double sh, sl, ch, cl, v;
+  crm_sincos_fast(x, &sh, &sl, &ch, &cl);
+  if (crm_round_test(ch, cl, fabs(ch) * 0x1p-63 + 0x1p-1000, &v)) return v;
+  return crm_cos_acc(x);
 }
 
 // pow(x, 0.5) as glibc's pow defines it; the correctly rounded value is sqrt
