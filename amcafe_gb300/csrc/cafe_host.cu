@@ -1154,6 +1154,9 @@ int cafe_sim_stats(cafe_sim *s, cafe_stats *st) {
   st->launches = (unsigned long long)s->launches;
   st->exact_scan_steps = v[STAT_SLOWSTEPS];
   st->row_evaluations = v[STAT_EVALS];
+  st->cycles_select = v[STAT_CYC_SELECT];
+  st->cycles_apply = v[STAT_CYC_APPLY];
+  st->cycles_fill = v[STAT_CYC_FILL];
   return CAFE_OK;
 }
 

@@ -673,6 +673,8 @@ __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
   __shared__ uint32_t s_rng;
   __shared__ unsigned int s_sdloc;
   __shared__ long long s_nnuc, s_negdt, s_evals;
+  __shared__ long long s_cyc[4];  // selection, capture apply, bookkeeping + new row, other
+  __shared__ long long s_t0;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int nthr = blockDim.x, nwarp = blockDim.x >> 5;
   const double V = K.vhat_cls[1];
@@ -693,6 +695,7 @@ __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
     s_evals = 0;
     s_ev = 0;
     s_switch = 0;
+    s_cyc[0] = s_cyc[1] = s_cyc[2] = s_cyc[3] = 0;
     D.ev_vs[0] = 0.0;
     D.ev_vd[0] = 0.0;
     D.ev_grew[0] = 0;
@@ -750,6 +753,7 @@ __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
     }
     __syncthreads();
     if (s_done) break;
+    if (tid == 0) s_t0 = clock64();
     CafeCand best;
     best.j = -1;
     best.t = 0;
@@ -818,6 +822,9 @@ __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
     if (lane == 0) red[warp] = best;
     __syncthreads();
     if (tid == 0) {
+      long long tn = clock64();
+      s_cyc[0] += tn - s_t0;
+      s_t0 = tn;
       CafeCand b = red[0];
       for (int w = 1; w < nwarp; ++w)
         if (cafe_cand_better(red[w], b)) b = red[w];
@@ -917,6 +924,9 @@ __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
         D.a_cz[icap] = cn[2];
       }
       s_tinc += s_dt;
+      long long tn = clock64();
+      s_cyc[1] += tn - s_t0;
+      s_t0 = tn;
     }
     __syncthreads();
     // ---- neighbours of the captured cell lose one liquid neighbour
@@ -978,6 +988,11 @@ __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
       }
     }
     __syncthreads();
+    if (tid == 0) {
+      long long tn = clock64();
+      s_cyc[2] += tn - s_t0;
+      s_t0 = tn;
+    }
     if (!s_slow && !s_done) {
       if (s_switch) {
         // a capturing cell with another growth velocity: bring every row up to
@@ -1023,6 +1038,7 @@ __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
     atomicAdd(&D.stat[STAT_SUMROWS], (unsigned long long)s_nrows);
     atomicAdd(&D.stat[STAT_EVALS], (unsigned long long)s_evals);
     if (s_slow) atomicAdd(&D.stat[STAT_SLOWSTEPS], 1ULL);
+    for (int c = 0; c < 4; ++c) atomicAdd(&D.stat[STAT_CYC_SELECT + c], (unsigned long long)s_cyc[c]);
   }
 }
 

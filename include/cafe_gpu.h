@@ -65,6 +65,9 @@ typedef struct {
   unsigned long long launches;     /* kernels launched by this handle since the last phase reset */
   unsigned long long exact_scan_steps; /* steps run with the full per-event scan */
   unsigned long long row_evaluations;  /* keyed-selection rounds that evaluated rows exactly */
+  unsigned long long cycles_select;    /* event-loop SM cycles in event selection */
+  unsigned long long cycles_apply;     /* ... applying the capture/nucleation */
+  unsigned long long cycles_fill;      /* ... neighbour bookkeeping and new frontier rows */
 } cafe_stats;
 
 /* Grid::Grid (Grid.C:15-109, deck parse Grid.C:165-318) + Partition::
