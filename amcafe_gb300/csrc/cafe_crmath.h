@@ -28,6 +28,7 @@
 #define CAFE_CRMATH_H
 
 #include <math.h>
+#include <string.h>
 
 #if defined(__CUDACC__)
 #define CRM_HD __host__ __device__ __forceinline__
@@ -53,9 +54,56 @@
 #undef CRM_TABLE_DECL
 #endif
 
+// Profiling builds count the calls that leave the fast paths.
+#if defined(CAFE_DETAIL_CYCLES) && defined(__CUDACC__)
+__device__ unsigned long long crm_fallback_calls, crm_special_calls;
+#ifdef __CUDA_ARCH__
+#define CRM_COUNT(c) atomicAdd(&(c), 1ULL)
+#else
+#define CRM_COUNT(c) ((void)0)
+#endif
+#else
+#define CRM_COUNT(c) ((void)0)
+#endif
+
 struct crm_dd {
   double hi, lo;
 };
+
+// Bit patterns of doubles (integer tests are cheaper than floating-point
+// compares on this hardware; for non-negative doubles the bit order is the
+// numeric order).
+CRM_HD long long crm_bits(double x) {
+#ifdef __CUDA_ARCH__
+  return __double_as_longlong(x);
+#else
+  long long b;
+  memcpy(&b, &x, sizeof b);
+  return b;
+#endif
+}
+CRM_HD double crm_from_bits(long long b) {
+#ifdef __CUDA_ARCH__
+  return __longlong_as_double(b);
+#else
+  double x;
+  memcpy(&x, &b, sizeof x);
+  return x;
+#endif
+}
+// Correctly rounded single-precision reciprocal (same bits on host and device).
+CRM_HD float crm_rcp_f32(float x) {
+#ifdef __CUDA_ARCH__
+  return __frcp_rn(x);
+#else
+  return 1.0f / x;
+#endif
+}
+#define CRM_ABS_MASK 0x7fffffffffffffffLL
+#define CRM_BITS_INF 0x7ff0000000000000LL
+#define CRM_BITS_2P20 0x4130000000000000LL    // 2^20
+#define CRM_BITS_PIO4 0x3fe921fb54442d18LL    // CRM_PIO2_1 / 2
+#define CRM_BITS_3PIO4 0x4002d97c7f3321d2LL   // 3 CRM_PIO2_1 / 2
 
 CRM_HD crm_dd crm_two_sum(double a, double b) {
   double s = a + b;
@@ -275,116 +323,156 @@ CRM_HD int crm_round_test(double s, double lo, double err, double *out) {
   return 0;
 }
 
-// atan(num/den), 0 <= num <= den, den > 0, as hi + lo.
-CRM_HD void crm_atan_unit_fast(double num, double den, double *hi, double *lo) {
-  double t = num / den;
-  double tl = fma(-t, den, num) / den;
-  int k = (int)(t * (double)CRM_ATAN_STEPS + 0.5);
+// atan(num/den) for 0 < num <= den, both finite, as hi + lo; returns 0 (no
+// result) for subnormal operands or num/den < 2^-1000. Both operands are first
+// scaled by the same power of two (den to [1,2)), which is exact. The table
+// point c = k/64 comes from a single-precision estimate of num/den (|t - c|
+// stays within 1/128 + 2^-23, inside the series' range), and
+// u = (num - c den)/(den + c num) = (t - c)/(1 + t c) is formed from
+// double-double numerator and denominator with one division; the remainder
+// term uses a single-precision reciprocal (relative error 2^-23 on a term below
+// 2^-53 |u|).
+CRM_HD int crm_atan_unit_fast(double num, double den, double *hi, double *lo) {
+  long long nb = crm_bits(num), db = crm_bits(den);
+  long long en = nb >> 52, ed = db >> 52;
+  if (en == 0 || ed == 0 || en - ed < -1000) return 0;
+  long long sh = (ed - 1023) << 52;
+  double dens = crm_from_bits(db - sh), nums = crm_from_bits(nb - sh);
+  float tf = (float)nums / (float)dens;
+  int k = (int)(tf * (float)CRM_ATAN_STEPS + 0.5f);
   if (k > CRM_ATAN_STEPS) k = CRM_ATAN_STEPS;
   double c = (double)k * (1.0 / CRM_ATAN_STEPS);
-  double dn = t - c;  // exact (Sterbenz)
-  double p = t * c;
-  double pe = fma(t, c, -p);
-  crm_dd d1 = crm_two_sum(1.0, p);
-  double den2 = d1.hi;
-  double den2l = d1.lo + pe + tl * c;
-  double uh = (dn + tl) / den2;
-  double r = fma(-uh, den2, dn) + tl - uh * den2l;
-  double ul = r / den2;
+  double p = c * dens, pe = fma(c, dens, -p);
+  crm_dd a = crm_two_sum(nums, -p);
+  double alo = a.lo - pe;
+  double qv = c * nums, qe = fma(c, nums, -qv);
+  crm_dd bd = crm_two_sum(dens, qv);
+  double blo = bd.lo + qe;
+  double uh = a.hi / bd.hi;
+  double rr = (fma(-uh, bd.hi, a.hi) + alo) - uh * blo;
+  double ul = rr * (double)crm_rcp_f32((float)bd.hi);
   double w = uh * uh;
   double poly = uh * w * (-1.0 / 3 + w * (1.0 / 5 + w * (-1.0 / 7 + w * (1.0 / 9 + w * (-1.0 / 11)))));
   double th = CRM_TAB(crm_atan_tab)[k][0], tlo = CRM_TAB(crm_atan_tab)[k][1];
   crm_dd sm = crm_two_sum(th, uh);
   *hi = sm.hi;
   *lo = sm.lo + (tlo + (ul + poly));
+  return 1;
 }
 
 CRM_HD double crm_atan2(double y, double x) {
-  if (y != y || x != x || y == 0.0 || x == 0.0 || fabs(y) == INFINITY || fabs(x) == INFINITY)
+  long long yb = crm_bits(y), xb = crm_bits(x);
+  long long ayb = yb & CRM_ABS_MASK, axb = xb & CRM_ABS_MASK;
+  if (ayb == 0 || axb == 0 || ayb >= CRM_BITS_INF || axb >= CRM_BITS_INF) {
+    CRM_COUNT(crm_special_calls);
     return crm_atan2_acc(y, x);
-  double ay = fabs(y), ax = fabs(x);
+  }
+  double ay = crm_from_bits(ayb), ax = crm_from_bits(axb);
   double h, l;
-  if (ay <= ax) {
-    crm_atan_unit_fast(ay, ax, &h, &l);
+  if (ayb <= axb) {
+    if (!crm_atan_unit_fast(ay, ax, &h, &l)) return crm_atan2_acc(y, x);
   } else {
     double h0, l0;
-    crm_atan_unit_fast(ax, ay, &h0, &l0);
+    if (!crm_atan_unit_fast(ax, ay, &h0, &l0)) return crm_atan2_acc(y, x);
     crm_dd d = crm_two_sum(CRM_PIO2_1, -h0);
     h = d.hi;
     l = d.lo + (CRM_PIO2_2 - l0);
   }
-  if (signbit(x)) {
+  if (xb < 0) {
     crm_dd d = crm_two_sum(CRM_PI_HI, -h);
     h = d.hi;
     l = d.lo + (CRM_PI_LO - l);
   }
   double v;
-  if (crm_round_test(h, l, fabs(h) * 0x1p-63, &v)) return signbit(y) ? -v : v;
+  if (crm_round_test(h, l, crm_from_bits(crm_bits(h) & CRM_ABS_MASK) * 0x1p-63, &v)) return yb < 0 ? -v : v;
+  CRM_COUNT(crm_fallback_calls);
   return crm_atan2_acc(y, x);
 }
 
-// sin and cos of x, |x| < 2^20, as hi + lo pairs (quadrant applied).
-CRM_HD void crm_sincos_fast(double x, double *sh, double *sl, double *ch, double *cl) {
-  double rh, rl;
-  int q;
-  if (fabs(x) <= 0.78) {
-    rh = x;
-    rl = 0.0;
-    q = 0;
-  } else {
-    crm_dd r = crm_reduce_pio2(x, &q);
-    rh = r.hi;
-    rl = r.lo;
-  }
-  int neg = rh < 0.0;
-  if (neg) {
-    rh = -rh;
-    rl = -rl;
-  }
+// Addition-formula cores around the table point c = j/128 nearest to rh, for
+// 0 <= rh <= pi/4 + 2^-20 and s = (rh - c) + rl: sin(c+s) = sin c + cos c s +
+// cos c (sin s - s) + sin c (cos s - 1) and cos(c+s) = cos c - sin c s -
+// sin c (sin s - s) + cos c (cos s - 1), as hi + lo.
+CRM_HD void crm_sc_core(double rh, double rl, int want_sin, double *h, double *l) {
   int j = (int)(rh * (double)CRM_SC_STEPS + 0.5);
   if (j > 103) j = 103;
   double c = (double)j * (1.0 / CRM_SC_STEPS);
   double sh0 = rh - c;  // exact (Sterbenz)
-  double slo = rl;
   double w = sh0 * sh0;
   double sm = sh0 * w * (-1.0 / 6 + w * (1.0 / 120 + w * (-1.0 / 5040)));            // sin s - s
-  double cm = w * (-0.5 + w * (1.0 / 24 + w * (-1.0 / 720 + w * (1.0 / 40320)))) - sh0 * slo;  // cos s - 1
+  double cm = w * (-0.5 + w * (1.0 / 24 + w * (-1.0 / 720 + w * (1.0 / 40320)))) - sh0 * rl;  // cos s - 1
   double sc = CRM_TAB(crm_sincos_tab)[j][0], scl = CRM_TAB(crm_sincos_tab)[j][1];
   double cc = CRM_TAB(crm_sincos_tab)[j][2], ccl = CRM_TAB(crm_sincos_tab)[j][3];
-  // sin(c+s) = sin c + cos c * s + cos c (sin s - s) + sin c (cos s - 1)
-  crm_dd p = crm_two_prod(cc, sh0);
-  crm_dd t = crm_two_sum(sc, p.hi);
-  double sinh = t.hi;
-  double sinl = t.lo + (scl + (p.lo + (cc * slo + (ccl * sh0 + (cc * sm + sc * cm)))));
-  // cos(c+s) = cos c - sin c * s - sin c (sin s - s) + cos c (cos s - 1)
-  crm_dd p2 = crm_two_prod(sc, sh0);
-  crm_dd t2 = crm_two_sum(cc, -p2.hi);
-  double cosh = t2.hi;
-  double cosl = t2.lo + (ccl + (-p2.lo + (-sc * slo + (-scl * sh0 + (-sc * sm + cc * cm)))));
-  if (neg) {
-    sinh = -sinh;
-    sinl = -sinl;
-  }
-  switch (q & 3) {
-    case 0: *sh = sinh; *sl = sinl; *ch = cosh; *cl = cosl; break;
-    case 1: *sh = cosh; *sl = cosl; *ch = -sinh; *cl = -sinl; break;
-    case 2: *sh = -sinh; *sl = -sinl; *ch = -cosh; *cl = -cosl; break;
-    default: *sh = -cosh; *sl = -cosl; *ch = sinh; *cl = sinl; break;
+  if (want_sin) {
+    crm_dd p = crm_two_prod(cc, sh0);
+    crm_dd t = crm_two_sum(sc, p.hi);
+    *h = t.hi;
+    *l = t.lo + (scl + (p.lo + (cc * rl + (ccl * sh0 + (cc * sm + sc * cm)))));
+  } else {
+    crm_dd p2 = crm_two_prod(sc, sh0);
+    crm_dd t2 = crm_two_sum(cc, -p2.hi);
+    *h = t2.hi;
+    *l = t2.lo + (ccl + (-p2.lo + (-sc * rl + (-scl * sh0 + (-sc * sm + cc * cm)))));
   }
 }
 
+// sin(x) (want_sin) or cos(x) for 0 < |x| < 2^20 as hi + lo. |x| <= pi/4 needs
+// no reduction; for pi/4 < |x| <= 3 pi/4 the reduction by pi/2 is
+// |x| - PIO2_1 (exact by Sterbenz) minus PIO2_2 and PIO2_3 (the remainder is at
+// least 6e-17 in magnitude, so the dropped PIO2_4 costs under 2^-100
+// relative); larger |x| use the Cody-Waite reduction.
+CRM_HD void crm_sincos1_fast(double x, int want_sin, double *h, double *l) {
+  long long b = crm_bits(x);
+  long long ab = b & CRM_ABS_MASK;
+  double ax = crm_from_bits(ab);
+  double rh, rl;
+  int q;
+  if (ab <= CRM_BITS_PIO4) {
+    rh = ax;
+    rl = 0.0;
+    q = 0;
+  } else if (ab <= CRM_BITS_3PIO4) {
+    crm_dd t = crm_two_sum(ax - CRM_PIO2_1, -CRM_PIO2_2);
+    crm_dd u = crm_fast_two_sum(t.hi, t.lo - CRM_PIO2_3);
+    rh = u.hi;
+    rl = u.lo;
+    q = 1;
+  } else {
+    crm_dd r = crm_reduce_pio2(ax, &q);
+    rh = r.hi;
+    rl = r.lo;
+  }
+  // |x| = q pi/2 + r; sin|x| is (sin r, cos r, -sin r, -cos r) and cos|x| is
+  // (cos r, -sin r, -cos r, sin r) for q = 0..3
+  int rneg = crm_bits(rh) < 0;
+  if (rneg) {
+    rh = -rh;
+    rl = -rl;
+  }
+  int sin_core = want_sin ? !(q & 1) : (q & 1);
+  double hh, ll;
+  crm_sc_core(rh, rl, sin_core, &hh, &ll);
+  int neg = (sin_core && rneg) ^ (want_sin ? ((q & 2) != 0) : (((q + 1) & 2) != 0)) ^ (want_sin && b < 0);
+  *h = neg ? -hh : hh;
+  *l = neg ? -ll : ll;
+}
+
 CRM_HD double crm_sin(double x) {
-  if (!(fabs(x) < 1048576.0) || x == 0.0) return crm_sin_acc(x);
-  double sh, sl, ch, cl, v;
-  crm_sincos_fast(x, &sh, &sl, &ch, &cl);
-  if (crm_round_test(sh, sl, fabs(sh) * 0x1p-63 + 0x1p-1000, &v)) return v;
+  long long ab = crm_bits(x) & CRM_ABS_MASK;
+  if (ab >= CRM_BITS_2P20 || ab == 0) return crm_sin_acc(x);
+  double sh, sl, v;
+  crm_sincos1_fast(x, 1, &sh, &sl);
+  if (crm_round_test(sh, sl, crm_from_bits(crm_bits(sh) & CRM_ABS_MASK) * 0x1p-63 + 0x1p-1000, &v)) return v;
+  CRM_COUNT(crm_fallback_calls);
   return crm_sin_acc(x);
 }
 CRM_HD double crm_cos(double x) {
-  if (!(fabs(x) < 1048576.0)) return crm_cos_acc(x);
-  double sh, sl, ch, cl, v;
-  crm_sincos_fast(x, &sh, &sl, &ch, &cl);
-  if (crm_round_test(ch, cl, fabs(ch) * 0x1p-63 + 0x1p-1000, &v)) return v;
+  long long ab = crm_bits(x) & CRM_ABS_MASK;
+  if (ab >= CRM_BITS_2P20) return crm_cos_acc(x);
+  double ch, cl, v;
+  crm_sincos1_fast(x, 0, &ch, &cl);
+  if (crm_round_test(ch, cl, crm_from_bits(crm_bits(ch) & CRM_ABS_MASK) * 0x1p-63 + 0x1p-1000, &v)) return v;
+  CRM_COUNT(crm_fallback_calls);
   return crm_cos_acc(x);
 }
 

@@ -92,6 +92,9 @@ struct CafeDev {
   uint8_t *row_alive, *row_ord;
   uint32_t *row_live;
   double *row_g;
+  // per (row, slot): extent and centre (x, y, z) given to the neighbour when
+  // this slot captures it, 4 doubles
+  double *row_geo;
   long long row_cap;
   // lazily grown rows: a_ext of the row's cell includes the growth of events
   // 1..row_m; the row grows at events (birth, row_death]; row_key orders the
@@ -130,7 +133,7 @@ enum {
 };
 enum { STAT_EVENTS = 0, STAT_NUC, STAT_MAXNA, STAT_MAXROWS, STAT_STEPS, STAT_NEGDT, STAT_SUMNA, STAT_SUMROWS,
        STAT_SLOWSTEPS, STAT_EVALS, STAT_CYC_SELECT, STAT_CYC_APPLY, STAT_CYC_FILL, STAT_CYC_OTHER,
-       STAT_COUNT };
+       STAT_DETAIL, STAT_COUNT = STAT_DETAIL + 24 };
 
 // --------------------------------------------------------------- temperature
 // TempField::AnalyticTempCurr (TempField.C:155-190) for one cell; returns the
@@ -196,65 +199,101 @@ __device__ __forceinline__ void cafe_rot_from_cth(const double *c, double *R) {
   R[8] = co + (a2 * a2) * (1 - co);
 }
 
-// Capture-time numerator pow(cos th sin ph,.5)*|R^T dn|_1 for the octahedron
-// at (c0,c1,c2) with rotation R and the neighbour cell at (i,j,k)
-// (VoxelsCA.C:409-424, without "- ExtA").
-__device__ __forceinline__ double cafe_candidate_g(const CafeConsts &K, double c0, double c1,
-                                                   double c2, const double *R, int i, int j, int k) {
-  double d0 = ((double)i + .5) * K.dx[0] - c0;
-  double d1 = ((double)j + .5) * K.dx[1] - c1;
-  double d2 = ((double)k + .5) * K.dx[2] - c2;
-  const double pi4 = 3.14159265358979323846 / 4.0, pi2 = 3.14159265358979323846 / 2.0;
-  double th = crm_atan2(fabs(d1), fabs(d0));
-  th = th > pi4 ? pi2 - th : th;
-  double ph = crm_atan2(crm_pow_half(d0 * d0 + d1 * d1), fabs(d2));
-  ph = ph < pi4 ? pi2 - ph : ph;
-  double l0 = fabs(R[0] * d0 + R[3] * d1 + R[6] * d2);
-  double l1 = fabs(R[1] * d0 + R[4] * d1 + R[7] * d2);
-  double l2 = fabs(R[2] * d0 + R[5] * d1 + R[8] * d2);
-  return crm_pow_half(crm_cos(th) * crm_sin(ph)) * (l0 + l1 + l2);
-}
-
-// projectPointLine (VoxelsCA.h:78-93)
-__device__ __forceinline__ void cafe_project(const double *A, const double *x0, const double *x1,
-                                             double *xp) {
-  double e0 = x1[0] - x0[0], e1 = x1[1] - x0[1], e2 = x1[2] - x0[2];
-  double snorm = crm_pow_half(e0 * e0 + e1 * e1 + e2 * e2);
-  double n0 = e0 / snorm, n1 = e1 / snorm, n2 = e2 / snorm;
-  double d = -(n0 * A[0] + n1 * A[1] + n2 * A[2]);
-  double t = (-d - n0 * x0[0] - n1 * x0[1] - n2 * x0[2]) / (n0 * e0 + n1 * e1 + n2 * e2);
-  xp[0] = x0[0] + e0 * t;
-  xp[1] = x0[1] + e1 * t;
-  xp[2] = x0[2] + e2 * t;
-}
-
-// Decentered-octahedron capture (VoxelsCA.C:528-605): captured cell (ci,cj,ck),
-// capturing cell (si,sj,sk) with centre cs and rotation R.
-__device__ __noinline__ void cafe_capture_geometry(const CafeConsts &K, int ci, int cj, int ck,
-                                                   int si, int sj, int sk, const double *cs,
-                                                   const double *R, double *ext_out,
-                                                   double *cen_out) {
-  const double pi4 = 3.14159265358979323846 / 4.0, pi2 = 3.14159265358979323846 / 2.0;
-  double q0 = (ci - si) * K.dx[0], q1 = (cj - sj) * K.dx[1], q2 = (ck - sk) * K.dx[2];
-  double l = crm_pow_half(q0 * q0 + q1 * q1 + q2 * q2);
-  double dn[3];
+// One neighbour slot of a capturing cell: the capturing cell (si,sj,sk) with
+// octahedron centre cs and rotation R, the liquid neighbour (ci,cj,ck).
+// g: the capture-time numerator pow(cos th sin ph,.5)*|R^T dn|_1
+// (VoxelsCA.C:409-424, without "- ExtA"); ext and cen: the extent and centre
+// the neighbour receives if this slot captures it (the decentered octahedron
+// construction, VoxelsCA.C:528-605). Both parts share dn, th, ph and R^T dn,
+// which the reference evaluates with identical expressions at the two places.
+//
+// The computation is split into parts with no data dependence between them
+// (the th and ph chains, the two point-line projections) so that the event
+// loop can run them in different warps; cafe_capture_geometry runs them all in
+// one thread. Every part is the same expression sequence wherever it runs.
+__device__ __forceinline__ void cafe_geo_dn(const CafeConsts &K, int ci, int cj, int ck, const double *cs,
+                                            double *dn) {
   dn[0] = ((double)ci + .5) * K.dx[0] - cs[0];
   dn[1] = ((double)cj + .5) * K.dx[1] - cs[1];
   dn[2] = ((double)ck + .5) * K.dx[2] - cs[2];
-  double loc[3];
+}
+// cos(th), th = atan2(|dy|,|dx|) folded at pi/4
+__device__ __forceinline__ double cafe_geo_costh(const double *dn) {
+  const double pi4 = 3.14159265358979323846 / 4.0, pi2 = 3.14159265358979323846 / 2.0;
+  double th = crm_atan2(fabs(dn[1]), fabs(dn[0]));
+  th = th > pi4 ? pi2 - th : th;
+  return crm_cos(th);
+}
+// sin(ph), ph = atan2(sqrt(dx^2+dy^2),|dz|) folded at pi/4
+__device__ __forceinline__ double cafe_geo_sinph(const double *dn) {
+  const double pi4 = 3.14159265358979323846 / 4.0, pi2 = 3.14159265358979323846 / 2.0;
+  double ph = crm_atan2(crm_pow_half(dn[0] * dn[0] + dn[1] * dn[1]), fabs(dn[2]));
+  ph = ph < pi4 ? pi2 - ph : ph;
+  return crm_sin(ph);
+}
+// distance between the capturing and the captured cell centres
+__device__ __forceinline__ double cafe_geo_l(const CafeConsts &K, int ci, int cj, int ck, int si, int sj,
+                                             int sk) {
+  double q0 = (ci - si) * K.dx[0], q1 = (cj - sj) * K.dx[1], q2 = (ck - sk) * K.dx[2];
+  return crm_pow_half(q0 * q0 + q1 * q1 + q2 * q2);
+}
+// dn in the crystal frame, R^T dn, and its 1-norm
+__device__ __forceinline__ double cafe_geo_loc(const double *R, const double *dn, double *loc) {
   loc[0] = R[0] * dn[0] + R[3] * dn[1] + R[6] * dn[2];
   loc[1] = R[1] * dn[0] + R[4] * dn[1] + R[7] * dn[2];
   loc[2] = R[2] * dn[0] + R[5] * dn[1] + R[8] * dn[2];
-  double th = crm_atan2(fabs(dn[1]), fabs(dn[0]));
-  th = th > pi4 ? pi2 - th : th;
-  double ph = crm_atan2(crm_pow_half(dn[0] * dn[0] + dn[1] * dn[1]), fabs(dn[2]));
-  ph = ph < pi4 ? pi2 - ph : ph;
-  double dr = fabs(loc[0]) + fabs(loc[1]) + fabs(loc[2]);
-  // octahedron corners S0*dr and the corner triple of the octant (loadS, VoxelsCA.h:56-77)
+  return fabs(loc[0]) + fabs(loc[1]) + fabs(loc[2]);
+}
+// Corner triple of the octant of loc on the octahedron of half-diagonal dr
+// (loadS, VoxelsCA.h:56-77), ordered nearest, middle, farthest from loc;
+// returns the index into S0 of the nearest corner's direction. A corner S0*dr
+// has one nonzero coordinate (+-dr; the others are +0 for finite dr), so
+// loc - corner is loc itself on two axes and the squared distances
+// e0*e0 + e1*e1 + e2*e2 share those squares; operands are selected per corner
+// so the sums keep the reference's order. Distances are compared as bit
+// patterns (non-negative doubles).
+__device__ __forceinline__ int cafe_geo_corners(const double *loc, double dr, double (*pk)[3]) {
   const signed char S0[6][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}, {-1, 0, 0}, {0, -1, 0}, {0, 0, -1}};
   const unsigned char SI[8][3] = {{0, 1, 2}, {1, 2, 3}, {0, 2, 4}, {2, 3, 4},
                                   {0, 1, 5}, {1, 3, 5}, {0, 4, 5}, {3, 4, 5}};
   int jInd = 4 * (signbit(loc[2]) ? 1 : 0) + 2 * (signbit(loc[1]) ? 1 : 0) + (signbit(loc[0]) ? 1 : 0);
+  int kk[3];
+  if ((crm_bits(dr) & CRM_BITS_INF) != CRM_BITS_INF) {
+    double L0 = loc[0] * loc[0], L1 = loc[1] * loc[1], L2 = loc[2] * loc[2];
+    long long db[3];
+    for (int a = 0; a < 3; ++a) {
+      int idx = SI[jInd][a];
+      int ax = idx < 3 ? idx : idx - 3;
+      double cv = idx < 3 ? dr : -dr;
+      double la = ax == 0 ? loc[0] : (ax == 1 ? loc[1] : loc[2]);
+      double e = la - cv;
+      double D = e * e;
+      double A = ax == 0 ? D : L0, B = ax == 1 ? D : L1, C = ax == 2 ? D : L2;
+      db[a] = crm_bits((A + B) + C);
+    }
+    int imin = 0, imax = 0;
+    for (int a = 1; a < 3; ++a) {
+      if (db[a] < db[imin]) imin = a;
+      if (db[imax] < db[a]) imax = a;
+    }
+    if (imin == imax) {
+      kk[0] = 0;
+      kk[1] = 1;
+      kk[2] = 2;
+    } else {
+      kk[0] = imin;
+      kk[2] = imax;
+      kk[1] = 3 - imin - imax;
+    }
+    for (int a = 0; a < 3; ++a) {
+      int idx = SI[jInd][kk[a]];
+      int ax = idx < 3 ? idx : idx - 3;
+      double cv = idx < 3 ? dr : -dr;
+      for (int b = 0; b < 3; ++b) pk[a][b] = b == ax ? cv : 0.0;
+    }
+    return SI[jInd][kk[0]];
+  }
+  // non-finite dr: the reference's arithmetic as written
   double corner[3][3];
   for (int a = 0; a < 3; ++a)
     for (int b = 0; b < 3; ++b) corner[a][b] = (double)S0[SI[jInd][a]][b] * dr;
@@ -268,45 +307,86 @@ __device__ __noinline__ void cafe_capture_geometry(const CafeConsts &K, int ci, 
     if (dnorm[a] < dnorm[imin]) imin = a;
     if (dnorm[imax] < dnorm[a]) imax = a;
   }
-  int k0, k1, k2;
   if (imin == imax) {
-    k0 = 0;
-    k1 = 1;
-    k2 = 2;
+    kk[0] = 0;
+    kk[1] = 1;
+    kk[2] = 2;
   } else {
-    k0 = imin;
-    k2 = imax;
-    k1 = 3 - imin - imax;
+    kk[0] = imin;
+    kk[2] = imax;
+    kk[1] = 3 - imin - imax;
   }
-  const double *p0 = corner[k0], *p1 = corner[k1], *p2 = corner[k2];
-  double xI[3], xJ[3];
-  cafe_project(loc, p0, p1, xI);
-  cafe_project(loc, p0, p2, xJ);
+  for (int a = 0; a < 3; ++a)
+    for (int b = 0; b < 3; ++b) pk[a][b] = corner[kk[a]][b];
+  return SI[jInd][kk[0]];
+}
+// projectPointLine (VoxelsCA.h:78-93)
+__device__ __forceinline__ void cafe_project(const double *A, const double *x0, const double *x1,
+                                             double *xp) {
+  double e0 = x1[0] - x0[0], e1 = x1[1] - x0[1], e2 = x1[2] - x0[2];
+  double snorm = crm_pow_half(e0 * e0 + e1 * e1 + e2 * e2);
+  double n0 = e0 / snorm, n1 = e1 / snorm, n2 = e2 / snorm;
+  double d = -(n0 * A[0] + n1 * A[1] + n2 * A[2]);
+  double t = (-d - n0 * x0[0] - n1 * x0[1] - n2 * x0[2]) / (n0 * e0 + n1 * e1 + n2 * e2);
+  xp[0] = x0[0] + e0 * t;
+  xp[1] = x0[1] + e1 * t;
+  xp[2] = x0[2] + e2 * t;
+}
+// Projection of loc onto the edge p0-p1 and the distances of the foot point
+// to p0 and to p1 (VoxelsCA.C:566-577 for one of the two edges).
+__device__ __forceinline__ void cafe_geo_edge(const double *loc, const double *p0, const double *p1,
+                                              double *d0, double *d1) {
+  double x[3];
+  cafe_project(loc, p0, p1, x);
   double e0, e1, e2;
-  e0 = p0[0] - xI[0]; e1 = p0[1] - xI[1]; e2 = p0[2] - xI[2];
-  double d1I = crm_pow_half(e0 * e0 + e1 * e1 + e2 * e2);
-  e0 = p1[0] - xI[0]; e1 = p1[1] - xI[1]; e2 = p1[2] - xI[2];
-  double dI2 = crm_pow_half(e0 * e0 + e1 * e1 + e2 * e2);
-  e0 = p0[0] - xJ[0]; e1 = p0[1] - xJ[1]; e2 = p0[2] - xJ[2];
-  double d1J = crm_pow_half(e0 * e0 + e1 * e1 + e2 * e2);
-  e0 = p2[0] - xJ[0]; e1 = p2[1] - xJ[1]; e2 = p2[2] - xJ[2];
-  double dJ3 = crm_pow_half(e0 * e0 + e1 * e1 + e2 * e2);
+  e0 = p0[0] - x[0]; e1 = p0[1] - x[1]; e2 = p0[2] - x[2];
+  *d0 = crm_pow_half(e0 * e0 + e1 * e1 + e2 * e2);
+  e0 = p1[0] - x[0]; e1 = p1[1] - x[1]; e2 = p1[2] - x[2];
+  *d1 = crm_pow_half(e0 * e0 + e1 * e1 + e2 * e2);
+}
+// Half-diagonal Lmud of the new octahedron (VoxelsCA.C:578-582).
+__device__ __forceinline__ double cafe_geo_lmud(const CafeConsts &K, double l, double d1I, double dI2,
+                                                double d1J, double dJ3) {
   double s3l = K.s3 * l;
   // std::min(a,b) = (b < a) ? b : a ; std::max(a,b) = (a < b) ? b : a
   double L12 = .5 * (((s3l < d1I) ? s3l : d1I) + ((s3l < dI2) ? s3l : dI2));
   double L13 = .5 * (((s3l < d1J) ? s3l : d1J) + ((s3l < dJ3) ? s3l : dJ3));
-  double Lmud = K.s3 * (K.s23 * ((L12 < L13) ? L13 : L12));
-  *ext_out = crm_pow_half(crm_cos(th) * crm_sin(ph)) * Lmud * 1.0;
-  const signed char *s0 = S0[SI[jInd][k0]];
+  return K.s3 * (K.s23 * ((L12 < L13) ? L13 : L12));
+}
+// Centre of the new octahedron (VoxelsCA.C:583-604): nearest corner p0 moved
+// back by Lmud along its direction, rotated to the lab frame, plus cs.
+__device__ __forceinline__ void cafe_geo_centre(const double *R, const double *cs, const double *p0, int s0i,
+                                                double Lmud, double *cen) {
+  const signed char S0[6][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}, {-1, 0, 0}, {0, -1, 0}, {0, 0, -1}};
+  const signed char *s0 = S0[s0i];
   double m0 = p0[0] - Lmud * (double)s0[0];
   double m1 = p0[1] - Lmud * (double)s0[1];
   double m2 = p0[2] - Lmud * (double)s0[2];
   double g0 = R[0] * m0 + R[1] * m1 + R[2] * m2;
   double g1 = R[3] * m0 + R[4] * m1 + R[5] * m2;
   double g2 = R[6] * m0 + R[7] * m1 + R[8] * m2;
-  cen_out[0] = cs[0] + g0;
-  cen_out[1] = cs[1] + g1;
-  cen_out[2] = cs[2] + g2;
+  cen[0] = cs[0] + g0;
+  cen[1] = cs[1] + g1;
+  cen[2] = cs[2] + g2;
+}
+__device__ __noinline__ void cafe_capture_geometry(const CafeConsts &K, int ci, int cj, int ck,
+                                                   int si, int sj, int sk, const double *cs,
+                                                   const double *R, double *g_out,
+                                                   double *ext_out, double *cen_out) {
+  double l = cafe_geo_l(K, ci, cj, ck, si, sj, sk);
+  double dn[3], loc[3];
+  cafe_geo_dn(K, ci, cj, ck, cs, dn);
+  double dr = cafe_geo_loc(R, dn, loc);
+  double f = crm_pow_half(cafe_geo_costh(dn) * cafe_geo_sinph(dn));
+  *g_out = f * dr;
+  double pk[3][3];
+  int s0i = cafe_geo_corners(loc, dr, pk);
+  double d1I, dI2, d1J, dJ3;
+  cafe_geo_edge(loc, pk[0], pk[1], &d1I, &dI2);
+  cafe_geo_edge(loc, pk[0], pk[2], &d1J, &dJ3);
+  double Lmud = cafe_geo_lmud(K, l, d1I, dI2, d1J, dJ3);
+  *ext_out = f * Lmud * 1.0;
+  cafe_geo_centre(R, cs, pk[0], s0i, Lmud, cen_out);
 }
 
 // One orientation of SampleOrientation::GenerateSamples (SampleOrientation.C:

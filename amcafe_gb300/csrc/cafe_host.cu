@@ -707,7 +707,10 @@ int cafe_sim_create(const char *deck_path, const cafe_options *opt, cafe_sim **o
   acap = std::min<long long>(acap, N);
   D.act_cap = acap;
   D.vs2_cap = acap;
-  D.row_cap = std::min<long long>(acap, 1LL << 22);
+  // frontier rows (mushy cells with a liquid neighbour): a thin shell around
+  // the pool, far smaller than the active list; an explicit active capacity
+  // raises this limit with it
+  D.row_cap = std::min<long long>(acap, opt && opt->active_capacity > 0 ? (1LL << 22) : (1LL << 20));
   D.ev_cap = acap + 2;
   double est = g.mu * (g.dX[0] * 1e6) * (g.dX[1] * 1e6) * g.nX[0] * g.nX[1] * (s->Nzh * g.dX[2] * 1e6) +
                (s->nlayerTot + 1) * g.lrate * (g.dX[0] * 1e6) * (g.dX[1] * 1e6) * g.nX[0] * g.nX[1] * (g.layerT * 1e6);
@@ -726,10 +729,11 @@ int cafe_sim_create(const char *deck_path, const cafe_options *opt, cafe_sim **o
       (rc = dalloc(&D.a_liq, acap, o)) || (rc = dalloc(&D.a_frow, acap, o)) ||
       (rc = dalloc(&D.a_nbr, (size_t)acap * CAFE_NSLOT, o)) || (rc = dalloc(&D.a_ext, acap, o)) ||
       (rc = dalloc(&D.a_cx, acap, o)) || (rc = dalloc(&D.a_cy, acap, o)) || (rc = dalloc(&D.a_cz, acap, o)) ||
-      (rc = dalloc(&D.a_ruq, acap, o)) || (rc = dalloc(&D.vs2, acap, o)) || (rc = dalloc(&D.row_pos, acap, o)) ||
-      (rc = dalloc(&D.row_j, acap, o)) || (rc = dalloc(&D.row_alive, acap, o)) ||
-      (rc = dalloc(&D.row_ord, (size_t)acap * CAFE_NSLOT, o)) || (rc = dalloc(&D.row_live, acap, o)) ||
-      (rc = dalloc(&D.row_g, (size_t)acap * CAFE_NSLOT, o)) || (rc = dalloc(&D.blk, D.blk_cap, o)) ||
+      (rc = dalloc(&D.a_ruq, acap, o)) || (rc = dalloc(&D.vs2, acap, o)) || (rc = dalloc(&D.row_pos, D.row_cap, o)) ||
+      (rc = dalloc(&D.row_j, D.row_cap, o)) || (rc = dalloc(&D.row_alive, D.row_cap, o)) ||
+      (rc = dalloc(&D.row_ord, (size_t)D.row_cap * CAFE_NSLOT, o)) || (rc = dalloc(&D.row_live, D.row_cap, o)) ||
+      (rc = dalloc(&D.row_g, (size_t)D.row_cap * CAFE_NSLOT, o)) ||
+      (rc = dalloc(&D.row_geo, (size_t)D.row_cap * CAFE_NSLOT * 4, o)) || (rc = dalloc(&D.blk, D.blk_cap, o)) ||
       (rc = dalloc(&D.row_m, D.row_cap, o)) || (rc = dalloc(&D.row_death, D.row_cap, o)) ||
       (rc = dalloc(&D.row_stamp, D.row_cap, o)) || (rc = dalloc(&D.row_bslot, D.row_cap, o)) ||
       (rc = dalloc(&D.row_key, D.row_cap, o)) || (rc = dalloc(&D.row_bt, D.row_cap, o)) ||
@@ -1157,6 +1161,11 @@ int cafe_sim_stats(cafe_sim *s, cafe_stats *st) {
   st->cycles_select = v[STAT_CYC_SELECT];
   st->cycles_apply = v[STAT_CYC_APPLY];
   st->cycles_fill = v[STAT_CYC_FILL];
+#ifdef CAFE_DETAIL_CYCLES
+  fprintf(stderr, "cafe detail cycles:");
+  for (int c = 0; c < 24; ++c) fprintf(stderr, " %llu", v[STAT_DETAIL + c]);
+  fprintf(stderr, "\n");
+#endif
   return CAFE_OK;
 }
 

@@ -444,61 +444,242 @@ __global__ void k_lists_scatter(CafeDev D) {
 }
 
 // ------------------------------------------------------------------ frontier rows
-// Candidate order inside a row: by g, NaN last, ties by slot.
-__device__ __forceinline__ bool cafe_g_before(double ga, int sa, double gb, int sb) {
-  bool na = ga != ga, nb = gb != gb;
-  if (na || nb) return nb && !na ? true : (na && nb ? sa < sb : false);
-  return ga < gb || (ga == gb && sa < sb);
+// Order keys: an unsigned integer order equal to the numeric order of the
+// doubles (negative values included); cafe_key_canon maps -0 to +0 first so
+// that equal values get equal keys.
+#define CAFE_KEY_NONE 0xffffffffffffffffULL
+__device__ __forceinline__ unsigned long long cafe_key(double x) {
+  unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  return (b >> 63) ? ~b : (b | 0x8000000000000000ULL);
+}
+__device__ __forceinline__ double cafe_unkey(unsigned long long k) {
+  unsigned long long b = (k >> 63) ? (k & 0x7fffffffffffffffULL) : ~k;
+  return __longlong_as_double((long long)b);
+}
+__device__ __forceinline__ unsigned long long cafe_key_canon(double x) {
+  unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  if (b == 0x8000000000000000ULL) b = 0;
+  return (b >> 63) ? ~b : (b | 0x8000000000000000ULL);
+}
+__device__ __forceinline__ unsigned long long cafe_shfl_u64(unsigned long long v, int src) {
+  return (unsigned long long)__shfl_sync(0xffffffffu, (long long)v, src);
 }
 
-// Fills row r for position p cooperatively within one warp: lane s computes
-// the numerator of slot s, lane 0 orders the live slots.
-__device__ void cafe_row_fill_warp(const CafeDev &D, const CafeConsts &K, long long r, int p) {
+// Row order, exact best candidate and largest |g| of row r (position p) once
+// every lane of the calling warp holds its slot: liv (the neighbour is liquid),
+// gv (its numerator g) and q (its position). The live slots are ordered by g
+// (NaN last, ties by slot) into row_ord, followed by the other slots. With
+// `eval`, the row's exact best candidate at iteration `ev` and time T is stored
+// (what cafe_row_best computes, one slot per lane). Returns, in every lane, the
+// order key of the largest finite |g| of the live slots, or 0 when none.
+__device__ unsigned long long cafe_row_finish_warp(const CafeDev &D, const CafeConsts &K, long long r, int p,
+                                                   int nn, bool liv, double gv, int q, bool eval, int ev,
+                                                   double T) {
+  const unsigned FULL = 0xffffffffu;
+  int lane = threadIdx.x & 31;
+  uint32_t live = __ballot_sync(FULL, liv);
+  // rank of this slot in the row order
+  unsigned long long key = (liv && gv == gv) ? cafe_key_canon(gv) : CAFE_KEY_NONE;
+  int rank = liv ? 0 : __popc(live);
+  for (int t = 0; t < nn; ++t) {
+    unsigned long long kt = cafe_shfl_u64(key, t);
+    bool lt = (live >> t) & 1u;
+    if (liv)
+      rank += lt && (kt < key || (kt == key && t < lane));
+    else
+      rank += !lt && t < lane;
+  }
+  if (lane < nn) D.row_ord[r * CAFE_NSLOT + rank] = (uint8_t)lane;
+  if (lane == 0) D.row_live[r] = live;
+  if (eval) {
+    double E = D.a_ext[p];
+    double v = K.vhat_cls[D.a_cls[p]];
+    double t = 0.0, ruqs = 0.0;
+    bool cand = false;
+    if (liv) {
+      double dr = gv - E;
+      t = dr / v;
+      cand = t == t;
+      ruqs = .5 * (D.a_ruq[p] + D.a_ruq[q]);
+    }
+    // lexicographic (t, ruqs, slot) minimum over the warp (VoxelsCA.C:427-440)
+    unsigned long long tk = cand ? cafe_key_canon(t) : CAFE_KEY_NONE;
+    unsigned long long rk = cand ? cafe_key_canon(ruqs) : CAFE_KEY_NONE;
+    int sl = cand ? lane : 255;
+    for (int o = 16; o > 0; o >>= 1) {
+      unsigned long long tk2 = (unsigned long long)__shfl_xor_sync(FULL, (long long)tk, o);
+      unsigned long long rk2 = (unsigned long long)__shfl_xor_sync(FULL, (long long)rk, o);
+      int sl2 = __shfl_xor_sync(FULL, sl, o);
+      if (tk2 < tk || (tk2 == tk && (rk2 < rk || (rk2 == rk && sl2 < sl)))) {
+        tk = tk2;
+        rk = rk2;
+        sl = sl2;
+      }
+    }
+    double bt = __shfl_sync(FULL, t, sl & 31);
+    double bruq = __shfl_sync(FULL, ruqs, sl & 31);
+    if (lane == 0) {
+      D.row_stamp[r] = ev + 1;
+      if (sl == 255) {
+        D.row_key[r] = CAFE_KEY_NONE;
+      } else {
+        D.row_bt[r] = bt;
+        D.row_bruq[r] = bruq;
+        D.row_bslot[r] = sl;
+        D.row_key[r] = cafe_key(T + bt);
+      }
+    }
+  }
+  unsigned long long ak = (liv && gv == gv) ? cafe_key(fabs(gv)) : 0ULL;
+  for (int o = 16; o > 0; o >>= 1) ak = max(ak, (unsigned long long)__shfl_xor_sync(FULL, (long long)ak, o));
+  __syncwarp();
+  return ak;
+}
+
+// Fills row r for position p within one warp: lane s evaluates neighbour slot
+// s completely (numerator and capture result), then cafe_row_finish_warp.
+__device__ unsigned long long cafe_row_fill_warp(const CafeDev &D, const CafeConsts &K, long long r,
+                                                 int p, bool eval, int ev, double T) {
   int lane = threadIdx.x & 31;
   int nn = D.a_nn[p];
-  double *g = D.row_g + r * CAFE_NSLOT;
   bool liv = false;
   int gp = D.a_gid[p];
   bool grain_ok = gp >= 1 && gp <= D.grain_cap;
+  double gv = 0.0;
+  int q = 0;
   if (lane < nn) {
-    int q = D.a_nbr[(long long)p * CAFE_NSLOT + lane];
-    if (D.a_state[q] == 1 && !grain_ok) {
-      g[lane] = NAN;  // a capturing cell without a grain never captures
+    q = D.a_nbr[(long long)p * CAFE_NSLOT + lane];
+    if (D.a_state[q] == 1) {
       liv = true;
-    } else if (D.a_state[q] == 1) {
-      const double *R = D.rot + 9LL * (gp - 1);
-      double Rm[9];
-      for (int a = 0; a < 9; ++a) Rm[a] = R[a];
-      int i, j, k;
-      cafe_cell_xyz(K, D.act[q], i, j, k);
-      g[lane] = cafe_candidate_g(K, D.a_cx[p], D.a_cy[p], D.a_cz[p], Rm, i, j, k);
-      liv = true;
-    }
-  }
-  uint32_t live = __ballot_sync(0xffffffffu, liv);
-  __syncwarp();
-  if (lane == 0) {
-    uint8_t *ord = D.row_ord + r * CAFE_NSLOT;
-    int no = 0;
-    for (int s = 0; s < nn; ++s) {
-      if (!(live >> s & 1u)) continue;
-      double gv = g[s];
-      int at = no;
-      while (at > 0 && cafe_g_before(gv, s, g[ord[at - 1]], ord[at - 1])) {
-        ord[at] = ord[at - 1];
-        --at;
+      if (!grain_ok) {
+        gv = NAN;  // a capturing cell without a grain never captures
+      } else {
+        const double *R = D.rot + 9LL * (gp - 1);
+        double Rm[9];
+        for (int a = 0; a < 9; ++a) Rm[a] = R[a];
+        int i, j, k, si, sj, sk;
+        cafe_cell_xyz(K, D.act[q], i, j, k);
+        cafe_cell_xyz(K, D.act[p], si, sj, sk);
+        double cs[3] = {D.a_cx[p], D.a_cy[p], D.a_cz[p]};
+        double e, cn[3];
+        cafe_capture_geometry(K, i, j, k, si, sj, sk, cs, Rm, &gv, &e, cn);
+        double *o = D.row_geo + (r * CAFE_NSLOT + lane) * 4;
+        o[0] = e;
+        o[1] = cn[0];
+        o[2] = cn[1];
+        o[3] = cn[2];
       }
-      ord[at] = (uint8_t)s;
-      ++no;
+      D.row_g[r * CAFE_NSLOT + lane] = gv;
     }
-    // slots that are not candidates follow, so ord is a permutation of 0..nn-1
-    for (int s = 0; s < nn; ++s)
-      if (!(live >> s & 1u)) ord[no++] = (uint8_t)s;
-    D.row_live[r] = live;
   }
-  __syncwarp();
+  return cafe_row_finish_warp(D, K, r, p, nn, liv, gv, q, eval, ev, T);
 }
 
+// Per-slot partial results passed between the four warps of cafe_row_fill_quad.
+struct CafeQuadScratch {
+  double cth[32], sph[32], l[32], d1I[32], dI2[32], d1J[32], dJ3[32], g[32];
+};
+#define CAFE_QUAD_THREADS 128
+__device__ __forceinline__ void cafe_bar_quad() { asm volatile("bar.sync 1, 128;" ::: "memory"); }
+
+// cafe_row_fill_warp for warps 0-3 of the block together (all 128 threads
+// must call it): a warp issues one FP64 instruction at a time whatever its
+// active lanes, so the independent chains of each slot's geometry run in
+// different warps, lane s of each warp on slot s:
+//   warp 0: cos th and the cell distance l; warp 1: sin ph;
+//   warp 2: the projection on edge p0-p1, then g and the extent;
+//   warp 3: the projection on edge p0-p2, then the new centre.
+// Warp 0 finishes the row; the return value is valid in warp 0.
+__device__ unsigned long long cafe_row_fill_quad(const CafeDev &D, const CafeConsts &K, long long r, int p,
+                                                 bool eval, int ev, double T, CafeQuadScratch &S) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#ifdef CAFE_DETAIL_CYCLES
+  long long fq0 = clock64();
+#endif
+  int nn = D.a_nn[p];
+  int gp = D.a_gid[p];
+  bool grain_ok = gp >= 1 && gp <= D.grain_cap;
+  bool liv = false;
+  int q = 0;
+  double dn[3] = {0.0, 0.0, 0.0}, cs[3] = {0.0, 0.0, 0.0};
+  int ci = 0, cj = 0, ck = 0, si = 0, sj = 0, sk = 0;
+  if (lane < nn) {
+    q = D.a_nbr[(long long)p * CAFE_NSLOT + lane];
+    liv = D.a_state[q] == 1;
+  }
+  const bool work = liv && grain_ok;
+  double R[9], loc[3], dr = 0.0, pk[3][3];
+  int s0i = 0;
+  if (work) {
+    cafe_cell_xyz(K, D.act[q], ci, cj, ck);
+    cafe_cell_xyz(K, D.act[p], si, sj, sk);
+    cs[0] = D.a_cx[p];
+    cs[1] = D.a_cy[p];
+    cs[2] = D.a_cz[p];
+    cafe_geo_dn(K, ci, cj, ck, cs, dn);
+    if (w == 0) {
+      S.cth[lane] = cafe_geo_costh(dn);
+      S.l[lane] = cafe_geo_l(K, ci, cj, ck, si, sj, sk);
+    } else if (w == 1) {
+      S.sph[lane] = cafe_geo_sinph(dn);
+    } else {
+      const double *Rg = D.rot + 9LL * (gp - 1);
+      for (int a = 0; a < 9; ++a) R[a] = Rg[a];
+      dr = cafe_geo_loc(R, dn, loc);
+      s0i = cafe_geo_corners(loc, dr, pk);
+      if (w == 2)
+        cafe_geo_edge(loc, pk[0], pk[1], &S.d1I[lane], &S.dI2[lane]);
+      else
+        cafe_geo_edge(loc, pk[0], pk[2], &S.d1J[lane], &S.dJ3[lane]);
+    }
+  }
+#ifdef CAFE_DETAIL_CYCLES
+  long long fq1 = clock64();
+#endif
+  cafe_bar_quad();
+#ifdef CAFE_DETAIL_CYCLES
+  long long fq2 = clock64();
+#endif
+  double gv = liv ? NAN : 0.0;  // a capturing cell without a grain never captures
+  if (work && w >= 2) {
+    double Lmud = cafe_geo_lmud(K, S.l[lane], S.d1I[lane], S.dI2[lane], S.d1J[lane], S.dJ3[lane]);
+    double *o = D.row_geo + (r * CAFE_NSLOT + lane) * 4;
+    if (w == 2) {
+      double f = crm_pow_half(S.cth[lane] * S.sph[lane]);
+      gv = f * dr;
+      S.g[lane] = gv;
+      o[0] = f * Lmud * 1.0;
+    } else {
+      double cn[3];
+      cafe_geo_centre(R, cs, pk[0], s0i, Lmud, cn);
+      o[1] = cn[0];
+      o[2] = cn[1];
+      o[3] = cn[2];
+    }
+  }
+#ifdef CAFE_DETAIL_CYCLES
+  long long fq3 = clock64();
+#endif
+  cafe_bar_quad();
+  unsigned long long ak = 0ULL;
+  if (w == 0) {
+    if (work) gv = S.g[lane];
+    if (liv) D.row_g[r * CAFE_NSLOT + lane] = gv;
+    ak = cafe_row_finish_warp(D, K, r, p, nn, liv, gv, q, eval, ev, T);
+  }
+#ifdef CAFE_DETAIL_CYCLES
+  if (lane == 0) {
+    long long fq4 = clock64();
+    atomicAdd(&D.stat[STAT_DETAIL + 16 + w], (unsigned long long)(fq1 - fq0));
+    if (w >= 2) atomicAdd(&D.stat[STAT_DETAIL + 18 + w], (unsigned long long)(fq3 - fq2));
+    if (w == 0) {
+      atomicAdd(&D.stat[STAT_DETAIL + 22], (unsigned long long)(fq4 - fq3));
+      atomicAdd(&D.stat[STAT_DETAIL + 23], 1ULL);
+    }
+  }
+#endif
+  return ak;
+}
 
 // ------------------------------------------------------------------ event loop
 struct CafeCand {
@@ -572,12 +753,18 @@ __device__ __forceinline__ void cafe_row_best(const CafeDev &D, const CafeConsts
   }
 }
 
+// Slot of `target` in q's neighbour list, -1 if absent. All CAFE_NSLOT entries
+// are loaded at once (the list storage is always that long) and masked by nn.
 __device__ __forceinline__ int cafe_find_slot(const CafeDev &D, int q, int target) {
   int nn = D.a_nn[q];
   const int32_t *nb = D.a_nbr + (long long)q * CAFE_NSLOT;
-  for (int s = 0; s < nn; ++s)
-    if (nb[s] == target) return s;
-  return -1;
+  int found = -1;
+#pragma unroll
+  for (int s = CAFE_NSLOT - 1; s >= 0; --s) {
+    int v = nb[s];
+    if (s < nn && v == target) found = s;
+  }
+  return found;
 }
 
 // ---- lazily grown rows ------------------------------------------------------
@@ -591,17 +778,7 @@ __device__ __forceinline__ int cafe_find_slot(const CafeDev &D, int q, int targe
 // whose key lies within twice that bound of the smallest key. The growth itself
 // is logged once per event and replayed per row when the row is evaluated, and
 // for every row at the end of the step (k_rows_finalize, across the GPU).
-#define CAFE_KEY_NONE 0xffffffffffffffffULL
 #define CAFE_M_DONE 0x7fffffff  // row extent needs no further replay
-
-__device__ __forceinline__ unsigned long long cafe_key(double x) {
-  unsigned long long b = (unsigned long long)__double_as_longlong(x);
-  return (b >> 63) ? ~b : (b | 0x8000000000000000ULL);
-}
-__device__ __forceinline__ double cafe_unkey(unsigned long long k) {
-  unsigned long long b = (k >> 63) ? (k & 0x7fffffffffffffffULL) : ~k;
-  return __longlong_as_double((long long)b);
-}
 
 // Applies the logged growth of events row_m+1 .. min(upto, row_death).
 __device__ __forceinline__ void cafe_row_replay(const CafeDev &D, int r, int upto) {
@@ -651,12 +828,11 @@ __global__ void k_rows_init(CafeDev D, CafeConsts K) {
   const double V = K.vhat_cls[1];
   for (int r = w; r < nrows; r += warps) {
     int p = D.row_pos[r];
-    cafe_row_fill_warp(D, K, r, p);
+    cafe_row_fill_warp(D, K, r, p, true, 0, 0.0);
     if (lane == 0) {
       D.row_m[r] = 0;
       D.row_death[r] = CAFE_M_DONE;
       if (D.a_cls[p] != 1 || !(V > 0.0 && V < INFINITY)) atomicOr(&D.ctr[CTR_SLOW], 1);
-      cafe_row_eval(D, K, r, 0, 0.0);
     }
   }
 }
@@ -667,7 +843,7 @@ __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
   __shared__ CafeCand red[CAFE_LOOP_THREADS / 32];
   __shared__ unsigned long long redk[CAFE_LOOP_THREADS / 32];
   __shared__ double s_tinc, s_dt, s_dsum, s_gmax, s_emax, s_vs;
-  __shared__ int s_nvs2, s_countS, s_nrows, s_ngrain, s_done, s_nuc, s_icap, s_jspos, s_na, s_slow,
+  __shared__ int s_nvs2, s_countS, s_nrows, s_ngrain, s_done, s_nuc, s_icap, s_jspos, s_bslot, s_na, s_slow,
       s_ev, s_switch;
   __shared__ unsigned long long s_kthr;
   __shared__ uint32_t s_rng;
@@ -675,6 +851,30 @@ __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
   __shared__ long long s_nnuc, s_negdt, s_evals;
   __shared__ long long s_cyc[4];  // selection, capture apply, bookkeeping + new row, other
   __shared__ long long s_t0;
+  __shared__ CafeQuadScratch s_quad;
+#ifdef CAFE_DETAIL_CYCLES
+  // finer event-loop sections, thread 0's clock (profiling builds only)
+  __shared__ long long s_dcyc[16], s_dt0;
+#define CAFE_DCYC(slot)                  \
+  do {                                   \
+    if (threadIdx.x == 0) {              \
+      long long _t = clock64();          \
+      s_dcyc[slot] += _t - s_dt0;        \
+      s_dt0 = _t;                        \
+    }                                    \
+  } while (0)
+  if (threadIdx.x < 16) s_dcyc[threadIdx.x] = 0;
+  __shared__ unsigned long long s_fb0, s_sp0;
+  if (threadIdx.x == 0) {
+    s_dt0 = clock64();
+    s_fb0 = *(volatile unsigned long long *)&crm_fallback_calls;
+    s_sp0 = *(volatile unsigned long long *)&crm_special_calls;
+  }
+#else
+#define CAFE_DCYC(slot) \
+  do {                  \
+  } while (0)
+#endif
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int nthr = blockDim.x, nwarp = blockDim.x >> 5;
   const double V = K.vhat_cls[1];
@@ -753,6 +953,7 @@ __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
     }
     __syncthreads();
     if (s_done) break;
+    CAFE_DCYC(15);
     if (tid == 0) s_t0 = clock64();
     CafeCand best;
     best.j = -1;
@@ -787,6 +988,7 @@ __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
           }
         }
         __syncthreads();
+        CAFE_DCYC(0);
         const unsigned long long kthr = s_kthr;
         int again = 0;
         if (kthr != CAFE_KEY_NONE) {
@@ -799,6 +1001,7 @@ __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
           }
         }
         again = __syncthreads_or(again);
+        CAFE_DCYC(1);
         if (tid == 0 && again) s_evals++;
         if (!again) break;
       }
@@ -821,6 +1024,7 @@ __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
     }
     if (lane == 0) red[warp] = best;
     __syncthreads();
+    CAFE_DCYC(2);
     if (tid == 0) {
       long long tn = clock64();
       s_cyc[0] += tn - s_t0;
@@ -828,6 +1032,7 @@ __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
       CafeCand b = red[0];
       for (int w = 1; w < nwarp; ++w)
         if (cafe_cand_better(red[w], b)) b = red[w];
+      CAFE_DCYC(3);
       if (b.j < 0 || !(b.t < 1e6) || s_ev >= max_events) {
         if (b.j >= 0 && b.t < 1e6) atomicOr(D.err, CAFE_ERR_ITER_CAP);
         s_done = 1;
@@ -838,6 +1043,7 @@ __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
         s_rng = st.x;
         int jspos = D.vs2[b.j];
         s_jspos = jspos;
+        s_bslot = b.s;
         s_icap = D.a_nbr[(long long)jspos * CAFE_NSLOT + b.s];
         s_nuc = U < K.rX;
         s_dt = s_nuc ? 0.0 : b.t;
@@ -853,6 +1059,7 @@ __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
           s_dsum += fabs(s_dt);
         }
       }
+      CAFE_DCYC(4);
     }
     __syncthreads();
     if (s_done) break;
@@ -877,6 +1084,7 @@ __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
       }
     }
     __syncthreads();
+    CAFE_DCYC(5);
     // ---- the captured cell (VoxelsCA.C:483-505 and 518-605)
     if (tid == 0) {
       int icap = s_icap, js = s_jspos;
@@ -888,9 +1096,9 @@ __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
         s_done = 1;
       }
       s_nvs2 += 1;
-      int ci, cj, ck;
-      cafe_cell_xyz(K, D.act[icap], ci, cj, ck);
       if (s_nuc) {
+        int ci, cj, ck;
+        cafe_cell_xyz(K, D.act[icap], ci, cj, ck);
         if (s_ngrain < D.grain_cap) {
           double q4[4];
           cafe_sample_orientation(K, s_sdloc, q4);
@@ -910,19 +1118,15 @@ __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
         D.a_ext[icap] = 0.0;
         s_nnuc++;
       } else {
-        int g = D.a_gid[js];
-        if (g < 1 || g > D.grain_cap) g = 1;  // unreachable: rows of grainless cells hold no finite time
+        // the capture result of this slot, computed when the row was filled
         D.a_gid[icap] = D.a_gid[js];
-        int si, sj, sk;
-        cafe_cell_xyz(K, D.act[js], si, sj, sk);
-        double cs[3] = {D.a_cx[js], D.a_cy[js], D.a_cz[js]};
-        double e, cn[3];
-        cafe_capture_geometry(K, ci, cj, ck, si, sj, sk, cs, D.rot + 9LL * (g - 1), &e, cn);
-        D.a_ext[icap] = e;
-        D.a_cx[icap] = cn[0];
-        D.a_cy[icap] = cn[1];
-        D.a_cz[icap] = cn[2];
+        const double *gq = D.row_geo + ((long long)D.a_frow[js] * CAFE_NSLOT + s_bslot) * 4;
+        D.a_ext[icap] = gq[0];
+        D.a_cx[icap] = gq[1];
+        D.a_cy[icap] = gq[2];
+        D.a_cz[icap] = gq[3];
       }
+      CAFE_DCYC(6);
       s_tinc += s_dt;
       long long tn = clock64();
       s_cyc[1] += tn - s_t0;
@@ -947,12 +1151,16 @@ __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
           }
         }
       }
-      __syncwarp();
-      // ---- the captured cell becomes a capturing cell if it qualifies
+    }
+    __syncthreads();
+    CAFE_DCYC(7);
+    // ---- the captured cell becomes a capturing cell if it qualifies (warps 0-3)
+    if (warp < CAFE_QUAD_THREADS / 32) {
+      int icap = s_icap;
       if (D.a_liq[icap] > 0 && D.a_cold[icap] && !s_done) {
         int r = s_nrows;
         if (r < D.row_cap) {
-          if (lane == 0) {
+          if (tid == 0) {
             D.row_pos[r] = icap;
             D.row_j[r] = s_nvs2 - 1;
             D.row_alive[r] = 1;
@@ -960,34 +1168,33 @@ __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
             D.row_death[r] = CAFE_M_DONE;
             D.row_m[r] = s_slow ? CAFE_M_DONE : s_ev;
           }
-          __syncwarp();
-          cafe_row_fill_warp(D, K, r, icap);
-          if (lane == 0) {
+          const bool same_v = D.a_cls[icap] == 1;
+          unsigned long long gk = cafe_row_fill_quad(D, K, r, icap, !s_slow && same_v, s_ev, s_tinc, s_quad);
+          CAFE_DCYC(8);
+          if (tid == 0) {
             if (!s_slow) {
-              if (D.a_cls[icap] != 1) {
+              if (!same_v) {
                 s_switch = 1;
               } else {
-                cafe_row_eval(D, K, r, s_ev, s_tinc);
-                int nn2 = D.a_nn[icap];
-                uint32_t live = D.row_live[r];
-                for (int k = 0; k < nn2; ++k)
-                  if (live >> k & 1u) {
-                    double gv = fabs(D.row_g[(long long)r * CAFE_NSLOT + k]);
-                    if (gv > s_gmax) s_gmax = gv;
-                  }
+                if (gk != 0ULL) {
+                  double gm = cafe_unkey(gk);
+                  if (gm > s_gmax) s_gmax = gm;
+                }
                 double ea = fabs(D.a_ext[icap]);
                 if (ea > s_emax) s_emax = ea;
+                CAFE_DCYC(10);
               }
             }
             s_nrows = r + 1;
           }
-        } else if (lane == 0) {
+        } else if (tid == 0) {
           atomicOr(D.err, CAFE_ERR_ROW_CAP);
           s_done = 1;
         }
       }
     }
     __syncthreads();
+    CAFE_DCYC(11);
     if (tid == 0) {
       long long tn = clock64();
       s_cyc[2] += tn - s_t0;
@@ -1021,6 +1228,7 @@ __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
       }
     }
     __syncthreads();
+    CAFE_DCYC(12);
   }
   if (tid == 0) {
     D.ctr[CTR_NGRAIN] = s_ngrain;
@@ -1039,6 +1247,12 @@ __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
     atomicAdd(&D.stat[STAT_EVALS], (unsigned long long)s_evals);
     if (s_slow) atomicAdd(&D.stat[STAT_SLOWSTEPS], 1ULL);
     for (int c = 0; c < 4; ++c) atomicAdd(&D.stat[STAT_CYC_SELECT + c], (unsigned long long)s_cyc[c]);
+#ifdef CAFE_DETAIL_CYCLES
+    for (int c = 0; c < 16; ++c)
+      if (c != 9 && c != 13 && c != 14) atomicAdd(&D.stat[STAT_DETAIL + c], (unsigned long long)s_dcyc[c]);
+    atomicAdd(&D.stat[STAT_DETAIL + 9], *(volatile unsigned long long *)&crm_fallback_calls - s_fb0);
+    atomicAdd(&D.stat[STAT_DETAIL + 13], *(volatile unsigned long long *)&crm_special_calls - s_sp0);
+#endif
   }
 }
 
