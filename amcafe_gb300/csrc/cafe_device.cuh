@@ -96,18 +96,15 @@ struct CafeDev {
   // this slot captures it, 4 doubles
   double *row_geo;
   long long row_cap;
-  // lazily grown rows: a_ext of the row's cell includes the growth of events
-  // 1..row_m; the row grows at events (birth, row_death]; row_key orders the
-  // rows by estimated absolute capture time; row_b* hold the exact best
-  // candidate of the iteration row_stamp
-  int32_t *row_m, *row_death, *row_stamp, *row_bslot;
+  // rows during the event loop: row_E is the row cell's extent (ExtA), kept
+  // current at every event and copied back to a_ext afterwards; a row grows at
+  // the events (birth, row_death]; row_key orders the rows by estimated
+  // absolute capture time; row_b* hold the exact best candidate of the
+  // iteration row_stamp
+  double *row_E;
+  int32_t *row_death, *row_stamp, *row_bslot;
   unsigned long long *row_key;
   double *row_bt, *row_bruq;
-  // per-event growth log: ev_vd[e] = fl(v * DtMin_e) for captures (ev_grew[e] = 1),
-  // ev_vs[e] = running sum of ev_vd
-  double *ev_vd, *ev_vs;
-  uint8_t *ev_grew;
-  long long ev_cap;
   // scan scratch
   int32_t *blk;       // per-block counts / offsets
   long long blk_cap;

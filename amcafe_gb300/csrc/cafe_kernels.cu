@@ -464,6 +464,15 @@ __device__ __forceinline__ unsigned long long cafe_key_canon(double x) {
 __device__ __forceinline__ unsigned long long cafe_shfl_u64(unsigned long long v, int src) {
   return (unsigned long long)__shfl_sync(0xffffffffu, (long long)v, src);
 }
+__device__ __forceinline__ unsigned long long cafe_shfl_u64_xor(unsigned long long v, int o) {
+  return (unsigned long long)__shfl_xor_sync(0xffffffffu, (long long)v, o);
+}
+__device__ __forceinline__ bool cafe_is_nan(double x) { return (crm_bits(x) & CRM_ABS_MASK) > CRM_BITS_INF; }
+// x < 0.0 (negative, nonzero, not NaN)
+__device__ __forceinline__ bool cafe_is_neg(double x) {
+  long long b = crm_bits(x);
+  return b < 0 && (b & CRM_ABS_MASK) != 0 && (b & CRM_ABS_MASK) <= CRM_BITS_INF;
+}
 
 // Row order, exact best candidate and largest |g| of row r (position p) once
 // every lane of the calling warp holds its slot: liv (the neighbour is liquid),
@@ -682,30 +691,50 @@ __device__ unsigned long long cafe_row_fill_quad(const CafeDev &D, const CafeCon
 }
 
 // ------------------------------------------------------------------ event loop
+// A capture candidate: time t and tie-break ruqs, compared through their
+// order keys (equal doubles give equal keys; NaN times are never candidates).
 struct CafeCand {
+  unsigned long long tk, rk;
   double t, ruqs;
   int j, s;  // vs2 index and neighbour slot of the capturing cell; j < 0 = none
 };
+__device__ __forceinline__ CafeCand cafe_cand_none() {
+  CafeCand c;
+  c.tk = c.rk = CAFE_KEY_NONE;
+  c.t = c.ruqs = 0.0;
+  c.j = -1;
+  c.s = 0;
+  return c;
+}
 __device__ __forceinline__ bool cafe_cand_better(const CafeCand &a, const CafeCand &b) {
   // lexicographic (t, ruqs, scan position): VoxelsCA.C:427-440 keeps the first
   // scanned candidate among full ties
   if (a.j < 0) return false;
   if (b.j < 0) return true;
-  if (a.t < b.t) return true;
-  if (b.t < a.t) return false;
-  if (a.ruqs < b.ruqs) return true;
-  if (b.ruqs < a.ruqs) return false;
+  if (a.tk != b.tk) return a.tk < b.tk;
+  if (a.rk != b.rk) return a.rk < b.rk;
   if (a.j != b.j) return a.j < b.j;
   return a.s < b.s;
 }
 __device__ __forceinline__ CafeCand cafe_shfl_cand(const CafeCand &c, int o) {
   CafeCand r;
-  r.t = __shfl_down_sync(0xffffffffu, c.t, o);
-  r.ruqs = __shfl_down_sync(0xffffffffu, c.ruqs, o);
-  r.j = __shfl_down_sync(0xffffffffu, c.j, o);
-  r.s = __shfl_down_sync(0xffffffffu, c.s, o);
+  r.tk = cafe_shfl_u64_xor(c.tk, o);
+  r.rk = cafe_shfl_u64_xor(c.rk, o);
+  r.t = __shfl_xor_sync(0xffffffffu, c.t, o);
+  r.ruqs = __shfl_xor_sync(0xffffffffu, c.ruqs, o);
+  r.j = __shfl_xor_sync(0xffffffffu, c.j, o);
+  r.s = __shfl_xor_sync(0xffffffffu, c.s, o);
   return r;
 }
+// Best candidate of the warp, in every lane.
+__device__ __forceinline__ CafeCand cafe_warp_best(CafeCand best) {
+  for (int o = 16; o > 0; o >>= 1) {
+    CafeCand c = cafe_shfl_cand(best, o);
+    if (cafe_cand_better(c, best)) best = c;
+  }
+  return best;
+}
+#define CAFE_KEY_1E6 0xc12e848000000000ULL  // cafe_key(1e6)
 
 // Best candidate of frontier row r (VoxelsCA.C:386-445 restricted to one cell)
 // with the row cell's current extent. For a positive finite growth velocity the
@@ -718,37 +747,41 @@ __device__ __forceinline__ void cafe_row_best(const CafeDev &D, const CafeConsts
   int p = D.row_pos[r];
   uint32_t live = D.row_live[r];
   if (!live) return;
-  double E = D.a_ext[p];
+  double E = D.row_E[r];
   double v = K.vhat_cls[D.a_cls[p]];
-  bool mono = (v > 0.0) && (v < INFINITY);
+  long long vb = crm_bits(v);
+  bool mono = vb > 0 && vb < CRM_BITS_INF;  // 0 < v < inf
   const double *g = D.row_g + r * CAFE_NSLOT;
   const uint8_t *ord = D.row_ord + r * CAFE_NSLOT;
   int nn = D.a_nn[p];
   int jrow = D.row_j[r];
   double ruq_p = D.a_ruq[p];
   bool have = false;
-  double tfirst = 0.0;
+  unsigned long long tfirst = 0;
   for (int k = 0; k < nn; ++k) {
     int s = mono ? ord[k] : k;
     if (!(live >> s & 1u)) continue;
     double dr = g[s] - E;
     double t = dr / v;
-    if (t != t) continue;
-    if (bounded && !(t <= 1e6)) {
+    if (cafe_is_nan(t)) continue;
+    unsigned long long tk = cafe_key_canon(t);
+    if (bounded && !(tk <= CAFE_KEY_1E6)) {
       if (mono) break;
       continue;
     }
-    if (mono && have && t > tfirst) break;
+    if (mono && have && tk > tfirst) break;
     int q = D.a_nbr[(long long)p * CAFE_NSLOT + s];
     CafeCand c;
     c.t = t;
+    c.tk = tk;
     c.ruqs = .5 * (ruq_p + D.a_ruq[q]);
+    c.rk = cafe_key_canon(c.ruqs);
     c.j = jrow;
     c.s = s;
     if (cafe_cand_better(c, best)) best = c;
     if (!have) {
       have = true;
-      tfirst = t;
+      tfirst = tk;
     }
   }
 }
@@ -767,7 +800,7 @@ __device__ __forceinline__ int cafe_find_slot(const CafeDev &D, int q, int targe
   return found;
 }
 
-// ---- lazily grown rows ------------------------------------------------------
+// ---- keyed rows -------------------------------------------------------------
 // Every frontier cell of a step grows by the same fl(v * DtMin) at every capture
 // event while it has a liquid neighbour (VoxelsCA.C:511-516), and a row's
 // candidate times all fall by about DtMin per event. A row therefore carries a
@@ -775,36 +808,16 @@ __device__ __forceinline__ int cafe_find_slot(const CafeDev &D, int q, int targe
 // evaluated exactly. Between evaluations the key is within a small rounding
 // bound of the row's exact current value (or below it once a candidate was
 // captured by someone else), so the event needs exact times only for the rows
-// whose key lies within twice that bound of the smallest key. The growth itself
-// is logged once per event and replayed per row when the row is evaluated, and
-// for every row at the end of the step (k_rows_finalize, across the GPU).
-#define CAFE_M_DONE 0x7fffffff  // row extent needs no further replay
-
-// Applies the logged growth of events row_m+1 .. min(upto, row_death).
-__device__ __forceinline__ void cafe_row_replay(const CafeDev &D, int r, int upto) {
-  int m = D.row_m[r];
-  int stop = min(upto, D.row_death[r]);
-  if (stop <= m) return;
-  int p = D.row_pos[r];
-  double E = D.a_ext[p];
-  for (int k = m + 1; k <= stop; ++k) {
-    if (D.ev_grew[k]) {
-      E = E + D.ev_vd[k];
-      E = (E < 0.0) ? 0.0 : E;
-    }
-  }
-  D.a_ext[p] = E;
-  D.row_m[r] = stop;
-}
+// whose key lies within twice that bound of the smallest key. An extent clamped
+// at zero by a negative event (VoxelsCA.C:515) breaks the bound; such rows are
+// stamped -1 and evaluated again. The growth itself is applied to every row at
+// every event, by the warps that do not take part in the capture.
+#define CAFE_ALIVE 0x7fffffff  // row_death of a row that is still alive
 
 // Exact evaluation of row r for the iteration after `ev` events at time T.
 __device__ __forceinline__ void cafe_row_eval(const CafeDev &D, const CafeConsts &K, int r, int ev,
                                               double T) {
-  cafe_row_replay(D, r, ev);
-  CafeCand b;
-  b.j = -1;
-  b.t = b.ruqs = 0;
-  b.s = 0;
+  CafeCand b = cafe_cand_none();
   cafe_row_best(D, K, r, b, false);
   D.row_stamp[r] = ev + 1;
   if (b.j < 0) {
@@ -830,8 +843,8 @@ __global__ void k_rows_init(CafeDev D, CafeConsts K) {
     int p = D.row_pos[r];
     cafe_row_fill_warp(D, K, r, p, true, 0, 0.0);
     if (lane == 0) {
-      D.row_m[r] = 0;
-      D.row_death[r] = CAFE_M_DONE;
+      D.row_E[r] = D.a_ext[p];
+      D.row_death[r] = CAFE_ALIVE;
       if (D.a_cls[p] != 1 || !(V > 0.0 && V < INFINITY)) atomicOr(&D.ctr[CTR_SLOW], 1);
     }
   }
@@ -842,10 +855,13 @@ __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
     k_event_loop(CafeDev D, CafeConsts K, CafeStepParams P, long long max_events, int allow_fast) {
   __shared__ CafeCand red[CAFE_LOOP_THREADS / 32];
   __shared__ unsigned long long redk[CAFE_LOOP_THREADS / 32];
-  __shared__ double s_tinc, s_dt, s_dsum, s_gmax, s_emax, s_vs;
+  __shared__ double s_tinc, s_dt, s_dsum, s_gmax, s_emax, s_vd;
   __shared__ int s_nvs2, s_countS, s_nrows, s_ngrain, s_done, s_nuc, s_icap, s_jspos, s_bslot, s_na, s_slow,
       s_ev, s_switch;
   __shared__ unsigned long long s_kthr;
+  __shared__ unsigned char s_dirty[CAFE_LOOP_THREADS];   // a row of thread i changed its key elsewhere
+  __shared__ unsigned char s_forced[CAFE_LOOP_THREADS];  // a row of thread i was stamped -1
+  __shared__ float s_magf, s_invVf;  // |T| + (gmax+emax)/v + 2 sum|dt| (upper bound), 1/v
   __shared__ uint32_t s_rng;
   __shared__ unsigned int s_sdloc;
   __shared__ long long s_nnuc, s_negdt, s_evals;
@@ -878,6 +894,10 @@ __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int nthr = blockDim.x, nwarp = blockDim.x >> 5;
   const double V = K.vhat_cls[1];
+  unsigned long long my_min = CAFE_KEY_NONE;  // smallest key of this thread's rows
+  bool my_forced = false;                     // one of them is stamped for re-evaluation
+  s_dirty[tid] = 1;
+  s_forced[tid] = 0;
   if (tid == 0) {
     s_na = D.ctr[CTR_NA];
     s_nvs2 = D.ctr[CTR_NVS2];
@@ -888,7 +908,7 @@ __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
     s_sdloc = K.seed0 + 32u * (unsigned int)P.tInd + 64u * (unsigned int)s_ngrain;
     s_tinc = 0.0;
     s_dsum = 0.0;
-    s_vs = 0.0;
+    s_vd = 0.0;
     s_countS = s_na;
     s_nnuc = 0;
     s_negdt = 0;
@@ -896,19 +916,10 @@ __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
     s_ev = 0;
     s_switch = 0;
     s_cyc[0] = s_cyc[1] = s_cyc[2] = s_cyc[3] = 0;
-    D.ev_vs[0] = 0.0;
-    D.ev_vd[0] = 0.0;
-    D.ev_grew[0] = 0;
+    s_invVf = 1.0f / (float)V;
+    s_magf = 0.0f;
     s_slow = !allow_fast || D.ctr[CTR_SLOW] != 0;
     s_done = (*D.err != 0) || (s_na > D.act_cap) || (s_nvs2 > D.vs2_cap) || (s_nrows > D.row_cap);
-    if (!s_done && s_slow) {
-      // exact per-event scan with eager growth; row extents are kept current
-      for (int r = 0; r < s_nrows; ++r) D.row_m[r] = CAFE_M_DONE;
-    }
-    if (s_na + 2 > D.ev_cap) {
-      atomicOr(D.err, CAFE_ERR_ITER_CAP);
-      s_done = 1;
-    }
   }
   __syncthreads();
   // magnitudes for the key rounding bound: largest numerator and extent
@@ -950,91 +961,119 @@ __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
       // while (vSind2 != countS && tinc < DelT)
       if (!(s_nvs2 != s_countS && s_tinc < K.DelT)) s_done = 1;
       s_countS = s_nvs2;
+      if (!s_slow)
+        s_magf = (float)fabs(s_tinc) + (float)(s_gmax + s_emax) * s_invVf + 2.0f * (float)s_dsum;
     }
     __syncthreads();
     if (s_done) break;
     CAFE_DCYC(15);
     if (tid == 0) s_t0 = clock64();
-    CafeCand best;
-    best.j = -1;
-    best.t = 0;
-    best.ruqs = 0;
-    best.s = 0;
+    CafeCand best = cafe_cand_none();
     if (s_slow) {
       // ---- exact scan of every row (VoxelsCA.C:386-445)
       for (int r = tid; r < s_nrows; r += nthr)
         if (D.row_alive[r]) cafe_row_best(D, K, r, best);
     } else {
-      // ---- keyed selection: exact evaluation only near the smallest key
+      // ---- keyed selection: exact evaluation only near the smallest key.
+      // Thread tid owns the rows r = tid (mod nthr) and keeps the smallest key
+      // among them in my_min; it rescans them when another thread changed one
+      // of their keys (s_dirty).
       const int ev = s_ev;
+      if (s_forced[tid]) {
+        s_forced[tid] = 0;
+        my_forced = true;
+      }
+      if (s_dirty[tid]) {
+        s_dirty[tid] = 0;
+        unsigned long long m = CAFE_KEY_NONE;
+        for (int r = tid; r < s_nrows; r += nthr) m = min(m, D.row_key[r]);
+        my_min = m;
+      }
       while (true) {
-        unsigned long long km = CAFE_KEY_NONE;
-        for (int r = tid; r < s_nrows; r += nthr)
-          if (D.row_alive[r]) km = min(km, D.row_key[r]);
-        for (int o = 16; o > 0; o >>= 1) km = min(km, __shfl_down_sync(0xffffffffu, km, o));
+        unsigned long long km = my_min;
+        for (int o = 16; o > 0; o >>= 1) km = min(km, cafe_shfl_u64_xor(km, o));
         if (lane == 0) redk[warp] = km;
         __syncthreads();
-        if (tid == 0) {
-          unsigned long long k0 = redk[0];
-          for (int w = 1; w < nwarp; ++w) k0 = min(k0, redk[w]);
-          if (k0 == CAFE_KEY_NONE) {
-            s_kthr = CAFE_KEY_NONE;
-          } else {
-            double kd = cafe_unkey(k0);
-            double mag = fabs(kd) + fabs(s_tinc) + (s_gmax + s_emax) / V + 2.0 * s_dsum + 1e-300;
-            double delta = (double)(ev + 16) * 0x1p-48 * mag;
-            double thr = kd + 2.0 * delta;
-            s_kthr = (thr == thr) ? cafe_key(thr) : CAFE_KEY_NONE;
+        if (warp == 0) {
+          km = lane < nwarp ? redk[lane] : CAFE_KEY_NONE;
+          for (int o = 16; o > 0; o >>= 1) km = min(km, cafe_shfl_u64_xor(km, o));
+          if (lane == 0) {
+            unsigned long long kt = CAFE_KEY_NONE;
+            if (km != CAFE_KEY_NONE) {
+              // rows whose exact value may be the minimum: keys within twice the
+              // rounding bound delta = (ev+16) 2^-48 (|K*| + |T| + (gmax+emax)/v
+              // + 2 sum|dt|), evaluated as a single-precision upper bound
+              double kd = cafe_unkey(km);
+              float mag = ((float)fabs(kd) + s_magf) * (1.0f + 0x1p-20f);
+              float delta2 = (float)(ev + 16) * 0x1p-47f * mag;
+              if (mag >= 1e-20f) {
+                double thr = kd + (double)delta2;
+                kt = cafe_is_nan(thr) ? CAFE_KEY_NONE : cafe_key(thr);
+              } else {
+                double magd = fabs(kd) + fabs(s_tinc) + (s_gmax + s_emax) / V + 2.0 * s_dsum + 1e-300;
+                double thr = kd + 2.0 * ((double)(ev + 16) * 0x1p-48 * magd);
+                kt = cafe_is_nan(thr) ? CAFE_KEY_NONE : cafe_key(thr);
+              }
+            }
+            s_kthr = kt;
           }
         }
         __syncthreads();
         CAFE_DCYC(0);
         const unsigned long long kthr = s_kthr;
         int again = 0;
-        if (kthr != CAFE_KEY_NONE) {
+        best = cafe_cand_none();
+        if (kthr != CAFE_KEY_NONE && (my_min <= kthr || my_forced)) {
+          unsigned long long m = CAFE_KEY_NONE;
           for (int r = tid; r < s_nrows; r += nthr) {
-            if (!D.row_alive[r]) continue;
-            int stamp = D.row_stamp[r];
-            if (stamp == ev + 1 || (D.row_key[r] > kthr && stamp != -1)) continue;
-            cafe_row_eval(D, K, r, ev, s_tinc);  // stamp -1: forced after a possible clamp
-            again = 1;
+            unsigned long long k = D.row_key[r];
+            if (k <= kthr || my_forced) {
+              int stamp = D.row_stamp[r];
+              // stamp -1: forced after a possible clamp of the row's extent
+              if ((k <= kthr && stamp != ev + 1) || (stamp == -1 && D.row_alive[r])) {
+                cafe_row_eval(D, K, r, ev, s_tinc);
+                k = D.row_key[r];
+                again = 1;
+              }
+              if (k <= kthr) {
+                CafeCand c;
+                c.t = D.row_bt[r];
+                c.ruqs = D.row_bruq[r];
+                c.tk = cafe_key_canon(c.t);
+                c.rk = cafe_key_canon(c.ruqs);
+                c.j = D.row_j[r];
+                c.s = D.row_bslot[r];
+                if (cafe_cand_better(c, best)) best = c;
+              }
+            }
+            m = min(m, k);
           }
+          my_min = m;
+          my_forced = false;
         }
         again = __syncthreads_or(again);
         CAFE_DCYC(1);
         if (tid == 0 && again) s_evals++;
         if (!again) break;
       }
-      const unsigned long long kthr = s_kthr;
-      if (kthr != CAFE_KEY_NONE) {
-        for (int r = tid; r < s_nrows; r += nthr) {
-          if (!D.row_alive[r] || D.row_key[r] > kthr) continue;
-          CafeCand c;
-          c.t = D.row_bt[r];
-          c.ruqs = D.row_bruq[r];
-          c.j = D.row_j[r];
-          c.s = D.row_bslot[r];
-          if (cafe_cand_better(c, best)) best = c;
-        }
-      }
     }
-    for (int o = 16; o > 0; o >>= 1) {
-      CafeCand c = cafe_shfl_cand(best, o);
-      if (cafe_cand_better(c, best)) best = c;
-    }
+    best = cafe_warp_best(best);
     if (lane == 0) red[warp] = best;
     __syncthreads();
     CAFE_DCYC(2);
+    if (warp == 0) {
+      CafeCand b = lane < nwarp ? red[lane] : cafe_cand_none();
+      b = cafe_warp_best(b);
+      if (lane == 0) red[0] = b;
+    }
     if (tid == 0) {
       long long tn = clock64();
       s_cyc[0] += tn - s_t0;
       s_t0 = tn;
       CafeCand b = red[0];
-      for (int w = 1; w < nwarp; ++w)
-        if (cafe_cand_better(red[w], b)) b = red[w];
       CAFE_DCYC(3);
-      if (b.j < 0 || !(b.t < 1e6) || s_ev >= max_events) {
-        if (b.j >= 0 && b.t < 1e6) atomicOr(D.err, CAFE_ERR_ITER_CAP);
+      if (b.j < 0 || !(b.tk < CAFE_KEY_1E6) || s_ev >= max_events) {
+        if (b.j >= 0 && b.tk < CAFE_KEY_1E6) atomicOr(D.err, CAFE_ERR_ITER_CAP);
         s_done = 1;
       } else {
         cafe_uniform_stream st;
@@ -1050,12 +1089,8 @@ __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
         if (s_dt < 0.0) s_negdt++;
         s_ev += 1;
         if (!s_slow) {
-          // log this event's growth (VoxelsCA.C:514) for the rows alive now
-          double vd = s_nuc ? 0.0 : V * s_dt;
-          D.ev_vd[s_ev] = vd;
-          D.ev_grew[s_ev] = s_nuc ? 0 : 1;
-          s_vs = s_vs + (s_nuc ? 0.0 : vd);
-          D.ev_vs[s_ev] = s_vs;
+          // this event's growth of every row (VoxelsCA.C:514)
+          s_vd = s_nuc ? 0.0 : V * s_dt;
           s_dsum += fabs(s_dt);
         }
       }
@@ -1063,110 +1098,117 @@ __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
     }
     __syncthreads();
     if (s_done) break;
+    // rows that exist at the start of this event (the fill below appends)
+    const int nrows_ev = s_nrows;
     // ---- growth of every mushy cell of the list (VoxelsCA.C:511-516), slow path
     if (s_slow && !s_nuc) {
       double d = s_dt;
       if (isfinite(d)) {
-        for (int r = tid; r < s_nrows; r += nthr) {
+        for (int r = tid; r < nrows_ev; r += nthr) {
           if (!D.row_alive[r]) continue;
           int p = D.row_pos[r];
-          double e = D.a_ext[p] + K.vhat_cls[D.a_cls[p]] * d;
-          D.a_ext[p] = (e < 0.0) ? 0.0 : e;
+          double e = D.row_E[r] + K.vhat_cls[D.a_cls[p]] * d;
+          D.row_E[r] = (e < 0.0) ? 0.0 : e;
         }
       } else {
+        // a non-finite DtMin also reaches the cells that have no liquid
+        // neighbour (0 * inf)
         for (int j = tid; j < s_countS; j += nthr) {
           int p = D.vs2[j];
           int r = D.a_frow[p];
           double v = (r >= 0 && D.row_alive[r]) ? K.vhat_cls[D.a_cls[p]] : 0.0;
-          double e = D.a_ext[p] + v * d;
-          D.a_ext[p] = (e < 0.0) ? 0.0 : e;
+          double *ep = r >= 0 ? &D.row_E[r] : &D.a_ext[p];
+          double e = *ep + v * d;
+          *ep = (e < 0.0) ? 0.0 : e;
         }
       }
     }
     __syncthreads();
     CAFE_DCYC(5);
-    // ---- the captured cell (VoxelsCA.C:483-505 and 518-605)
-    if (tid == 0) {
-      int icap = s_icap, js = s_jspos;
-      D.a_state[icap] = 2;
-      if (s_nvs2 < D.vs2_cap) {
-        D.vs2[s_nvs2] = icap;
-      } else {
-        atomicOr(D.err, CAFE_ERR_MUSHY_CAP);
-        s_done = 1;
-      }
-      s_nvs2 += 1;
-      if (s_nuc) {
-        int ci, cj, ck;
-        cafe_cell_xyz(K, D.act[icap], ci, cj, ck);
-        if (s_ngrain < D.grain_cap) {
-          double q4[4];
-          cafe_sample_orientation(K, s_sdloc, q4);
-          double *c = D.cth + 4LL * s_ngrain;
-          for (int a = 0; a < 4; ++a) c[a] = q4[a];
-          cafe_rot_from_cth(c, D.rot + 9LL * s_ngrain);
+    if (warp < CAFE_QUAD_THREADS / 32) {
+      // ---- the captured cell (VoxelsCA.C:483-505 and 518-605)
+      if (tid == 0) {
+        int icap = s_icap, js = s_jspos;
+        D.a_state[icap] = 2;
+        if (s_nvs2 < D.vs2_cap) {
+          D.vs2[s_nvs2] = icap;
         } else {
-          atomicOr(D.err, CAFE_ERR_GRAIN_CAP);
+          atomicOr(D.err, CAFE_ERR_MUSHY_CAP);
           s_done = 1;
         }
-        s_ngrain += 1;
-        D.a_gid[icap] = s_ngrain;
-        D.a_cx[icap] = ((double)ci + .5) * K.dx[0];
-        D.a_cy[icap] = ((double)cj + .5) * K.dx[1];
-        D.a_cz[icap] = ((double)ck + .5) * K.dx[2];
-        s_sdloc += 10u;
-        D.a_ext[icap] = 0.0;
-        s_nnuc++;
-      } else {
-        // the capture result of this slot, computed when the row was filled
-        D.a_gid[icap] = D.a_gid[js];
-        const double *gq = D.row_geo + ((long long)D.a_frow[js] * CAFE_NSLOT + s_bslot) * 4;
-        D.a_ext[icap] = gq[0];
-        D.a_cx[icap] = gq[1];
-        D.a_cy[icap] = gq[2];
-        D.a_cz[icap] = gq[3];
+        s_nvs2 += 1;
+        if (s_nuc) {
+          int ci, cj, ck;
+          cafe_cell_xyz(K, D.act[icap], ci, cj, ck);
+          if (s_ngrain < D.grain_cap) {
+            double q4[4];
+            cafe_sample_orientation(K, s_sdloc, q4);
+            double *c = D.cth + 4LL * s_ngrain;
+            for (int a = 0; a < 4; ++a) c[a] = q4[a];
+            cafe_rot_from_cth(c, D.rot + 9LL * s_ngrain);
+          } else {
+            atomicOr(D.err, CAFE_ERR_GRAIN_CAP);
+            s_done = 1;
+          }
+          s_ngrain += 1;
+          D.a_gid[icap] = s_ngrain;
+          D.a_cx[icap] = ((double)ci + .5) * K.dx[0];
+          D.a_cy[icap] = ((double)cj + .5) * K.dx[1];
+          D.a_cz[icap] = ((double)ck + .5) * K.dx[2];
+          s_sdloc += 10u;
+          D.a_ext[icap] = 0.0;
+          s_nnuc++;
+        } else {
+          // the capture result of this slot, computed when the row was filled
+          D.a_gid[icap] = D.a_gid[js];
+          const double *gq = D.row_geo + ((long long)D.a_frow[js] * CAFE_NSLOT + s_bslot) * 4;
+          D.a_ext[icap] = gq[0];
+          D.a_cx[icap] = gq[1];
+          D.a_cy[icap] = gq[2];
+          D.a_cz[icap] = gq[3];
+        }
+        CAFE_DCYC(6);
+        s_tinc += s_dt;
+        long long tn = clock64();
+        s_cyc[1] += tn - s_t0;
+        s_t0 = tn;
       }
-      CAFE_DCYC(6);
-      s_tinc += s_dt;
-      long long tn = clock64();
-      s_cyc[1] += tn - s_t0;
-      s_t0 = tn;
-    }
-    __syncthreads();
-    // ---- neighbours of the captured cell lose one liquid neighbour
-    if (warp == 0) {
-      int icap = s_icap;
-      int nn = D.a_nn[icap];
-      if (lane < nn) {
-        int q = D.a_nbr[(long long)icap * CAFE_NSLOT + lane];
-        int left = --D.a_liq[q];
-        int r = D.a_frow[q];
-        if (r >= 0 && D.row_alive[r]) {
-          int s = cafe_find_slot(D, q, icap);
-          if (s >= 0) D.row_live[r] &= ~(1u << s);
-          if (left <= 0) {
-            D.row_alive[r] = 0;
-            if (!s_slow) D.row_death[r] = s_ev;  // it grew at this event too
-            D.row_key[r] = CAFE_KEY_NONE;
+      cafe_bar_quad();
+      // ---- neighbours of the captured cell lose one liquid neighbour
+      if (warp == 0) {
+        int icap = s_icap;
+        int nn = D.a_nn[icap];
+        if (lane < nn) {
+          int q = D.a_nbr[(long long)icap * CAFE_NSLOT + lane];
+          int left = --D.a_liq[q];
+          int r = D.a_frow[q];
+          if (r >= 0 && D.row_alive[r]) {
+            int s = cafe_find_slot(D, q, icap);
+            if (s >= 0) D.row_live[r] &= ~(1u << s);
+            if (left <= 0) {
+              D.row_alive[r] = 0;
+              D.row_death[r] = s_ev;  // it grew at this event too
+              D.row_key[r] = CAFE_KEY_NONE;
+              s_dirty[r % nthr] = 1;
+            }
           }
         }
       }
-    }
-    __syncthreads();
-    CAFE_DCYC(7);
-    // ---- the captured cell becomes a capturing cell if it qualifies (warps 0-3)
-    if (warp < CAFE_QUAD_THREADS / 32) {
+      cafe_bar_quad();
+      CAFE_DCYC(7);
+      // ---- the captured cell becomes a capturing cell if it qualifies
       int icap = s_icap;
       if (D.a_liq[icap] > 0 && D.a_cold[icap] && !s_done) {
         int r = s_nrows;
         if (r < D.row_cap) {
           if (tid == 0) {
+            s_dirty[r % nthr] = 1;
             D.row_pos[r] = icap;
             D.row_j[r] = s_nvs2 - 1;
             D.row_alive[r] = 1;
             D.a_frow[icap] = r;
-            D.row_death[r] = CAFE_M_DONE;
-            D.row_m[r] = s_slow ? CAFE_M_DONE : s_ev;
+            D.row_death[r] = CAFE_ALIVE;
+            D.row_E[r] = D.a_ext[icap];
           }
           const bool same_v = D.a_cls[icap] == 1;
           unsigned long long gk = cafe_row_fill_quad(D, K, r, icap, !s_slow && same_v, s_ev, s_tinc, s_quad);
@@ -1192,6 +1234,23 @@ __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
           s_done = 1;
         }
       }
+    } else if (!s_slow && !s_nuc) {
+      // ---- this event's growth of the rows (VoxelsCA.C:511-516), by the warps
+      // not busy with the capture; rows dying at this event grow too
+      const double vd = s_vd;
+      for (int r = tid - CAFE_QUAD_THREADS; r < nrows_ev; r += nthr - CAFE_QUAD_THREADS) {
+        if (D.row_death[r] < s_ev) continue;
+        double e = D.row_E[r] + vd;
+        if (cafe_is_neg(e)) {
+          e = 0.0;
+          if (vd < 0.0) {
+            // clamped by a negative event: the key bound no longer holds
+            D.row_stamp[r] = -1;
+            s_forced[r % nthr] = 1;
+          }
+        }
+        D.row_E[r] = e;
+      }
     }
     __syncthreads();
     CAFE_DCYC(11);
@@ -1199,32 +1258,11 @@ __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
       long long tn = clock64();
       s_cyc[2] += tn - s_t0;
       s_t0 = tn;
-    }
-    if (!s_slow && !s_done) {
       if (s_switch) {
-        // a capturing cell with another growth velocity: bring every row up to
-        // date and continue with the exact per-event scan
-        for (int r = tid; r < s_nrows; r += nthr) {
-          cafe_row_replay(D, r, s_ev);
-          D.row_m[r] = CAFE_M_DONE;
-        }
-        __syncthreads();
-        if (tid == 0) {
-          s_slow = 1;
-          s_switch = 0;
-        }
-      } else if (!s_nuc && s_dt < 0.0) {
-        // a negative event may clamp a small extent at zero (VoxelsCA.C:515),
-        // which breaks the key bound of that row: re-evaluate such rows
-        const double vd = D.ev_vd[s_ev];
-        const double margin = (double)(s_ev + 16) * 0x1p-48 * (s_emax + s_gmax + V * s_dsum + 1e-300);
-        for (int r = tid; r < s_nrows; r += nthr) {
-          if (!D.row_alive[r]) continue;
-          int m = D.row_m[r];
-          if (m >= s_ev) continue;
-          double elb = D.a_ext[D.row_pos[r]] + (D.ev_vs[s_ev - 1] - D.ev_vs[m]);
-          if (elb + vd < margin) D.row_stamp[r] = -1;
-        }
+        // a capturing cell with another growth velocity: continue with the
+        // exact per-event scan (the extents are current)
+        s_slow = 1;
+        s_switch = 0;
       }
     }
     __syncthreads();
@@ -1256,14 +1294,13 @@ __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
   }
 }
 
-// Brings every row's extent up to the end of the step (the lazily applied
-// growth of VoxelsCA.C:511-516), spread over the whole GPU.
+// Copies the rows' extents, kept in row order during the event loop, back to
+// their active-list positions.
 __global__ void k_rows_finalize(CafeDev D) {
   int nrows = D.ctr[CTR_NROWS_END];
-  int nev = D.ctr[CTR_NEV];
   if (nrows > D.row_cap) nrows = (int)D.row_cap;
   for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < nrows; r += gridDim.x * blockDim.x)
-    cafe_row_replay(D, r, nev);
+    D.a_ext[D.row_pos[r]] = D.row_E[r];
 }
 
 // ------------------------------------------------------------------ write back
