@@ -96,15 +96,19 @@ struct CafeDev {
   // this slot captures it, 4 doubles
   double *row_geo;
   long long row_cap;
-  // rows during the event loop: row_E is the row cell's extent (ExtA), kept
-  // current at every event and copied back to a_ext afterwards; a row grows at
-  // the events (birth, row_death]; row_key orders the rows by estimated
-  // absolute capture time; row_b* hold the exact best candidate of the
-  // iteration row_stamp
+  // rows during the event loop: row_E is the row cell's extent (ExtA)
+  // including the growth of events 1..row_m, copied back to a_ext afterwards;
+  // a row grows at the events (birth, row_death]; row_key orders the rows by
+  // estimated absolute capture time; row_b* hold the exact best candidate of
+  // the iteration row_stamp
   double *row_E;
-  int32_t *row_death, *row_stamp, *row_bslot;
+  int32_t *row_m, *row_death, *row_stamp, *row_bslot;
   unsigned long long *row_key;
   double *row_bt, *row_bruq;
+  // per-event growth: ev_vd[e] = fl(v * DtMin_e) (+0 for a nucleation),
+  // ev_vs[e] = running sum of ev_vd
+  double *ev_vd, *ev_vs;
+  long long ev_cap;
   // scan scratch
   int32_t *blk;       // per-block counts / offsets
   long long blk_cap;
@@ -130,7 +134,7 @@ enum {
 };
 enum { STAT_EVENTS = 0, STAT_NUC, STAT_MAXNA, STAT_MAXROWS, STAT_STEPS, STAT_NEGDT, STAT_SUMNA, STAT_SUMROWS,
        STAT_SLOWSTEPS, STAT_EVALS, STAT_CYC_SELECT, STAT_CYC_APPLY, STAT_CYC_FILL, STAT_CYC_OTHER,
-       STAT_DETAIL, STAT_COUNT = STAT_DETAIL + 24 };
+       STAT_DETAIL, STAT_COUNT = STAT_DETAIL + 32 };
 
 // --------------------------------------------------------------- temperature
 // TempField::AnalyticTempCurr (TempField.C:155-190) for one cell; returns the

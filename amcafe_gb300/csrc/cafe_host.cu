@@ -711,6 +711,7 @@ int cafe_sim_create(const char *deck_path, const cafe_options *opt, cafe_sim **o
   // the pool, far smaller than the active list; an explicit active capacity
   // raises this limit with it
   D.row_cap = std::min<long long>(acap, opt && opt->active_capacity > 0 ? (1LL << 22) : (1LL << 20));
+  D.ev_cap = acap + 2;  // an event captures or nucleates one active cell
   double est = g.mu * (g.dX[0] * 1e6) * (g.dX[1] * 1e6) * g.nX[0] * g.nX[1] * (s->Nzh * g.dX[2] * 1e6) +
                (s->nlayerTot + 1) * g.lrate * (g.dX[0] * 1e6) * (g.dX[1] * 1e6) * g.nX[0] * g.nX[1] * (g.layerT * 1e6);
   long long gcap = opt && opt->grain_capacity > 0 ? opt->grain_capacity : (long long)(2 * est) + (1 << 16);
@@ -734,6 +735,8 @@ int cafe_sim_create(const char *deck_path, const cafe_options *opt, cafe_sim **o
       (rc = dalloc(&D.row_g, (size_t)D.row_cap * CAFE_NSLOT, o)) ||
       (rc = dalloc(&D.row_geo, (size_t)D.row_cap * CAFE_NSLOT * 4, o)) || (rc = dalloc(&D.blk, D.blk_cap, o)) ||
       (rc = dalloc(&D.row_E, D.row_cap, o)) || (rc = dalloc(&D.row_death, D.row_cap, o)) ||
+      (rc = dalloc(&D.row_m, D.row_cap, o)) || (rc = dalloc(&D.ev_vd, D.ev_cap, o)) ||
+      (rc = dalloc(&D.ev_vs, D.ev_cap, o)) ||
       (rc = dalloc(&D.row_stamp, D.row_cap, o)) || (rc = dalloc(&D.row_bslot, D.row_cap, o)) ||
       (rc = dalloc(&D.row_key, D.row_cap, o)) || (rc = dalloc(&D.row_bt, D.row_cap, o)) ||
       (rc = dalloc(&D.row_bruq, D.row_cap, o)) ||
@@ -1161,7 +1164,7 @@ int cafe_sim_stats(cafe_sim *s, cafe_stats *st) {
   st->cycles_fill = v[STAT_CYC_FILL];
 #ifdef CAFE_DETAIL_CYCLES
   fprintf(stderr, "cafe detail cycles:");
-  for (int c = 0; c < 24; ++c) fprintf(stderr, " %llu", v[STAT_DETAIL + c]);
+  for (int c = 0; c < 32; ++c) fprintf(stderr, " %llu", v[STAT_DETAIL + c]);
   fprintf(stderr, "\n");
 #endif
   return CAFE_OK;

@@ -473,6 +473,16 @@ __device__ __forceinline__ bool cafe_is_neg(double x) {
   long long b = crm_bits(x);
   return b < 0 && (b & CRM_ABS_MASK) != 0 && (b & CRM_ABS_MASK) <= CRM_BITS_INF;
 }
+// e with |x| < 2^e (a large value for inf and NaN)
+__device__ __forceinline__ int cafe_exp_ub(double x) {
+  int f = (int)((crm_bits(x) >> 52) & 0x7ff);
+  return f == 0x7ff ? 4096 : (f == 0 ? -1022 : f - 1022);
+}
+// e with |x| >= 2^e for a normal x (a small value for zero and subnormals)
+__device__ __forceinline__ int cafe_exp_lb(double x) {
+  int f = (int)((crm_bits(x) >> 52) & 0x7ff);
+  return f == 0 ? -4096 : f - 1023;
+}
 
 // Row order, exact best candidate and largest |g| of row r (position p) once
 // every lane of the calling warp holds its slot: liv (the neighbour is liquid),
@@ -483,12 +493,17 @@ __device__ __forceinline__ bool cafe_is_neg(double x) {
 // order key of the largest finite |g| of the live slots, or 0 when none.
 __device__ unsigned long long cafe_row_finish_warp(const CafeDev &D, const CafeConsts &K, long long r, int p,
                                                    int nn, bool liv, double gv, int q, bool eval, int ev,
-                                                   double T) {
+                                                   double T, bool have_t = false, double t_pre = 0.0,
+                                                   double ruqs_pre = 0.0) {
   const unsigned FULL = 0xffffffffu;
   int lane = threadIdx.x & 31;
   uint32_t live = __ballot_sync(FULL, liv);
   // rank of this slot in the row order
-  unsigned long long key = (liv && gv == gv) ? cafe_key_canon(gv) : CAFE_KEY_NONE;
+#ifdef CAFE_DETAIL_CYCLES
+  long long fz0 = clock64();
+#endif
+  const bool gfin = !cafe_is_nan(gv);
+  unsigned long long key = (liv && gfin) ? cafe_key_canon(gv) : CAFE_KEY_NONE;
   int rank = liv ? 0 : __popc(live);
   for (int t = 0; t < nn; ++t) {
     unsigned long long kt = cafe_shfl_u64(key, t);
@@ -500,16 +515,25 @@ __device__ unsigned long long cafe_row_finish_warp(const CafeDev &D, const CafeC
   }
   if (lane < nn) D.row_ord[r * CAFE_NSLOT + rank] = (uint8_t)lane;
   if (lane == 0) D.row_live[r] = live;
+#ifdef CAFE_DETAIL_CYCLES
+  long long fz1 = clock64();
+#endif
   if (eval) {
-    double E = D.a_ext[p];
-    double v = K.vhat_cls[D.a_cls[p]];
+    // t and ruqs of each live slot (given by the caller when have_t)
     double t = 0.0, ruqs = 0.0;
     bool cand = false;
     if (liv) {
-      double dr = gv - E;
-      t = dr / v;
-      cand = t == t;
-      ruqs = .5 * (D.a_ruq[p] + D.a_ruq[q]);
+      if (have_t) {
+        t = t_pre;
+        ruqs = ruqs_pre;
+      } else {
+        double E = D.a_ext[p];
+        double v = K.vhat_cls[D.a_cls[p]];
+        double dr = gv - E;
+        t = dr / v;
+        ruqs = .5 * (D.a_ruq[p] + D.a_ruq[q]);
+      }
+      cand = !cafe_is_nan(t);
     }
     // lexicographic (t, ruqs, slot) minimum over the warp (VoxelsCA.C:427-440)
     unsigned long long tk = cand ? cafe_key_canon(t) : CAFE_KEY_NONE;
@@ -539,9 +563,20 @@ __device__ unsigned long long cafe_row_finish_warp(const CafeDev &D, const CafeC
       }
     }
   }
-  unsigned long long ak = (liv && gv == gv) ? cafe_key(fabs(gv)) : 0ULL;
+#ifdef CAFE_DETAIL_CYCLES
+  long long fz2 = clock64();
+#endif
+  unsigned long long ak = (liv && gfin) ? cafe_key(fabs(gv)) : 0ULL;
   for (int o = 16; o > 0; o >>= 1) ak = max(ak, (unsigned long long)__shfl_xor_sync(FULL, (long long)ak, o));
   __syncwarp();
+#ifdef CAFE_DETAIL_CYCLES
+  if (gridDim.x == 1 && lane == 0) {
+    long long fz3 = clock64();
+    atomicAdd(&D.stat[STAT_DETAIL + 24], (unsigned long long)(fz1 - fz0));
+    atomicAdd(&D.stat[STAT_DETAIL + 25], (unsigned long long)(fz2 - fz1));
+    atomicAdd(&D.stat[STAT_DETAIL + 26], (unsigned long long)(fz3 - fz2));
+  }
+#endif
   return ak;
 }
 
@@ -586,18 +621,22 @@ __device__ unsigned long long cafe_row_fill_warp(const CafeDev &D, const CafeCon
 
 // Per-slot partial results passed between the four warps of cafe_row_fill_quad.
 struct CafeQuadScratch {
-  double cth[32], sph[32], l[32], d1I[32], dI2[32], d1J[32], dJ3[32], g[32];
+  double cth[32], sph[32], l[32], d1I[32], dI2[32], d1J[32], dJ3[32], g[32], t[32], ruqs[32];
 };
 #define CAFE_QUAD_THREADS 128
 __device__ __forceinline__ void cafe_bar_quad() { asm volatile("bar.sync 1, 128;" ::: "memory"); }
+// Barrier of the event loop's warps 4 and up (n threads).
+__device__ __forceinline__ void cafe_bar_helpers(int n) { asm volatile("bar.sync 2, %0;" ::"r"(n) : "memory"); }
 
 // cafe_row_fill_warp for warps 0-3 of the block together (all 128 threads
 // must call it): a warp issues one FP64 instruction at a time whatever its
 // active lanes, so the independent chains of each slot's geometry run in
 // different warps, lane s of each warp on slot s:
 //   warp 0: cos th and the cell distance l; warp 1: sin ph;
-//   warp 2: the projection on edge p0-p1, then g and the extent;
-//   warp 3: the projection on edge p0-p2, then the new centre.
+//   warp 2: the projection on edge p0-p1, then g, the extent and (with
+//           eval) the capture time t = (g - ExtA)/v;
+//   warp 3: the projection on edge p0-p2 and the tie-break ruqs, then the new
+//           centre.
 // Warp 0 finishes the row; the return value is valid in warp 0.
 __device__ unsigned long long cafe_row_fill_quad(const CafeDev &D, const CafeConsts &K, long long r, int p,
                                                  bool eval, int ev, double T, CafeQuadScratch &S) {
@@ -618,6 +657,7 @@ __device__ unsigned long long cafe_row_fill_quad(const CafeDev &D, const CafeCon
   }
   const bool work = liv && grain_ok;
   double R[9], loc[3], dr = 0.0, pk[3][3];
+  double E2 = 0.0, v2 = 1.0;  // warp 2: the row's extent and velocity for t
   int s0i = 0;
   if (work) {
     cafe_cell_xyz(K, D.act[q], ci, cj, ck);
@@ -636,10 +676,16 @@ __device__ unsigned long long cafe_row_fill_quad(const CafeDev &D, const CafeCon
       for (int a = 0; a < 9; ++a) R[a] = Rg[a];
       dr = cafe_geo_loc(R, dn, loc);
       s0i = cafe_geo_corners(loc, dr, pk);
-      if (w == 2)
+      if (w == 2) {
+        if (eval) {
+          E2 = D.a_ext[p];
+          v2 = K.vhat_cls[D.a_cls[p]];
+        }
         cafe_geo_edge(loc, pk[0], pk[1], &S.d1I[lane], &S.dI2[lane]);
-      else
+      } else {
         cafe_geo_edge(loc, pk[0], pk[2], &S.d1J[lane], &S.dJ3[lane]);
+        if (eval) S.ruqs[lane] = .5 * (D.a_ruq[p] + D.a_ruq[q]);
+      }
     }
   }
 #ifdef CAFE_DETAIL_CYCLES
@@ -658,6 +704,10 @@ __device__ unsigned long long cafe_row_fill_quad(const CafeDev &D, const CafeCon
       gv = f * dr;
       S.g[lane] = gv;
       o[0] = f * Lmud * 1.0;
+      if (eval) {
+        double dr2 = gv - E2;
+        S.t[lane] = dr2 / v2;
+      }
     } else {
       double cn[3];
       cafe_geo_centre(R, cs, pk[0], s0i, Lmud, cn);
@@ -674,7 +724,8 @@ __device__ unsigned long long cafe_row_fill_quad(const CafeDev &D, const CafeCon
   if (w == 0) {
     if (work) gv = S.g[lane];
     if (liv) D.row_g[r * CAFE_NSLOT + lane] = gv;
-    ak = cafe_row_finish_warp(D, K, r, p, nn, liv, gv, q, eval, ev, T);
+    ak = cafe_row_finish_warp(D, K, r, p, nn, liv, gv, q, eval, ev, T, true, work ? S.t[lane] : (double)NAN,
+                              work ? S.ruqs[lane] : 0.0);
   }
 #ifdef CAFE_DETAIL_CYCLES
   if (lane == 0) {
@@ -742,10 +793,9 @@ __device__ __forceinline__ CafeCand cafe_warp_best(CafeCand best) {
 // visited in g order and the visit stops at the first time above the row's
 // minimum; otherwise every live slot is evaluated. `bounded` applies the
 // reference's acceptance limit t <= 1e6 (VoxelsCA.C:383, 427).
-__device__ __forceinline__ void cafe_row_best(const CafeDev &D, const CafeConsts &K, long long r,
-                                              CafeCand &best, bool bounded = true) {
+__device__ __forceinline__ void cafe_row_best_live(const CafeDev &D, const CafeConsts &K, long long r,
+                                                   uint32_t live, CafeCand &best, bool bounded) {
   int p = D.row_pos[r];
-  uint32_t live = D.row_live[r];
   if (!live) return;
   double E = D.row_E[r];
   double v = K.vhat_cls[D.a_cls[p]];
@@ -785,6 +835,10 @@ __device__ __forceinline__ void cafe_row_best(const CafeDev &D, const CafeConsts
     }
   }
 }
+__device__ __forceinline__ void cafe_row_best(const CafeDev &D, const CafeConsts &K, long long r,
+                                              CafeCand &best, bool bounded = true) {
+  cafe_row_best_live(D, K, r, D.row_live[r], best, bounded);
+}
 
 // Slot of `target` in q's neighbour list, -1 if absent. All CAFE_NSLOT entries
 // are loaded at once (the list storage is always that long) and masked by nn.
@@ -808,17 +862,36 @@ __device__ __forceinline__ int cafe_find_slot(const CafeDev &D, int q, int targe
 // evaluated exactly. Between evaluations the key is within a small rounding
 // bound of the row's exact current value (or below it once a candidate was
 // captured by someone else), so the event needs exact times only for the rows
-// whose key lies within twice that bound of the smallest key. An extent clamped
-// at zero by a negative event (VoxelsCA.C:515) breaks the bound; such rows are
-// stamped -1 and evaluated again. The growth itself is applied to every row at
-// every event, by the warps that do not take part in the capture.
-#define CAFE_ALIVE 0x7fffffff  // row_death of a row that is still alive
+// whose key lies within twice that bound of the smallest key. An extent that a
+// negative event may clamp at zero (VoxelsCA.C:515) breaks the bound; such rows
+// are stamped -1 and evaluated again. The growth is logged once per event and
+// replayed per row when the row is evaluated, and for every row at the end of
+// the step (k_rows_finalize).
+#define CAFE_ALIVE 0x7fffffff   // row_death of a row that is still alive
+#define CAFE_M_DONE 0x7fffffff  // row_m of a row whose extent is kept current
 
-// Exact evaluation of row r for the iteration after `ev` events at time T.
-__device__ __forceinline__ void cafe_row_eval(const CafeDev &D, const CafeConsts &K, int r, int ev,
-                                              double T) {
+// Applies the logged growth of events row_m+1 .. min(upto, row_death). A
+// nucleation logs +0, which leaves an extent unchanged (extents are never -0).
+__device__ __forceinline__ void cafe_row_replay(const CafeDev &D, int r, int upto) {
+  int m = D.row_m[r];
+  int stop = min(upto, D.row_death[r]);
+  if (stop <= m) return;
+  double E = D.row_E[r];
+  for (int k = m + 1; k <= stop; ++k) {
+    E = E + D.ev_vd[k];
+    E = cafe_is_neg(E) ? 0.0 : E;  // (E < 0.0) ? 0.0 : E
+  }
+  D.row_E[r] = E;
+  D.row_m[r] = stop;
+}
+
+// Exact evaluation of row r (live slots `live`) for the iteration after `ev`
+// events at time T.
+__device__ __forceinline__ void cafe_row_eval_live(const CafeDev &D, const CafeConsts &K, int r, int ev,
+                                                   double T, uint32_t live) {
+  cafe_row_replay(D, r, ev);
   CafeCand b = cafe_cand_none();
-  cafe_row_best(D, K, r, b, false);
+  cafe_row_best_live(D, K, r, live, b, false);
   D.row_stamp[r] = ev + 1;
   if (b.j < 0) {
     D.row_key[r] = CAFE_KEY_NONE;
@@ -828,6 +901,10 @@ __device__ __forceinline__ void cafe_row_eval(const CafeDev &D, const CafeConsts
   D.row_bruq[r] = b.ruqs;
   D.row_bslot[r] = b.s;
   D.row_key[r] = cafe_key(T + b.t);
+}
+__device__ __forceinline__ void cafe_row_eval(const CafeDev &D, const CafeConsts &K, int r, int ev,
+                                              double T) {
+  cafe_row_eval_live(D, K, r, ev, T, D.row_live[r]);
 }
 
 // Frontier rows of the step: numerators, order, and (when every row grows
@@ -844,6 +921,7 @@ __global__ void k_rows_init(CafeDev D, CafeConsts K) {
     cafe_row_fill_warp(D, K, r, p, true, 0, 0.0);
     if (lane == 0) {
       D.row_E[r] = D.a_ext[p];
+      D.row_m[r] = 0;
       D.row_death[r] = CAFE_ALIVE;
       if (D.a_cls[p] != 1 || !(V > 0.0 && V < INFINITY)) atomicOr(&D.ctr[CTR_SLOW], 1);
     }
@@ -859,9 +937,11 @@ __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
   __shared__ int s_nvs2, s_countS, s_nrows, s_ngrain, s_done, s_nuc, s_icap, s_jspos, s_bslot, s_na, s_slow,
       s_ev, s_switch;
   __shared__ unsigned long long s_kthr;
-  __shared__ unsigned char s_dirty[CAFE_LOOP_THREADS];   // a row of thread i changed its key elsewhere
+  __shared__ unsigned char s_dirty[CAFE_LOOP_THREADS];  // a row of thread i changed its key elsewhere
   __shared__ unsigned char s_forced[CAFE_LOOP_THREADS];  // a row of thread i was stamped -1
-  __shared__ float s_magf, s_invVf;  // |T| + (gmax+emax)/v + 2 sum|dt| (upper bound), 1/v
+  __shared__ double s_vs;                                // running sum of the logged growth
+  __shared__ unsigned long long s_hk[CAFE_LOOP_THREADS / 32][2];  // helper warps: two smallest keys
+  __shared__ int s_hr[CAFE_LOOP_THREADS / 32][2];                 // ... and their rows
   __shared__ uint32_t s_rng;
   __shared__ unsigned int s_sdloc;
   __shared__ long long s_nnuc, s_negdt, s_evals;
@@ -870,7 +950,7 @@ __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
   __shared__ CafeQuadScratch s_quad;
 #ifdef CAFE_DETAIL_CYCLES
   // finer event-loop sections, thread 0's clock (profiling builds only)
-  __shared__ long long s_dcyc[16], s_dt0;
+  __shared__ long long s_dcyc[16], s_dt0, s_d27;
 #define CAFE_DCYC(slot)                  \
   do {                                   \
     if (threadIdx.x == 0) {              \
@@ -880,6 +960,7 @@ __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
     }                                    \
   } while (0)
   if (threadIdx.x < 16) s_dcyc[threadIdx.x] = 0;
+  if (threadIdx.x == 0) s_d27 = 0;
   __shared__ unsigned long long s_fb0, s_sp0;
   if (threadIdx.x == 0) {
     s_dt0 = clock64();
@@ -895,7 +976,7 @@ __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
   const int nthr = blockDim.x, nwarp = blockDim.x >> 5;
   const double V = K.vhat_cls[1];
   unsigned long long my_min = CAFE_KEY_NONE;  // smallest key of this thread's rows
-  bool my_forced = false;                     // one of them is stamped for re-evaluation
+  bool my_forced = false;                     // one of them is stamped -1
   s_dirty[tid] = 1;
   s_forced[tid] = 0;
   if (tid == 0) {
@@ -916,12 +997,19 @@ __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
     s_ev = 0;
     s_switch = 0;
     s_cyc[0] = s_cyc[1] = s_cyc[2] = s_cyc[3] = 0;
-    s_invVf = 1.0f / (float)V;
-    s_magf = 0.0f;
+    s_vs = 0.0;
+    D.ev_vd[0] = 0.0;
+    D.ev_vs[0] = 0.0;
     s_slow = !allow_fast || D.ctr[CTR_SLOW] != 0;
     s_done = (*D.err != 0) || (s_na > D.act_cap) || (s_nvs2 > D.vs2_cap) || (s_nrows > D.row_cap);
+    if (s_na + 2 > D.ev_cap) {
+      atomicOr(D.err, CAFE_ERR_ITER_CAP);
+      s_done = 1;
+    }
   }
   __syncthreads();
+  if (s_slow)  // exact per-event scan with eager growth: extents are kept current
+    for (int r = tid; r < s_nrows; r += nthr) D.row_m[r] = CAFE_M_DONE;
   // magnitudes for the key rounding bound: largest numerator and extent
   if (!s_slow && !s_done) {
     unsigned long long gk = 0, ek = 0;
@@ -961,8 +1049,10 @@ __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
       // while (vSind2 != countS && tinc < DelT)
       if (!(s_nvs2 != s_countS && s_tinc < K.DelT)) s_done = 1;
       s_countS = s_nvs2;
-      if (!s_slow)
-        s_magf = (float)fabs(s_tinc) + (float)(s_gmax + s_emax) * s_invVf + 2.0f * (float)s_dsum;
+#ifdef CAFE_DETAIL_CYCLES
+      long long _t = clock64();
+      s_d27 += _t - s_dt0;
+#endif
     }
     __syncthreads();
     if (s_done) break;
@@ -1002,11 +1092,14 @@ __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
             if (km != CAFE_KEY_NONE) {
               // rows whose exact value may be the minimum: keys within twice the
               // rounding bound delta = (ev+16) 2^-48 (|K*| + |T| + (gmax+emax)/v
-              // + 2 sum|dt|), evaluated as a single-precision upper bound
+              // + 2 sum|dt| + 1e-300); the magnitude is bounded by a power of
+              // two from the exponents of its terms (below 8 times the largest)
               double kd = cafe_unkey(km);
-              float mag = ((float)fabs(kd) + s_magf) * (1.0f + 0x1p-20f);
-              float delta2 = (float)(ev + 16) * 0x1p-47f * mag;
-              if (mag >= 1e-20f) {
+              int eg = max(cafe_exp_ub(s_gmax), cafe_exp_ub(s_emax)) + 1 - cafe_exp_lb(V);
+              int em = max(max(cafe_exp_ub(kd), cafe_exp_ub(s_tinc)), max(eg, cafe_exp_ub(s_dsum) + 1)) + 3;
+              int ed = em - 47;  // 2 delta < (ev+16) 2^ed
+              if (ed > -126 && ed < 100 && ev < (1 << 24)) {
+                float delta2 = (float)(ev + 16) * __int_as_float((ed + 127) << 23);
                 double thr = kd + (double)delta2;
                 kt = cafe_is_nan(thr) ? CAFE_KEY_NONE : cafe_key(thr);
               } else {
@@ -1089,8 +1182,11 @@ __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
         if (s_dt < 0.0) s_negdt++;
         s_ev += 1;
         if (!s_slow) {
-          // this event's growth of every row (VoxelsCA.C:514)
+          // log this event's growth of the rows (VoxelsCA.C:514)
           s_vd = s_nuc ? 0.0 : V * s_dt;
+          D.ev_vd[s_ev] = s_vd;
+          s_vs = s_vs + s_vd;
+          D.ev_vs[s_ev] = s_vs;
           s_dsum += fabs(s_dt);
         }
       }
@@ -1100,6 +1196,7 @@ __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
     if (s_done) break;
     // rows that exist at the start of this event (the fill below appends)
     const int nrows_ev = s_nrows;
+    const double tinc_prev = s_tinc;  // the capture below advances s_tinc
     // ---- growth of every mushy cell of the list (VoxelsCA.C:511-516), slow path
     if (s_slow && !s_nuc) {
       double d = s_dt;
@@ -1209,6 +1306,7 @@ __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
             D.a_frow[icap] = r;
             D.row_death[r] = CAFE_ALIVE;
             D.row_E[r] = D.a_ext[icap];
+            D.row_m[r] = s_slow ? CAFE_M_DONE : s_ev;
           }
           const bool same_v = D.a_cls[icap] == 1;
           unsigned long long gk = cafe_row_fill_quad(D, K, r, icap, !s_slow && same_v, s_ev, s_tinc, s_quad);
@@ -1234,22 +1332,113 @@ __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
           s_done = 1;
         }
       }
-    } else if (!s_slow && !s_nuc) {
-      // ---- this event's growth of the rows (VoxelsCA.C:511-516), by the warps
-      // not busy with the capture; rows dying at this event grow too
-      const double vd = s_vd;
-      for (int r = tid - CAFE_QUAD_THREADS; r < nrows_ev; r += nthr - CAFE_QUAD_THREADS) {
-        if (D.row_death[r] < s_ev) continue;
-        double e = D.row_E[r] + vd;
-        if (cafe_is_neg(e)) {
-          e = 0.0;
-          if (vd < 0.0) {
-            // clamped by a negative event: the key bound no longer holds
+    } else if (!s_slow) {
+      // ---- warps 4..: evaluate ahead, for the next event, the rows it will
+      // most likely need exactly: the rows that lose the captured cell as a
+      // candidate (among them the capturing row) and the rows with the two
+      // smallest other keys. Selection still checks every row it needs.
+      const int e = s_ev, icap = s_icap;
+      const double T1 = tinc_prev + s_dt;  // s_tinc after this event
+      const int hid = tid - CAFE_QUAD_THREADS, nh = nthr - CAFE_QUAD_THREADS;
+      const int hw = warp - CAFE_QUAD_THREADS / 32;
+      if (!s_nuc && cafe_is_neg(s_dt)) {
+        // a negative event may clamp a small extent at zero (VoxelsCA.C:515),
+        // which breaks the key bound of that row: mark the rows whose
+        // extrapolated extent comes near zero for re-evaluation
+        const double vd = s_vd;
+        const double margin = (double)(e + 16) * 0x1p-48 * (s_emax + s_gmax + V * s_dsum + 1e-300);
+        const double vs_prev = D.ev_vs[e - 1];
+        for (int r = hid; r < nrows_ev; r += nh) {
+          if (D.row_death[r] < e) continue;
+          int m = D.row_m[r];
+          if (m >= e) continue;
+          double elb = D.row_E[r] + (vs_prev - D.ev_vs[m]);
+          if (elb + vd < margin) {
             D.row_stamp[r] = -1;
             s_forced[r % nthr] = 1;
           }
         }
-        D.row_E[r] = e;
+      }
+      unsigned long long k1 = CAFE_KEY_NONE, k2 = CAFE_KEY_NONE;
+      int r1 = -1, r2 = -1;
+      for (int r = hid; r < nrows_ev; r += nh) {
+        unsigned long long k = D.row_key[r];
+        if (k < k2) {
+          if (k < k1) {
+            k2 = k1;
+            r2 = r1;
+            k1 = k;
+            r1 = r;
+          } else {
+            k2 = k;
+            r2 = r;
+          }
+        }
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        unsigned long long ka = cafe_shfl_u64_xor(k1, o), kb = cafe_shfl_u64_xor(k2, o);
+        int ra = __shfl_xor_sync(0xffffffffu, r1, o), rb = __shfl_xor_sync(0xffffffffu, r2, o);
+        // two smallest (key, row) of {k1, k2, ka, kb}
+        bool a_first = ka < k1 || (ka == k1 && ra < r1);
+        unsigned long long n1 = a_first ? ka : k1;
+        int m1 = a_first ? ra : r1;
+        unsigned long long c1 = a_first ? k1 : k2, c2 = a_first ? kb : ka;
+        int d1 = a_first ? r1 : r2, d2 = a_first ? rb : ra;
+        bool c_first = c1 < c2 || (c1 == c2 && d1 < d2);
+        k1 = n1;
+        r1 = m1;
+        k2 = c_first ? c1 : c2;
+        r2 = c_first ? d1 : d2;
+      }
+      if (lane == 0) {
+        s_hk[hw][0] = k1;
+        s_hk[hw][1] = k2;
+        s_hr[hw][0] = r1;
+        s_hr[hw][1] = r2;
+      }
+      cafe_bar_helpers(nh);
+      // the pre-evaluations run in warps 6 and 7, whose sub-partitions host
+      // the shorter chains of the row fill
+      if (hw == 2) {
+        // rows of the captured cell's neighbours lose it as a candidate
+        const int nn = D.a_nn[icap];
+        if (lane < nn) {
+          int q = D.a_nbr[(long long)icap * CAFE_NSLOT + lane];
+          int r = D.a_frow[q];
+          if (r >= 0 && r < nrows_ev && D.row_death[r] >= e) {
+            int sl = cafe_find_slot(D, q, icap);
+            uint32_t live = D.row_live[r] & ~(sl >= 0 ? (1u << sl) : 0u);
+            if (live != 0u) {  // otherwise the row dies at this event
+              cafe_row_eval_live(D, K, r, e, T1, live);
+              s_dirty[r % nthr] = 1;
+            }
+          }
+        }
+      } else if (hw == 3 && lane < 2) {
+        unsigned long long b1 = CAFE_KEY_NONE, b2 = CAFE_KEY_NONE;
+        int q1 = -1, q2 = -1;
+        for (int w = 0; w < nh / 32; ++w)
+          for (int c = 0; c < 2; ++c) {
+            unsigned long long k = s_hk[w][c];
+            int r = s_hr[w][c];
+            if (r < 0) continue;
+            if (k < b1 || (k == b1 && r < q1)) {
+              b2 = b1;
+              q2 = q1;
+              b1 = k;
+              q1 = r;
+            } else if (k < b2 || (k == b2 && r < q2)) {
+              b2 = k;
+              q2 = r;
+            }
+          }
+        int r = lane == 0 ? q1 : q2;
+        unsigned long long k = lane == 0 ? b1 : b2;
+        // rows next to the captured cell are left to warp 6
+        if (r >= 0 && k != CAFE_KEY_NONE && cafe_find_slot(D, D.row_pos[r], icap) < 0) {
+          cafe_row_eval(D, K, r, e, T1);
+          s_dirty[r % nthr] = 1;
+        }
       }
     }
     __syncthreads();
@@ -1258,9 +1447,16 @@ __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
       long long tn = clock64();
       s_cyc[2] += tn - s_t0;
       s_t0 = tn;
-      if (s_switch) {
-        // a capturing cell with another growth velocity: continue with the
-        // exact per-event scan (the extents are current)
+    }
+    if (s_switch) {
+      // a capturing cell with another growth velocity: bring every row up to
+      // date and continue with the exact per-event scan
+      for (int r = tid; r < s_nrows; r += nthr) {
+        cafe_row_replay(D, r, s_ev);
+        D.row_m[r] = CAFE_M_DONE;
+      }
+      __syncthreads();
+      if (tid == 0) {
         s_slow = 1;
         s_switch = 0;
       }
@@ -1288,19 +1484,24 @@ __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
 #ifdef CAFE_DETAIL_CYCLES
     for (int c = 0; c < 16; ++c)
       if (c != 9 && c != 13 && c != 14) atomicAdd(&D.stat[STAT_DETAIL + c], (unsigned long long)s_dcyc[c]);
+    atomicAdd(&D.stat[STAT_DETAIL + 27], (unsigned long long)s_d27);
     atomicAdd(&D.stat[STAT_DETAIL + 9], *(volatile unsigned long long *)&crm_fallback_calls - s_fb0);
     atomicAdd(&D.stat[STAT_DETAIL + 13], *(volatile unsigned long long *)&crm_special_calls - s_sp0);
 #endif
   }
 }
 
-// Copies the rows' extents, kept in row order during the event loop, back to
-// their active-list positions.
+// Brings every row's extent up to the end of the step (the lazily applied
+// growth of VoxelsCA.C:511-516), spread over the whole GPU, and copies it back
+// to the row cell's active-list position.
 __global__ void k_rows_finalize(CafeDev D) {
   int nrows = D.ctr[CTR_NROWS_END];
   if (nrows > D.row_cap) nrows = (int)D.row_cap;
-  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < nrows; r += gridDim.x * blockDim.x)
+  int nev = D.ctr[CTR_NEV];
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < nrows; r += gridDim.x * blockDim.x) {
+    cafe_row_replay(D, r, nev);
     D.a_ext[D.row_pos[r]] = D.row_E[r];
+  }
 }
 
 // ------------------------------------------------------------------ write back
