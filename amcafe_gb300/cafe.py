@@ -90,13 +90,22 @@ class Simulation:
         check(self._lib.cafe_sim_stats(self._h, ctypes.byref(s)))
         return {f: getattr(s, f) for f, _ in CafeStats._fields_}
 
-    def state(self):
+    def state(self, out=None):
+        """gID, vState, extents, centroid (x,y,z interleaved) and buildj as
+        numpy arrays. `out` may hold preallocated contiguous arrays under the
+        same keys (for example views of pinned host memory), filled in place."""
         n = self.ncell
-        gid = np.empty(n, np.int32)
-        vs = np.empty(n, np.int32)
-        ext = np.empty(n, np.float64)
-        cen = np.empty(3 * n, np.float64)
-        bj = np.empty(n, np.int32)
+        shapes = dict(gID=(n, np.int32), vState=(n, np.int32), extents=(n, np.float64),
+                      centroid=(3 * n, np.float64), buildj=(n, np.int32))
+        arrs = {}
+        for k, (m, dt) in shapes.items():
+            a = None if out is None else out.get(k)
+            if a is None:
+                a = np.empty(m, dt)
+            elif a.dtype != dt or a.size != m or not a.flags["C_CONTIGUOUS"]:
+                raise ValueError("out[%r] must be a contiguous %s array of %d elements" % (k, np.dtype(dt), m))
+            arrs[k] = a
+        gid, vs, ext, cen, bj = (arrs[k] for k in ("gID", "vState", "extents", "centroid", "buildj"))
         check(self._lib.cafe_sim_download_state(self._h, _ptr(gid, ctypes.c_int32), _ptr(vs, ctypes.c_int32),
                                                 _ptr(ext, ctypes.c_double), _ptr(cen, ctypes.c_double),
                                                 _ptr(bj, ctypes.c_int32)))

@@ -371,6 +371,9 @@ struct cafe_sim {
   int event_scan = 0;     // 1: evaluate every frontier row at every event
   std::vector<void *> owned;
   int *h_pinned = nullptr;  // pinned host mirror of ctr + err
+  // staging for host transfers (allocated on first use)
+  unsigned char *xfer = nullptr;
+  int *d_bad = nullptr;
   // per-phase device timing (CUDA events on `stream`) and kernel-launch counts
   bool timing = false;
   cudaEvent_t marks[8] = {nullptr};
@@ -1222,34 +1225,51 @@ int cafe_sim_stream(cafe_sim *s, void **stream) {
   return CAFE_OK;
 }
 
+// Staging buffer for layout conversions of host transfers: CAFE_XFER_BYTES
+// of device memory plus an error word, allocated once per handle.
+#define CAFE_XFER_BYTES (64LL << 20)
+static int ensure_xfer(cafe_sim *s) {
+  if (s->xfer) return CAFE_OK;
+  int rc = dalloc(&s->xfer, CAFE_XFER_BYTES, s->owned);
+  if (!rc) rc = dalloc(&s->d_bad, 1, s->owned);
+  return rc;
+}
+
 int cafe_sim_download_state(cafe_sim *s, int32_t *gID, int32_t *vState, double *extents,
                             double *centroid, int32_t *buildjID) {
   if (!s) return fail(CAFE_E_ARG, "null handle");
   CUDA_TRY(cudaSetDevice(s->device));
   int rc = sim_sync(s);
   if (rc) return rc;
-  long long N = s->K.N;
-  if (gID) CUDA_TRY(cudaMemcpy(gID, s->D.gid, N * sizeof(int32_t), cudaMemcpyDeviceToHost));
-  if (extents) CUDA_TRY(cudaMemcpy(extents, s->D.ext, N * sizeof(double), cudaMemcpyDeviceToHost));
-  if (vState || buildjID) {
-    std::vector<uint8_t> b(N);
-    if (vState) {
-      CUDA_TRY(cudaMemcpy(b.data(), s->D.state, N, cudaMemcpyDeviceToHost));
-      for (long long i = 0; i < N; ++i) vState[i] = b[i];
-    }
-    if (buildjID) {
-      CUDA_TRY(cudaMemcpy(b.data(), s->D.buildj, N, cudaMemcpyDeviceToHost));
-      for (long long i = 0; i < N; ++i) buildjID[i] = b[i];
+  if ((rc = ensure_xfer(s))) return rc;
+  const long long N = s->K.N;
+  cudaStream_t st = s->stream;
+  // same layout: straight copies; others converted on the device chunk by chunk
+  if (gID) CUDA_TRY(cudaMemcpyAsync(gID, s->D.gid, N * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+  if (extents) CUDA_TRY(cudaMemcpyAsync(extents, s->D.ext, N * sizeof(double), cudaMemcpyDeviceToHost, st));
+  const uint8_t *u8src[2] = {s->D.state, s->D.buildj};
+  int32_t *i32dst[2] = {vState, buildjID};
+  const long long ci = CAFE_XFER_BYTES / (long long)sizeof(int32_t);
+  for (int f = 0; f < 2; ++f) {
+    if (!i32dst[f]) continue;
+    for (long long off = 0; off < N; off += ci) {
+      long long n = std::min(ci, N - off);
+      k_u8_to_i32<<<grid_blocks(n, 256, s), 256, 0, st>>>(u8src[f] + off, (int32_t *)s->xfer, n);
+      CUDA_TRY(cudaGetLastError());
+      CUDA_TRY(cudaMemcpyAsync(i32dst[f] + off, s->xfer, n * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
     }
   }
   if (centroid) {
-    std::vector<double> c(N);
-    double *src[3] = {s->D.cx, s->D.cy, s->D.cz};
-    for (int a = 0; a < 3; ++a) {
-      CUDA_TRY(cudaMemcpy(c.data(), src[a], N * sizeof(double), cudaMemcpyDeviceToHost));
-      for (long long i = 0; i < N; ++i) centroid[3 * i + a] = c[i];
+    const long long cc = CAFE_XFER_BYTES / (3LL * (long long)sizeof(double));
+    for (long long off = 0; off < N; off += cc) {
+      long long n = std::min(cc, N - off);
+      k_interleave3<<<grid_blocks(n, 256, s), 256, 0, st>>>(s->D.cx + off, s->D.cy + off, s->D.cz + off,
+                                                              (double *)s->xfer, n);
+      CUDA_TRY(cudaGetLastError());
+      CUDA_TRY(cudaMemcpyAsync(centroid + 3 * off, s->xfer, 3 * n * sizeof(double), cudaMemcpyDeviceToHost, st));
     }
   }
+  CUDA_TRY(cudaStreamSynchronize(st));
   return CAFE_OK;
 }
 
@@ -1291,33 +1311,49 @@ int cafe_sim_upload_state(cafe_sim *s, const int32_t *gID, const int32_t *vState
   if (!s || !gID || !vState || !extents || !centroid || !ctheta || ngrain < 0)
     return fail(CAFE_E_ARG, "null or negative argument");
   CUDA_TRY(cudaSetDevice(s->device));
-  long long N = s->K.N;
-  for (long long i = 0; i < N; ++i) {
-    if (vState[i] < 0 || vState[i] > 3) return fail(CAFE_E_ARG, "vState[%lld] = %d outside 0..3", i, vState[i]);
-    if (gID[i] < 0 || gID[i] > ngrain) return fail(CAFE_E_ARG, "gID[%lld] = %d outside 0..nGrain", i, gID[i]);
-  }
-  int rc = grow_grains(s, (long long)ngrain + 1);
+  int rc = sim_sync(s);
   if (rc) return rc;
-  std::vector<uint8_t> b(N);
-  for (long long i = 0; i < N; ++i) b[i] = (uint8_t)vState[i];
-  CUDA_TRY(cudaMemcpy(s->D.state, b.data(), N, cudaMemcpyHostToDevice));
-  CUDA_TRY(cudaMemcpy(s->D.gid, gID, N * sizeof(int32_t), cudaMemcpyHostToDevice));
-  CUDA_TRY(cudaMemcpy(s->D.ext, extents, N * sizeof(double), cudaMemcpyHostToDevice));
-  std::vector<double> c(N);
-  double *dst[3] = {s->D.cx, s->D.cy, s->D.cz};
-  for (int a = 0; a < 3; ++a) {
-    for (long long i = 0; i < N; ++i) c[i] = centroid[3 * i + a];
-    CUDA_TRY(cudaMemcpy(dst[a], c.data(), N * sizeof(double), cudaMemcpyHostToDevice));
-  }
-  if (ngrain > 0) {
-    CUDA_TRY(cudaMemcpy(s->D.cth, ctheta, 4LL * ngrain * sizeof(double), cudaMemcpyHostToDevice));
-    k_rot_range<<<grid_blocks(ngrain, 128, s), 128, 0, s->stream>>>(s->D, 0, ngrain);
+  if ((rc = ensure_xfer(s)) || (rc = grow_grains(s, (long long)ngrain + 1))) return rc;
+  const long long N = s->K.N;
+  cudaStream_t st = s->stream;
+  // the state is replaced from here on: the handle is usable again only after
+  // a successful upload
+  s->initialized = false;
+  CUDA_TRY(cudaMemsetAsync(s->d_bad, 0, sizeof(int), st));
+  CUDA_TRY(cudaMemcpyAsync(s->D.gid, gID, N * sizeof(int32_t), cudaMemcpyHostToDevice, st));
+  k_check_range_i32<<<grid_blocks(N, 256, s), 256, 0, st>>>(s->D.gid, N, ngrain, s->d_bad, 2);
+  CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaMemcpyAsync(s->D.ext, extents, N * sizeof(double), cudaMemcpyHostToDevice, st));
+  const long long ci = CAFE_XFER_BYTES / (long long)sizeof(int32_t);
+  for (long long off = 0; off < N; off += ci) {
+    long long n = std::min(ci, N - off);
+    CUDA_TRY(cudaMemcpyAsync(s->xfer, vState + off, n * sizeof(int32_t), cudaMemcpyHostToDevice, st));
+    k_i32_to_u8_check<<<grid_blocks(n, 256, s), 256, 0, st>>>((const int32_t *)s->xfer, s->D.state + off, n, 3,
+                                                                s->d_bad, 1);
     CUDA_TRY(cudaGetLastError());
   }
+  const long long cc = CAFE_XFER_BYTES / (3LL * (long long)sizeof(double));
+  for (long long off = 0; off < N; off += cc) {
+    long long n = std::min(cc, N - off);
+    CUDA_TRY(cudaMemcpyAsync(s->xfer, centroid + 3 * off, 3 * n * sizeof(double), cudaMemcpyHostToDevice, st));
+    k_deinterleave3<<<grid_blocks(n, 256, s), 256, 0, st>>>((const double *)s->xfer, s->D.cx + off, s->D.cy + off,
+                                                              s->D.cz + off, n);
+    CUDA_TRY(cudaGetLastError());
+  }
+  if (ngrain > 0) {
+    CUDA_TRY(cudaMemcpyAsync(s->D.cth, ctheta, 4LL * ngrain * sizeof(double), cudaMemcpyHostToDevice, st));
+    k_rot_range<<<grid_blocks(ngrain, 128, s), 128, 0, st>>>(s->D, 0, ngrain);
+    CUDA_TRY(cudaGetLastError());
+  }
+  CUDA_TRY(cudaMemcpyAsync(s->h_pinned + 3, s->d_bad, sizeof(int), cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaStreamSynchronize(st));
+  int bad = s->h_pinned[3];
+  if (bad & 1) return fail(CAFE_E_ARG, "vState value outside 0..3");
+  if (bad & 2) return fail(CAFE_E_ARG, "gID value outside 0..nGrain (%d)", ngrain);
   s->nGrain = ngrain;
   s->h_pinned[2] = ngrain;
-  CUDA_TRY(cudaMemcpyAsync(s->D.ctr + CTR_NGRAIN, s->h_pinned + 2, sizeof(int), cudaMemcpyHostToDevice, s->stream));
-  CUDA_TRY(cudaMemsetAsync(s->D.ctr + CTR_NLIQ, 0, sizeof(int), s->stream));
+  CUDA_TRY(cudaMemcpyAsync(s->D.ctr + CTR_NGRAIN, s->h_pinned + 2, sizeof(int), cudaMemcpyHostToDevice, st));
+  CUDA_TRY(cudaMemsetAsync(s->D.ctr + CTR_NLIQ, 0, sizeof(int), st));
   s->full_k2 = true;
   s->have_prev_box = false;
   s->initialized = true;

@@ -1739,3 +1739,39 @@ __global__ void k_temperature(CafeConsts K, CafeStepParams P, double *T) {
     T[idx] = K.Tcls[cafe_temp_class_exact(K, P, i, j, k)];
   }
 }
+
+// ------------------------------------------------------------------ host transfers
+// Layout conversions between the device state and the C ABI's host layout
+// (int32 vState/BuildjID, interleaved centres), one staging chunk at a time.
+__global__ void k_u8_to_i32(const uint8_t *src, int32_t *dst, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    dst[i] = src[i];
+}
+// Converts and checks 0 <= v <= vmax; a bad value sets bit `bad_bit` of *bad.
+__global__ void k_i32_to_u8_check(const int32_t *src, uint8_t *dst, long long n, int vmax, int *bad, int bad_bit) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    int v = src[i];
+    if (v < 0 || v > vmax) atomicOr(bad, bad_bit);
+    dst[i] = (uint8_t)v;
+  }
+}
+__global__ void k_check_range_i32(const int32_t *a, long long n, int vmax, int *bad, int bad_bit) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    int v = a[i];
+    if (v < 0 || v > vmax) atomicOr(bad, bad_bit);
+  }
+}
+__global__ void k_interleave3(const double *x, const double *y, const double *z, double *dst, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    dst[3 * i] = x[i];
+    dst[3 * i + 1] = y[i];
+    dst[3 * i + 2] = z[i];
+  }
+}
+__global__ void k_deinterleave3(const double *src, double *x, double *y, double *z, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    x[i] = src[3 * i];
+    y[i] = src[3 * i + 1];
+    z[i] = src[3 * i + 2];
+  }
+}

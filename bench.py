@@ -305,7 +305,18 @@ def main():
     # ---- end to end through the C ABI with host buffers
     e2e = None
     if not args.no_e2e and not done:
-        st_host = sim.state()
+        # host buffers in pinned memory, as a host program driving the engine
+        # would keep them
+        import torch
+
+        def pinned(n, dt):
+            return torch.empty(n, dtype=dt, pin_memory=True).numpy()
+
+        ncell = sim.ncell
+        st_host = sim.state(out=dict(gID=pinned(ncell, torch.int32), vState=pinned(ncell, torch.int32),
+                                     extents=pinned(ncell, torch.float64),
+                                     centroid=pinned(3 * ncell, torch.float64),
+                                     buildj=pinned(ncell, torch.int32)))
         cth_host = sim.ctheta()
         h2d = sum(a.nbytes for a in (st_host["gID"], st_host["vState"], st_host["extents"], st_host["centroid"])) \
             + cth_host.nbytes
@@ -322,7 +333,7 @@ def main():
             inf = sim.info()  # per-step result read back to the host
             per_step_d2h += 8
             n_e += 1
-        out_state = sim.state()
+        out_state = sim.state(out=st_host)
         te = time.time() - te0
         te = reduce_max(dist, te)
         e2e = {"value": ws * nvox * n_e / te, "unit": "voxel-updates/s",
