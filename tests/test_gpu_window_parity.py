@@ -1,0 +1,50 @@
+"""GPU against the oracle at config-1 size (512x256x128 voxels, 16.8 M cells).
+
+The oracle cannot run config 1 from the start in test time, so the GPU state at
+a step (fields, grain table, laser and layer counters, genlayer engine state)
+is handed to the oracle, both advance the same number of steps, and the
+results must agree: integer fields bit-exact, floats within 1e-12 relative.
+Windows: in the first track (step 300) and at the benchmark's window (step
+2000, four tracks into the first layers).
+"""
+import os
+
+import numpy as np
+import pytest
+
+import cafe_oracle as orc
+from _compare import compare_states
+
+pytestmark = pytest.mark.gpu
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+C1 = os.path.join(ROOT, "amcafe_gb300", "decks", "c1.in")
+WINDOW = 6
+
+
+def _compare_window(sim, where):
+    info = sim.info()
+    st = sim.state()
+    cth = sim.ctheta()
+    ost, _, ostats = orc.run_window(C1, info, st, cth, WINDOW, libm=orc.LIBM_CR)
+    for _ in range(WINDOW):
+        sim.step()
+    got = sim.state()
+    compare_states(got, ost, where=where)
+    assert ostats["steps"] == WINDOW, ostats
+    assert sim.info()["nGrain"] == ostats["nGrain"], where
+
+
+def test_config1_windows_match_oracle():
+    from amcafe_gb300 import Simulation
+
+    sim = Simulation(C1, device=0)
+    sim.InitializeVoxels()
+    sim.begin()
+    sim.run(300)
+    _compare_window(sim, "config 1, steps 300-%d" % (300 + WINDOW))
+    sim.run(2000 - 300 - WINDOW)
+    _compare_window(sim, "config 1, steps 2000-%d" % (2000 + WINDOW))
+    stats = sim.stats()
+    assert stats["exact_scan_steps"] == 0
+    assert stats["events"] > 0 and stats["nucleations"] > 0, stats
+    sim.close()
