@@ -29,6 +29,14 @@
 #define CAFE_CELLS_PER_THREAD 8
 #define CAFE_CELLS_PER_BLOCK (CAFE_DENSE_THREADS * CAFE_CELLS_PER_THREAD)
 #define CAFE_LOOP_THREADS 512
+#ifdef CAFE_DETAIL_CYCLES
+// clock read ordered with the surrounding memory operations and barriers
+__device__ __forceinline__ long long cafe_clock_ordered() {
+  long long t;
+  asm volatile("mov.u64 %0, %%clock64;" : "=l"(t)::"memory");
+  return t;
+}
+#endif
 
 // ------------------------------------------------------------------ helpers
 __device__ __forceinline__ int cafe_hot(const CafeDev &D, const CafeConsts &K, const CafeStepParams &P,
@@ -625,8 +633,6 @@ struct CafeQuadScratch {
 };
 #define CAFE_QUAD_THREADS 128
 __device__ __forceinline__ void cafe_bar_quad() { asm volatile("bar.sync 1, 128;" ::: "memory"); }
-// Barrier of the event loop's warps 4 and up (n threads).
-__device__ __forceinline__ void cafe_bar_helpers(int n) { asm volatile("bar.sync 2, %0;" ::"r"(n) : "memory"); }
 
 // cafe_row_fill_warp for warps 0-3 of the block together (all 128 threads
 // must call it): a warp issues one FP64 instruction at a time whatever its
@@ -928,42 +934,201 @@ __global__ void k_rows_init(CafeDev D, CafeConsts K) {
   }
 }
 
+// ---- event selection by a group of warps ------------------------------------
+// Shared scratch of one selecting group (up to 16 warps).
+struct CafeSelShared {
+  unsigned long long redk[16];
+  CafeCand red[16];
+  unsigned long long kthr;
+  long long evals;  // selection rounds that evaluated rows exactly
+#ifdef CAFE_DETAIL_CYCLES
+  long long cyc[4], rounds;
+#endif
+};
+// bar.sync on a named barrier, with an OR reduction of v over the n threads.
+__device__ __forceinline__ int cafe_bar_or(int id, int n, int v) {
+  int r;
+  asm volatile(
+      "{ .reg .pred p, q;\n\t"
+      "setp.ne.s32 q, %1, 0;\n\t"
+      "bar.red.or.pred p, %2, %3, q;\n\t"
+      "selp.s32 %0, 1, 0, p; }"
+      : "=r"(r)
+      : "r"(v), "r"(id), "r"(n)
+      : "memory");
+  return r;
+}
+__device__ __forceinline__ void cafe_bar_n(int id, int n) { asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory"); }
+
+// Keyed selection of the best capture among rows [0, nrows) for the iteration
+// after `ev` events at time T (VoxelsCA.C:386-480 restricted to the rows that
+// can hold the minimum), by the group of gn threads (gtid = 0..gn-1) that
+// shares named barrier `bar`. Thread gtid owns rows r = gtid (mod gn) and keeps
+// the smallest key among them in my_min, rescanned when dirty[gtid] is set; a
+// forced[gtid] flag makes it evaluate its rows stamped -1. The result is left
+// in S.red[0] (valid after the group's next barrier; every group thread has
+// passed the last barrier when this returns).
+__device__ void cafe_select_keyed(const CafeDev &D, const CafeConsts &K, int ev, double T, int nrows, int gtid,
+                                  int gn, int bar, unsigned long long &my_min, bool &my_forced,
+                                  unsigned char *dirty, unsigned char *forced, CafeSelShared &S, double gmax,
+                                  double emax, double dsum, double V) {
+  const int lane = gtid & 31, gw = gtid >> 5, ngw = gn >> 5;
+#ifdef CAFE_DETAIL_CYCLES
+  long long sc0 = cafe_clock_ordered();
+#endif
+  if (forced[gtid]) {
+    forced[gtid] = 0;
+    my_forced = true;
+  }
+  if (dirty[gtid]) {
+    dirty[gtid] = 0;
+    unsigned long long m = CAFE_KEY_NONE;
+    for (int r = gtid; r < nrows; r += gn) m = min(m, D.row_key[r]);
+    my_min = m;
+  }
+  CafeCand best;
+#ifdef CAFE_DETAIL_CYCLES
+  long long sc1 = cafe_clock_ordered();
+  if (gtid == 0) S.cyc[0] += sc1 - sc0;  // dirty rescan
+#endif
+  while (true) {
+#ifdef CAFE_DETAIL_CYCLES
+    long long sr0 = cafe_clock_ordered();
+#endif
+    unsigned long long km = my_min;
+    for (int o = 16; o > 0; o >>= 1) km = min(km, cafe_shfl_u64_xor(km, o));
+    if (lane == 0) S.redk[gw] = km;
+    cafe_bar_n(bar, gn);
+    if (gw == 0) {
+      km = lane < ngw ? S.redk[lane] : CAFE_KEY_NONE;
+      for (int o = 16; o > 0; o >>= 1) km = min(km, cafe_shfl_u64_xor(km, o));
+      if (lane == 0) {
+        unsigned long long kt = CAFE_KEY_NONE;
+        if (km != CAFE_KEY_NONE) {
+          // rows whose exact value may be the minimum: keys within twice the
+          // rounding bound delta = (ev+16) 2^-48 (|K*| + |T| + (gmax+emax)/v
+          // + 2 sum|dt| + 1e-300); the magnitude is bounded by a power of
+          // two from the exponents of its terms (below 8 times the largest)
+          double kd = cafe_unkey(km);
+          int eg = max(cafe_exp_ub(gmax), cafe_exp_ub(emax)) + 1 - cafe_exp_lb(V);
+          int em = max(max(cafe_exp_ub(kd), cafe_exp_ub(T)), max(eg, cafe_exp_ub(dsum) + 1)) + 3;
+          int ed = em - 47;  // 2 delta < (ev+16) 2^ed
+          if (ed > -126 && ed < 100 && ev < (1 << 24)) {
+            float delta2 = (float)(ev + 16) * __int_as_float((ed + 127) << 23);
+            double thr = kd + (double)delta2;
+            kt = cafe_is_nan(thr) ? CAFE_KEY_NONE : cafe_key(thr);
+          } else {
+            double magd = fabs(kd) + fabs(T) + (gmax + emax) / V + 2.0 * dsum + 1e-300;
+            double thr = kd + 2.0 * ((double)(ev + 16) * 0x1p-48 * magd);
+            kt = cafe_is_nan(thr) ? CAFE_KEY_NONE : cafe_key(thr);
+          }
+        }
+        S.kthr = kt;
+      }
+    }
+    cafe_bar_n(bar, gn);
+#ifdef CAFE_DETAIL_CYCLES
+    long long sr1 = cafe_clock_ordered();
+    if (gtid == 0) S.cyc[1] += sr1 - sr0;  // minimum and threshold
+#endif
+    const unsigned long long kthr = S.kthr;
+    int again = 0;
+    best = cafe_cand_none();
+    if (kthr != CAFE_KEY_NONE && (my_min <= kthr || my_forced)) {
+      unsigned long long m = CAFE_KEY_NONE;
+      for (int r = gtid; r < nrows; r += gn) {
+        unsigned long long k = D.row_key[r];
+        if (k <= kthr || my_forced) {
+          int stamp = D.row_stamp[r];
+          // stamp -1: forced after a possible clamp of the row's extent
+          if ((k <= kthr && stamp != ev + 1) || (stamp == -1 && D.row_alive[r])) {
+            cafe_row_eval(D, K, r, ev, T);
+            k = D.row_key[r];
+            again = 1;
+          }
+          if (k <= kthr) {
+            CafeCand c;
+            c.t = D.row_bt[r];
+            c.ruqs = D.row_bruq[r];
+            c.tk = cafe_key_canon(c.t);
+            c.rk = cafe_key_canon(c.ruqs);
+            c.j = D.row_j[r];
+            c.s = D.row_bslot[r];
+            if (cafe_cand_better(c, best)) best = c;
+          }
+        }
+        m = min(m, k);
+      }
+      my_min = m;
+      my_forced = false;
+    }
+#ifdef CAFE_DETAIL_CYCLES
+    long long sr2 = cafe_clock_ordered();
+    if (gtid == 0) S.cyc[2] += sr2 - sr1;  // scan and evaluations (this thread)
+#endif
+    again = cafe_bar_or(bar, gn, again);
+#ifdef CAFE_DETAIL_CYCLES
+    if (gtid == 0) {
+      S.cyc[3] += cafe_clock_ordered() - sr2;  // waiting for the slowest thread's evaluations
+      S.rounds++;
+    }
+#endif
+    if (gtid == 0 && again) S.evals++;
+    if (!again) break;
+  }
+  best = cafe_warp_best(best);
+  if (lane == 0) S.red[gw] = best;
+  cafe_bar_n(bar, gn);
+  if (gw == 0) {
+    CafeCand b = lane < ngw ? S.red[lane] : cafe_cand_none();
+    b = cafe_warp_best(b);
+    if (lane == 0) S.red[0] = b;
+  }
+}
+
 // The capture/nucleation loop of one step (VoxelsCA.C:381-610), one block.
+//
+// Keyed mode (every frontier row grows with one velocity) pipelines two events:
+// after the winner of event e is applied and the captured cell's neighbours are
+// updated, warps 0-3 fill the row of the newly captured cell while warps 4-15
+// select the best capture of event e+1 among the other rows. The winner of
+// e+1 is the better of that selection and the new row's own exact best
+// candidate: a row not evaluated by the selection has a key above the
+// threshold, so its exact time is above the selected one. Exact mode (the
+// reference's per-event scan of every row, also the fallback when the rows
+// stop sharing one velocity) evaluates every row at every event.
 __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
     k_event_loop(CafeDev D, CafeConsts K, CafeStepParams P, long long max_events, int allow_fast) {
+  constexpr int NSEL = CAFE_LOOP_THREADS - CAFE_QUAD_THREADS;  // threads of the selecting warps
   __shared__ CafeCand red[CAFE_LOOP_THREADS / 32];
-  __shared__ unsigned long long redk[CAFE_LOOP_THREADS / 32];
-  __shared__ double s_tinc, s_dt, s_dsum, s_gmax, s_emax, s_vd;
+  __shared__ CafeSelShared s_sel;
+  __shared__ CafeCand s_best;  // winner of the next event (keyed mode)
+  __shared__ double s_tinc, s_dt, s_dsum, s_gmax, s_emax, s_vd, s_vs;
   __shared__ int s_nvs2, s_countS, s_nrows, s_ngrain, s_done, s_nuc, s_icap, s_jspos, s_bslot, s_na, s_slow,
-      s_ev, s_switch;
-  __shared__ unsigned long long s_kthr;
-  __shared__ unsigned char s_dirty[CAFE_LOOP_THREADS];  // a row of thread i changed its key elsewhere
-  __shared__ unsigned char s_forced[CAFE_LOOP_THREADS];  // a row of thread i was stamped -1
-  __shared__ double s_vs;                                // running sum of the logged growth
-  __shared__ unsigned long long s_hk[CAFE_LOOP_THREADS / 32][2];  // helper warps: two smallest keys
-  __shared__ int s_hr[CAFE_LOOP_THREADS / 32][2];                 // ... and their rows
+      s_ev, s_switch, s_newrow;
+  __shared__ unsigned char s_dirty[NSEL];   // a row of selecting thread i changed its key elsewhere
+  __shared__ unsigned char s_forced[NSEL];  // a row of selecting thread i was stamped -1
   __shared__ uint32_t s_rng;
   __shared__ unsigned int s_sdloc;
-  __shared__ long long s_nnuc, s_negdt, s_evals;
-  __shared__ long long s_cyc[4];  // selection, capture apply, bookkeeping + new row, other
+  __shared__ long long s_nnuc, s_negdt;
+  __shared__ long long s_cyc[4];  // winner, capture + bookkeeping, new row || selection, merge
   __shared__ long long s_t0;
   __shared__ CafeQuadScratch s_quad;
 #ifdef CAFE_DETAIL_CYCLES
   // finer event-loop sections, thread 0's clock (profiling builds only)
-  __shared__ long long s_dcyc[16], s_dt0, s_d27;
-#define CAFE_DCYC(slot)                  \
-  do {                                   \
-    if (threadIdx.x == 0) {              \
-      long long _t = clock64();          \
-      s_dcyc[slot] += _t - s_dt0;        \
-      s_dt0 = _t;                        \
-    }                                    \
+  __shared__ long long s_dcyc[16], s_dt0;
+#define CAFE_DCYC(slot)                          \
+  do {                                           \
+    if (threadIdx.x == 0) {                      \
+      long long _t = cafe_clock_ordered();       \
+      s_dcyc[slot] += _t - s_dt0;                \
+      s_dt0 = _t;                                \
+    }                                            \
   } while (0)
   if (threadIdx.x < 16) s_dcyc[threadIdx.x] = 0;
-  if (threadIdx.x == 0) s_d27 = 0;
   __shared__ unsigned long long s_fb0, s_sp0;
   if (threadIdx.x == 0) {
-    s_dt0 = clock64();
+    s_dt0 = cafe_clock_ordered();
     s_fb0 = *(volatile unsigned long long *)&crm_fallback_calls;
     s_sp0 = *(volatile unsigned long long *)&crm_special_calls;
   }
@@ -974,11 +1139,14 @@ __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
 #endif
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int nthr = blockDim.x, nwarp = blockDim.x >> 5;
+  const int hid = tid - CAFE_QUAD_THREADS;  // index among the selecting warps (>= 0 there)
   const double V = K.vhat_cls[1];
-  unsigned long long my_min = CAFE_KEY_NONE;  // smallest key of this thread's rows
+  unsigned long long my_min = CAFE_KEY_NONE;  // smallest key of this selecting thread's rows
   bool my_forced = false;                     // one of them is stamped -1
-  s_dirty[tid] = 1;
-  s_forced[tid] = 0;
+  if (hid >= 0) {
+    s_dirty[hid] = 1;
+    s_forced[hid] = 0;
+  }
   if (tid == 0) {
     s_na = D.ctr[CTR_NA];
     s_nvs2 = D.ctr[CTR_NVS2];
@@ -990,14 +1158,18 @@ __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
     s_tinc = 0.0;
     s_dsum = 0.0;
     s_vd = 0.0;
+    s_vs = 0.0;
     s_countS = s_na;
     s_nnuc = 0;
     s_negdt = 0;
-    s_evals = 0;
+    s_sel.evals = 0;
+#ifdef CAFE_DETAIL_CYCLES
+    s_sel.cyc[0] = s_sel.cyc[1] = s_sel.cyc[2] = s_sel.cyc[3] = s_sel.rounds = 0;
+#endif
     s_ev = 0;
     s_switch = 0;
+    s_newrow = -1;
     s_cyc[0] = s_cyc[1] = s_cyc[2] = s_cyc[3] = 0;
-    s_vs = 0.0;
     D.ev_vd[0] = 0.0;
     D.ev_vs[0] = 0.0;
     s_slow = !allow_fast || D.ctr[CTR_SLOW] != 0;
@@ -1008,224 +1180,98 @@ __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
     }
   }
   __syncthreads();
-  if (s_slow)  // exact per-event scan with eager growth: extents are kept current
-    for (int r = tid; r < s_nrows; r += nthr) D.row_m[r] = CAFE_M_DONE;
-  // magnitudes for the key rounding bound: largest numerator and extent
+  // ======================================================== keyed, pipelined
   if (!s_slow && !s_done) {
-    unsigned long long gk = 0, ek = 0;
-    for (int r = tid; r < s_nrows; r += nthr) {
-      int p = D.row_pos[r];
-      uint32_t live = D.row_live[r];
-      int nn = D.a_nn[p];
-      for (int k = 0; k < nn; ++k)
-        if (live >> k & 1u) {
-          double gv = fabs(D.row_g[(long long)r * CAFE_NSLOT + k]);
-          if (gv == gv) gk = max(gk, cafe_key(gv));
-        }
-      ek = max(ek, cafe_key(fabs(D.a_ext[p])));
-    }
-    for (int o = 16; o > 0; o >>= 1) {
-      gk = max(gk, __shfl_down_sync(0xffffffffu, gk, o));
-      ek = max(ek, __shfl_down_sync(0xffffffffu, ek, o));
-    }
-    if (lane == 0) {
-      red[warp].t = cafe_unkey(gk);
-      red[warp].ruqs = cafe_unkey(ek);
-    }
-    __syncthreads();
-    if (tid == 0) {
-      double gm = 0, em = 0;
-      for (int w = 0; w < nwarp; ++w) {
-        gm = fmax(gm, red[w].t);
-        em = fmax(em, red[w].ruqs);
-      }
-      s_gmax = gm;
-      s_emax = em;
-    }
-    __syncthreads();
-  }
-  while (true) {
-    if (tid == 0) {
-      // while (vSind2 != countS && tinc < DelT)
-      if (!(s_nvs2 != s_countS && s_tinc < K.DelT)) s_done = 1;
-      s_countS = s_nvs2;
-#ifdef CAFE_DETAIL_CYCLES
-      long long _t = clock64();
-      s_d27 += _t - s_dt0;
-#endif
-    }
-    __syncthreads();
-    if (s_done) break;
-    CAFE_DCYC(15);
-    if (tid == 0) s_t0 = clock64();
-    CafeCand best = cafe_cand_none();
-    if (s_slow) {
-      // ---- exact scan of every row (VoxelsCA.C:386-445)
-      for (int r = tid; r < s_nrows; r += nthr)
-        if (D.row_alive[r]) cafe_row_best(D, K, r, best);
-    } else {
-      // ---- keyed selection: exact evaluation only near the smallest key.
-      // Thread tid owns the rows r = tid (mod nthr) and keeps the smallest key
-      // among them in my_min; it rescans them when another thread changed one
-      // of their keys (s_dirty).
-      const int ev = s_ev;
-      if (s_forced[tid]) {
-        s_forced[tid] = 0;
-        my_forced = true;
-      }
-      if (s_dirty[tid]) {
-        s_dirty[tid] = 0;
-        unsigned long long m = CAFE_KEY_NONE;
-        for (int r = tid; r < s_nrows; r += nthr) m = min(m, D.row_key[r]);
-        my_min = m;
-      }
-      while (true) {
-        unsigned long long km = my_min;
-        for (int o = 16; o > 0; o >>= 1) km = min(km, cafe_shfl_u64_xor(km, o));
-        if (lane == 0) redk[warp] = km;
-        __syncthreads();
-        if (warp == 0) {
-          km = lane < nwarp ? redk[lane] : CAFE_KEY_NONE;
-          for (int o = 16; o > 0; o >>= 1) km = min(km, cafe_shfl_u64_xor(km, o));
-          if (lane == 0) {
-            unsigned long long kt = CAFE_KEY_NONE;
-            if (km != CAFE_KEY_NONE) {
-              // rows whose exact value may be the minimum: keys within twice the
-              // rounding bound delta = (ev+16) 2^-48 (|K*| + |T| + (gmax+emax)/v
-              // + 2 sum|dt| + 1e-300); the magnitude is bounded by a power of
-              // two from the exponents of its terms (below 8 times the largest)
-              double kd = cafe_unkey(km);
-              int eg = max(cafe_exp_ub(s_gmax), cafe_exp_ub(s_emax)) + 1 - cafe_exp_lb(V);
-              int em = max(max(cafe_exp_ub(kd), cafe_exp_ub(s_tinc)), max(eg, cafe_exp_ub(s_dsum) + 1)) + 3;
-              int ed = em - 47;  // 2 delta < (ev+16) 2^ed
-              if (ed > -126 && ed < 100 && ev < (1 << 24)) {
-                float delta2 = (float)(ev + 16) * __int_as_float((ed + 127) << 23);
-                double thr = kd + (double)delta2;
-                kt = cafe_is_nan(thr) ? CAFE_KEY_NONE : cafe_key(thr);
-              } else {
-                double magd = fabs(kd) + fabs(s_tinc) + (s_gmax + s_emax) / V + 2.0 * s_dsum + 1e-300;
-                double thr = kd + 2.0 * ((double)(ev + 16) * 0x1p-48 * magd);
-                kt = cafe_is_nan(thr) ? CAFE_KEY_NONE : cafe_key(thr);
-              }
-            }
-            s_kthr = kt;
+    // magnitudes for the key rounding bound: largest numerator and extent
+    {
+      unsigned long long gk = 0, ek = 0;
+      for (int r = tid; r < s_nrows; r += nthr) {
+        int p = D.row_pos[r];
+        uint32_t live = D.row_live[r];
+        int nn = D.a_nn[p];
+        for (int k = 0; k < nn; ++k)
+          if (live >> k & 1u) {
+            double gv = fabs(D.row_g[(long long)r * CAFE_NSLOT + k]);
+            if (!cafe_is_nan(gv)) gk = max(gk, cafe_key(gv));
           }
-        }
-        __syncthreads();
-        CAFE_DCYC(0);
-        const unsigned long long kthr = s_kthr;
-        int again = 0;
-        best = cafe_cand_none();
-        if (kthr != CAFE_KEY_NONE && (my_min <= kthr || my_forced)) {
-          unsigned long long m = CAFE_KEY_NONE;
-          for (int r = tid; r < s_nrows; r += nthr) {
-            unsigned long long k = D.row_key[r];
-            if (k <= kthr || my_forced) {
-              int stamp = D.row_stamp[r];
-              // stamp -1: forced after a possible clamp of the row's extent
-              if ((k <= kthr && stamp != ev + 1) || (stamp == -1 && D.row_alive[r])) {
-                cafe_row_eval(D, K, r, ev, s_tinc);
-                k = D.row_key[r];
-                again = 1;
-              }
-              if (k <= kthr) {
-                CafeCand c;
-                c.t = D.row_bt[r];
-                c.ruqs = D.row_bruq[r];
-                c.tk = cafe_key_canon(c.t);
-                c.rk = cafe_key_canon(c.ruqs);
-                c.j = D.row_j[r];
-                c.s = D.row_bslot[r];
-                if (cafe_cand_better(c, best)) best = c;
-              }
-            }
-            m = min(m, k);
-          }
-          my_min = m;
-          my_forced = false;
-        }
-        again = __syncthreads_or(again);
-        CAFE_DCYC(1);
-        if (tid == 0 && again) s_evals++;
-        if (!again) break;
+        const double er = D.row_E[r];  // NaN extents occur (the reference's 0/0) and are left out
+        if (!cafe_is_nan(er)) ek = max(ek, cafe_key(fabs(er)));
       }
-    }
-    best = cafe_warp_best(best);
-    if (lane == 0) red[warp] = best;
-    __syncthreads();
-    CAFE_DCYC(2);
-    if (warp == 0) {
-      CafeCand b = lane < nwarp ? red[lane] : cafe_cand_none();
-      b = cafe_warp_best(b);
-      if (lane == 0) red[0] = b;
-    }
-    if (tid == 0) {
-      long long tn = clock64();
-      s_cyc[0] += tn - s_t0;
-      s_t0 = tn;
-      CafeCand b = red[0];
-      CAFE_DCYC(3);
-      if (b.j < 0 || !(b.tk < CAFE_KEY_1E6) || s_ev >= max_events) {
-        if (b.j >= 0 && b.tk < CAFE_KEY_1E6) atomicOr(D.err, CAFE_ERR_ITER_CAP);
-        s_done = 1;
-      } else {
-        cafe_uniform_stream st;
-        st.x = s_rng;
-        double U = cafe_uniform_next(&st);
-        s_rng = st.x;
-        int jspos = D.vs2[b.j];
-        s_jspos = jspos;
-        s_bslot = b.s;
-        s_icap = D.a_nbr[(long long)jspos * CAFE_NSLOT + b.s];
-        s_nuc = U < K.rX;
-        s_dt = s_nuc ? 0.0 : b.t;
-        if (s_dt < 0.0) s_negdt++;
-        s_ev += 1;
-        if (!s_slow) {
-          // log this event's growth of the rows (VoxelsCA.C:514)
-          s_vd = s_nuc ? 0.0 : V * s_dt;
-          D.ev_vd[s_ev] = s_vd;
-          s_vs = s_vs + s_vd;
-          D.ev_vs[s_ev] = s_vs;
-          s_dsum += fabs(s_dt);
-        }
+      for (int o = 16; o > 0; o >>= 1) {
+        gk = max(gk, cafe_shfl_u64_xor(gk, o));
+        ek = max(ek, cafe_shfl_u64_xor(ek, o));
       }
-      CAFE_DCYC(4);
-    }
-    __syncthreads();
-    if (s_done) break;
-    // rows that exist at the start of this event (the fill below appends)
-    const int nrows_ev = s_nrows;
-    const double tinc_prev = s_tinc;  // the capture below advances s_tinc
-    // ---- growth of every mushy cell of the list (VoxelsCA.C:511-516), slow path
-    if (s_slow && !s_nuc) {
-      double d = s_dt;
-      if (isfinite(d)) {
-        for (int r = tid; r < nrows_ev; r += nthr) {
-          if (!D.row_alive[r]) continue;
-          int p = D.row_pos[r];
-          double e = D.row_E[r] + K.vhat_cls[D.a_cls[p]] * d;
-          D.row_E[r] = (e < 0.0) ? 0.0 : e;
-        }
-      } else {
-        // a non-finite DtMin also reaches the cells that have no liquid
-        // neighbour (0 * inf)
-        for (int j = tid; j < s_countS; j += nthr) {
-          int p = D.vs2[j];
-          int r = D.a_frow[p];
-          double v = (r >= 0 && D.row_alive[r]) ? K.vhat_cls[D.a_cls[p]] : 0.0;
-          double *ep = r >= 0 ? &D.row_E[r] : &D.a_ext[p];
-          double e = *ep + v * d;
-          *ep = (e < 0.0) ? 0.0 : e;
-        }
+      if (lane == 0) {
+        red[warp].tk = gk;
+        red[warp].rk = ek;
       }
-    }
-    __syncthreads();
-    CAFE_DCYC(5);
-    if (warp < CAFE_QUAD_THREADS / 32) {
-      // ---- the captured cell (VoxelsCA.C:483-505 and 518-605)
+      __syncthreads();
       if (tid == 0) {
-        int icap = s_icap, js = s_jspos;
+        unsigned long long g2 = 0, e2 = 0;
+        for (int w = 0; w < nwarp; ++w) {
+          g2 = max(g2, red[w].tk);
+          e2 = max(e2, red[w].rk);
+        }
+        s_gmax = g2 ? cafe_unkey(g2) : 0.0;
+        s_emax = e2 ? cafe_unkey(e2) : 0.0;
+      }
+      __syncthreads();
+    }
+    // selection of the first event
+    if (hid >= 0)
+      cafe_select_keyed(D, K, 0, 0.0, s_nrows, hid, NSEL, 2, my_min, my_forced, s_dirty, s_forced, s_sel, s_gmax,
+                        s_emax, s_dsum, V);
+    __syncthreads();
+    if (tid == 0) s_best = s_sel.red[0];
+    __syncthreads();
+    while (true) {
+      // ---- (1) the winner of this event (VoxelsCA.C:427-505), thread 0
+      if (tid == 0) {
+        s_t0 = clock64();
+        // while (vSind2 != countS && tinc < DelT)
+        const bool tin = !cafe_is_nan(s_tinc) && cafe_key(s_tinc) < cafe_key(K.DelT);
+        if (!(s_nvs2 != s_countS && tin)) s_done = 1;
+        s_countS = s_nvs2;
+        CafeCand b = s_best;
+        if (!s_done) {
+          if (b.j < 0 || !(b.tk < CAFE_KEY_1E6) || s_ev >= max_events) {
+            if (b.j >= 0 && b.tk < CAFE_KEY_1E6) atomicOr(D.err, CAFE_ERR_ITER_CAP);
+            s_done = 1;
+          } else {
+            cafe_uniform_stream st;
+            st.x = s_rng;
+            double U = cafe_uniform_next(&st);
+            s_rng = st.x;
+            int jspos = D.vs2[b.j];
+            s_jspos = jspos;
+            s_bslot = b.s;
+            s_icap = D.a_nbr[(long long)jspos * CAFE_NSLOT + b.s];
+            s_nuc = U < K.rX;
+            s_dt = s_nuc ? 0.0 : b.t;
+            if (cafe_is_neg(s_dt)) s_negdt++;
+            s_ev += 1;
+            // log this event's growth of the rows (VoxelsCA.C:514)
+            s_vd = s_nuc ? 0.0 : V * s_dt;
+            D.ev_vd[s_ev] = s_vd;
+            s_vs = s_vs + s_vd;
+            D.ev_vs[s_ev] = s_vs;
+            s_dsum += fabs(s_dt);
+            s_tinc += s_dt;
+          }
+        }
+        long long tn = clock64();
+        s_cyc[0] += tn - s_t0;
+        s_t0 = tn;
+      }
+      __syncthreads();
+      if (s_done) break;
+      CAFE_DCYC(0);
+      const int e = s_ev, icap = s_icap;
+      const int nrows_ev = s_nrows;  // rows before this event's new row
+      // ---- (2) the captured cell, its neighbours' rows, clamp flags
+      if (tid == 0) {
+        // the captured cell (VoxelsCA.C:483-505 and 518-605)
+        const int js = s_jspos;
         D.a_state[icap] = 2;
         if (s_nvs2 < D.vs2_cap) {
           D.vs2[s_nvs2] = icap;
@@ -1264,55 +1310,66 @@ __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
           D.a_cy[icap] = gq[2];
           D.a_cz[icap] = gq[3];
         }
-        CAFE_DCYC(6);
-        s_tinc += s_dt;
-        long long tn = clock64();
-        s_cyc[1] += tn - s_t0;
-        s_t0 = tn;
-      }
-      cafe_bar_quad();
-      // ---- neighbours of the captured cell lose one liquid neighbour
-      if (warp == 0) {
-        int icap = s_icap;
-        int nn = D.a_nn[icap];
+      } else if (warp == 1) {
+        // neighbours of the captured cell lose one liquid neighbour
+        const int nn = D.a_nn[icap];
         if (lane < nn) {
           int q = D.a_nbr[(long long)icap * CAFE_NSLOT + lane];
           int left = --D.a_liq[q];
           int r = D.a_frow[q];
           if (r >= 0 && D.row_alive[r]) {
-            int s = cafe_find_slot(D, q, icap);
-            if (s >= 0) D.row_live[r] &= ~(1u << s);
+            int sl = cafe_find_slot(D, q, icap);
+            if (sl >= 0) D.row_live[r] &= ~(1u << sl);
             if (left <= 0) {
               D.row_alive[r] = 0;
-              D.row_death[r] = s_ev;  // it grew at this event too
+              D.row_death[r] = e;  // it grew at this event too
               D.row_key[r] = CAFE_KEY_NONE;
-              s_dirty[r % nthr] = 1;
+              s_dirty[r % NSEL] = 1;
             }
           }
         }
-      }
-      cafe_bar_quad();
-      CAFE_DCYC(7);
-      // ---- the captured cell becomes a capturing cell if it qualifies
-      int icap = s_icap;
-      if (D.a_liq[icap] > 0 && D.a_cold[icap] && !s_done) {
-        int r = s_nrows;
-        if (r < D.row_cap) {
-          if (tid == 0) {
-            s_dirty[r % nthr] = 1;
-            D.row_pos[r] = icap;
-            D.row_j[r] = s_nvs2 - 1;
-            D.row_alive[r] = 1;
-            D.a_frow[icap] = r;
-            D.row_death[r] = CAFE_ALIVE;
-            D.row_E[r] = D.a_ext[icap];
-            D.row_m[r] = s_slow ? CAFE_M_DONE : s_ev;
+      } else if (hid >= 0 && !s_nuc && cafe_is_neg(s_dt)) {
+        // a negative event may clamp a small extent at zero (VoxelsCA.C:515),
+        // which breaks the key bound of that row: mark the rows whose
+        // extrapolated extent comes near zero for re-evaluation
+        const double vd = s_vd;
+        const double margin = (double)(e + 16) * 0x1p-48 * (s_emax + s_gmax + V * s_dsum + 1e-300);
+        const double vs_prev = D.ev_vs[e - 1];
+        for (int r = hid; r < nrows_ev; r += NSEL) {
+          if (D.row_death[r] < e) continue;
+          int m = D.row_m[r];
+          if (m >= e) continue;
+          double elb = D.row_E[r] + (vs_prev - D.ev_vs[m]);
+          if (elb + vd < margin) {
+            D.row_stamp[r] = -1;
+            s_forced[r % NSEL] = 1;
           }
-          const bool same_v = D.a_cls[icap] == 1;
-          unsigned long long gk = cafe_row_fill_quad(D, K, r, icap, !s_slow && same_v, s_ev, s_tinc, s_quad);
-          CAFE_DCYC(8);
-          if (tid == 0) {
-            if (!s_slow) {
+        }
+      }
+      __syncthreads();
+      CAFE_DCYC(1);
+      if (tid == 0) {
+        long long tn = clock64();
+        s_cyc[1] += tn - s_t0;
+        s_t0 = tn;
+      }
+      // ---- (3) the new row (warps 0-3) || selection of the next event (the rest)
+      if (warp < CAFE_QUAD_THREADS / 32) {
+        if (D.a_liq[icap] > 0 && D.a_cold[icap] && !s_done) {
+          int r = nrows_ev;
+          if (r < D.row_cap) {
+            if (tid == 0) {
+              D.row_pos[r] = icap;
+              D.row_j[r] = s_nvs2 - 1;
+              D.row_alive[r] = 1;
+              D.a_frow[icap] = r;
+              D.row_death[r] = CAFE_ALIVE;
+              D.row_E[r] = D.a_ext[icap];
+              D.row_m[r] = e;
+            }
+            const bool same_v = D.a_cls[icap] == 1;
+            unsigned long long gk = cafe_row_fill_quad(D, K, r, icap, same_v, e, s_tinc, s_quad);
+            if (tid == 0) {
               if (!same_v) {
                 s_switch = 1;
               } else {
@@ -1322,133 +1379,52 @@ __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
                 }
                 double ea = fabs(D.a_ext[icap]);
                 if (ea > s_emax) s_emax = ea;
-                CAFE_DCYC(10);
               }
+              s_nrows = r + 1;
+              s_newrow = r;
             }
-            s_nrows = r + 1;
-          }
-        } else if (tid == 0) {
-          atomicOr(D.err, CAFE_ERR_ROW_CAP);
-          s_done = 1;
-        }
-      }
-    } else if (!s_slow) {
-      // ---- warps 4..: evaluate ahead, for the next event, the rows it will
-      // most likely need exactly: the rows that lose the captured cell as a
-      // candidate (among them the capturing row) and the rows with the two
-      // smallest other keys. Selection still checks every row it needs.
-      const int e = s_ev, icap = s_icap;
-      const double T1 = tinc_prev + s_dt;  // s_tinc after this event
-      const int hid = tid - CAFE_QUAD_THREADS, nh = nthr - CAFE_QUAD_THREADS;
-      const int hw = warp - CAFE_QUAD_THREADS / 32;
-      if (!s_nuc && cafe_is_neg(s_dt)) {
-        // a negative event may clamp a small extent at zero (VoxelsCA.C:515),
-        // which breaks the key bound of that row: mark the rows whose
-        // extrapolated extent comes near zero for re-evaluation
-        const double vd = s_vd;
-        const double margin = (double)(e + 16) * 0x1p-48 * (s_emax + s_gmax + V * s_dsum + 1e-300);
-        const double vs_prev = D.ev_vs[e - 1];
-        for (int r = hid; r < nrows_ev; r += nh) {
-          if (D.row_death[r] < e) continue;
-          int m = D.row_m[r];
-          if (m >= e) continue;
-          double elb = D.row_E[r] + (vs_prev - D.ev_vs[m]);
-          if (elb + vd < margin) {
-            D.row_stamp[r] = -1;
-            s_forced[r % nthr] = 1;
+          } else if (tid == 0) {
+            atomicOr(D.err, CAFE_ERR_ROW_CAP);
+            s_done = 1;
           }
         }
+      } else {
+        cafe_select_keyed(D, K, e, s_tinc, nrows_ev, hid, NSEL, 2, my_min, my_forced, s_dirty, s_forced, s_sel,
+                          s_gmax, s_emax, s_dsum, V);
       }
-      unsigned long long k1 = CAFE_KEY_NONE, k2 = CAFE_KEY_NONE;
-      int r1 = -1, r2 = -1;
-      for (int r = hid; r < nrows_ev; r += nh) {
-        unsigned long long k = D.row_key[r];
-        if (k < k2) {
-          if (k < k1) {
-            k2 = k1;
-            r2 = r1;
-            k1 = k;
-            r1 = r;
-          } else {
-            k2 = k;
-            r2 = r;
+      __syncthreads();
+      CAFE_DCYC(2);
+      // ---- (4) the winner of the next event: selection or the new row
+      if (tid == 0) {
+        long long tn = clock64();
+        s_cyc[2] += tn - s_t0;
+        s_t0 = tn;
+        CafeCand b = s_sel.red[0];
+        const int r = s_newrow;
+        if (r >= 0) {
+          s_newrow = -1;
+          s_dirty[r % NSEL] = 1;  // the row joins its owner's set
+          if (D.row_key[r] != CAFE_KEY_NONE) {
+            CafeCand c;
+            c.t = D.row_bt[r];
+            c.ruqs = D.row_bruq[r];
+            c.tk = cafe_key_canon(c.t);
+            c.rk = cafe_key_canon(c.ruqs);
+            c.j = D.row_j[r];
+            c.s = D.row_bslot[r];
+            if (cafe_cand_better(c, b)) b = c;
           }
         }
+        s_best = b;
+        tn = clock64();
+        s_cyc[3] += tn - s_t0;
+        s_t0 = tn;
       }
-      for (int o = 16; o > 0; o >>= 1) {
-        unsigned long long ka = cafe_shfl_u64_xor(k1, o), kb = cafe_shfl_u64_xor(k2, o);
-        int ra = __shfl_xor_sync(0xffffffffu, r1, o), rb = __shfl_xor_sync(0xffffffffu, r2, o);
-        // two smallest (key, row) of {k1, k2, ka, kb}
-        bool a_first = ka < k1 || (ka == k1 && ra < r1);
-        unsigned long long n1 = a_first ? ka : k1;
-        int m1 = a_first ? ra : r1;
-        unsigned long long c1 = a_first ? k1 : k2, c2 = a_first ? kb : ka;
-        int d1 = a_first ? r1 : r2, d2 = a_first ? rb : ra;
-        bool c_first = c1 < c2 || (c1 == c2 && d1 < d2);
-        k1 = n1;
-        r1 = m1;
-        k2 = c_first ? c1 : c2;
-        r2 = c_first ? d1 : d2;
-      }
-      if (lane == 0) {
-        s_hk[hw][0] = k1;
-        s_hk[hw][1] = k2;
-        s_hr[hw][0] = r1;
-        s_hr[hw][1] = r2;
-      }
-      cafe_bar_helpers(nh);
-      // the pre-evaluations run in warps 6 and 7, whose sub-partitions host
-      // the shorter chains of the row fill
-      if (hw == 2) {
-        // rows of the captured cell's neighbours lose it as a candidate
-        const int nn = D.a_nn[icap];
-        if (lane < nn) {
-          int q = D.a_nbr[(long long)icap * CAFE_NSLOT + lane];
-          int r = D.a_frow[q];
-          if (r >= 0 && r < nrows_ev && D.row_death[r] >= e) {
-            int sl = cafe_find_slot(D, q, icap);
-            uint32_t live = D.row_live[r] & ~(sl >= 0 ? (1u << sl) : 0u);
-            if (live != 0u) {  // otherwise the row dies at this event
-              cafe_row_eval_live(D, K, r, e, T1, live);
-              s_dirty[r % nthr] = 1;
-            }
-          }
-        }
-      } else if (hw == 3 && lane < 2) {
-        unsigned long long b1 = CAFE_KEY_NONE, b2 = CAFE_KEY_NONE;
-        int q1 = -1, q2 = -1;
-        for (int w = 0; w < nh / 32; ++w)
-          for (int c = 0; c < 2; ++c) {
-            unsigned long long k = s_hk[w][c];
-            int r = s_hr[w][c];
-            if (r < 0) continue;
-            if (k < b1 || (k == b1 && r < q1)) {
-              b2 = b1;
-              q2 = q1;
-              b1 = k;
-              q1 = r;
-            } else if (k < b2 || (k == b2 && r < q2)) {
-              b2 = k;
-              q2 = r;
-            }
-          }
-        int r = lane == 0 ? q1 : q2;
-        unsigned long long k = lane == 0 ? b1 : b2;
-        // rows next to the captured cell are left to warp 6
-        if (r >= 0 && k != CAFE_KEY_NONE && cafe_find_slot(D, D.row_pos[r], icap) < 0) {
-          cafe_row_eval(D, K, r, e, T1);
-          s_dirty[r % nthr] = 1;
-        }
-      }
+      __syncthreads();
+      CAFE_DCYC(3);
+      if (s_switch) break;
     }
-    __syncthreads();
-    CAFE_DCYC(11);
-    if (tid == 0) {
-      long long tn = clock64();
-      s_cyc[2] += tn - s_t0;
-      s_t0 = tn;
-    }
-    if (s_switch) {
+    if (s_switch && !s_done) {
       // a capturing cell with another growth velocity: bring every row up to
       // date and continue with the exact per-event scan
       for (int r = tid; r < s_nrows; r += nthr) {
@@ -1456,13 +1432,163 @@ __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
         D.row_m[r] = CAFE_M_DONE;
       }
       __syncthreads();
-      if (tid == 0) {
-        s_slow = 1;
-        s_switch = 0;
+      if (tid == 0) s_slow = 1;
+      __syncthreads();
+    }
+  } else if (s_slow && !s_done) {
+    // exact per-event scan with eager growth: extents are kept current
+    for (int r = tid; r < s_nrows; r += nthr) D.row_m[r] = CAFE_M_DONE;
+    __syncthreads();
+  }
+  // ======================================================== exact scan
+  while (s_slow && !s_done) {
+    if (tid == 0) {
+      // while (vSind2 != countS && tinc < DelT)
+      if (!(s_nvs2 != s_countS && s_tinc < K.DelT)) s_done = 1;
+      s_countS = s_nvs2;
+    }
+    __syncthreads();
+    if (s_done) break;
+    // ---- every row's best candidate (VoxelsCA.C:386-445)
+    CafeCand best = cafe_cand_none();
+    for (int r = tid; r < s_nrows; r += nthr)
+      if (D.row_alive[r]) cafe_row_best(D, K, r, best);
+    best = cafe_warp_best(best);
+    if (lane == 0) red[warp] = best;
+    __syncthreads();
+    if (warp == 0) {
+      CafeCand b = lane < nwarp ? red[lane] : cafe_cand_none();
+      b = cafe_warp_best(b);
+      if (lane == 0) {
+        if (b.j < 0 || !(b.tk < CAFE_KEY_1E6) || s_ev >= max_events) {
+          if (b.j >= 0 && b.tk < CAFE_KEY_1E6) atomicOr(D.err, CAFE_ERR_ITER_CAP);
+          s_done = 1;
+        } else {
+          cafe_uniform_stream st;
+          st.x = s_rng;
+          double U = cafe_uniform_next(&st);
+          s_rng = st.x;
+          int jspos = D.vs2[b.j];
+          s_jspos = jspos;
+          s_bslot = b.s;
+          s_icap = D.a_nbr[(long long)jspos * CAFE_NSLOT + b.s];
+          s_nuc = U < K.rX;
+          s_dt = s_nuc ? 0.0 : b.t;
+          if (s_dt < 0.0) s_negdt++;
+          s_ev += 1;
+        }
       }
     }
     __syncthreads();
-    CAFE_DCYC(12);
+    if (s_done) break;
+    // ---- growth of every mushy cell of the list (VoxelsCA.C:511-516)
+    if (!s_nuc) {
+      double d = s_dt;
+      if (isfinite(d)) {
+        for (int r = tid; r < s_nrows; r += nthr) {
+          if (!D.row_alive[r]) continue;
+          int p = D.row_pos[r];
+          double e = D.row_E[r] + K.vhat_cls[D.a_cls[p]] * d;
+          D.row_E[r] = (e < 0.0) ? 0.0 : e;
+        }
+      } else {
+        // a non-finite DtMin also reaches the cells that have no liquid
+        // neighbour (0 * inf)
+        for (int j = tid; j < s_countS; j += nthr) {
+          int p = D.vs2[j];
+          int r = D.a_frow[p];
+          double v = (r >= 0 && D.row_alive[r]) ? K.vhat_cls[D.a_cls[p]] : 0.0;
+          double *ep = r >= 0 ? &D.row_E[r] : &D.a_ext[p];
+          double e = *ep + v * d;
+          *ep = (e < 0.0) ? 0.0 : e;
+        }
+      }
+    }
+    __syncthreads();
+    const int icap = s_icap;
+    // ---- the captured cell (VoxelsCA.C:483-505 and 518-605)
+    if (tid == 0) {
+      const int js = s_jspos;
+      D.a_state[icap] = 2;
+      if (s_nvs2 < D.vs2_cap) {
+        D.vs2[s_nvs2] = icap;
+      } else {
+        atomicOr(D.err, CAFE_ERR_MUSHY_CAP);
+        s_done = 1;
+      }
+      s_nvs2 += 1;
+      if (s_nuc) {
+        int ci, cj, ck;
+        cafe_cell_xyz(K, D.act[icap], ci, cj, ck);
+        if (s_ngrain < D.grain_cap) {
+          double q4[4];
+          cafe_sample_orientation(K, s_sdloc, q4);
+          double *c = D.cth + 4LL * s_ngrain;
+          for (int a = 0; a < 4; ++a) c[a] = q4[a];
+          cafe_rot_from_cth(c, D.rot + 9LL * s_ngrain);
+        } else {
+          atomicOr(D.err, CAFE_ERR_GRAIN_CAP);
+          s_done = 1;
+        }
+        s_ngrain += 1;
+        D.a_gid[icap] = s_ngrain;
+        D.a_cx[icap] = ((double)ci + .5) * K.dx[0];
+        D.a_cy[icap] = ((double)cj + .5) * K.dx[1];
+        D.a_cz[icap] = ((double)ck + .5) * K.dx[2];
+        s_sdloc += 10u;
+        D.a_ext[icap] = 0.0;
+        s_nnuc++;
+      } else {
+        D.a_gid[icap] = D.a_gid[js];
+        const double *gq = D.row_geo + ((long long)D.a_frow[js] * CAFE_NSLOT + s_bslot) * 4;
+        D.a_ext[icap] = gq[0];
+        D.a_cx[icap] = gq[1];
+        D.a_cy[icap] = gq[2];
+        D.a_cz[icap] = gq[3];
+      }
+      s_tinc += s_dt;
+    } else if (warp == 1) {
+      // ---- neighbours of the captured cell lose one liquid neighbour
+      const int nn = D.a_nn[icap];
+      if (lane < nn) {
+        int q = D.a_nbr[(long long)icap * CAFE_NSLOT + lane];
+        int left = --D.a_liq[q];
+        int r = D.a_frow[q];
+        if (r >= 0 && D.row_alive[r]) {
+          int sl = cafe_find_slot(D, q, icap);
+          if (sl >= 0) D.row_live[r] &= ~(1u << sl);
+          if (left <= 0) {
+            D.row_alive[r] = 0;
+            D.row_death[r] = s_ev;
+            D.row_key[r] = CAFE_KEY_NONE;
+          }
+        }
+      }
+    }
+    __syncthreads();
+    // ---- the captured cell becomes a capturing cell if it qualifies
+    if (warp < CAFE_QUAD_THREADS / 32) {
+      if (D.a_liq[icap] > 0 && D.a_cold[icap] && !s_done) {
+        int r = s_nrows;
+        if (r < D.row_cap) {
+          if (tid == 0) {
+            D.row_pos[r] = icap;
+            D.row_j[r] = s_nvs2 - 1;
+            D.row_alive[r] = 1;
+            D.a_frow[icap] = r;
+            D.row_death[r] = CAFE_ALIVE;
+            D.row_E[r] = D.a_ext[icap];
+            D.row_m[r] = CAFE_M_DONE;
+          }
+          cafe_row_fill_quad(D, K, r, icap, false, s_ev, s_tinc, s_quad);
+          if (tid == 0) s_nrows = r + 1;
+        } else if (tid == 0) {
+          atomicOr(D.err, CAFE_ERR_ROW_CAP);
+          s_done = 1;
+        }
+      }
+    }
+    __syncthreads();
   }
   if (tid == 0) {
     D.ctr[CTR_NGRAIN] = s_ngrain;
@@ -1478,17 +1604,19 @@ __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
     atomicAdd(&D.stat[STAT_STEPS], 1ULL);
     atomicAdd(&D.stat[STAT_SUMNA], (unsigned long long)s_na);
     atomicAdd(&D.stat[STAT_SUMROWS], (unsigned long long)s_nrows);
-    atomicAdd(&D.stat[STAT_EVALS], (unsigned long long)s_evals);
+    atomicAdd(&D.stat[STAT_EVALS], (unsigned long long)s_sel.evals);
     if (s_slow) atomicAdd(&D.stat[STAT_SLOWSTEPS], 1ULL);
     for (int c = 0; c < 4; ++c) atomicAdd(&D.stat[STAT_CYC_SELECT + c], (unsigned long long)s_cyc[c]);
 #ifdef CAFE_DETAIL_CYCLES
     for (int c = 0; c < 16; ++c)
       if (c != 9 && c != 13 && c != 14) atomicAdd(&D.stat[STAT_DETAIL + c], (unsigned long long)s_dcyc[c]);
-    atomicAdd(&D.stat[STAT_DETAIL + 27], (unsigned long long)s_d27);
     atomicAdd(&D.stat[STAT_DETAIL + 9], *(volatile unsigned long long *)&crm_fallback_calls - s_fb0);
     atomicAdd(&D.stat[STAT_DETAIL + 13], *(volatile unsigned long long *)&crm_special_calls - s_sp0);
+    for (int c = 0; c < 4; ++c) atomicAdd(&D.stat[STAT_DETAIL + 4 + c], (unsigned long long)s_sel.cyc[c]);
+    atomicAdd(&D.stat[STAT_DETAIL + 8], (unsigned long long)s_sel.rounds);
 #endif
   }
+#undef CAFE_DCYC
 }
 
 // Brings every row's extent up to the end of the step (the lazily applied
