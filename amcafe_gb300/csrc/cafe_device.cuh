@@ -96,6 +96,9 @@ struct CafeDev {
   // this slot captures it, 4 doubles
   double *row_geo;
   long long row_cap;
+  // (row, slot) pairs whose capture geometry the row set-up evaluates, as
+  // row * 32 + slot, row_cap * CAFE_NSLOT entries
+  int32_t *row_pairs;
   // rows during the event loop: row_E is the row cell's extent (ExtA)
   // including the growth of events 1..row_m, copied back to a_ext afterwards;
   // a row grows at the events (birth, row_death]; row_key orders the rows by
@@ -130,6 +133,7 @@ enum {
   CTR_NLIQ,        // liquid cells listed by the last write-back
   CTR_SLOW,        // 1: this step's rows do not share one growth velocity
   CTR_NROWS_END,   // frontier rows after the event loop
+  CTR_NPAIRS,      // (row, slot) pairs listed for the row set-up
   CTR_COUNT
 };
 enum { STAT_EVENTS = 0, STAT_NUC, STAT_MAXNA, STAT_MAXROWS, STAT_STEPS, STAT_NEGDT, STAT_SUMNA, STAT_SUMROWS,

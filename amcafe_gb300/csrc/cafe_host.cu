@@ -736,7 +736,8 @@ int cafe_sim_create(const char *deck_path, const cafe_options *opt, cafe_sim **o
       (rc = dalloc(&D.row_j, D.row_cap, o)) || (rc = dalloc(&D.row_alive, D.row_cap, o)) ||
       (rc = dalloc(&D.row_ord, (size_t)D.row_cap * CAFE_NSLOT, o)) || (rc = dalloc(&D.row_live, D.row_cap, o)) ||
       (rc = dalloc(&D.row_g, (size_t)D.row_cap * CAFE_NSLOT, o)) ||
-      (rc = dalloc(&D.row_geo, (size_t)D.row_cap * CAFE_NSLOT * 4, o)) || (rc = dalloc(&D.blk, D.blk_cap, o)) ||
+      (rc = dalloc(&D.row_geo, (size_t)D.row_cap * CAFE_NSLOT * 4, o)) ||
+      (rc = dalloc(&D.row_pairs, (size_t)D.row_cap * CAFE_NSLOT, o)) || (rc = dalloc(&D.blk, D.blk_cap, o)) ||
       (rc = dalloc(&D.row_E, D.row_cap, o)) || (rc = dalloc(&D.row_death, D.row_cap, o)) ||
       (rc = dalloc(&D.row_m, D.row_cap, o)) || (rc = dalloc(&D.ev_vd, D.ev_cap, o)) ||
       (rc = dalloc(&D.ev_vs, D.ev_cap, o)) ||
@@ -1000,8 +1001,11 @@ int cafe_sim_update_voxels(cafe_sim *s) {
     k_scan_pairs<<<1, 1024, 0, st>>>(D.blk, s->nblk_pos, D.ctr + CTR_NVS2, D.ctr + CTR_NROWS);
     k_lists_scatter<<<nbp, CAFE_DENSE_THREADS, 0, st>>>(D);
     CUDA_TRY(cudaMemsetAsync(D.ctr + CTR_SLOW, 0, sizeof(int), st));
-    k_rows_init<<<s->nsm * 4, 256, 0, st>>>(D, K);
-    LAUNCHED(CAFE_PH_GATHER, 5);
+    CUDA_TRY(cudaMemsetAsync(D.ctr + CTR_NPAIRS, 0, sizeof(int), st));
+    k_rows_prep<<<s->nsm * 4, 256, 0, st>>>(D, K);
+    k_rows_geo<<<s->nsm * 8, 256, 0, st>>>(D, K);
+    k_rows_order<<<s->nsm * 4, 256, 0, st>>>(D, K);
+    LAUNCHED(CAFE_PH_GATHER, 7);
   }
   {
     PhaseScope ps(s, CAFE_PH_EVENTS);

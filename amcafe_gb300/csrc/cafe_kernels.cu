@@ -12,7 +12,7 @@
 //   k_gather        per-position copies, neighbour positions (VoxelsCA.C:
 //                   283-335), ruq offsets (VoxelsCA.C:380) by RNG jump-ahead
 //   k_lists_*       vs2ind (mushy positions in order) and frontier rows
-//   k_rows_init     capture-time numerators per (frontier cell, liquid
+//   k_rows_*        capture-time numerators per (frontier cell, liquid
 //                   neighbour), sorted per cell
 //   k_event_loop    the sequential capture/nucleation loop (VoxelsCA.C:
 //                   381-610), one thread block
@@ -588,45 +588,6 @@ __device__ unsigned long long cafe_row_finish_warp(const CafeDev &D, const CafeC
   return ak;
 }
 
-// Fills row r for position p within one warp: lane s evaluates neighbour slot
-// s completely (numerator and capture result), then cafe_row_finish_warp.
-__device__ unsigned long long cafe_row_fill_warp(const CafeDev &D, const CafeConsts &K, long long r,
-                                                 int p, bool eval, int ev, double T) {
-  int lane = threadIdx.x & 31;
-  int nn = D.a_nn[p];
-  bool liv = false;
-  int gp = D.a_gid[p];
-  bool grain_ok = gp >= 1 && gp <= D.grain_cap;
-  double gv = 0.0;
-  int q = 0;
-  if (lane < nn) {
-    q = D.a_nbr[(long long)p * CAFE_NSLOT + lane];
-    if (D.a_state[q] == 1) {
-      liv = true;
-      if (!grain_ok) {
-        gv = NAN;  // a capturing cell without a grain never captures
-      } else {
-        const double *R = D.rot + 9LL * (gp - 1);
-        double Rm[9];
-        for (int a = 0; a < 9; ++a) Rm[a] = R[a];
-        int i, j, k, si, sj, sk;
-        cafe_cell_xyz(K, D.act[q], i, j, k);
-        cafe_cell_xyz(K, D.act[p], si, sj, sk);
-        double cs[3] = {D.a_cx[p], D.a_cy[p], D.a_cz[p]};
-        double e, cn[3];
-        cafe_capture_geometry(K, i, j, k, si, sj, sk, cs, Rm, &gv, &e, cn);
-        double *o = D.row_geo + (r * CAFE_NSLOT + lane) * 4;
-        o[0] = e;
-        o[1] = cn[0];
-        o[2] = cn[1];
-        o[3] = cn[2];
-      }
-      D.row_g[r * CAFE_NSLOT + lane] = gv;
-    }
-  }
-  return cafe_row_finish_warp(D, K, r, p, nn, liv, gv, q, eval, ev, T);
-}
-
 // Per-slot partial results passed between the four warps of cafe_row_fill_quad.
 struct CafeQuadScratch {
   double cth[32], sph[32], l[32], d1I[32], dI2[32], d1J[32], dJ3[32], g[32], t[32], ruqs[32];
@@ -634,8 +595,11 @@ struct CafeQuadScratch {
 #define CAFE_QUAD_THREADS 128
 __device__ __forceinline__ void cafe_bar_quad() { asm volatile("bar.sync 1, 128;" ::: "memory"); }
 
-// cafe_row_fill_warp for warps 0-3 of the block together (all 128 threads
-// must call it): a warp issues one FP64 instruction at a time whatever its
+// Fills row r for position p, the cell just captured, with warps 0-3 of the
+// block together (all 128 threads must call it): every liquid neighbour slot
+// gets its numerator g and capture result (extent, centre), the slots are
+// ordered and, with `eval`, the row's exact best candidate at iteration `ev`
+// and time T is stored. A warp issues one FP64 instruction at a time whatever its
 // active lanes, so the independent chains of each slot's geometry run in
 // different warps, lane s of each warp on slot s:
 //   warp 0: cos th and the cell distance l; warp 1: sin ph;
@@ -913,24 +877,89 @@ __device__ __forceinline__ void cafe_row_eval(const CafeDev &D, const CafeConsts
   cafe_row_eval_live(D, K, r, ev, T, D.row_live[r]);
 }
 
-// Frontier rows of the step: numerators, order, and (when every row grows
-// with the same velocity) the initial exact evaluation and keys.
-__global__ void k_rows_init(CafeDev D, CafeConsts K) {
+// Frontier rows of the step, in three passes so that the capture geometry,
+// the expensive part, runs with one (row, slot) pair per lane:
+// k_rows_prep (one warp per row) finds each row's liquid neighbours, sets the
+// row's extent and growth watermark, and lists the pairs that need geometry;
+// k_rows_geo evaluates the listed pairs; k_rows_order (one warp per row)
+// orders each row's slots and, when every row grows with the same velocity,
+// takes its exact best candidate and key.
+__global__ void k_rows_prep(CafeDev D, CafeConsts K) {
   int nrows = D.ctr[CTR_NROWS];
   if (nrows > D.row_cap) nrows = (int)D.row_cap;
-  int warps = (gridDim.x * blockDim.x) >> 5;
-  int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  int lane = threadIdx.x & 31;
+  const int warps = (gridDim.x * blockDim.x) >> 5;
+  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  const unsigned FULL = 0xffffffffu;
   const double V = K.vhat_cls[1];
   for (int r = w; r < nrows; r += warps) {
     int p = D.row_pos[r];
-    cafe_row_fill_warp(D, K, r, p, true, 0, 0.0);
+    int nn = D.a_nn[p];
+    int gp = D.a_gid[p];
+    bool grain_ok = gp >= 1 && gp <= D.grain_cap;
+    bool liv = false;
+    if (lane < nn) liv = D.a_state[D.a_nbr[(long long)p * CAFE_NSLOT + lane]] == 1;
+    if (liv && !grain_ok) D.row_g[(long long)r * CAFE_NSLOT + lane] = NAN;  // never captures
+    uint32_t work = __ballot_sync(FULL, liv && grain_ok);
+    int base = 0;
+    if (lane == 0 && work) base = atomicAdd(&D.ctr[CTR_NPAIRS], __popc(work));
+    base = __shfl_sync(FULL, base, 0);
+    if (work >> lane & 1u) D.row_pairs[base + __popc(work & ((1u << lane) - 1u))] = r * 32 + lane;
     if (lane == 0) {
       D.row_E[r] = D.a_ext[p];
       D.row_m[r] = 0;
       D.row_death[r] = CAFE_ALIVE;
       if (D.a_cls[p] != 1 || !(V > 0.0 && V < INFINITY)) atomicOr(&D.ctr[CTR_SLOW], 1);
     }
+  }
+}
+
+__global__ void k_rows_geo(CafeDev D, CafeConsts K) {
+  int n = D.ctr[CTR_NPAIRS];
+  const long long cap = D.row_cap * CAFE_NSLOT;
+  if (n > cap) n = (int)cap;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    int v = D.row_pairs[i];
+    int r = v >> 5, sl = v & 31;
+    int p = D.row_pos[r];
+    int q = D.a_nbr[(long long)p * CAFE_NSLOT + sl];
+    const double *Rg = D.rot + 9LL * (D.a_gid[p] - 1);
+    double Rm[9];
+    for (int a = 0; a < 9; ++a) Rm[a] = Rg[a];
+    int i0, j0, k0, si, sj, sk;
+    cafe_cell_xyz(K, D.act[q], i0, j0, k0);
+    cafe_cell_xyz(K, D.act[p], si, sj, sk);
+    double cs[3] = {D.a_cx[p], D.a_cy[p], D.a_cz[p]};
+    double g, e, cn[3];
+    cafe_capture_geometry(K, i0, j0, k0, si, sj, sk, cs, Rm, &g, &e, cn);
+    long long o = (long long)r * CAFE_NSLOT + sl;
+    D.row_g[o] = g;
+    double *og = D.row_geo + o * 4;
+    og[0] = e;
+    og[1] = cn[0];
+    og[2] = cn[1];
+    og[3] = cn[2];
+  }
+}
+
+__global__ void k_rows_order(CafeDev D, CafeConsts K) {
+  int nrows = D.ctr[CTR_NROWS];
+  if (nrows > D.row_cap) nrows = (int)D.row_cap;
+  const int warps = (gridDim.x * blockDim.x) >> 5;
+  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  for (int r = w; r < nrows; r += warps) {
+    int p = D.row_pos[r];
+    int nn = D.a_nn[p];
+    int q = 0;
+    bool liv = false;
+    double gv = 0.0;
+    if (lane < nn) {
+      q = D.a_nbr[(long long)p * CAFE_NSLOT + lane];
+      liv = D.a_state[q] == 1;
+      if (liv) gv = D.row_g[(long long)r * CAFE_NSLOT + lane];
+    }
+    cafe_row_finish_warp(D, K, r, p, nn, liv, gv, q, true, 0, 0.0);
   }
 }
 
