@@ -382,7 +382,9 @@ struct cafe_sim {
   double phase_ms[CAFE_NPHASE] = {0};
   long long phase_launch[CAFE_NPHASE] = {0};
   long long launches = 0;
-  long long nblk = 0;       // dense compaction blocks
+  long long nblk = 0;       // dense pass blocks
+  long long nblk_act = 0;   // active-set compaction blocks
+  int act_chunks = 1;       // 8-cell chunks per thread of the compaction
   long long nblk_pos = 0;   // position compaction blocks
   int nsm = 1;
 };
@@ -720,6 +722,11 @@ int cafe_sim_create(const char *deck_path, const cafe_options *opt, cafe_sim **o
   long long gcap = opt && opt->grain_capacity > 0 ? opt->grain_capacity : (long long)(2 * est) + (1 << 16);
   D.grain_cap = (int)std::min<long long>(gcap, 2000000000LL);
   s->nblk = (N + CAFE_CELLS_PER_BLOCK - 1) / CAFE_CELLS_PER_BLOCK;
+  s->act_chunks = N >= (1LL << 26) ? CAFE_ACT_MAX_CHUNKS : 1;
+  {
+    long long per_block = (long long)CAFE_CELLS_PER_BLOCK * s->act_chunks;
+    s->nblk_act = (N + per_block - 1) / per_block;
+  }
   s->nblk_pos = (acap + CAFE_CELLS_PER_BLOCK - 1) / CAFE_CELLS_PER_BLOCK;
   D.blk_cap = std::max(s->nblk, 2 * s->nblk_pos);
   auto &o = s->owned;
@@ -987,9 +994,9 @@ int cafe_sim_update_voxels(cafe_sim *s) {
       LAUNCHED(CAFE_PH_CLASSIFY, 1);
     }
     CUDA_TRY(cudaMemsetAsync(D.ctr + CTR_NLIQ, 0, sizeof(int), st));
-    k_active_count<<<nb, CAFE_DENSE_THREADS, 0, st>>>(D, K, P);
-    k_scan_blocks<<<1, 1024, 0, st>>>(D.blk, s->nblk, D.ctr + CTR_NA);
-    k_active_scatter<<<nb, CAFE_DENSE_THREADS, 0, st>>>(D, K, P);
+    k_active_count<<<(int)s->nblk_act, CAFE_DENSE_THREADS, 0, st>>>(D, K, P, s->act_chunks);
+    k_scan_blocks<<<1, 1024, 0, st>>>(D.blk, s->nblk_act, D.ctr + CTR_NA);
+    k_active_scatter<<<(int)s->nblk_act, CAFE_DENSE_THREADS, 0, st>>>(D, K, P, s->act_chunks);
     LAUNCHED(CAFE_PH_CLASSIFY, 3);
   }
   int gb = s->nsm * 8;
@@ -998,7 +1005,7 @@ int cafe_sim_update_voxels(cafe_sim *s) {
     k_gather<<<gb, 256, 0, st>>>(D, K, P);
     int nbp = (int)s->nblk_pos;
     k_lists_count<<<nbp, CAFE_DENSE_THREADS, 0, st>>>(D);
-    k_scan_pairs<<<1, 1024, 0, st>>>(D.blk, s->nblk_pos, D.ctr + CTR_NVS2, D.ctr + CTR_NROWS);
+    k_scan_pairs<<<1, 1024, 0, st>>>(D.blk, s->nblk_pos, D.ctr + CTR_NA, D.ctr + CTR_NVS2, D.ctr + CTR_NROWS);
     k_lists_scatter<<<nbp, CAFE_DENSE_THREADS, 0, st>>>(D);
     CUDA_TRY(cudaMemsetAsync(D.ctr + CTR_SLOW, 0, sizeof(int), st));
     CUDA_TRY(cudaMemsetAsync(D.ctr + CTR_NPAIRS, 0, sizeof(int), st));

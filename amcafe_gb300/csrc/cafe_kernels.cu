@@ -28,6 +28,11 @@
 #define CAFE_DENSE_THREADS 256
 #define CAFE_CELLS_PER_THREAD 8
 #define CAFE_CELLS_PER_BLOCK (CAFE_DENSE_THREADS * CAFE_CELLS_PER_THREAD)
+// The active-set compaction takes `chunks` (1..4) 8-cell chunks per thread:
+// more per thread on very large grids, where nearly every chunk is decided
+// from its state bytes and the number of blocks dominates; one per thread
+// otherwise, where the cell-by-cell tests inside the pool box set the pace.
+#define CAFE_ACT_MAX_CHUNKS 4
 #define CAFE_LOOP_THREADS 512
 #ifdef CAFE_DETAIL_CYCLES
 // clock read ordered with the surrounding memory operations and barriers
@@ -181,14 +186,56 @@ __device__ __forceinline__ bool cafe_is_active(const CafeDev &D, const CafeConst
   return false;
 }
 
-__global__ void k_active_count(CafeDev D, CafeConsts K, CafeStepParams P) {
-  __shared__ int wsum[CAFE_DENSE_THREADS / 32];
-  long long base = ((long long)blockIdx.x * blockDim.x + threadIdx.x) * CAFE_CELLS_PER_THREAD;
-  int cnt = 0;
+// Activity flags of the CAFE_CELLS_PER_THREAD (8) cells from `base` (bit c
+// for cell base + c). A cell that cannot be at or above the liquidus (outside
+// the pool box, or not below the laser plane) is active exactly when it is
+// liquid or mushy, so a chunk lying in one row outside the hot region is
+// decided from its state bytes, loaded as one 64-bit word; other chunks take
+// the cell-by-cell test.
+__device__ __forceinline__ uint32_t cafe_chunk_active(const CafeDev &D, const CafeConsts &K,
+                                                      const CafeStepParams &P, long long base) {
+  static_assert(CAFE_CELLS_PER_THREAD == 8, "one 64-bit word of states per thread");
+  uint32_t flags = 0;
+  if (base + 8 <= K.N) {
+    int i0, j0, k0, i1, j1, k1;
+    cafe_cell_xyz(K, base, i0, j0, k0);
+    cafe_cell_xyz(K, base + 7, i1, j1, k1);
+    bool cold = false;
+    // (with any_hot_full, T0 or tS reaches the liquidus and no class is cold)
+    if (!P.any_hot_full && j0 == j1 && k0 == k1)
+      cold = k0 >= P.kabove || k0 < P.lo[2] || k0 >= P.hi[2] || j0 < P.lo[1] || j0 >= P.hi[1] || i1 < P.lo[0] ||
+             i0 >= P.hi[0];
+    if (cold) {
+      unsigned long long w = *(const unsigned long long *)(D.state + base);
+      for (int c = 0; c < 8; ++c) {
+        unsigned int b = (unsigned int)(w >> (8 * c)) & 0xffu;
+        flags |= (b - 1u < 2u ? 1u : 0u) << c;
+      }
+      return flags;
+    }
+  }
   for (int c = 0; c < CAFE_CELLS_PER_THREAD; ++c) {
     long long idx = base + c;
-    if (idx < K.N && cafe_is_active(D, K, P, idx)) ++cnt;
+    if (idx < K.N && cafe_is_active(D, K, P, idx)) flags |= 1u << c;
   }
+  return flags;
+}
+
+// Activity flags of this thread's `chunks` chunks (bit 8 c + j for cell
+// base + 8 c + j).
+__device__ __forceinline__ uint32_t cafe_thread_active(const CafeDev &D, const CafeConsts &K,
+                                                       const CafeStepParams &P, long long base, int chunks) {
+  uint32_t f = 0;
+#pragma unroll
+  for (int c = 0; c < CAFE_ACT_MAX_CHUNKS; ++c)
+    if (c < chunks) f |= cafe_chunk_active(D, K, P, base + 8 * c) << (8 * c);
+  return f;
+}
+
+__global__ void k_active_count(CafeDev D, CafeConsts K, CafeStepParams P, int chunks) {
+  __shared__ int wsum[CAFE_DENSE_THREADS / 32];
+  long long base = ((long long)blockIdx.x * blockDim.x + threadIdx.x) * (CAFE_CELLS_PER_THREAD * chunks);
+  int cnt = __popc(cafe_thread_active(D, K, P, base, chunks));
   for (int o = 16; o > 0; o >>= 1) cnt += __shfl_down_sync(0xffffffffu, cnt, o);
   if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = cnt;
   __syncthreads();
@@ -205,6 +252,7 @@ __global__ void k_scan_blocks(int32_t *blk, long long n, int *total) {
   long long per = (n + blockDim.x - 1) / blockDim.x;
   long long b0 = threadIdx.x * per, b1 = b0 + per < n ? b0 + per : n;
   long long s = 0;
+#pragma unroll 8
   for (long long b = b0; b < b1; ++b) s += blk[b];
   part[threadIdx.x] = s;
   __syncthreads();
@@ -226,18 +274,11 @@ __global__ void k_scan_blocks(int32_t *blk, long long n, int *total) {
   }
 }
 
-__global__ void k_active_scatter(CafeDev D, CafeConsts K, CafeStepParams P) {
+__global__ void k_active_scatter(CafeDev D, CafeConsts K, CafeStepParams P, int chunks) {
   __shared__ int wsum[CAFE_DENSE_THREADS / 32];
-  long long base = ((long long)blockIdx.x * blockDim.x + threadIdx.x) * CAFE_CELLS_PER_THREAD;
-  uint32_t flags = 0;
-  int cnt = 0;
-  for (int c = 0; c < CAFE_CELLS_PER_THREAD; ++c) {
-    long long idx = base + c;
-    if (idx < K.N && cafe_is_active(D, K, P, idx)) {
-      flags |= 1u << c;
-      ++cnt;
-    }
-  }
+  long long base = ((long long)blockIdx.x * blockDim.x + threadIdx.x) * (CAFE_CELLS_PER_THREAD * chunks);
+  const uint32_t flags = cafe_thread_active(D, K, P, base, chunks);
+  const int cnt = __popc(flags);
   // block-exclusive scan of per-thread counts
   int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   int incl = cnt;
@@ -258,7 +299,7 @@ __global__ void k_active_scatter(CafeDev D, CafeConsts K, CafeStepParams P) {
   }
   __syncthreads();
   long long pos = (long long)D.blk[blockIdx.x] + wsum[w] + (incl - cnt);
-  for (int c = 0; c < CAFE_CELLS_PER_THREAD; ++c) {
+  for (int c = 0; c < CAFE_CELLS_PER_THREAD * chunks; ++c) {
     if (!(flags >> c & 1u)) continue;
     long long idx = base + c;
     if (pos < D.act_cap) {
@@ -352,11 +393,18 @@ __global__ void k_lists_count(CafeDev D) {
 }
 
 // Exclusive scan of interleaved pairs (blk[2b], blk[2b+1]), b < n, one block.
-__global__ void k_scan_pairs(int32_t *blk, long long n, int *tot0, int *tot1) {
+// Exclusive scan of the (mushy, frontier) count pairs of the position blocks
+// that hold active positions (na from *na_ptr); totals to *tot0, *tot1.
+__global__ void k_scan_pairs(int32_t *blk, long long n, const int *na_ptr, int *tot0, int *tot1) {
   __shared__ long long part[2][1024];
+  {
+    long long used = ((long long)*na_ptr + CAFE_CELLS_PER_BLOCK - 1) / CAFE_CELLS_PER_BLOCK;
+    if (used < n) n = used;
+  }
   long long per = (n + blockDim.x - 1) / blockDim.x;
   long long b0 = threadIdx.x * per, b1 = b0 + per < n ? b0 + per : n;
   long long s0 = 0, s1 = 0;
+#pragma unroll 8
   for (long long b = b0; b < b1; ++b) {
     s0 += blk[2 * b];
     s1 += blk[2 * b + 1];
