@@ -525,7 +525,7 @@ static const int kSeed0 = 2132512, kSeed1 = 2912351;
 struct State {
   Grid g;
   int N = 0, nx = 0, ny = 0, nz = 0, nxy = 0;
-  std::vector<int> gID, vState, buildj;
+  std::vector<int> gID, vState, buildj, build;
   std::vector<double> extents, cen, temp, cTheta;
   int nGrain = 0, Nzh = 0;
   std::default_random_engine genlayer;
@@ -1162,6 +1162,160 @@ static void dump_state(FILE *fp, int tag, const State &S) {
   std::fwrite(S.cTheta.data(), 8, 4 * (size_t)S.nGrain, fp);
 }
 
+// VoxelsCA::SetBuild(TempField::BuildjID) (VoxelsCA.C:76-115): every voxel
+// of a grain that has a melted voxel (BuildjID = 1) or a Build voxel becomes
+// Build = 1; Build is never reset. (The reference's lists of grain IDs, with
+// consecutive repeats removed, hold every grain that occurs, so membership is
+// a per-grain flag.)
+static void set_build(State &S) {
+  std::vector<char> g1(S.nGrain + 2, 0), g2(S.nGrain + 2, 0);
+  for (int j = 0; j < S.N; ++j)
+    if (S.buildj[j] == 1 && S.gID[j] > 0) g1[S.gID[j]] = 1;
+  for (int j = 0; j < S.N; ++j)
+    if (S.gID[j] > 0 && g1[S.gID[j]]) S.build[j] = 1;
+  for (int j = 0; j < S.N; ++j)
+    if (S.build[j] == 1 && S.gID[j] > 0) g2[S.gID[j]] = 1;
+  for (int j = 0; j < S.N; ++j)
+    if (S.gID[j] > 0 && g2[S.gID[j]]) S.build[j] = 1;
+}
+
+// ---------------------------------------------------------------- output
+// Inverse-pole-figure colouring of VoxelsCA::WriteToHDF1 (VoxelsCA.C:1592-
+// 1810) for one grain: RGB (as floats) of the sample z (build), x and y
+// directions in the crystal frame. The constants of the colour triangle come
+// from the same expressions as the reference's; `hx` carries the hue of the x
+// direction into the y direction, where the reference adds to it instead of
+// starting from the y direction's own hue, and the hue fraction is H/6 as the
+// reference writes it.
+struct IpfConsts {
+  double x0, y0, sMax, hoff;  // hoff = atan((triPts[1][2]-y0)/(triPts[0][2]-x0))*180/M_PI
+};
+static IpfConsts ipf_consts() {
+  double tp[2][3] = {{0.0, 2. / std::pow(2, .5) / (1. + 1. / std::pow(2, .5)),
+                      2. / std::pow(3, .5) / (1. + 1. / std::pow(3, .5))},
+                     {0.0, 0.0, 2. / std::pow(3, .5) / (1. + 1. / std::pow(3, .5))}};
+  double m = std::tan(1. / 2. * std::atan2(tp[1][2], tp[0][2]));
+  double a = std::pow(std::pow(tp[1][2] - tp[1][1], 2.) + std::pow(tp[0][2] - tp[0][1], 2.), .5);
+  double b = std::pow(std::pow(tp[0][1], 2.) + std::pow(tp[1][1], 2.), 0.5);
+  double c = std::pow(std::pow(tp[0][2], 2.) + std::pow(tp[1][2], 2.), 0.5);
+  IpfConsts K;
+  K.y0 = 1. / 2. * std::pow((b + c - a) * (c + a - b) * (a + b - c) / (a + b + c), .5);
+  K.x0 = K.y0 / m;
+  K.sMax = std::pow(std::pow(K.x0, 2.) + std::pow(K.y0, 2.), .5);
+  K.hoff = std::atan((tp[1][2] - K.y0) / (tp[0][2] - K.x0)) * 180 / M_PI;
+  return K;
+}
+static double m_atan(double x) {
+  if (g_libm.mode == 1) return crm_atan2(x, 1.0);
+  return perturb(std::atan(x));
+}
+// one direction: H enters as the hue to start from when !own_hue
+static void ipf_dir(const IpfConsts &K, const double R[3][3], const double v[3], bool own_hue, double &H,
+                    float rgb[3]) {
+  double vCD[3];
+  vCD[0] = std::fabs(R[0][0] * v[0] + R[1][0] * v[1] + R[2][0] * v[2]);
+  vCD[1] = std::fabs(R[0][1] * v[0] + R[1][1] * v[1] + R[2][1] * v[2]);
+  vCD[2] = std::fabs(R[0][2] * v[0] + R[1][2] * v[1] + R[2][2] * v[2]);
+  std::sort(vCD, vCD + 3);
+  std::swap(vCD[0], vCD[1]);
+  vCD[2] = smin(vCD[2], 1.0);
+  double xp = 2. * vCD[0] / (1. + vCD[2]);
+  double yp = 2. * vCD[1] / (1. + vCD[2]);
+  if (own_hue) {
+    H = m_atan((yp - K.y0) / (xp - K.x0)) * 180. / M_PI;
+    if (xp < K.x0) H += 180;
+  }
+  H = H + 240 - K.hoff;
+  double V = 1.;
+  double S = m_powh(m_pow2(xp - K.x0) + m_pow2(yp - K.y0));
+  S = S / K.sMax * 0.8 + 0.2;
+  if (H >= 360.0) H = 0.0;
+  int icase = (int)std::floor(H / 60.0);
+  double ff = H / 6.0 - icase;
+  double p = V * (1. - S), q = V * (1. - S * ff), t = V * (1. - (S * (1. - ff)));
+  rgb[0] = rgb[1] = rgb[2] = 0.0f;
+  if (S <= 0.0) return;
+  double r = 0, gg = 0, bb = 0;
+  bool set = true;
+  switch (icase) {
+    case 0: r = V; gg = t; bb = p; break;
+    case 1: r = q; gg = V; bb = p; break;
+    case 2: r = p; gg = V; bb = t; break;
+    case 3: r = p; gg = q; bb = V; break;
+    case 4: r = t; gg = p; bb = V; break;
+    case 5: r = V; gg = p; bb = q; break;
+    default: set = false;
+  }
+  if (set) {
+    rgb[0] = (float)r;
+    rgb[1] = (float)gg;
+    rgb[2] = (float)bb;
+  }
+}
+// rotation of WriteToHDF1 (VoxelsCA.C:1635-1644), with pow(a, 2.0)
+static void ipf_rot(const double *c, double R[3][3]) {
+  double omega = c[0], ax[3] = {c[1], c[2], c[3]};
+  R[0][0] = m_cos(omega) + m_pow2(ax[0]) * (1 - m_cos(omega));
+  R[0][1] = ax[0] * ax[1] * (1 - m_cos(omega)) - ax[2] * m_sin(omega);
+  R[0][2] = ax[0] * ax[2] * (1 - m_cos(omega)) + ax[1] * m_sin(omega);
+  R[1][0] = ax[0] * ax[1] * (1 - m_cos(omega)) + ax[2] * m_sin(omega);
+  R[1][1] = m_cos(omega) + m_pow2(ax[1]) * (1 - m_cos(omega));
+  R[1][2] = ax[1] * ax[2] * (1 - m_cos(omega)) - ax[0] * m_sin(omega);
+  R[2][0] = ax[2] * ax[0] * (1 - m_cos(omega)) - ax[1] * m_sin(omega);
+  R[2][1] = ax[2] * ax[1] * (1 - m_cos(omega)) + ax[0] * m_sin(omega);
+  R[2][2] = m_cos(omega) + m_pow2(ax[2]) * (1 - m_cos(omega));
+}
+// IPF colours of grains 1..ngrain (9 floats per grain: z, x, y directions).
+static void ipf_grains(const std::vector<double> &cTheta, int ngrain, std::vector<float> &out) {
+  IpfConsts K = ipf_consts();
+  out.assign(9 * (size_t)ngrain, 0.0f);
+  const double vz[3] = {0.0, 0.0, 1.0}, vx[3] = {1.0, 0.0, 0.0}, vy[3] = {0.0, 1.0, 0.0};
+  for (int g = 0; g < ngrain; ++g) {
+    double R[3][3], H = 0.0;
+    ipf_rot(&cTheta[4 * (size_t)g], R);
+    ipf_dir(K, R, vz, true, H, &out[9 * (size_t)g]);
+    ipf_dir(K, R, vx, true, H, &out[9 * (size_t)g + 3]);
+    ipf_dir(K, R, vy, false, H, &out[9 * (size_t)g + 6]);
+  }
+}
+
+static std::string g_out_dir;  // output directory (empty: no output)
+static long g_out_every = 1;
+
+static void write_bin(const std::string &path, const void *p, size_t bytes) {
+  FILE *fp = std::fopen(path.c_str(), "wb");
+  if (!fp) return;
+  std::fwrite(p, 1, bytes, fp);
+  std::fclose(fp);
+}
+// The datasets of WriteToHDF1 (VoxelsCA.C:1822-1854) as raw files
+// <dir>/<name>.h5.<dataset>.bin.
+static void write_output(const State &S, const std::string &name) {
+  const std::string b = g_out_dir + "/" + name + ".h5.";
+  std::vector<float> ipf;
+  ipf_grains(S.cTheta, S.nGrain, ipf);
+  std::vector<float> z(3 * (size_t)S.N, 0.0f), x(3 * (size_t)S.N, 0.0f), y(3 * (size_t)S.N, 0.0f), T(S.N);
+  for (int j = 0; j < S.N; ++j) {
+    T[j] = (float)S.temp[j];
+    int g = S.gID[j];
+    if (g < 1) continue;
+    for (int a = 0; a < 3; ++a) {
+      z[3 * (size_t)j + a] = ipf[9 * (size_t)(g - 1) + a];
+      x[3 * (size_t)j + a] = ipf[9 * (size_t)(g - 1) + 3 + a];
+      y[3 * (size_t)j + a] = ipf[9 * (size_t)(g - 1) + 6 + a];
+    }
+  }
+  std::vector<float> cth(S.cTheta.begin(), S.cTheta.begin() + 4 * (size_t)S.nGrain);
+  write_bin(b + "gID.bin", S.gID.data(), 4 * (size_t)S.N);
+  write_bin(b + "vState.bin", S.vState.data(), 4 * (size_t)S.N);
+  write_bin(b + "Build.bin", S.build.data(), 4 * (size_t)S.N);
+  write_bin(b + "Temperature.bin", T.data(), 4 * (size_t)S.N);
+  write_bin(b + "IPFz.bin", z.data(), 12 * (size_t)S.N);
+  write_bin(b + "IPFx.bin", x.data(), 12 * (size_t)S.N);
+  write_bin(b + "IPFy.bin", y.data(), 12 * (size_t)S.N);
+  write_bin(b + "angleAxis.bin", cth.data(), 4 * cth.size());
+}
+
 static int setup(State &S, const char *deck) {
   std::string err;
   if (!read_deck(deck, S.g, err)) {
@@ -1177,12 +1331,16 @@ static int setup(State &S, const char *deck) {
   S.gID.assign(S.N, 0);
   S.vState.assign(S.N, 0);
   S.buildj.assign(S.N, 0);
+  S.build.assign(S.N, 0);  // VoxelsCA::Build (VoxelsCA.C:43)
   S.extents.assign(S.N, 0.0);
   S.cen.assign(3 * (size_t)S.N, 0.0);
   S.temp.assign(S.N, 0.0);
   S.genlayer.seed(kSeed1);
   init_tempfield(S);
   init_baseplate(S);
+  // every baseplate cell with a grain starts as Build (VoxelsCA.C:156-159)
+  for (int k = 0; k < S.N; ++k)
+    if (S.gID[k] != 0) S.build[k] = 1;
   return 0;
 }
 
@@ -1196,6 +1354,15 @@ static double g_max_seconds = 0.0;
 extern "C" {
 
 void cafe_oracle_set_budget(double seconds) { g_max_seconds = seconds; }
+
+// Output of the following cafe_oracle_run calls: the datasets of
+// VoxelsCA::WriteToHDF1 as raw files <dir>/out<tInd>.h5.<name>.bin at every
+// `every`-th output point and <dir>/final.h5.<name>.bin after the closing
+// CleanLayer; dir NULL or empty turns output off.
+void cafe_oracle_set_output(const char *dir, long every) {
+  g_out_dir = dir ? dir : "";
+  g_out_every = every > 0 ? every : 1;
+}
 
 // Runs the whole main1.C time loop on deck `deck`. dump_stride: 0 = write only
 // the initial and final records, k > 0 = also every k-th step. max_steps > 0
@@ -1226,6 +1393,11 @@ int cafe_oracle_run(const char *deck, const char *dump_path, long max_steps, int
     update_laser(g);
     bcheck = g.indlayer > nlayerTot;
     if (g.inewlayerflg == 1) clean_layer(S);
+    // output point of main1.C:76-84: SetBuild, then WriteToHDF1
+    if (S.tf_tInd % g.outint == 0 || bcheck || (g.inewlayerflg == 1 && g.outNL == 0)) {
+      set_build(S);
+      if (!g_out_dir.empty() && (nstep + 1) % g_out_every == 0) write_output(S, "out" + std::to_string(S.tf_tInd));
+    }
     // UpdateTime2 (Grid.C:334-339)
     g.time += S.DelT;
     g.tInd += 1;
@@ -1242,6 +1414,7 @@ int cafe_oracle_run(const char *deck, const char *dump_path, long max_steps, int
   clock_gettime(CLOCK_MONOTONIC, &t1);
   if (bcheck) {
     clean_layer(S);
+    if (!g_out_dir.empty()) write_output(S, "final");  // main1.C:95-97
     dump_state(fp, 2, S);
   } else if (dump_stride <= 0 || nstep % dump_stride != 0) {
     dump_state(fp, 1, S);

@@ -80,6 +80,16 @@ def run(deck, dump_path="", max_steps=-1, dump_stride=1, libm=LIBM_GLIBC, pertur
     return dict(zip(keys, list(st)[:8]))
 
 
+def set_output(out_dir, every=1):
+    """Makes the following run() calls write the datasets of
+    VoxelsCA::WriteToHDF1 as raw files <out_dir>/out<tInd>.h5.<name>.bin at
+    every `every`-th output point and final.h5.<name>.bin after the closing
+    CleanLayer; out_dir None turns output off."""
+    lib = load()
+    lib.cafe_oracle_set_output.argtypes = [ctypes.c_char_p, ctypes.c_long]
+    lib.cafe_oracle_set_output(str(out_dir).encode() if out_dir else None, int(every))
+
+
 def set_budget(seconds):
     """Wall-clock limit (s) for the oracle's loops; 0 = none."""
     lib = load()

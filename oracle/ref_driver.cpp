@@ -5,8 +5,11 @@
 // the single-rank shims in ref_shims/) and runs the same time loop as
 // src/src-mpi/main1.C:18-101, writing the full CA state after every step so the
 // oracle restatement and the GPU path can be compared with the reference
-// itself. HDF5 output (WriteToHDF1) is skipped; SetBuild is still called where
-// main1.C calls it so that the Build field evolves as in the reference.
+// itself. SetBuild is called where main1.C calls it so that the Build field
+// evolves as in the reference. When CAFE_REF_DUMP_DIR is set, WriteToHDF1 also
+// runs at every CAFE_REF_OUT_EVERY-th output point (default 1) as
+// "out<tInd>" and after the closing CleanLayer as "final"; the ADIOS2 shim
+// then writes its datasets as raw files into that directory.
 //
 // Usage: cafe_ref_dump <deck.in> <out.bin> [max_steps]
 // Record layout (little-endian): see oracle/cafe_dump.py.
@@ -69,6 +72,9 @@ int main(int argc, char *argv[]) {
   ut.InitializeUT();
   VoxelsCA vox(g, TempF, part);
   vox.InitializeVoxels(bp);
+  const char *out_dir = std::getenv("CAFE_REF_DUMP_DIR");
+  long out_every = std::getenv("CAFE_REF_OUT_EVERY") ? std::atol(std::getenv("CAFE_REF_OUT_EVERY")) : 1;
+  if (out_every < 1) out_every = 1;
   FILE *fp = std::fopen(argv[2], "wb");
   if (!fp) return 3;
   int nlayerTot = int(ceil((double)(g.nX[2] - bp.Nzh) / (double)g.nZlayer));
@@ -91,6 +97,7 @@ int main(int argc, char *argv[]) {
     int indOut = TempF.tInd % g.outint;
     if (indOut == 0 || bcheck || (g.inewlayerflg == 1 && g.outNL == 0)) {
       vox.SetBuild(TempF.BuildjID, Ntot);
+      if (out_dir && (nstep + 1) % out_every == 0) vox.WriteToHDF1("out" + std::to_string(TempF.tInd));
     }
     g.UpdateTime2(TempF.DelT);
     if (g.inewlayerflg == 1) vox.AddLayer1();
@@ -100,6 +107,7 @@ int main(int argc, char *argv[]) {
   }
   if (bcheck) {
     vox.CleanLayer();
+    if (out_dir) vox.WriteToHDF1("final");
     dump_state(fp, 2, g, TempF, vox, Ntot);  // final state after the closing CleanLayer (tag 2)
   }
   std::fclose(fp);

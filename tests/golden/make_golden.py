@@ -62,5 +62,31 @@ def main():
         print(name, len(recs), "records")
 
 
+# Output of VoxelsCA::WriteToHDF1 (through the ADIOS2 shim's raw files) on
+# three decks: deck, every k-th output point (outint is 1 in these decks).
+OUTPUT_DECKS = [("track_r0", 10), ("track_nuc", 10), ("layers_rot", 40)]
+
+
+def output_digests():
+    """SHA-256 of every dataset file the reference writes (dims and VoxelDX
+    aside) -> tests/golden/output_digests.npz, keys '<deck>/<file>'."""
+    out = {}
+    for name, every in OUTPUT_DECKS:
+        deck = os.path.join(HERE, "decks", name + ".in")
+        with tempfile.TemporaryDirectory() as td:
+            env = dict(os.environ, CAFE_REF_DUMP_DIR=td, CAFE_REF_OUT_EVERY=str(every))
+            subprocess.run([REF, deck, os.path.join(td, "ref.bin")], check=True, env=env,
+                           stdout=subprocess.DEVNULL)
+            for f in sorted(os.listdir(td)):
+                if not f.endswith(".bin") or f == "ref.bin" or ".dims." in f or ".VoxelDX." in f:
+                    continue
+                with open(os.path.join(td, f), "rb") as fh:
+                    out[name + "/" + f] = np.array(hashlib.sha256(fh.read()).hexdigest())
+        out[name + "/every"] = np.array(every)
+    np.savez_compressed(os.path.join(HERE, "output_digests.npz"), **out)
+    print("output digests:", len(out))
+
+
 if __name__ == "__main__":
     main()
+    output_digests()

@@ -66,3 +66,27 @@ def test_oracle_glibc_reproduces_reference(name, tmp_path):
 @pytest.mark.parametrize("name", DECKS)
 def test_oracle_correctly_rounded_libm_keeps_reference_integers(name, tmp_path):
     _check(name, orc.LIBM_CR, tmp_path, check_floats=False)
+
+
+@pytest.mark.parametrize("libm", [orc.LIBM_GLIBC, orc.LIBM_CR])
+def test_oracle_output_matches_reference(libm, tmp_path):
+    """SetBuild and the datasets of WriteToHDF1 (gID, vState, Build, float
+    Temperature, the three IPF colour maps, angle-axis table) at the output
+    points, byte for byte against the reference's own files."""
+    d = np.load(os.path.join(HERE, "golden", "output_digests.npz"))
+    decks = sorted({k.split("/")[0] for k in d.files})
+    assert decks
+    for name in decks:
+        out = tmp_path / name
+        out.mkdir()
+        orc.set_output(str(out), int(d[name + "/every"]))
+        try:
+            orc.run(os.path.join(HERE, "golden", "decks", name + ".in"), "", libm=libm)
+        finally:
+            orc.set_output(None)
+        keys = [k for k in d.files if k.startswith(name + "/") and not k.endswith("/every")]
+        assert keys
+        for k in keys:
+            path = out / k.split("/", 1)[1]
+            assert path.exists(), k
+            assert hashlib.sha256(path.read_bytes()).hexdigest() == str(d[k]), k
