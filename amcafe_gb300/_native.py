@@ -19,6 +19,7 @@ EXPORTS = (
     "cafe_sim_download_state", "cafe_sim_download_temperature", "cafe_sim_download_ctheta",
     "cafe_sim_upload_state", "cafe_last_error", "cafe_sim_set_timing", "cafe_sim_phase_times",
     "cafe_sim_stream", "cafe_sim_mark", "cafe_sim_elapsed", "cafe_clean_layer_noalloc",
+    "cafe_sim_set_build", "cafe_sim_download_build", "cafe_sim_download_output", "cafe_sim_write_output",
 )
 PHASES = ("melt", "classify", "gather", "events", "writeback", "layer")
 NPHASE = 8
@@ -35,7 +36,8 @@ class CafeInfo(ctypes.Structure):
                 ("isp", ctypes.c_int), ("indlayer", ctypes.c_int), ("inewlayerflg", ctypes.c_int),
                 ("inewscanflg", ctypes.c_int), ("ilaserLoc", ctypes.c_int), ("nGrain", ctypes.c_int),
                 ("nlayerTot", ctypes.c_int), ("Nzh", ctypes.c_int), ("done", ctypes.c_int),
-                ("steps", ctypes.c_longlong), ("gth", ctypes.c_double), ("genlayer_state", ctypes.c_uint)]
+                ("steps", ctypes.c_longlong), ("gth", ctypes.c_double), ("genlayer_state", ctypes.c_uint),
+                ("tf_tInd", ctypes.c_int), ("output_due", ctypes.c_int)]
 
 
 class CafeStats(ctypes.Structure):
@@ -62,6 +64,7 @@ def load():
     P, I, LL, D = ctypes.c_void_p, ctypes.c_int, ctypes.c_longlong, ctypes.c_double
     i32p = ctypes.POINTER(ctypes.c_int32)
     f64p = ctypes.POINTER(ctypes.c_double)
+    f32p = ctypes.POINTER(ctypes.c_float)
     sig = {
         "cafe_sim_create": (I, [ctypes.c_char_p, ctypes.POINTER(CafeOptions), ctypes.POINTER(P)]),
         "cafe_sim_destroy": (None, [P]),
@@ -89,6 +92,10 @@ def load():
         "cafe_sim_mark": (I, [P, I]),
         "cafe_sim_elapsed": (I, [P, I, I, ctypes.POINTER(D)]),
         "cafe_clean_layer_noalloc": (I, [P, LL, P, I, ctypes.POINTER(I), P]),
+        "cafe_sim_set_build": (I, [P]),
+        "cafe_sim_download_build": (I, [P, i32p]),
+        "cafe_sim_download_output": (I, [P, f32p, f32p, f32p, f32p]),
+        "cafe_sim_write_output": (I, [P, ctypes.c_char_p]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

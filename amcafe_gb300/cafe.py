@@ -16,9 +16,12 @@ with the reference's names (InitializeVoxels, AddLayer1, UpdateLaser,
 AnalyticTempCurr, UpdateVoxels, CleanLayer, UpdateTime2) and as `step()` /
 `run()` for the loop body and the whole loop. The public fields (gID, vState,
 extents, centroidOct, TempCurr, BuildjID, cTheta, nGrain) are read with
-`state()`, `temperature()` and `ctheta()`.
+`state()`, `temperature()` and `ctheta()`. At the output points of the loop
+(`info()["output_due"]`) `step()` has called SetBuild; `build()`, `output()`
+and `WriteToHDF1(prefix)` give Build and the datasets the reference writes.
 """
 import ctypes
+import os
 
 import numpy as np
 
@@ -122,6 +125,31 @@ class Simulation:
         out = np.empty(4 * max(ng.value, 1), np.float64)
         check(self._lib.cafe_sim_download_ctheta(self._h, _ptr(out, ctypes.c_double), out.size, ctypes.byref(ng)))
         return out[:4 * ng.value]
+
+    # -- output (VoxelsCA::SetBuild / WriteToHDF1) ---------------------------
+    def SetBuild(self):
+        check(self._lib.cafe_sim_set_build(self._h))
+
+    def build(self):
+        """VoxelsCA::Build as an int32 array."""
+        b = np.empty(self.ncell, np.int32)
+        check(self._lib.cafe_sim_download_build(self._h, _ptr(b, ctypes.c_int32)))
+        return b
+
+    def output(self):
+        """The derived datasets of WriteToHDF1: Temperature (float32, one per
+        cell) and IPFz, IPFx, IPFy (float32 RGB, 3 per cell)."""
+        n = self.ncell
+        t = np.empty(n, np.float32)
+        z, x, y = (np.empty(3 * n, np.float32) for _ in range(3))
+        f = ctypes.c_float
+        check(self._lib.cafe_sim_download_output(self._h, _ptr(t, f), _ptr(z, f), _ptr(x, f), _ptr(y, f)))
+        return dict(Temperature=t, IPFz=z, IPFx=x, IPFy=y)
+
+    def WriteToHDF1(self, prefix):
+        """Writes the datasets of VoxelsCA::WriteToHDF1 as raw files
+        <prefix>.<dataset>.bin (prefix such as "out/run120.h5")."""
+        check(self._lib.cafe_sim_write_output(self._h, os.fsencode(prefix)))
 
     def upload_state(self, gID, vState, extents, centroid, ctheta):
         gID = np.ascontiguousarray(gID, np.int32)

@@ -42,6 +42,13 @@ struct CafeStepParams {
   int any_hot_full;   // 1: evaluate T exactly everywhere below the plane
 };
 
+// Constants of the inverse-pole-figure colour triangle of
+// VoxelsCA::WriteToHDF1 (VoxelsCA.C:1597-1613), computed on the host.
+struct CafeIpfConsts {
+  double x0, y0, sMax;
+  double hoff;  // atan((triPts[1][2]-y0)/(triPts[0][2]-x0))*180/M_PI
+};
+
 // Scalars fixed for a run.
 struct CafeConsts {
   int nx, ny, nz, nxy;
@@ -74,6 +81,8 @@ struct CafeDev {
   // temperature class of every cell of the pool box, written by k_melt
   uint8_t *tcls;
   long long tcls_cap;
+  // VoxelsCA::Build (0/1 per cell)
+  uint8_t *build;
   // liquid cells left by the previous step (cell indices)
   int32_t *liq;
   // grains

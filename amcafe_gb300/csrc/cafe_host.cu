@@ -387,6 +387,11 @@ struct cafe_sim {
   int act_chunks = 1;       // 8-cell chunks per thread of the compaction
   long long nblk_pos = 0;   // position compaction blocks
   int nsm = 1;
+  // output (SetBuild / WriteToHDF1)
+  bool output_due = false;
+  uint8_t *gflag = nullptr;   // per-grain flags of SetBuild
+  long long gflag_cap = 0;
+  unsigned char *h_out = nullptr;  // pinned bounce buffer of the file writer
 };
 
 namespace {
@@ -732,7 +737,7 @@ int cafe_sim_create(const char *deck_path, const cafe_options *opt, cafe_sim **o
   auto &o = s->owned;
   if ((rc = dalloc(&D.state, N, o)) || (rc = dalloc(&D.gid, N, o)) || (rc = dalloc(&D.ext, N, o)) ||
       (rc = dalloc(&D.cx, N, o)) || (rc = dalloc(&D.cy, N, o)) || (rc = dalloc(&D.cz, N, o)) ||
-      (rc = dalloc(&D.buildj, N, o)) || (rc = dalloc(&D.pos_of, N, o)) || (rc = dalloc(&D.liq, acap, o)) ||
+      (rc = dalloc(&D.buildj, N, o)) || (rc = dalloc(&D.build, N, o)) || (rc = dalloc(&D.pos_of, N, o)) || (rc = dalloc(&D.liq, acap, o)) ||
       (rc = dalloc(&D.cth, 4 * (size_t)D.grain_cap, o)) || (rc = dalloc(&D.rot, 9 * (size_t)D.grain_cap, o)) ||
       (rc = dalloc(&D.act, acap, o)) || (rc = dalloc(&D.a_state, acap, o)) || (rc = dalloc(&D.a_cls, acap, o)) ||
       (rc = dalloc(&D.a_nn, acap, o)) || (rc = dalloc(&D.a_cold, acap, o)) || (rc = dalloc(&D.a_gid, acap, o)) ||
@@ -766,6 +771,7 @@ int cafe_sim_create(const char *deck_path, const cafe_options *opt, cafe_sim **o
   cudaMemsetAsync(D.cy, 0, N * sizeof(double), s->stream);
   cudaMemsetAsync(D.cz, 0, N * sizeof(double), s->stream);
   cudaMemsetAsync(D.buildj, 0, N, s->stream);
+  cudaMemsetAsync(D.build, 0, N, s->stream);
   cudaMemsetAsync(D.pos_of, 0xff, N * sizeof(int32_t), s->stream);
   cudaMemsetAsync(D.ctr, 0, CTR_COUNT * sizeof(int), s->stream);
   cudaMemsetAsync(D.err, 0, sizeof(int), s->stream);
@@ -789,6 +795,7 @@ void cafe_sim_destroy(cafe_sim *s) {
     if (e) cudaEventDestroy(e);
   for (void *p : s->owned) cudaFree(p);
   if (s->h_pinned) cudaFreeHost(s->h_pinned);
+  if (s->h_out) cudaFreeHost(s->h_out);
   if (s->stream) cudaStreamDestroy(s->stream);
   delete s;
 }
@@ -824,6 +831,9 @@ int cafe_sim_initialize_voxels(cafe_sim *s) {
   if ((rc = upload_site_grid(s, xs, G, dv, tmp))) return rc;
   long long nbp = (long long)s->Nzh * K.nxy;
   if (nbp > 0) k_baseplate<<<grid_blocks(nbp, 256, s), 256, 0, s->stream>>>(s->D, K, dv, s->Nzh);
+  CUDA_TRY(cudaGetLastError());
+  // VoxelsCA::Build of the baseplate cells (VoxelsCA.C:156-159)
+  k_build_init<<<grid_blocks(K.N, 256, s), 256, 0, s->stream>>>(s->D, K);
   CUDA_TRY(cudaGetLastError());
   // orientations (BasePlate.C:83-96)
   std::default_random_engine g1(531231);
@@ -1100,6 +1110,10 @@ int cafe_sim_step(cafe_sim *s, int *done) {
   grid_update_laser(s->g);
   bool bcheck = s->g.indlayer > s->nlayerTot;
   if (s->g.inewlayerflg == 1 && (rc = cafe_sim_clean_layer(s))) return rc;
+  // output point (main1.C:77-84): SetBuild; WriteToHDF1 is the caller's
+  const GridH &g = s->g;
+  s->output_due = (g.outint > 0 && s->tf_tInd % g.outint == 0) || bcheck || (g.inewlayerflg == 1 && g.outNL == 0);
+  if (s->output_due && (rc = cafe_sim_set_build(s))) return rc;
   cafe_sim_update_time(s);
   if (s->g.inewlayerflg == 1 && (rc = cafe_sim_add_layer(s))) return rc;
   s->steps++;
@@ -1154,6 +1168,8 @@ int cafe_sim_info(cafe_sim *s, cafe_info *info) {
     os << s->genlayer;
     info->genlayer_state = (unsigned int)std::stoul(os.str());
   }
+  info->tf_tInd = s->tf_tInd;
+  info->output_due = s->output_due ? 1 : 0;
   return CAFE_OK;
 }
 
@@ -1369,6 +1385,256 @@ int cafe_sim_upload_state(cafe_sim *s, const int32_t *gID, const int32_t *vState
   s->have_prev_box = false;
   s->initialized = true;
   return sim_sync(s);
+}
+
+// ------------------------------------------------------------------ output
+int cafe_sim_set_build(cafe_sim *s) {
+  if (!s || !s->initialized) return fail(CAFE_E_STATE, "set_build before initialize_voxels");
+  CUDA_TRY(cudaSetDevice(s->device));
+  int rc = read_ctr(s, CTR_NGRAIN, &s->nGrain);
+  if (rc) return rc;
+  long long need = (long long)s->nGrain + 2;
+  if (need > s->gflag_cap) {
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    for (auto &p : s->owned)
+      if (p == (void *)s->gflag) {
+        cudaFree(p);
+        p = nullptr;
+      }
+    long long cap = std::max<long long>(need, 2 * s->gflag_cap + 4096);
+    s->gflag = nullptr;
+    s->gflag_cap = 0;
+    if ((rc = dalloc(&s->gflag, cap, s->owned))) return rc;
+    s->gflag_cap = cap;
+  }
+  CUDA_TRY(cudaMemsetAsync(s->gflag, 0, need, s->stream));
+  k_build_flag<<<grid_blocks(s->K.N, 256, s), 256, 0, s->stream>>>(s->D, s->K, s->gflag);
+  k_build_mark<<<grid_blocks(s->K.N, 256, s), 256, 0, s->stream>>>(s->D, s->K, s->gflag);
+  LAUNCHED(CAFE_PH_LAYER, 2);
+  CUDA_TRY(cudaGetLastError());
+  return CAFE_OK;
+}
+
+int cafe_sim_download_build(cafe_sim *s, int32_t *build) {
+  if (!s || !build) return fail(CAFE_E_ARG, "null argument");
+  CUDA_TRY(cudaSetDevice(s->device));
+  int rc = sim_sync(s);
+  if (rc) return rc;
+  if ((rc = ensure_xfer(s))) return rc;
+  const long long N = s->K.N, ci = CAFE_XFER_BYTES / (long long)sizeof(int32_t);
+  for (long long off = 0; off < N; off += ci) {
+    long long n = std::min(ci, N - off);
+    k_u8_to_i32<<<grid_blocks(n, 256, s), 256, 0, s->stream>>>(s->D.build + off, (int32_t *)s->xfer, n);
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaMemcpyAsync(build + off, s->xfer, n * sizeof(int32_t), cudaMemcpyDeviceToHost, s->stream));
+  }
+  CUDA_TRY(cudaStreamSynchronize(s->stream));
+  return CAFE_OK;
+}
+
+namespace {
+
+// Constants of the colour triangle of WriteToHDF1 (VoxelsCA.C:1597-1613),
+// evaluated by the host's libm as the reference evaluates them.
+CafeIpfConsts ipf_consts() {
+  double tp[2][3] = {{0.0, 2. / std::pow(2, .5) / (1. + 1. / std::pow(2, .5)),
+                      2. / std::pow(3, .5) / (1. + 1. / std::pow(3, .5))},
+                     {0.0, 0.0, 2. / std::pow(3, .5) / (1. + 1. / std::pow(3, .5))}};
+  double m = std::tan(1. / 2. * std::atan2(tp[1][2], tp[0][2]));
+  double a = std::pow(std::pow(tp[1][2] - tp[1][1], 2.) + std::pow(tp[0][2] - tp[0][1], 2.), .5);
+  double b = std::pow(std::pow(tp[0][1], 2.) + std::pow(tp[1][1], 2.), 0.5);
+  double c = std::pow(std::pow(tp[0][2], 2.) + std::pow(tp[1][2], 2.), 0.5);
+  CafeIpfConsts C;
+  C.y0 = 1. / 2. * std::pow((b + c - a) * (c + a - b) * (a + b - c) / (a + b + c), .5);
+  C.x0 = C.y0 / m;
+  C.sMax = std::pow(std::pow(C.x0, 2.) + std::pow(C.y0, 2.), .5);
+  C.hoff = std::atan((tp[1][2] - C.y0) / (tp[0][2] - C.x0)) * 180 / M_PI;
+  return C;
+}
+
+// The per-cell output datasets, produced chunk by chunk into the staging
+// buffer: 0 Temperature, 1 IPFz, 2 IPFx, 3 IPFy, 4 Build (int32).
+struct OutputSource {
+  cafe_sim *s;
+  float *gcol = nullptr;  // IPF colours per grain (9 floats)
+  int ngrain = 0;
+  ~OutputSource() {
+    if (gcol) cudaFree(gcol);
+  }
+  int prepare(bool need_ipf) {
+    int rc = ensure_xfer(s);
+    if (rc) return rc;
+    if ((rc = read_ctr(s, CTR_NGRAIN, &s->nGrain))) return rc;
+    ngrain = s->nGrain;
+    if (need_ipf && ngrain > 0) {
+      CUDA_TRY(cudaMalloc((void **)&gcol, 9LL * ngrain * sizeof(float)));
+      k_ipf_grains<<<grid_blocks(ngrain, 128, s), 128, 0, s->stream>>>(s->D.cth, ngrain, ipf_consts(), gcol);
+      CUDA_TRY(cudaGetLastError());
+    }
+    return CAFE_OK;
+  }
+  static int cell_bytes(int which) { return (which >= 1 && which <= 3) ? 12 : 4; }
+  long long chunk(int which) const { return CAFE_XFER_BYTES / cell_bytes(which); }
+  // queues the production of cells [off, off+n) of dataset `which` into xfer
+  int produce(int which, long long off, long long n) {
+    cudaStream_t st = s->stream;
+    int nb = grid_blocks(n, 256, s);
+    if (which == 0) {
+      if (s->have_P)
+        k_temperature_f<<<nb, 256, 0, st>>>(s->K, s->P, off, n, (float *)s->xfer);
+      else
+        CUDA_TRY(cudaMemsetAsync(s->xfer, 0, n * sizeof(float), st));
+    } else if (which <= 3) {
+      if (gcol)
+        k_ipf_cells<<<nb, 256, 0, st>>>(s->D, gcol, which - 1, off, n, (float *)s->xfer);
+      else
+        CUDA_TRY(cudaMemsetAsync(s->xfer, 0, 12 * n, st));
+    } else {
+      k_build_i32<<<nb, 256, 0, st>>>(s->D, off, n, (int32_t *)s->xfer);
+    }
+    CUDA_TRY(cudaGetLastError());
+    return CAFE_OK;
+  }
+};
+
+int write_file(const std::string &path, const void *p, size_t bytes) {
+  FILE *fp = std::fopen(path.c_str(), "wb");
+  if (!fp) return fail(CAFE_E_IO, "cannot open '%s' for writing", path.c_str());
+  size_t w = bytes ? std::fwrite(p, 1, bytes, fp) : 0;
+  int cl = std::fclose(fp);
+  if (w != bytes || cl != 0) return fail(CAFE_E_IO, "write to '%s' failed", path.c_str());
+  return CAFE_OK;
+}
+
+// Streams `bytes` of device memory into an open file through the pinned
+// bounce buffer.
+int stream_to_file(cafe_sim *s, FILE *fp, const std::string &path, long long bytes, const void *dsrc) {
+  for (long long off = 0; off < bytes; off += CAFE_XFER_BYTES) {
+    long long n = std::min<long long>(CAFE_XFER_BYTES, bytes - off);
+    CUDA_TRY(cudaMemcpyAsync(s->h_out, (const unsigned char *)dsrc + off, n, cudaMemcpyDeviceToHost, s->stream));
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    if (std::fwrite(s->h_out, 1, n, fp) != (size_t)n) return fail(CAFE_E_IO, "write to '%s' failed", path.c_str());
+  }
+  return CAFE_OK;
+}
+
+// <prefix>.xdmf: an XDMF description of the raw files, so that viewers read
+// them as cell data on the uniform voxel grid (cell j = i + nx*(j + ny*k)).
+int write_xdmf(cafe_sim *s, const char *prefix) {
+  const GridH &g = s->g;
+  std::string pre(prefix), leaf = pre.substr(pre.find_last_of('/') + 1);
+  std::ostringstream x;
+  x.precision(17);
+  const int nx = g.nX[0], ny = g.nX[1], nz = g.nX[2];
+  x << "<?xml version=\"1.0\" ?>\n<Xdmf Version=\"3.0\">\n <Domain>\n  <Grid Name=\"CA\" GridType=\"Uniform\">\n";
+  x << "   <Topology TopologyType=\"3DCoRectMesh\" Dimensions=\"" << nz + 1 << " " << ny + 1 << " " << nx + 1
+    << "\"/>\n";
+  x << "   <Geometry GeometryType=\"ORIGIN_DXDYDZ\">\n";
+  x << "    <DataItem Dimensions=\"3\" Format=\"XML\">0 0 0</DataItem>\n";
+  x << "    <DataItem Dimensions=\"3\" Format=\"XML\">" << g.dX[2] << " " << g.dX[1] << " " << g.dX[0]
+    << "</DataItem>\n   </Geometry>\n";
+  struct Item {
+    const char *name, *type;
+    int comps;
+  } items[7] = {{"gID", "Int", 1},           {"vState", "Int", 1}, {"Build", "Int", 1}, {"Temperature", "Float", 1},
+                {"IPFz", "Float", 3},        {"IPFx", "Float", 3}, {"IPFy", "Float", 3}};
+  for (const Item &it : items) {
+    x << "   <Attribute Name=\"" << it.name << "\" AttributeType=\"" << (it.comps == 3 ? "Vector" : "Scalar")
+      << "\" Center=\"Cell\">\n    <DataItem Dimensions=\"" << nz << " " << ny << " " << nx;
+    if (it.comps == 3) x << " 3";
+    x << "\" NumberType=\"" << it.type << "\" Precision=\"4\" Format=\"Binary\" Endian=\"Native\">" << leaf << "."
+      << it.name << ".bin</DataItem>\n   </Attribute>\n";
+  }
+  x << "  </Grid>\n </Domain>\n</Xdmf>\n";
+  const std::string body = x.str();
+  return write_file(pre + ".xdmf", body.data(), body.size());
+}
+
+}  // namespace
+
+int cafe_sim_download_output(cafe_sim *s, float *temperature, float *ipfz, float *ipfx, float *ipfy) {
+  if (!s) return fail(CAFE_E_ARG, "null handle");
+  CUDA_TRY(cudaSetDevice(s->device));
+  int rc = sim_sync(s);
+  if (rc) return rc;
+  OutputSource src{s};
+  if ((rc = src.prepare(ipfz || ipfx || ipfy))) return rc;
+  float *dst[4] = {temperature, ipfz, ipfx, ipfy};
+  const long long N = s->K.N;
+  for (int w = 0; w < 4; ++w) {
+    if (!dst[w]) continue;
+    const int per = OutputSource::cell_bytes(w) / 4;
+    const long long c = src.chunk(w);
+    for (long long off = 0; off < N; off += c) {
+      long long n = std::min(c, N - off);
+      if ((rc = src.produce(w, off, n))) return rc;
+      CUDA_TRY(cudaMemcpyAsync(dst[w] + per * off, s->xfer, n * OutputSource::cell_bytes(w), cudaMemcpyDeviceToHost,
+                               s->stream));
+    }
+  }
+  CUDA_TRY(cudaStreamSynchronize(s->stream));
+  return CAFE_OK;
+}
+
+int cafe_sim_write_output(cafe_sim *s, const char *prefix) {
+  if (!s || !prefix) return fail(CAFE_E_ARG, "null argument");
+  if (!s->initialized) return fail(CAFE_E_STATE, "write_output before initialize_voxels");
+  CUDA_TRY(cudaSetDevice(s->device));
+  int rc = sim_sync(s);
+  if (rc) return rc;
+  if (!s->h_out && cudaMallocHost((void **)&s->h_out, CAFE_XFER_BYTES) != cudaSuccess) {
+    s->h_out = nullptr;
+    return fail(CAFE_E_CUDA, "cudaMallocHost of the output buffer failed");
+  }
+  OutputSource src{s};
+  if ((rc = src.prepare(true))) return rc;
+  const std::string base = std::string(prefix) + ".";
+  const long long N = s->K.N;
+  const GridH &g = s->g;
+  int32_t dims[3] = {g.nX[0], g.nX[1], g.nX[2]};
+  float vdx[3] = {(float)g.dX[0], (float)g.dX[1], (float)g.dX[2]};
+  if ((rc = write_file(base + "dims.bin", dims, sizeof dims)) || (rc = write_file(base + "VoxelDX.bin", vdx, sizeof vdx)))
+    return rc;
+  // datasets in the reference's order
+  const char *names[8] = {"gID", "vState", "Build", "Temperature", "IPFz", "IPFx", "IPFy", "angleAxis"};
+  for (int d = 0; d < 8; ++d) {
+    const std::string path = base + names[d] + ".bin";
+    FILE *fp = std::fopen(path.c_str(), "wb");
+    if (!fp) return fail(CAFE_E_IO, "cannot open '%s' for writing", path.c_str());
+    rc = CAFE_OK;
+    if (d == 0) {
+      rc = stream_to_file(s, fp, path, N * (long long)sizeof(int32_t), s->D.gid);
+    } else if (d == 1) {
+      const long long ci = CAFE_XFER_BYTES / (long long)sizeof(int32_t);
+      for (long long off = 0; off < N && !rc; off += ci) {
+        long long n = std::min(ci, N - off);
+        k_u8_to_i32<<<grid_blocks(n, 256, s), 256, 0, s->stream>>>(s->D.state + off, (int32_t *)s->xfer, n);
+        if (cudaGetLastError() != cudaSuccess) rc = fail(CAFE_E_CUDA, "vState conversion failed");
+        if (!rc) rc = stream_to_file(s, fp, path, n * (long long)sizeof(int32_t), s->xfer);
+      }
+    } else if (d == 7) {
+      // cTheta as float (VoxelsCA.C:1811)
+      std::vector<double> cth(4 * (size_t)src.ngrain);
+      std::vector<float> f(cth.size());
+      if (!cth.empty() &&
+          cudaMemcpy(cth.data(), s->D.cth, cth.size() * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess)
+        rc = fail(CAFE_E_CUDA, "cTheta download failed");
+      for (size_t j = 0; j < cth.size(); ++j) f[j] = (float)cth[j];
+      if (!rc && !f.empty() && std::fwrite(f.data(), sizeof(float), f.size(), fp) != f.size())
+        rc = fail(CAFE_E_IO, "write to '%s' failed", path.c_str());
+    } else {
+      int which = d == 2 ? 4 : d - 3;  // Build, Temperature, IPFz, IPFx, IPFy
+      const long long c = src.chunk(which);
+      for (long long off = 0; off < N && !rc; off += c) {
+        long long n = std::min(c, N - off);
+        rc = src.produce(which, off, n);
+        if (!rc) rc = stream_to_file(s, fp, path, n * OutputSource::cell_bytes(which), s->xfer);
+      }
+    }
+    if (std::fclose(fp) != 0 && !rc) rc = fail(CAFE_E_IO, "write to '%s' failed", path.c_str());
+    if (rc) return rc;
+  }
+  return write_xdmf(s, prefix);
 }
 
 }  // extern "C"

@@ -1980,3 +1980,130 @@ __global__ void k_deinterleave3(const double *src, double *x, double *y, double 
     z[i] = src[3 * i + 2];
   }
 }
+
+// ------------------------------------------------------------------ output
+// VoxelsCA::Build. InitializeVoxels marks the baseplate cells that carry a
+// grain (VoxelsCA.C:156-159); SetBuild (VoxelsCA.C:76-115) marks every cell of
+// every grain that has a melted cell (BuildjID = 1) or a Build cell. The
+// reference does this in two passes; the grains of its second pass are those
+// of the first plus those of the Build cells, so one flag pass over both
+// conditions and one marking pass give the same field.
+__global__ void k_build_init(CafeDev D, CafeConsts K) {
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < K.N;
+       idx += (long long)gridDim.x * blockDim.x)
+    D.build[idx] = D.gid[idx] != 0;
+}
+__global__ void k_build_flag(CafeDev D, CafeConsts K, uint8_t *gflag) {
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < K.N;
+       idx += (long long)gridDim.x * blockDim.x) {
+    int g = D.gid[idx];
+    if (g > 0 && (D.buildj[idx] == 1 || D.build[idx] == 1)) gflag[g] = 1;
+  }
+}
+__global__ void k_build_mark(CafeDev D, CafeConsts K, const uint8_t *gflag) {
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < K.N;
+       idx += (long long)gridDim.x * blockDim.x) {
+    int g = D.gid[idx];
+    if (g > 0 && gflag[g]) D.build[idx] = 1;
+  }
+}
+
+// One direction of the IPF colouring (VoxelsCA.C:1645-1702 for z, 1703-1760
+// for x, 1761-1810 for y) for rotation R. With own_hue false the hue starts
+// from H as given (the reference's y direction adds to the x direction's hue),
+// and the hue fraction is H/6 as the reference writes it.
+__device__ void cafe_ipf_dir(const CafeIpfConsts &C, const double R[3][3], int dir, bool own_hue, double &H,
+                             float *rgb) {
+  const double v[3] = {dir == 1 ? 1.0 : 0.0, dir == 2 ? 1.0 : 0.0, dir == 0 ? 1.0 : 0.0};
+  double a = fabs(R[0][0] * v[0] + R[1][0] * v[1] + R[2][0] * v[2]);
+  double b = fabs(R[0][1] * v[0] + R[1][1] * v[1] + R[2][1] * v[2]);
+  double c = fabs(R[0][2] * v[0] + R[1][2] * v[1] + R[2][2] * v[2]);
+  // std::sort of three (libstdc++'s insertion sort, order of comparisons
+  // kept), then the swap of the first two
+  if (b < a) { double t = a; a = b; b = t; }
+  if (c < a) { double t = c; c = b; b = a; a = t; }
+  else if (c < b) { double t = c; c = b; b = t; }
+  double v0 = b, v1 = a, v2 = (1.0 < c) ? 1.0 : c;
+  double xp = 2. * v0 / (1. + v2);
+  double yp = 2. * v1 / (1. + v2);
+  if (own_hue) {
+    H = crm_atan2((yp - C.y0) / (xp - C.x0), 1.0) * 180. / 3.14159265358979323846;
+    if (xp < C.x0) H += 180;
+  }
+  H = H + 240 - C.hoff;
+  const double V = 1.;
+  double S = crm_pow_half((xp - C.x0) * (xp - C.x0) + (yp - C.y0) * (yp - C.y0));
+  S = S / C.sMax * 0.8 + 0.2;
+  if (H >= 360.0) H = 0.0;
+  int icase = (int)floor(H / 60.0);
+  double ff = H / 6.0 - icase;
+  double p = V * (1. - S), q = V * (1. - S * ff), tt = V * (1. - (S * (1. - ff)));
+  float r0 = 0.0f, r1 = 0.0f, r2 = 0.0f;
+  if (!(S <= 0.0)) {
+    switch (icase) {
+      case 0: r0 = (float)V; r1 = (float)tt; r2 = (float)p; break;
+      case 1: r0 = (float)q; r1 = (float)V; r2 = (float)p; break;
+      case 2: r0 = (float)p; r1 = (float)V; r2 = (float)tt; break;
+      case 3: r0 = (float)p; r1 = (float)q; r2 = (float)V; break;
+      case 4: r0 = (float)tt; r1 = (float)p; r2 = (float)V; break;
+      case 5: r0 = (float)V; r1 = (float)p; r2 = (float)q; break;
+      default: break;
+    }
+  }
+  rgb[0] = r0;
+  rgb[1] = r1;
+  rgb[2] = r2;
+}
+// IPF colours of grains [0, ngrain): 9 floats per grain (z, x, y directions).
+__global__ void k_ipf_grains(const double *cth, int ngrain, CafeIpfConsts C, float *out) {
+  for (int gi = blockIdx.x * blockDim.x + threadIdx.x; gi < ngrain; gi += gridDim.x * blockDim.x) {
+    const double *cc = cth + 4LL * gi;
+    double omega = cc[0], ax[3] = {cc[1], cc[2], cc[3]};
+    double co = crm_cos(omega), so = crm_sin(omega);
+    double R[3][3];
+    // VoxelsCA.C:1635-1644, with pow(a, 2.0) = a*a
+    R[0][0] = co + (ax[0] * ax[0]) * (1 - co);
+    R[0][1] = ax[0] * ax[1] * (1 - co) - ax[2] * so;
+    R[0][2] = ax[0] * ax[2] * (1 - co) + ax[1] * so;
+    R[1][0] = ax[0] * ax[1] * (1 - co) + ax[2] * so;
+    R[1][1] = co + (ax[1] * ax[1]) * (1 - co);
+    R[1][2] = ax[1] * ax[2] * (1 - co) - ax[0] * so;
+    R[2][0] = ax[2] * ax[0] * (1 - co) - ax[1] * so;
+    R[2][1] = ax[2] * ax[1] * (1 - co) + ax[0] * so;
+    R[2][2] = co + (ax[2] * ax[2]) * (1 - co);
+    double H = 0.0;
+    float *o = out + 9LL * gi;
+    cafe_ipf_dir(C, R, 0, true, H, o);
+    cafe_ipf_dir(C, R, 1, true, H, o + 3);
+    cafe_ipf_dir(C, R, 2, false, H, o + 6);
+  }
+}
+// Per-cell colours of direction `d` (0 z, 1 x, 2 y) for cells [off, off+n).
+__global__ void k_ipf_cells(CafeDev D, const float *gcol, int d, long long off, long long n, float *out) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    int g = D.gid[off + i];
+    float r = 0.0f, gg = 0.0f, b = 0.0f;
+    if (g >= 1) {
+      const float *c = gcol + 9LL * (g - 1) + 3 * d;
+      r = c[0];
+      gg = c[1];
+      b = c[2];
+    }
+    out[3 * i] = r;
+    out[3 * i + 1] = gg;
+    out[3 * i + 2] = b;
+  }
+}
+// TempField::TempCurr as float for cells [off, off+n) (WriteToHDF1's TempOut).
+__global__ void k_temperature_f(CafeConsts K, CafeStepParams P, long long off, long long n, float *out) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    int a, b, c;
+    cafe_cell_xyz(K, off + i, a, b, c);
+    out[i] = (float)K.Tcls[cafe_temp_class_exact(K, P, a, b, c)];
+  }
+}
+// Build as int32 for cells [off, off+n).
+__global__ void k_build_i32(CafeDev D, long long off, long long n, int32_t *out) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    out[i] = D.build[off + i];
+}

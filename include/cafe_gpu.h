@@ -51,6 +51,10 @@ typedef struct {
   long long steps; /* loop iterations executed */
   double gth;      /* Grid::gth, current rotation of the laser grid */
   unsigned int genlayer_state; /* VoxelsCA::genlayer engine state (minstd_rand0) */
+  int tf_tInd;     /* TempField::tInd of the last step (main1.C:64) */
+  int output_due;  /* 1 when the last cafe_sim_step reached an output point of
+                      main1.C:77-78 (it called SetBuild there; the reference
+                      writes WriteToHDF1("<base>" + tf_tInd) at this point) */
 } cafe_info;
 
 typedef struct {
@@ -99,8 +103,9 @@ int cafe_sim_update_time(cafe_sim *sim);
 /* main1.C:60-61: AddLayer1 then the first UpdateLaser (after
  * initialize_voxels). */
 int cafe_sim_begin(cafe_sim *sim);
-/* One iteration of the main1.C:62-93 loop body (without HDF5 output);
- * *done = 1 when the loop condition ends the run. */
+/* One iteration of the main1.C:62-93 loop body, SetBuild at the output
+ * points included, WriteToHDF1 left to the caller (cafe_info.output_due and
+ * cafe_sim_write_output); *done = 1 when the loop condition ends the run. */
 int cafe_sim_step(cafe_sim *sim, int *done);
 /* Runs loop iterations until done or max_steps (> 0) iterations; then, when
  * done, the closing CleanLayer (main1.C:95). */
@@ -145,6 +150,29 @@ int cafe_sim_download_ctheta(cafe_sim *sim, double *ctheta, long long cap, int *
 int cafe_sim_upload_state(cafe_sim *sim, const int32_t *gID, const int32_t *vState,
                           const double *extents, const double *centroid, const double *ctheta,
                           int ngrain);
+
+/* VoxelsCA::SetBuild(TempField::BuildjID) (VoxelsCA.C:76-115): every cell
+ * of a grain that has a melted cell or a Build cell gets Build = 1. */
+int cafe_sim_set_build(cafe_sim *sim);
+/* VoxelsCA::Build (0/1), N entries. */
+int cafe_sim_download_build(cafe_sim *sim, int32_t *build);
+/* The per-cell datasets that VoxelsCA::WriteToHDF1 (VoxelsCA.C:1592-1854)
+ * derives for output: Temperature (TempCurr of the last cafe_sim_temperature
+ * call, as float; N entries) and the inverse-pole-figure colour maps IPFz,
+ * IPFx, IPFy (RGB of the sample's build, x and y directions in each cell's
+ * crystal frame, 3 floats per cell; 0 for cells without a grain), with the
+ * reference's colouring as written (the y map's hue starts from the x map's
+ * hue; the hue fraction is H/6). Any pointer may be NULL. */
+int cafe_sim_download_output(cafe_sim *sim, float *temperature, float *ipfz, float *ipfx, float *ipfy);
+/* VoxelsCA::WriteToHDF1(name) (VoxelsCA.C:1592-1854) with one raw file per
+ * dataset in place of the HDF5 file: <prefix>.<dataset>.bin for the datasets
+ * dims (3 int32: nX), VoxelDX (3 float: dX), gID, vState, Build (int32 per
+ * cell), Temperature (float per cell), IPFz, IPFx, IPFy (3 float per cell)
+ * and angleAxis (cTheta as float, 4 per grain), native byte order, in the
+ * reference's cell order, and <prefix>.xdmf, an XDMF description of the
+ * per-cell files as cell data on the voxel grid. The reference's file
+ * <base><tInd>.h5 corresponds to prefix "<base><tInd>.h5". */
+int cafe_sim_write_output(cafe_sim *sim, const char *prefix);
 
 /* Allocation-free CleanLayer renumbering on caller-owned device arrays. No
  * counterpart in the reference: it serves callers that cannot go to the CUDA
