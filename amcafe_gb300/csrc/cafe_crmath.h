@@ -505,4 +505,193 @@ CRM_HD double crm_pow_int(double x, int e) {
   return crm_dd_round(acc);
 }
 
+// ---- exp ----------------------------------------------------------------
+// exp(x) = 2^m * 2^(j/128) * exp(r), k = 128 m + j = round(x * 128/ln2),
+// r = x - k ln2/128 with ln2/128 in three parts (the first two of 35 bits, so
+// k times them is exact for |k| < 2^18) and |r| <= ln2/256 + 2^-60. The fast
+// evaluation takes exp(r) - 1 = r + r^2/2 + ... + r^6/720 with the quadratic
+// tail in double (relative error below 2^-67 overall); the accurate one takes
+// the terms to r^4/24 in double-double and the rest to r^10 in double (error
+// below about 2^-100). Results below the normal range are rounded once, on the
+// subnormal grid, from the double-double value.
+
+// Rounds (h + l) * 2^m to the nearest double (ties to even) for m <= -1022
+// and h + l in [0.99, 2]: results on the subnormal grid (step 2^-1074, which is
+// also the step of the lowest normal binade), rounded once from the
+// double-double value. `err` bounds the absolute error of h + l. Returns 0 when
+// the rounding is not decided within it, unless `force` (then the value itself
+// decides).
+CRM_HD int crm_round_scaled_sub(double h, double l, double err, int m, int force, double *out) {
+  int sh = m + 1074;  // the grid step becomes 1; sh <= 52
+  if (sh < -2) {      // below a quarter of the smallest subnormal
+    *out = 0.0;
+    return 1;
+  }
+  double sc = crm_from_bits((long long)(1023 + sh) << 52);
+  double uh = h * sc, ul = l * sc;                 // exact: powers of two, normal range
+  double ue = err * sc + 0x1p-53;                  // + the rounding of f below
+  double n0 = uh >= 0x1p52 ? uh : (uh + 0x1p52) - 0x1p52;  // nearest integer, 0 <= uh < 2^53
+  double f = (uh - n0) + ul;                       // uh - n0 is exact, |f| <~ 1/2
+  double n;
+  if (f - ue > 0.5) {
+    n = n0 + 1.0;
+  } else if (f + ue < -0.5) {
+    n = n0 - 1.0;
+  } else if (f - ue > -0.5 && f + ue < 0.5) {
+    n = n0;
+  } else if (!force) {
+    return 0;
+  } else if (f > 0.5 || f < -0.5) {
+    n = f > 0.5 ? n0 + 1.0 : n0 - 1.0;
+  } else if (f == 0.5 || f == -0.5) {  // tie: the even neighbour
+    double o = f > 0.0 ? n0 + 1.0 : n0 - 1.0;
+    n = (n0 * 0.5 == (double)(long long)(n0 * 0.5)) ? n0 : o;
+  } else {
+    n = n0;
+  }
+  *out = (n * 0x1p-1022) * 0x1p-52;  // n 2^-1074, exact in two steps
+  return 1;
+}
+
+// Reduction shared by both evaluations: k, and r as rh + rl.
+CRM_HD void crm_exp_reduce(double x, long long *k, double *rh, double *rl) {
+  const double MAGIC = 0x1.8p52;
+  double kd = (x * CRM_INV_LN2_128 + MAGIC) - MAGIC;
+  *k = (long long)kd;
+  double a = x - kd * CRM_LN2_128_1;  // exact
+  crm_dd t = crm_two_sum(a, -(kd * CRM_LN2_128_2));
+  double c = kd * CRM_LN2_128_3;
+  crm_dd r = crm_fast_two_sum(t.hi, t.lo - c);
+  *rh = r.hi;
+  *rl = r.lo;
+}
+
+// Final scaling of T (1 + p) = s + lo by 2^m; returns 0 if undecided.
+CRM_HD int crm_exp_finish(double s, double lo, double err, int m, int force, double *out) {
+  if (m >= -1021) {
+    double v;
+    if (!crm_round_test(s, lo, err, &v)) return 0;
+    if (m > 1023) {  // v * 2^m in two exact-or-overflowing steps
+      *out = (v * 0x1p1023) * crm_from_bits((long long)(1023 + m - 1023) << 52);
+    } else {
+      *out = v * crm_from_bits((long long)(1023 + m) << 52);
+    }
+    return 1;
+  }
+  return crm_round_scaled_sub(s, lo, err, m, force, out);
+}
+
+CRM_HD double crm_exp_acc(double x) {
+  long long k;
+  double rh, rl;
+  crm_exp_reduce(x, &k, &rh, &rl);
+  int j = (int)(k & (CRM_EXP_STEPS - 1));
+  int m = (int)((k - j) / CRM_EXP_STEPS);
+  // tail r^5/120 + ... + r^10/10! in double
+  double c5 = 1.0 / 120 + rh * (1.0 / 720 + rh * (1.0 / 5040 + rh * (1.0 / 40320 + rh * (1.0 / 362880 + rh * (1.0 / 3628800)))));
+  crm_dd r = {rh, rl};
+  crm_dd t = crm_dd_add(crm_dd{CRM_INV_FACT24_HI, CRM_INV_FACT24_LO}, crm_dd{rh * c5, 0.0});
+  t = crm_dd_add(crm_dd{CRM_INV_FACT6_HI, CRM_INV_FACT6_LO}, crm_dd_mul(r, t));
+  t = crm_dd_add(crm_dd{0.5, 0.0}, crm_dd_mul(r, t));
+  t = crm_dd_add(crm_dd{1.0, 0.0}, crm_dd_mul(r, t));
+  crm_dd p = crm_dd_mul(r, t);  // exp(r) - 1
+  crm_dd T = {CRM_TAB(crm_exp2_tab)[j][0], CRM_TAB(crm_exp2_tab)[j][1]};
+  crm_dd y = crm_dd_add(T, crm_dd_mul(T, p));
+  double v;
+  crm_exp_finish(y.hi, y.lo, 0.0, m, 1, &v);
+  return v;
+}
+
+// exp(x), nearly correctly rounded (see above); same bits on host and device.
+CRM_HD double crm_exp(double x) {
+  if (x != x) return x + x;
+  if (x > 709.8) return INFINITY;
+  if (x < -745.2) return 0.0;
+  long long k;
+  double rh, rl;
+  crm_exp_reduce(x, &k, &rh, &rl);
+  int j = (int)(k & (CRM_EXP_STEPS - 1));
+  int m = (int)((k - j) / CRM_EXP_STEPS);
+  double q = rh * rh * (0.5 + rh * (1.0 / 6 + rh * (1.0 / 24 + rh * (1.0 / 120 + rh * (1.0 / 720)))));
+  crm_dd p = crm_fast_two_sum(rh, rl + q);  // exp(r) - 1, |rh| > |rl + q| or rh = 0
+  double th = CRM_TAB(crm_exp2_tab)[j][0], tl = CRM_TAB(crm_exp2_tab)[j][1];
+  crm_dd a = crm_two_prod(th, p.hi);
+  crm_dd s = crm_fast_two_sum(th, a.hi);
+  double lo = s.lo + (a.lo + (th * p.lo + (tl + tl * p.hi)));
+  double v;
+  if (crm_exp_finish(s.hi, lo, s.hi * 0x1p-66, m, 0, &v)) return v;
+  CRM_COUNT(crm_fallback_calls);
+  return crm_exp_acc(x);
+}
+
+// ---- pow(x, -0.5) ------------------------------------------------------------
+// Sign of the exact sum of n doubles (n <= 8), by Shewchuk's expansion growth.
+CRM_HD int crm_sum_sign(const double *t, int n) {
+  double e[9];
+  int len = 0;
+  for (int i = 0; i < n; ++i) {
+    double q = t[i];
+    int nl = 0;
+    for (int k = 0; k < len; ++k) {
+      crm_dd s = crm_two_sum(q, e[k]);
+      q = s.hi;
+      if (s.lo != 0.0) e[nl++] = s.lo;
+    }
+    if (q != 0.0) e[nl++] = q;
+    len = nl;
+  }
+  // components are non-overlapping and ascending: the last one has the sign
+  if (len == 0) return 0;
+  return e[len - 1] > 0.0 ? 1 : -1;
+}
+
+// x^(-1/2) as pow(x, -0.5) defines it, correctly rounded. x = x' 4^h with x'
+// in [1, 4) (subnormal x first scaled by 2^108); y = 1/sqrt(x') is refined
+// with the residual 1 - x' y^2 (double-double, error below 2^-100), and when
+// that does not decide the rounding, x' m^2 is compared with 1 exactly at the
+// midpoint m between the two candidate doubles. (An exact result needs x' = 1
+// and a tie is impossible, so the comparison always decides.)
+CRM_HD double crm_pow_mhalf(double x) {
+  if (x != x) return x + x;
+  if (x == 0.0) return INFINITY;
+  if (x < 0.0) return (x - x) / (x - x);  // NaN (also for -inf)
+  if (x == INFINITY) return 0.0;
+  int post = 0;  // result exponent adjustment
+  if (x < 0x1p-1022) {
+    x = x * 0x1p108;
+    post = 54;
+  }
+  int ex = (int)((crm_bits(x) >> 52) & 0x7ff) - 1023;
+  int h2 = ex >> 1;  // floor(ex / 2)
+  double xs = x * crm_from_bits((long long)(1023 - 2 * h2) << 52);  // in [1, 4)
+  post -= h2;
+  double y = 1.0 / sqrt(xs);
+  crm_dd y2 = crm_two_prod(y, y);
+  crm_dd b = crm_two_prod(xs, y2.hi);
+  double c = xs * y2.lo;
+  double e = ((1.0 - b.hi) - b.lo) - c;       // 1 - x' y^2
+  double corr = y * (e * (0.5 + 0.375 * e));  // y ((1 - e)^(-1/2) - 1) to O(e^3)
+  double v;
+  if (!crm_round_test(y, corr, y * 0x1p-98, &v)) {
+    double v0 = y + corr;
+    long long vb = crm_bits(v0);
+    double resid = (y - v0) + corr;  // the side of v0 the exact value lies on
+    double nb = crm_from_bits(resid >= 0.0 ? vb + 1 : vb - 1);
+    double hh = (nb - v0) * 0.5;     // half the gap, a power of two
+    // x' (v0 + hh)^2 - 1 as an exact sum
+    crm_dd v2 = crm_two_prod(v0, v0);
+    crm_dd t1 = crm_two_prod(xs, v2.hi);
+    crm_dd t2 = crm_two_prod(xs, v2.lo);
+    crm_dd t3 = crm_two_prod(xs, 2.0 * v0 * hh);
+    double terms[8] = {-1.0, t1.hi, t1.lo, t2.hi, t2.lo, t3.hi, t3.lo, xs * (hh * hh)};
+    int sg = crm_sum_sign(terms, 8);  // > 0: the midpoint lies above the exact value
+    if (resid >= 0.0)
+      v = sg > 0 ? v0 : nb;
+    else
+      v = sg < 0 ? v0 : nb;
+    CRM_COUNT(crm_fallback_calls);
+  }
+  return v * crm_from_bits((long long)(1023 + post) << 52);
+}
+
 #endif

@@ -57,6 +57,32 @@ def main():
     out.append("#define CRM_PI_HI %s" % hx(pih))
     out.append("#define CRM_PI_LO %s" % hx(pil))
     out.append("#define CRM_TWO_OVER_PI %s" % hx(mpmath.libmp.to_float((2 / mpmath.pi)._mpf_, rnd="n")))
+    # exp: x = k ln2/128 + r, exp(x) = 2^(k>>7) 2^((k&127)/128) exp(r)
+    c = mpmath.log(2) / 128
+
+    def round_bits(v, bits):
+        return mpmath.libmp.to_float(mpmath.libmp.normalize(*mpmath.mpf(v)._mpf_[:3], mpmath.mpf(v)._mpf_[3],
+                                                            bits, "n"), rnd="n")
+
+    l1 = round_bits(c, 35)
+    l2 = round_bits(c - l1, 35)
+    l3 = mpmath.libmp.to_float((c - l1 - l2)._mpf_, rnd="n")
+    out.append("#define CRM_EXP_STEPS 128")
+    out.append("#define CRM_LN2_128_1 %s" % hx(l1))
+    out.append("#define CRM_LN2_128_2 %s" % hx(l2))
+    out.append("#define CRM_LN2_128_3 %s" % hx(l3))
+    out.append("#define CRM_INV_LN2_128 %s" % hx(mpmath.libmp.to_float((128 / mpmath.log(2))._mpf_, rnd="n")))
+    rows = []
+    for j in range(128):
+        h, l = split(mpmath.power(2, mpmath.mpf(j) / 128))
+        rows.append("  {%s, %s}," % (hx(h), hx(l)))
+    out.append("CRM_TABLE_DECL(double, crm_exp2_tab, [128][2]) = {")
+    out += rows
+    out.append("};")
+    for n, name in ((3, "6"), (4, "24")):
+        h, l = split(1 / mpmath.factorial(n))
+        out.append("#define CRM_INV_FACT%s_HI %s" % (name, hx(h)))
+        out.append("#define CRM_INV_FACT%s_LO %s" % (name, hx(l)))
     out.append("#endif")
     print("\n".join(out))
 

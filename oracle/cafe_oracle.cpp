@@ -6,7 +6,8 @@
 //
 // It restates, in single-rank form, the reference's main loop (main1.C:18-101)
 // and everything it calls on the hot path: the .in parser and laser state
-// machine (Grid.C), the analytic double-ellipsoid temperature (TempField.C),
+// machine (Grid.C), the analytic double-ellipsoid temperature and the EASM
+// moving-Gaussian-source temperature (TempField.C, Utilities.C),
 // Voronoi baseplate and powder layers (BasePlate.C, VoxelsCA.C AddLayer1),
 // orientation sampling (SampleOrientation.C) and the CA step
 // (VoxelsCA.C UpdateVoxels/SetLiquid3/ConvertSolid1/CleanLayer). Each routine
@@ -48,6 +49,7 @@
 #include <time.h>
 
 #include "../amcafe_gb300/csrc/cafe_crmath.h"
+#include "../amcafe_gb300/csrc/cafe_quadrature.h"
 
 namespace orc {
 
@@ -196,6 +198,9 @@ static bool read_deck(const char *path, Grid &g, std::string &err) {
         next_d(g.offset[2]);
       }
       // Grid.C:276 compares the lowercased keyword with "EASM": never true.
+      // The keyword "easm" selects the EASM temperature here (the flag that
+      // keyword was meant to set); the reference reads it as an unknown word.
+      if (kw == "easm") next_i(g.EASM_Flag);
       if (kw == "meltparam") {
         next_d(g.meltparam[0]);
         next_d(g.meltparam[1]);
@@ -781,6 +786,155 @@ static void analytic_temp(State &S) {
       g.indlayer += 1;
     }
   }
+}
+
+// ---------------------------------------------------------------- EASM
+// TempField::EASM (TempField.C:79-137) with Utilities::EASM_Temp_LG, Integral,
+// Temp_Fun_G and the 316L properties (Utilities.C:39-76, 105-140, 228-249).
+// The 25-node Gauss-Legendre rule of the GSL call comes from
+// cafe_quadrature.h, as in the reference built here (oracle/ref_shims).
+static double m_exp(double x) {
+  if (g_libm.mode == 1) return crm_exp(x);
+  return perturb(std::exp(x));
+}
+// pow(x, -0.5)
+static double m_pow_mhalf(double x) {
+  if (g_libm.mode == 1) return crm_pow_mhalf(x);
+  return perturb(std::pow(x, -0.5));
+}
+// pow(10, -e) of the property polynomials (correctly rounded: the decimal literal)
+static double m_p10(int e) {
+  if (g_libm.mode == 1) return e == 2 ? 1e-2 : e == 3 ? 1e-3 : e == 4 ? 1e-4 : 1e-5;
+  return std::pow(10, -e);
+}
+// Utilities::Materials_316L: {cP, k, rho, alpha}
+static void easm_materials(double T, double M[4]) {
+  double rho, cP, k;
+  if (T < 1660)
+    rho = 8084.2 - 0.42086 * T - 3.8942 * m_p10(5) * T * T;
+  else if (T >= 1660 && T < 3090)
+    rho = 7432.7 + 3.9338 * m_p10(2) * T - 1.8007 * m_p10(4) * T * T;
+  else
+    rho = 6124.72;
+  if (T < 1660)
+    cP = 458.984 + 0.1328 * T;
+  else
+    cP = 769.855;
+  if (T < 1660)
+    k = 9.248 + 1.571 * m_p10(2) * T;
+  else if (T >= 1660 && T < 3090)
+    k = 12.41 + 3.279 * m_p10(3) * T;
+  else
+    k = 21.6465;
+  M[0] = cP;
+  M[1] = k;
+  M[2] = rho;
+  M[3] = k / (rho * cP);
+}
+struct EasmCtx {
+  double L[3], R[3];
+  double bmV, Q;
+  double qx[25], qw[25];
+};
+// Utilities::Temp_Fun_G at time x of the integral (t = 8e-4 s)
+static double easm_kernel(const EasmCtx &E, const double M[4], double x) {
+  const double sigma = 50.0e-6, eta = 0.56, t = 80.0e-5;
+  double C = eta * E.Q / (M_PI * M[2] * M[0] * std::sqrt(4 * M_PI * M[3]));
+  double x0 = E.L[0] - E.bmV * t;
+  double Lx = x0 + E.bmV * x;
+  double Ly = E.L[1], Lz = E.L[2];
+  double tx = t - x;
+  double sig2 = m_pow2(sigma);
+  double dx = E.R[0] - Lx, dy = E.R[1] - Ly, dz = std::fabs(E.R[2] - Lz);
+  return C * m_pow_mhalf(tx) / (2 * M[3] * tx + sig2) *
+         m_exp(-1 * (m_pow2(dx) + m_pow2(dy)) / (4 * M[3] * tx + 2 * sig2) - m_pow2(dz) / (4 * M[3] * tx));
+}
+// Utilities::Integral: 300 + sum_i w_i f(x_i)
+static double easm_integral(const EasmCtx &E, double T) {
+  double M[4];
+  easm_materials(T, M);
+  double s = 0.0;
+  for (int i = 0; i < 25; ++i) s += E.qw[i] * easm_kernel(E, M, E.qx[i]);
+  return 300 + s;
+}
+// Utilities::EASM_Temp_LG: damped fixed point on the property temperature
+static double easm_temp_lg(const EasmCtx &E, double T) {
+  double Told = T;
+  int n = 0, nlim = 100;
+  double tol = 10;
+  double Tnew = easm_integral(E, T);
+  while (std::fabs(Told - Tnew) > tol && n < nlim) {
+    Told = Tnew;
+    double T_temp = easm_integral(E, Told);
+    Tnew = 0.5 * (Told + T_temp);
+    n++;
+  }
+  return Tnew;
+}
+static void easm_temp(State &S) {
+  Grid &g = S.g;
+  std::fill(S.temp.begin(), S.temp.end(), 0.0);  // TempOut.assign(Ntot, 0)
+  EasmCtx E;
+  cafe_gauss_legendre(25, 0.0, 80.0e-5, E.qx, E.qw);
+  E.bmV = g.bmV;
+  E.Q = g.bmP;
+  const int *isv = S.ispvec.data();
+  double x = g.lcoor[2 * isv[g.isp]] - g.offset[0];
+  double y = g.lcoor[2 * isv[g.isp] + 1] - g.offset[1];
+  double z = g.ilaserLoc * g.dX[2] - g.offset[2];
+  double cg = std::cos(g.gth), sg = std::sin(g.gth);
+  E.L[0] = x;
+  E.L[1] = y;
+  E.L[2] = z;
+  for (int j = 0; j < S.N; ++j) {
+    int c[3];
+    cell_xyz(S, j, c);
+    double x0 = (double(c[0]) + .5) * (g.dX[0]);
+    double y0 = (double(c[1]) + .5) * (g.dX[1]);
+    double zp = (double(c[2]) + .5) * (g.dX[2]);
+    if (zp > z) continue;
+    double xp = cg * (x0 - g.LX[0] / 2.) + sg * (y0 - g.LX[1] / 2.) + g.LX[0] / 2.;
+    double yp = -sg * (x0 - g.LX[0] / 2.) + cg * (y0 - g.LX[1] / 2.) + g.LX[1] / 2.;
+    double T;
+    if ((x0 > x) && (zp > (z - g.layerT))) {
+      T = .99 * g.T0;
+    } else {
+      E.R[0] = xp;
+      E.R[1] = yp;
+      E.R[2] = zp;
+      T = easm_temp_lg(E, S.temp[j]);
+    }
+    S.temp[j] = T;
+    if (T > g.tL)
+      S.buildj[j] = 1;
+    else if (T < g.T0)
+      S.buildj[j] = 0;
+  }
+  double lx = g.lcoor2[2 * isv[g.isp]] - g.offset[0];
+  double ly = g.lcoor2[2 * isv[g.isp] + 1] - g.offset[1];
+  if (lx < g.gbox[0] || lx > g.gbox[1] || ly < g.gbox[2] || ly > g.gbox[3]) {
+    // all_of(T >= tL) here, where AnalyticTempCurr asks any_of
+    int all = 1;
+    for (int j = 0; j < S.N; ++j)
+      if (!(S.temp[j] >= g.tL)) {
+        all = 0;
+        break;
+      }
+    if (all == 0 || std::fmod(g.isp + 1, g.Nsd) == 0) g.inewscanflg = 1;
+    if (g.isp == (g.NpT - 1)) {
+      g.inewscanflg = 1;
+      g.inewlayerflg = 1;
+      g.isp = 0;
+      g.indlayer += 1;
+    }
+  }
+}
+// main1.C:65-70: EASM when Grid::EASM_Flag is 1, else the analytic field
+static void temperature(State &S) {
+  if (S.g.EASM_Flag == 1)
+    easm_temp(S);
+  else
+    analytic_temp(S);
 }
 
 // VoxelsCA::ConvertSolid1 (VoxelsCA.C:712-799), two-phase.
@@ -1388,7 +1542,7 @@ int cafe_oracle_run(const char *deck, const char *dump_path, long max_steps, int
   clock_gettime(CLOCK_MONOTONIC, &t0);
   while (!bcheck) {
     S.tf_tInd = int(std::round(g.time / S.DelT));
-    analytic_temp(S);
+    temperature(S);
     update_voxels(S);
     update_laser(g);
     bcheck = g.indlayer > nlayerTot;
@@ -1499,7 +1653,7 @@ int cafe_oracle_run_window(const char *deck, const cafe_oracle_window *w, int32_
       if ((t1.tv_sec - t0.tv_sec) + 1e-9 * (t1.tv_nsec - t0.tv_nsec) > g_max_seconds) break;
     }
     S.tf_tInd = int(std::round(g.time / S.DelT));
-    analytic_temp(S);
+    temperature(S);
     update_voxels(S);
     update_laser(g);
     bcheck = g.indlayer > nlayerTot;

@@ -11,7 +11,7 @@
 // "out<tInd>" and after the closing CleanLayer as "final"; the ADIOS2 shim
 // then writes its datasets as raw files into that directory.
 //
-// Usage: cafe_ref_dump <deck.in> <out.bin> [max_steps]
+// Usage: cafe_ref_dump <deck.in> <out.bin> [max_steps]   (CAFE_REF_EASM=1: EASM temperature)
 // Record layout (little-endian): see oracle/cafe_dump.py.
 #include <cmath>
 #include <cstdint>
@@ -62,6 +62,10 @@ int main(int argc, char *argv[]) {
   int nprocs = 1, myid = 0;
   std::string filParamIn = argv[1];
   Grid g(filParamIn, myid, nprocs);
+  // Grid::readInputFile lowercases each keyword before comparing it with
+  // "EASM" (Grid.C:197-198, 276), so no deck selects the EASM temperature;
+  // CAFE_REF_EASM=1 sets the flag that keyword was meant to set.
+  if (std::getenv("CAFE_REF_EASM") && std::atoi(std::getenv("CAFE_REF_EASM")) == 1) g.EASM_Flag = 1;
   Partition part(g, myid, nprocs);
   part.PartitionGraph2();
   BasePlate bp(g, part);

@@ -2,8 +2,10 @@
  * (gsl_integration_fixed with gsl_integration_fixed_legendre), the only GSL
  * facility the reference uses (Utilities.C:112-122, the EASM temperature).
  * Test infrastructure: nodes and weights come from Newton iteration on the
- * Legendre polynomial P_n (ref_shims_impl.cpp), not from GSL itself, so the
- * EASM path of a reference built on this shim is "parity unpinned". */
+ * Legendre polynomial P_n (amcafe_gb300/csrc/cafe_quadrature.h, correctly
+ * rounded for n = 25), not from GSL itself (which solves the Golub-Welsch
+ * eigenproblem), so the EASM path of a reference built on this shim is pinned
+ * only up to the last bits of GSL's nodes. */
 #ifndef CAFE_REF_SHIM_GSL_INTEGRATION_H
 #define CAFE_REF_SHIM_GSL_INTEGRATION_H
 #include <stddef.h>

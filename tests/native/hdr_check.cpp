@@ -24,6 +24,8 @@ void hc_eval(int fn, long n, const double *x, const double *y, double *out) {
       case 2: out[i] = crm_sin(x[i]); break;
       case 3: out[i] = crm_acos(x[i]); break;
       case 4: out[i] = crm_pow_half(x[i]); break;
+      case 6: out[i] = crm_exp(x[i]); break;
+      case 7: out[i] = crm_pow_mhalf(x[i]); break;
       default: out[i] = crm_pow_int(x[i], (int)y[i]); break;
     }
   }

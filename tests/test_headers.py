@@ -60,7 +60,8 @@ def test_uniform_jump_ahead(hc):
         assert np.array_equal(got, want)
 
 
-@pytest.mark.parametrize("fn,name", [(0, "atan2"), (1, "cos"), (2, "sin"), (3, "acos"), (5, "pow_int")])
+@pytest.mark.parametrize("fn,name", [(0, "atan2"), (1, "cos"), (2, "sin"), (3, "acos"), (5, "pow_int"), (6, "exp"),
+                                     (7, "pow_mhalf")])
 def test_crmath_correctly_rounded(hc, fn, name):
     g = np.load(os.path.join(HERE, "golden", "crmath.npz"))
     x = np.ascontiguousarray(g[name + "_x"])

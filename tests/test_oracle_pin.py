@@ -6,7 +6,9 @@ make_golden.py). The oracle restatement with glibc libm must reproduce every
 dumped record: integer fields bit for bit (SHA-256), float fields to 1e-12
 relative (bit-exact on the machine that made the fixtures).
 The correctly-rounded-libm mode (the arithmetic the GPU uses) must reproduce
-the integer fields too on these decks.
+the integer fields too on these decks. The two track_easm decks run the EASM
+temperature (TempField::EASM, Utilities.C), which the reference reaches only
+with the CAFE_REF_EASM switch of its driver (its parser cannot select it).
 """
 import hashlib
 import os
@@ -17,7 +19,7 @@ import pytest
 import cafe_oracle as orc
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-DECKS = ["track_r0", "track_nuc", "layers_rot", "c0_small"]
+DECKS = ["track_r0", "track_nuc", "layers_rot", "c0_small", "track_easm", "track_easm60"]
 
 
 def _digest(a):
