@@ -69,6 +69,20 @@ struct CafeConsts {
   // SampleOrientation constants (SampleOrientation.C:15-22)
   double so_R1, so_a, so_aprime, so_beta, so_s2, so_s2q, so_s6pi, so_spi, so_s24, so_coeffA[7];
   double s3, s23;     // pow(3,.5), pow(2/3,.5) (VoxelsCA.C:583-585)
+  // EASM temperature (TempField::EASM): per-cell temperatures in CafeDev::temp
+  // and per-cell growth velocities in CafeDev::a_vh
+  int easm;
+  double Avel;        // Grid::Avel
+  int nvel_i;         // Grid::nvel (an integer when easm)
+};
+
+// Tables of the EASM temperature (TempField.C:79-137, Utilities.C:105-140,
+// 228-249), computed on the host: the 25-node Gauss-Legendre rule on
+// [0, 8e-4 s], t - x_i and (t - x_i)^(-1/2) per node.
+#define CAFE_EASM_NODES 25
+struct CafeEasm {
+  double qw[CAFE_EASM_NODES], qx[CAFE_EASM_NODES], tx[CAFE_EASM_NODES], r[CAFE_EASM_NODES];
+  double bmV, Q, layerT;
 };
 
 struct CafeDev {
@@ -83,6 +97,8 @@ struct CafeDev {
   long long tcls_cap;
   // VoxelsCA::Build (0/1 per cell)
   uint8_t *build;
+  // EASM mode: TempField::TempCurr per cell, growth velocity per active position
+  double *temp, *a_vh;
   // liquid cells left by the previous step (cell indices)
   int32_t *liq;
   // grains
@@ -143,6 +159,8 @@ enum {
   CTR_SLOW,        // 1: this step's rows do not share one growth velocity
   CTR_NROWS_END,   // frontier rows after the event loop
   CTR_NPAIRS,      // (row, slot) pairs listed for the row set-up
+  CTR_EASM_BOX,    // 6 slots: box of the cells at or above the liquidus (EASM)
+  CTR_EASM_COLD = CTR_EASM_BOX + 6,  // 1: some cell below the liquidus (EASM)
   CTR_COUNT
 };
 enum { STAT_EVENTS = 0, STAT_NUC, STAT_MAXNA, STAT_MAXROWS, STAT_STEPS, STAT_NEGDT, STAT_SUMNA, STAT_SUMROWS,

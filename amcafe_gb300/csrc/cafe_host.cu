@@ -27,6 +27,7 @@
 
 #include "../../include/cafe_gpu.h"
 #include "cafe_kernels.cu"
+#include "cafe_quadrature.h"
 
 namespace {
 
@@ -57,6 +58,7 @@ struct GridH {
   int nX[3] = {128, 128, 64};
   double dX[3] = {1e-6, 1e-6, 1e-6};
   int outint = 1, patternID = 1, outNL = 0;
+  int EASM_Flag = 0;  // Grid::EASM_Flag (keyword "easm", see parse_deck)
   double tL = 1620, tS = 1531.5, T0 = 300, layerT = 25e-6, bpH = 0.0, mu = .01, lrate = 0;
   double meltparam[4] = {75e-6, 162.75e-6, 75e-6, 75e-6};
   double bhatch = 0, bmDelT = 0, bmV = 500e-3, bmP = 0, rNmax = .002;
@@ -131,6 +133,9 @@ int parse_deck(const char *path, GridH &g) {
     else if (key == "gridsize") ok = num(g.gsize[0]) && num(g.gsize[1]);
     else if (key == "gridtheta") ok = num(g.gth0);
     else if (key == "dendritegrowth2") ok = num(g.Avel) && num(g.nvel);
+    // Grid.C:276 compares the lowercased keyword with "EASM", which never
+    // matches; "easm 1" sets the flag that keyword was meant to set.
+    else if (key == "easm") ok = inum(g.EASM_Flag);
     if (!ok) return fail(CAFE_E_ARG, "deck '%s': bad value after keyword '%s'", path, key.c_str());
     in >> kw;
   }
@@ -364,6 +369,8 @@ struct cafe_sim {
   CafeConsts K;
   CafeDev D;
   CafeStepParams P;      // last temperature parameters
+  CafeEasm E;            // EASM tables (K.easm)
+  bool easm_cold = false;  // some cell below the liquidus after the last EASM field
   bool have_P = false;
   bool have_prev_box = false;
   int prev_lo[3] = {0, 0, 0}, prev_hi[3] = {0, 0, 0};
@@ -613,6 +620,36 @@ void make_step_params(cafe_sim *s, CafeStepParams &P) {
   }
 }
 
+// TempField::EASM over the cells below the laser plane; the step's box becomes
+// the box of the cells at or above the liquidus.
+int easm_field(cafe_sim *s) {
+  CafeStepParams &P = s->P;
+  const CafeConsts &K = s->K;
+  P.any_hot_full = 0;
+  long long ncell = std::min<long long>(K.N, (long long)P.kabove * K.nxy);
+  {
+    PhaseScope ps(s, CAFE_PH_MELT);
+    k_easm_reset<<<1, 32, 0, s->stream>>>(s->D);
+    if (ncell > 0)
+      k_easm<<<grid_blocks(ncell, 256, s), 256, 0, s->stream>>>(s->D, K, P, s->E, ncell);
+    LAUNCHED(CAFE_PH_MELT, 2);
+  }
+  CUDA_TRY(cudaGetLastError());
+  int *h = s->h_pinned + 8;  // 7 ints: box lo, box hi, cold
+  CUDA_TRY(cudaMemcpyAsync(h, s->D.ctr + CTR_EASM_BOX, 7 * sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+  CUDA_TRY(cudaStreamSynchronize(s->stream));
+  s->easm_cold = h[6] != 0;
+  if (h[3] < 0) {
+    for (int a = 0; a < 3; ++a) P.lo[a] = P.hi[a] = 0;
+  } else {
+    for (int a = 0; a < 3; ++a) {
+      P.lo[a] = h[a];
+      P.hi[a] = h[3 + a] + 1;
+    }
+  }
+  return CAFE_OK;
+}
+
 }  // namespace
 
 // ====================================================================== C ABI
@@ -690,6 +727,28 @@ int cafe_sim_create(const char *deck_path, const cafe_options *opt, cafe_sim **o
     K.gt_cls[c] = T > g.tL;
     K.vhat_cls[c] = T >= g.tL ? 0.0 : g.Avel * std::pow(g.tL - T, g.nvel);
   }
+  K.easm = g.EASM_Flag == 1;
+  K.Avel = g.Avel;
+  K.nvel_i = 0;
+  if (K.easm) {
+    // per-cell velocities Avel pow(tL - T, nvel) are evaluated on the device
+    // as correctly rounded integer powers
+    if (!(g.nvel >= 1 && g.nvel <= 64 && g.nvel == (double)(int)g.nvel)) {
+      cafe_sim_destroy(s);
+      return fail(CAFE_E_ARG, "EASM temperature needs an integer growth exponent in 1..64 (dendritegrowth2)");
+    }
+    K.nvel_i = (int)g.nvel;
+    CafeEasm &E = s->E;
+    const double t = 80.0e-5;
+    cafe_gauss_legendre(CAFE_EASM_NODES, 0.0, t, E.qx, E.qw);
+    for (int i = 0; i < CAFE_EASM_NODES; ++i) {
+      E.tx[i] = t - E.qx[i];
+      E.r[i] = crm_pow_mhalf(E.tx[i]);
+    }
+    E.bmV = g.bmV;  // Utilities::InitializeUT (Utilities.C:143-146)
+    E.Q = g.bmP;
+    E.layerT = g.layerT;
+  }
   K.rX = g.rNmax * std::pow(g.dX[0] * 1e6, 3.);
   K.DelT = s->DelT;
   K.ruq_dx = g.dX[0];
@@ -756,7 +815,8 @@ int cafe_sim_create(const char *deck_path, const cafe_options *opt, cafe_sim **o
       (rc = dalloc(&D.row_stamp, D.row_cap, o)) || (rc = dalloc(&D.row_bslot, D.row_cap, o)) ||
       (rc = dalloc(&D.row_key, D.row_cap, o)) || (rc = dalloc(&D.row_bt, D.row_cap, o)) ||
       (rc = dalloc(&D.row_bruq, D.row_cap, o)) ||
-      (rc = dalloc(&D.ctr, CTR_COUNT, o)) || (rc = dalloc(&D.err, 1, o)) || (rc = dalloc(&D.stat, STAT_COUNT, o))) {
+      (rc = dalloc(&D.ctr, CTR_COUNT, o)) || (rc = dalloc(&D.err, 1, o)) || (rc = dalloc(&D.stat, STAT_COUNT, o)) ||
+      (K.easm && ((rc = dalloc(&D.temp, N, o)) || (rc = dalloc(&D.a_vh, acap, o))))) {
     cafe_sim_destroy(s);
     return rc;
   }
@@ -772,6 +832,7 @@ int cafe_sim_create(const char *deck_path, const cafe_options *opt, cafe_sim **o
   cudaMemsetAsync(D.cz, 0, N * sizeof(double), s->stream);
   cudaMemsetAsync(D.buildj, 0, N, s->stream);
   cudaMemsetAsync(D.build, 0, N, s->stream);
+  if (K.easm) cudaMemsetAsync(D.temp, 0, N * sizeof(double), s->stream);
   cudaMemsetAsync(D.pos_of, 0xff, N * sizeof(int32_t), s->stream);
   cudaMemsetAsync(D.ctr, 0, CTR_COUNT * sizeof(int), s->stream);
   cudaMemsetAsync(D.err, 0, sizeof(int), s->stream);
@@ -936,6 +997,10 @@ int cafe_sim_temperature(cafe_sim *s) {
     return fail(CAFE_E_STATE, "laser index %d outside the scan grid", g.isp);
   make_step_params(s, s->P);
   s->have_P = true;
+  if (s->K.easm) {
+    int rc = easm_field(s);
+    if (rc) return rc;
+  }
   const CafeStepParams &P = s->P;
   CUDA_TRY(cudaMemsetAsync(s->D.ctr + CTR_HOT, 0, sizeof(int), s->stream));
   long long nbox = (long long)(P.hi[0] - P.lo[0]) * (P.hi[1] - P.lo[1]) * (P.hi[2] - P.lo[2]);
@@ -954,7 +1019,10 @@ int cafe_sim_temperature(cafe_sim *s) {
   }
   if (nbox > 0) {
     PhaseScope ps(s, CAFE_PH_MELT);
-    k_melt<<<grid_blocks(nbox, 256, s), 256, 0, s->stream>>>(s->D, s->K, P);
+    if (s->K.easm)
+      k_melt_easm<<<grid_blocks(nbox, 256, s), 256, 0, s->stream>>>(s->D, s->K, P);
+    else
+      k_melt<<<grid_blocks(nbox, 256, s), 256, 0, s->stream>>>(s->D, s->K, P);
     LAUNCHED(CAFE_PH_MELT, 1);
   }
   CUDA_TRY(cudaGetLastError());
@@ -964,8 +1032,14 @@ int cafe_sim_temperature(cafe_sim *s) {
   double y = g.lcoor2[2 * isv[g.isp] + 1] - g.offset[1];
   if (x < g.gbox[0] || x > g.gbox[1] || y < g.gbox[2] || y > g.gbox[3]) {
     int hot = 0;
-    int rc = read_ctr(s, CTR_HOT, &hot);
-    if (rc) return rc;
+    if (s->K.easm) {
+      // TempField::EASM asks all_of(T >= tL) (TempField.C:123-125); cells
+      // above the laser plane hold T = 0
+      hot = (P.kabove >= g.nX[2] && !s->easm_cold) ? 1 : 0;
+    } else {
+      int rc = read_ctr(s, CTR_HOT, &hot);
+      if (rc) return rc;
+    }
     if (hot == 0 || std::fmod(g.isp + 1, g.Nsd) == 0) g.inewscanflg = 1;
     if (g.isp == g.NpT - 1) {
       g.inewscanflg = 1;
@@ -1017,7 +1091,10 @@ int cafe_sim_update_voxels(cafe_sim *s) {
     k_lists_count<<<nbp, CAFE_DENSE_THREADS, 0, st>>>(D);
     k_scan_pairs<<<1, 1024, 0, st>>>(D.blk, s->nblk_pos, D.ctr + CTR_NA, D.ctr + CTR_NVS2, D.ctr + CTR_NROWS);
     k_lists_scatter<<<nbp, CAFE_DENSE_THREADS, 0, st>>>(D);
-    CUDA_TRY(cudaMemsetAsync(D.ctr + CTR_SLOW, 0, sizeof(int), st));
+    if (K.easm)  // rows grow with per-cell velocities: the exact per-event scan
+      k_set_int<<<1, 1, 0, st>>>(D.ctr + CTR_SLOW, 1);
+    else
+      CUDA_TRY(cudaMemsetAsync(D.ctr + CTR_SLOW, 0, sizeof(int), st));
     CUDA_TRY(cudaMemsetAsync(D.ctr + CTR_NPAIRS, 0, sizeof(int), st));
     k_rows_prep<<<s->nsm * 4, 256, 0, st>>>(D, K);
     k_rows_geo<<<s->nsm * 8, 256, 0, st>>>(D, K);
@@ -1308,6 +1385,11 @@ int cafe_sim_download_temperature(cafe_sim *s, double *temp) {
     for (long long i = 0; i < N; ++i) temp[i] = 0.0;
     return CAFE_OK;
   }
+  if (s->K.easm) {
+    CUDA_TRY(cudaMemcpyAsync(temp, s->D.temp, N * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    return CAFE_OK;
+  }
   double *d;
   CUDA_TRY(cudaMalloc((void **)&d, N * sizeof(double)));
   k_temperature<<<grid_blocks(N, 256, s), 256, 0, s->stream>>>(s->K, s->P, d);
@@ -1480,7 +1562,9 @@ struct OutputSource {
     cudaStream_t st = s->stream;
     int nb = grid_blocks(n, 256, s);
     if (which == 0) {
-      if (s->have_P)
+      if (s->K.easm)
+        k_temp_copy_f<<<nb, 256, 0, st>>>(s->D.temp, off, n, (float *)s->xfer);
+      else if (s->have_P)
         k_temperature_f<<<nb, 256, 0, st>>>(s->K, s->P, off, n, (float *)s->xfer);
       else
         CUDA_TRY(cudaMemsetAsync(s->xfer, 0, n * sizeof(float), st));

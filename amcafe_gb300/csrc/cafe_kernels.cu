@@ -44,6 +44,12 @@ __device__ __forceinline__ long long cafe_clock_ordered() {
 #endif
 
 // ------------------------------------------------------------------ helpers
+// Growth velocity of active position p (VoxelsCA.C:405): per temperature class
+// with the analytic field, per cell with the EASM field.
+__device__ __forceinline__ double cafe_vh(const CafeDev &D, const CafeConsts &K, int p) {
+  return K.easm ? D.a_vh[p] : K.vhat_cls[D.a_cls[p]];
+}
+
 __device__ __forceinline__ int cafe_hot(const CafeDev &D, const CafeConsts &K, const CafeStepParams &P,
                                         int i, int j, int k) {
   return K.hot_cls[cafe_cls(D, P, i, j, k)];
@@ -332,6 +338,11 @@ __global__ void k_gather(CafeDev D, CafeConsts K, CafeStepParams P) {
     D.a_cy[p] = D.cy[idx];
     D.a_cz[p] = D.cz[idx];
     D.a_cls[p] = (uint8_t)cafe_cls(D, P, i, j, k);
+    if (K.easm) {
+      // VoxelsCA.C:405: T >= tL ? 0 : Avel pow(tL - T, nvel)
+      double T = D.temp[idx];
+      D.a_vh[p] = T >= K.tL ? 0.0 : K.Avel * crm_pow_int(K.tL - T, K.nvel_i);
+    }
     long long nb[26];
     int n = cafe_moore(K, i, j, k, nb);
     int m = 0, liq = 0, cold = 1;
@@ -584,7 +595,7 @@ __device__ unsigned long long cafe_row_finish_warp(const CafeDev &D, const CafeC
         ruqs = ruqs_pre;
       } else {
         double E = D.a_ext[p];
-        double v = K.vhat_cls[D.a_cls[p]];
+        double v = cafe_vh(D, K, p);
         double dr = gv - E;
         t = dr / v;
         ruqs = .5 * (D.a_ruq[p] + D.a_ruq[q]);
@@ -697,7 +708,7 @@ __device__ unsigned long long cafe_row_fill_quad(const CafeDev &D, const CafeCon
       if (w == 2) {
         if (eval) {
           E2 = D.a_ext[p];
-          v2 = K.vhat_cls[D.a_cls[p]];
+          v2 = cafe_vh(D, K, p);
         }
         cafe_geo_edge(loc, pk[0], pk[1], &S.d1I[lane], &S.dI2[lane]);
       } else {
@@ -816,7 +827,7 @@ __device__ __forceinline__ void cafe_row_best_live(const CafeDev &D, const CafeC
   int p = D.row_pos[r];
   if (!live) return;
   double E = D.row_E[r];
-  double v = K.vhat_cls[D.a_cls[p]];
+  double v = cafe_vh(D, K, p);
   long long vb = crm_bits(v);
   bool mono = vb > 0 && vb < CRM_BITS_INF;  // 0 < v < inf
   const double *g = D.row_g + r * CAFE_NSLOT;
@@ -1565,7 +1576,7 @@ __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
         for (int r = tid; r < s_nrows; r += nthr) {
           if (!D.row_alive[r]) continue;
           int p = D.row_pos[r];
-          double e = D.row_E[r] + K.vhat_cls[D.a_cls[p]] * d;
+          double e = D.row_E[r] + cafe_vh(D, K, p) * d;
           D.row_E[r] = (e < 0.0) ? 0.0 : e;
         }
       } else {
@@ -1574,7 +1585,7 @@ __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
         for (int j = tid; j < s_countS; j += nthr) {
           int p = D.vs2[j];
           int r = D.a_frow[p];
-          double v = (r >= 0 && D.row_alive[r]) ? K.vhat_cls[D.a_cls[p]] : 0.0;
+          double v = (r >= 0 && D.row_alive[r]) ? cafe_vh(D, K, p) : 0.0;
           double *ep = r >= 0 ? &D.row_E[r] : &D.a_ext[p];
           double e = *ep + v * d;
           *ep = (e < 0.0) ? 0.0 : e;
@@ -2106,4 +2117,165 @@ __global__ void k_temperature_f(CafeConsts K, CafeStepParams P, long long off, l
 __global__ void k_build_i32(CafeDev D, long long off, long long n, int32_t *out) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
     out[i] = D.build[off + i];
+}
+
+// ------------------------------------------------------------------ EASM
+// TempField::EASM (TempField.C:79-137): per cell below the laser plane the
+// damped fixed point of Utilities::EASM_Temp_LG (Utilities.C:128-140) on
+// Utilities::Integral (Utilities.C:105-124) = 300 + sum_i w_i f(x_i), f the
+// moving-Gaussian-source kernel Temp_Fun_G (Utilities.C:228-249) with the 316L
+// properties at the iterate (Utilities.C:39-76). Expressions keep the
+// reference's order; pow(x, 2) is x*x, pow(t - x, -0.5) and exp are the
+// correctly rounded functions of cafe_crmath.h.
+__device__ __forceinline__ void cafe_easm_materials(double T, double M[4]) {
+  double rho, cP, k;
+  if (T < 1660)
+    rho = 8084.2 - 0.42086 * T - 3.8942 * 1e-5 * T * T;
+  else if (T >= 1660 && T < 3090)
+    rho = 7432.7 + 3.9338 * 1e-2 * T - 1.8007 * 1e-4 * T * T;
+  else
+    rho = 6124.72;
+  if (T < 1660)
+    cP = 458.984 + 0.1328 * T;
+  else
+    cP = 769.855;
+  if (T < 1660)
+    k = 9.248 + 1.571 * 1e-2 * T;
+  else if (T >= 1660 && T < 3090)
+    k = 12.41 + 3.279 * 1e-3 * T;
+  else
+    k = 21.6465;
+  M[0] = cP;
+  M[1] = k;
+  M[2] = rho;
+  M[3] = k / (rho * cP);
+}
+__device__ __forceinline__ double cafe_easm_integral(const CafeEasm &E, const double *Lx, double R0, double R1,
+                                                     double R2, double Ly, double Lz, double T) {
+  const double sigma = 50.0e-6, eta = 0.56, pi = 3.14159265358979323846;
+  double M[4];
+  cafe_easm_materials(T, M);
+  double C = eta * E.Q / (pi * M[2] * M[0] * sqrt(4 * pi * M[3]));
+  double sig2 = sigma * sigma;
+  double dy = R1 - Ly, dz = fabs(R2 - Lz);
+  double dy2 = dy * dy, dz2 = dz * dz;
+  double s = 0.0;
+  for (int i = 0; i < CAFE_EASM_NODES; ++i) {
+    double tx = E.tx[i];
+    double dx = R0 - Lx[i];
+    double a = C * E.r[i] / (2 * M[3] * tx + sig2);
+    double arg = -1 * (dx * dx + dy2) / (4 * M[3] * tx + 2 * sig2) - dz2 / (4 * M[3] * tx);
+    // exp(arg) is exactly 0 below -745.2, and so is this term
+    double f = arg < -745.2 ? a * 0.0 : a * crm_exp(arg);
+    s += E.qw[i] * f;
+  }
+  return 300 + s;
+}
+__global__ void k_set_int(int *p, int v) { *p = v; }
+__global__ void k_easm_reset(CafeDev D) {
+  int t = threadIdx.x;
+  if (t < 3) D.ctr[CTR_EASM_BOX + t] = 0x7fffffff;
+  else if (t < 6) D.ctr[CTR_EASM_BOX + t] = -1;
+  else if (t == 6) D.ctr[CTR_EASM_COLD] = 0;
+}
+// Cells [0, ncell) (cells above the laser plane keep T = 0). Writes temp,
+// BuildjID, the box of the cells at or above the liquidus and the "some cell
+// below the liquidus" flag.
+__global__ void k_easm(CafeDev D, CafeConsts K, CafeStepParams P, CafeEasm E, long long ncell) {
+  __shared__ double s_Lx[CAFE_EASM_NODES];
+  __shared__ int s_box[6], s_cold;
+  const double t = 80.0e-5;
+  if (threadIdx.x < CAFE_EASM_NODES) {
+    double x0 = P.lx - E.bmV * t;  // Utilities.C:243-244
+    s_Lx[threadIdx.x] = x0 + E.bmV * E.qx[threadIdx.x];
+  }
+  if (threadIdx.x < 3) {
+    s_box[threadIdx.x] = 0x7fffffff;
+    s_box[3 + threadIdx.x] = -1;
+  }
+  if (threadIdx.x == 0) s_cold = 0;
+  __syncthreads();
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < ncell;
+       idx += (long long)gridDim.x * blockDim.x) {
+    int i, j, k;
+    cafe_cell_xyz(K, idx, i, j, k);
+    double x0 = ((double)i + .5) * K.dx[0];
+    double y0 = ((double)j + .5) * K.dx[1];
+    double zp = ((double)k + .5) * K.dx[2];
+    if (zp > P.lz) continue;
+    double xp = P.cg * (x0 - K.hLX0) + P.sg * (y0 - K.hLX1) + K.hLX0;
+    double yp = -P.sg * (x0 - K.hLX0) + P.cg * (y0 - K.hLX1) + K.hLX1;
+    double T;
+    if ((x0 > P.lx) && (zp > (P.lz - E.layerT))) {
+      T = .99 * K.T0;
+    } else {
+      double Told = 0.0;
+      double Tnew = cafe_easm_integral(E, s_Lx, xp, yp, zp, P.ly, P.lz, 0.0);
+      int n = 0;
+      while (fabs(Told - Tnew) > 10.0 && n < 100) {
+        Told = Tnew;
+        double Tt = cafe_easm_integral(E, s_Lx, xp, yp, zp, P.ly, P.lz, Told);
+        Tnew = 0.5 * (Told + Tt);
+        n++;
+      }
+      T = Tnew;
+    }
+    D.temp[idx] = T;
+    if (T > K.tL)
+      D.buildj[idx] = 1;
+    else if (T < K.T0)
+      D.buildj[idx] = 0;
+    if (T >= K.tL) {
+      atomicMin(&s_box[0], i);
+      atomicMin(&s_box[1], j);
+      atomicMin(&s_box[2], k);
+      atomicMax(&s_box[3], i);
+      atomicMax(&s_box[4], j);
+      atomicMax(&s_box[5], k);
+    } else {
+      s_cold = 1;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x < 3 && s_box[3 + threadIdx.x] >= 0) {
+    atomicMin(&D.ctr[CTR_EASM_BOX + threadIdx.x], s_box[threadIdx.x]);
+    atomicMax(&D.ctr[CTR_EASM_BOX + 3 + threadIdx.x], s_box[3 + threadIdx.x]);
+  }
+  if (threadIdx.x == 0 && s_cold) D.ctr[CTR_EASM_COLD] = 1;
+}
+// SetLiquid3 (VoxelsCA.C:1098-1116) and the class map over the box of the
+// cells at or above the liquidus, from the EASM temperatures.
+__global__ void k_melt_easm(CafeDev D, CafeConsts K, CafeStepParams P) {
+  int bx = P.hi[0] - P.lo[0], by = P.hi[1] - P.lo[1], bz = P.hi[2] - P.lo[2];
+  long long nbox = (long long)bx * by * bz;
+  long long iz1 = (long long)P.ilaserLoc * K.nxy;
+  int any = 0;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < nbox;
+       t += (long long)gridDim.x * blockDim.x) {
+    int i = P.lo[0] + (int)(t % bx);
+    long long r = t / bx;
+    int j = P.lo[1] + (int)(r % by);
+    int k = P.lo[2] + (int)(r / by);
+    long long idx = (long long)K.nxy * k + (long long)K.nx * j + i;
+    double zp = ((double)k + .5) * K.dx[2];
+    double T = D.temp[idx];
+    int c = zp > P.lz ? 0 : (T >= K.tL ? 2 : 1);
+    D.tcls[t] = (uint8_t)c;
+    if (c == 2) {
+      any = 1;
+      if (idx < K.nxy) {
+        D.state[idx] = 2;
+      } else if (idx < iz1) {
+        D.state[idx] = 1;
+        D.gid[idx] = 0;
+      }
+      D.ext[idx] = 0.0;
+    }
+  }
+  if (__syncthreads_or(any) && threadIdx.x == 0) atomicOr(&D.ctr[CTR_HOT], 1);
+}
+// Temperatures of cells [off, off+n) as float (output) from the EASM field.
+__global__ void k_temp_copy_f(const double *T, long long off, long long n, float *out) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    out[i] = (float)T[off + i];
 }

@@ -1163,7 +1163,13 @@ static void update_voxels(State &S) {
       if (!(T[nid[t]] < tL)) cold[p] = 0;
     }
   // per-position growth velocity (VoxelsCA.C:405)
-  auto vhat_of = [&](int p) { return T[p] >= tL ? 0.0 : g.Avel * std::pow(tL - T[p], g.nvel); };
+  // (the device evaluates the per-cell velocities of the EASM field as
+  // correctly rounded integer powers)
+  const bool cr_pow = g_libm.mode == 1 && g.EASM_Flag == 1 && g.nvel >= 1 && g.nvel <= 64 && g.nvel == (int)g.nvel;
+  auto vhat_of = [&](int p) {
+    if (T[p] >= tL) return 0.0;
+    return g.Avel * (cr_pow ? crm_pow_int(tL - T[p], (int)g.nvel) : std::pow(tL - T[p], g.nvel));
+  };
   // frontier: indices j into vs2ind with a liquid neighbour and all-cold neighbours
   std::vector<int> fr;
   for (int j = 0; j < vSind2; ++j)

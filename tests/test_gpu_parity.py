@@ -75,6 +75,15 @@ def test_gpu_matches_oracle(tmp_path, deck, nsteps, stride):
     print("%s: max float rel diff %g, %s" % (deck, worst, stats))
 
 
+@pytest.mark.parametrize("deck", ["track_easm.in", "track_easm60.in"])
+def test_gpu_easm_matches_oracle(tmp_path, deck):
+    """EASM temperature (keyword easm): per-cell temperatures and velocities,
+    rows evaluated with the exact per-event scan."""
+    worst, stats = run_and_compare(deck, 0, 1, tmp_path)
+    assert stats["exact_scan_steps"] == stats["steps"]
+    print("%s: max float rel diff %g, %s" % (deck, worst, stats))
+
+
 @pytest.mark.parametrize("deck,nsteps,stride", [("track_nuc.in", 0, 1), ("layers_rot.in", 0, 20)])
 def test_gpu_full_scan_matches_oracle(tmp_path, deck, nsteps, stride):
     """The reference's per-event scan of every frontier cell (event_scan=1)."""
