@@ -20,6 +20,8 @@ EXPORTS = (
     "cafe_sim_upload_state", "cafe_last_error", "cafe_sim_set_timing", "cafe_sim_phase_times",
     "cafe_sim_stream", "cafe_sim_mark", "cafe_sim_elapsed", "cafe_clean_layer_noalloc",
     "cafe_sim_set_build", "cafe_sim_download_build", "cafe_sim_download_output", "cafe_sim_write_output",
+    "cafe_batch_create", "cafe_batch_run", "cafe_batch_size", "cafe_batch_sim", "cafe_batch_finished",
+    "cafe_batch_destroy",
 )
 PHASES = ("melt", "classify", "gather", "events", "writeback", "layer")
 NPHASE = 8
@@ -96,6 +98,13 @@ def load():
         "cafe_sim_download_build": (I, [P, i32p]),
         "cafe_sim_download_output": (I, [P, f32p, f32p, f32p, f32p]),
         "cafe_sim_write_output": (I, [P, ctypes.c_char_p]),
+        "cafe_batch_create": (I, [ctypes.POINTER(ctypes.c_char_p), I, ctypes.POINTER(CafeOptions), I,
+                                  ctypes.POINTER(P)]),
+        "cafe_batch_run": (I, [P, LL, ctypes.POINTER(LL)]),
+        "cafe_batch_size": (I, [P]),
+        "cafe_batch_sim": (P, [P, I]),
+        "cafe_batch_finished": (I, [P, I]),
+        "cafe_batch_destroy": (None, [P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

@@ -33,11 +33,15 @@ def _ptr(a, ct):
 
 
 class Simulation:
-    def __init__(self, deck, device=0, active_capacity=0, grain_capacity=0, event_scan=0):
+    def __init__(self, deck, device=0, active_capacity=0, grain_capacity=0, event_scan=0, _handle=None):
         self._lib = load()
-        self._h = ctypes.c_void_p()
-        opt = CafeOptions(device, active_capacity, grain_capacity, event_scan)
-        check(self._lib.cafe_sim_create(str(deck).encode(), ctypes.byref(opt), ctypes.byref(self._h)))
+        self._owned = _handle is None
+        if _handle is not None:  # a realisation owned by a Batch
+            self._h = ctypes.c_void_p(_handle)
+        else:
+            self._h = ctypes.c_void_p()
+            opt = CafeOptions(device, active_capacity, grain_capacity, event_scan)
+            check(self._lib.cafe_sim_create(str(deck).encode(), ctypes.byref(opt), ctypes.byref(self._h)))
         inf = self.info()
         self.shape = (inf["nz"], inf["ny"], inf["nx"])
         self.ncell = inf["nx"] * inf["ny"] * inf["nz"]
@@ -187,9 +191,9 @@ class Simulation:
         return p.value or 0
 
     def close(self):
-        if self._h:
+        if self._h and self._owned:
             self._lib.cafe_sim_destroy(self._h)
-            self._h = ctypes.c_void_p()
+        self._h = ctypes.c_void_p()
 
     def __del__(self):
         try:
@@ -211,3 +215,45 @@ def run_deck(deck, max_steps=0, device=0, **kw):
     sim.begin()
     sim.run(max_steps)
     return sim
+
+
+class Batch:
+    """Independent realisations (one deck each) stepped concurrently on one GPU
+    (cafe_batch_*). `sims[i]` reads realisation i like a Simulation."""
+
+    def __init__(self, decks, device=0, threads=0, active_capacity=0, grain_capacity=0, event_scan=0):
+        self._lib = load()
+        self._h = ctypes.c_void_p()
+        arr = (ctypes.c_char_p * len(decks))(*[str(d).encode() for d in decks])
+        opt = CafeOptions(device, active_capacity, grain_capacity, event_scan)
+        check(self._lib.cafe_batch_create(arr, len(decks), ctypes.byref(opt), int(threads), ctypes.byref(self._h)))
+        self.sims = [Simulation(None, _handle=self._lib.cafe_batch_sim(self._h, i)) for i in range(len(decks))]
+
+    def run(self, max_steps=0):
+        """Runs every realisation's loop to its end (or max_steps iterations
+        each); returns the loop iterations of all realisations."""
+        n = ctypes.c_longlong(0)
+        check(self._lib.cafe_batch_run(self._h, int(max_steps), ctypes.byref(n)))
+        return n.value
+
+    def finished(self, i):
+        return self._lib.cafe_batch_finished(self._h, i) == 1
+
+    def close(self):
+        if self._h:
+            for s in self.sims:
+                s._h = ctypes.c_void_p()
+            self._lib.cafe_batch_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()

@@ -52,6 +52,7 @@ int fail(int code, const char *fmt, ...) {
   } while (0)
 
 const int kSeed0 = 2132512, kSeed1 = 2912351;  // VoxelsCA.C:47-48
+const unsigned int kSeedStride = 10000019u;     // per-realisation seed offset (keyword "seed")
 
 // ------------------------------------------------------------------ Grid
 struct GridH {
@@ -59,6 +60,7 @@ struct GridH {
   double dX[3] = {1e-6, 1e-6, 1e-6};
   int outint = 1, patternID = 1, outNL = 0;
   int EASM_Flag = 0;  // Grid::EASM_Flag (keyword "easm", see parse_deck)
+  int seed = 1;       // extension keyword "seed" (1: the reference's seeds)
   double tL = 1620, tS = 1531.5, T0 = 300, layerT = 25e-6, bpH = 0.0, mu = .01, lrate = 0;
   double meltparam[4] = {75e-6, 162.75e-6, 75e-6, 75e-6};
   double bhatch = 0, bmDelT = 0, bmV = 500e-3, bmP = 0, rNmax = .002;
@@ -136,6 +138,10 @@ int parse_deck(const char *path, GridH &g) {
     // Grid.C:276 compares the lowercased keyword with "EASM", which never
     // matches; "easm 1" sets the flag that keyword was meant to set.
     else if (key == "easm") ok = inum(g.EASM_Flag);
+    // extension: realisation seed s >= 1; offsets VoxelsCA's seed0/seed1
+    // (VoxelsCA.C:47-48) by (s - 1) * kSeedStride and seeds the BasePlate
+    // engine (BasePlate.h:28, default seed 1) with s, so s = 1 is the reference
+    else if (key == "seed") ok = inum(g.seed) && g.seed >= 1;
     if (!ok) return fail(CAFE_E_ARG, "deck '%s': bad value after keyword '%s'", path, key.c_str());
     in >> kw;
   }
@@ -696,7 +702,10 @@ int cafe_sim_create(const char *deck_path, const cafe_options *opt, cafe_sim **o
   // BasePlate (BasePlate.C:20-30), main1.C:59
   s->Nzh = std::min(g.nX[2], int(std::ceil(g.bpH * .9999 / g.dX[2])));
   s->nlayerTot = int(std::ceil((double)(g.nX[2] - s->Nzh) / (double)g.nZlayer));
-  s->genlayer.seed(kSeed1);
+  const unsigned int seed0 = (unsigned int)kSeed0 + (unsigned int)(g.seed - 1) * kSeedStride;
+  const unsigned int seed1 = (unsigned int)kSeed1 + (unsigned int)(g.seed - 1) * kSeedStride;
+  s->genlayer.seed(seed1);
+  s->bp_generator.seed((unsigned int)g.seed);
   // constants
   CafeConsts &K = s->K;
   K.nx = g.nX[0];
@@ -752,8 +761,8 @@ int cafe_sim_create(const char *deck_path, const cafe_options *opt, cafe_sim **o
   K.rX = g.rNmax * std::pow(g.dX[0] * 1e6, 3.);
   K.DelT = s->DelT;
   K.ruq_dx = g.dX[0];
-  K.seed0 = (unsigned int)kSeed0;
-  K.seed1 = (unsigned int)kSeed1;
+  K.seed0 = seed0;
+  K.seed1 = seed1;
   OrientConsts oc = orient_consts();
   K.so_R1 = oc.R1;
   K.so_a = oc.a;

@@ -174,6 +174,26 @@ int cafe_sim_download_output(cafe_sim *sim, float *temperature, float *ipfz, flo
  * <base><tInd>.h5 corresponds to prefix "<base><tInd>.h5". */
 int cafe_sim_write_output(cafe_sim *sim, const char *prefix);
 
+/* Batched ensemble (no counterpart in the reference, which runs one
+ * realisation per MPI job): n independent realisations, one deck each, on
+ * one device. Each is a cafe_sim handle with its own stream; `threads` host
+ * threads (0: up to 16, one per hardware thread) step them round-robin so
+ * that their device work overlaps. Every realisation runs exactly the calls of
+ * a plain run (initialize_voxels, begin, step until done, the closing
+ * clean_layer), so its results are bit-identical to its plain run. */
+typedef struct cafe_batch cafe_batch;
+int cafe_batch_create(const char *const *decks, int n, const cafe_options *opt, int threads, cafe_batch **out);
+/* Initialises every realisation that is new and runs each loop to its end, or
+ * to max_steps (> 0) iterations per realisation; *steps_done (may be NULL)
+ * gets the loop iterations of all realisations. Returns the first error. */
+int cafe_batch_run(cafe_batch *b, long long max_steps, long long *steps_done);
+int cafe_batch_size(const cafe_batch *b);
+/* The i-th realisation's handle (owned by the batch), NULL if out of range. */
+cafe_sim *cafe_batch_sim(cafe_batch *b, int i);
+/* 1 when realisation i has finished its loop (closing CleanLayer applied). */
+int cafe_batch_finished(const cafe_batch *b, int i);
+void cafe_batch_destroy(cafe_batch *b);
+
 /* Allocation-free CleanLayer renumbering on caller-owned device arrays. No
  * counterpart in the reference: it serves callers that cannot go to the CUDA
  * allocator mid-run (device memory owned by their own pool, or no tolerance

@@ -113,6 +113,7 @@ struct Grid {
   int nX[3] = {128, 128, 64};
   double dX[3] = {1e-6, 1e-6, 1e-6};
   int outint = 1, patternID = 1, outNL = 0, nTsd = 0, EASM_Flag = 0;
+  int seed = 1;  // extension keyword "seed" (1: the reference's seeds)
   double tL = 1620, tS = 1531.5, T0 = 300, layerT = 25e-6, bpH = 0.0, mu = .01;
   double lrate = 0.0;
   bool have_lrate = false, have_bmdelt = false;
@@ -214,6 +215,7 @@ static bool read_deck(const char *path, Grid &g, std::string &err) {
         next_d(g.gsize[1]);
       }
       if (kw == "gridtheta") next_d(g.gth0);
+      if (kw == "seed") next_i(g.seed);
       if (kw == "dendritegrowth2") {
         next_d(g.Avel);
         next_d(g.nvel);
@@ -525,8 +527,13 @@ static int site_grid_nearest(const SiteGrid &G, const double q[3], Dist dist) {
 }
 
 // ---------------------------------------------------------------- CA state
-// Hard-coded seeds of the reference (VoxelsCA.C:47-49).
+// Hard-coded seeds of the reference (VoxelsCA.C:47-49). The extension keyword
+// "seed s" offsets both by (s - 1) * kSeedStride and seeds the baseplate
+// engine with s (its default seed is 1), so s = 1 is the reference.
 static const int kSeed0 = 2132512, kSeed1 = 2912351;
+static const unsigned int kSeedStride = 10000019u;
+static unsigned int seed0_of(const Grid &g) { return (unsigned int)kSeed0 + (unsigned int)(g.seed - 1) * kSeedStride; }
+static unsigned int seed1_of(const Grid &g) { return (unsigned int)kSeed1 + (unsigned int)(g.seed - 1) * kSeedStride; }
 struct State {
   Grid g;
   int N = 0, nx = 0, ny = 0, nz = 0, nxy = 0;
@@ -575,7 +582,7 @@ static void init_baseplate(State &S) {
   Grid &g = S.g;
   S.Nzh = std::min(g.nX[2], int(std::ceil(g.bpH * .9999 / g.dX[2])));
   double height = S.Nzh * (g.dX[2]);
-  std::default_random_engine generator;  // BasePlate.h:28, default seed
+  std::default_random_engine generator((unsigned int)g.seed);  // BasePlate.h:28 (default seed 1)
   double rate = g.mu * (g.dX[0] * 1e6) * (g.dX[1] * 1e6) * g.nX[0] * g.nX[1] * (height * 1e6);
   std::poisson_distribution<int> ng(rate);
   int Ngrain = 0;
@@ -1143,8 +1150,8 @@ static void update_voxels(State &S) {
     }
     nptr[Na] = (int)nid.size();
   }
-  unsigned int sdloc = kSeed0 + 32 * g.tInd + 64 * S.nGrain;
-  std::default_random_engine g1(30 * g.tInd + kSeed1);
+  unsigned int sdloc = seed0_of(g) + 32 * g.tInd + 64 * S.nGrain;
+  std::default_random_engine g1(30 * g.tInd + seed1_of(g));
   std::uniform_real_distribution<double> xrand1(0.0, 1.0);
   double rX = g.rNmax * std::pow(g.dX[0] * 1e6, 3.);
   std::vector<int> vs2ind;
@@ -1495,7 +1502,7 @@ static int setup(State &S, const char *deck) {
   S.extents.assign(S.N, 0.0);
   S.cen.assign(3 * (size_t)S.N, 0.0);
   S.temp.assign(S.N, 0.0);
-  S.genlayer.seed(kSeed1);
+  S.genlayer.seed(seed1_of(S.g));
   init_tempfield(S);
   init_baseplate(S);
   // every baseplate cell with a grain starts as Build (VoxelsCA.C:156-159)

@@ -31,3 +31,23 @@ def test_error_reporting_without_gpu():
     rc = lib.cafe_sim_create(b"/nonexistent/deck.in", None, ctypes.byref(h))
     assert rc == 5  # CAFE_E_IO
     assert b"cannot open deck" in lib.cafe_last_error()
+
+
+def test_rosenthal_pool_sizes_the_config_decks():
+    """The Rosenthal sizer reproduces the meltparam of the config 0 and 2 decks."""
+    from amcafe_gb300.rosenthal import pool
+
+    for P, v, want in ((200.0, 1.0, (16.31e-6, 425.5e-6, 55.11e-6)), (200.0, 0.8, (19.32e-6, 425.5e-6, 61.39e-6))):
+        f, r, w, d = pool(P, v)
+        assert abs(f - want[0]) < 0.01e-6 and abs(r - want[1]) < 0.1e-6 and abs(w - want[2]) < 0.01e-6 and w == d
+
+
+def test_ensemble_decks_are_deterministic(tmp_path):
+    from amcafe_gb300.ensemble import make_decks
+
+    a = make_decks(str(tmp_path / "a"), n=4)
+    b = make_decks(str(tmp_path / "b"), n=4)
+    for x, y in zip(a, b):
+        assert open(x).read() == open(y).read()
+    txt = open(a[2]).read()
+    assert "seed 3" in txt and "nX " in txt

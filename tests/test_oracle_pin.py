@@ -31,11 +31,11 @@ def _rel(a, b):
     return 0.0 if a == b else abs(a - b) / max(abs(b), 1e-300)
 
 
-def _check(name, libm, tmp_path, check_floats):
+def _check(name, libm, tmp_path, check_floats, deck=None):
     g = np.load(os.path.join(HERE, "golden", name + ".npz"))
     nsteps, stride = int(g["nsteps"]), int(g["stride"])
     dump = str(tmp_path / (name + ".bin"))
-    orc.run(os.path.join(HERE, "golden", "decks", name + ".in"), dump, max_steps=nsteps, dump_stride=stride,
+    orc.run(deck or os.path.join(HERE, "golden", "decks", name + ".in"), dump, max_steps=nsteps, dump_stride=stride,
             libm=libm)
     recs = orc.read_dump(dump)
     assert len(recs) == len(g["index"]), "%s: %d records vs %d in the fixture" % (name, len(recs), len(g["index"]))
@@ -92,3 +92,11 @@ def test_oracle_output_matches_reference(libm, tmp_path):
             path = out / k.split("/", 1)[1]
             assert path.exists(), k
             assert hashlib.sha256(path.read_bytes()).hexdigest() == str(d[k]), k
+
+
+def test_seed_one_is_the_reference(tmp_path):
+    """The extension keyword "seed" with s = 1 leaves the reference's seeds."""
+    deck = tmp_path / "track_nuc_s1.in"
+    with open(os.path.join(HERE, "golden", "decks", "track_nuc.in")) as f:
+        deck.write_text(f.read() + "seed 1\n")
+    _check("track_nuc", orc.LIBM_GLIBC, tmp_path, check_floats=True, deck=str(deck))
