@@ -49,7 +49,8 @@ class CafeStats(ctypes.Structure):
                 ("sum_active", ctypes.c_ulonglong), ("sum_rows", ctypes.c_ulonglong),
                 ("launches", ctypes.c_ulonglong), ("exact_scan_steps", ctypes.c_ulonglong),
                 ("row_evaluations", ctypes.c_ulonglong), ("cycles_select", ctypes.c_ulonglong),
-                ("cycles_apply", ctypes.c_ulonglong), ("cycles_fill", ctypes.c_ulonglong)]
+                ("cycles_apply", ctypes.c_ulonglong), ("cycles_fill", ctypes.c_ulonglong),
+                ("graph_captures", ctypes.c_ulonglong)]
 
 
 _lib = None

@@ -5,10 +5,11 @@
 // different realisations overlaps on the device: the capture/nucleation loop
 // of each step is one thread block, and a batch keeps one such block per
 // realisation in flight at once instead of one for the whole GPU. Host threads
-// (each owning every T-th realisation) issue the steps round-robin; each
-// realisation runs the same calls in the same order as a plain run
-// (cafe_sim_initialize_voxels, cafe_sim_begin, cafe_sim_step until done, the
-// closing cafe_sim_clean_layer), so its results are those of its plain run.
+// (one by default; each owning every T-th realisation) issue the steps
+// round-robin, one step (one CUDA graph launch) per realisation and turn; each
+// realisation runs the same loop as a plain run (cafe_sim_initialize_voxels,
+// cafe_sim_begin, the loop iterations until done, the closing
+// cafe_sim_clean_layer), so its results are those of its plain run.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -19,6 +20,8 @@
 #include "../../include/cafe_gpu.h"
 
 void cafe_internal_set_error(const char *msg);
+void cafe_internal_set_share(cafe_sim *s, int share, int graphs);
+int cafe_internal_advance(cafe_sim *s, int max_k, int *ran, int *done);
 
 struct cafe_batch {
   std::vector<cafe_sim *> sims;
@@ -49,9 +52,11 @@ int cafe_batch_create(const char *const *decks, int n, const cafe_options *opt, 
   }
   b->steps.assign(n, 0);
   b->phase.assign(n, 0);
-  unsigned hc = std::thread::hardware_concurrency();
-  int t = threads > 0 ? threads : (int)std::max(1u, std::min(hc ? hc : 1u, 16u));
-  b->threads = std::max(1, std::min(t, n));
+  // one host thread by default: a step is two launches (parameters and the
+  // step's CUDA graph), and one thread issues them for many realisations
+  // faster than several threads contending for the driver
+  b->threads = std::max(1, std::min(threads > 0 ? threads : 1, n));
+  for (cafe_sim *s : b->sims) cafe_internal_set_share(s, n, b->threads == 1);
   *out = b;
   return CAFE_OK;
 }
@@ -98,13 +103,16 @@ int cafe_batch_run(cafe_batch *b, long long max_steps, long long *steps_done) {
       for (int i : mine) {
         if (b->phase[i] != 1 || rcs[i]) continue;
         if (max_steps > 0 && b->steps[i] >= max_steps) continue;
-        int done = 0;
-        int rc = cafe_sim_step(b->sims[i], &done);
+        // one loop iteration per turn: measured on GB300, 64 realisations
+        // finish sooner with one single-step graph each per turn than with
+        // chunks of 4 or 16 steps per graph
+        int done = 0, ran = 0;
+        int rc = cafe_internal_advance(b->sims[i], 1, &ran, &done);
         if (rc) {
           fail(i, rc);
           continue;
         }
-        b->steps[i] += 1;
+        b->steps[i] += ran;
         if (done) {
           rc = cafe_sim_clean_layer(b->sims[i]);  // main1.C:95
           if (rc) fail(i, rc);

@@ -354,8 +354,20 @@ int dalloc(T **p, size_t n, std::vector<void *> &owned) {
 
 }  // namespace
 
-// Lets the other translation unit of the library (cafe_noalloc.cu) report errors.
+// Lets the other translation units of the library (cafe_noalloc.cu,
+// cafe_batch.cu) report errors.
 void cafe_internal_set_error(const char *msg) { g_last_error = msg ? msg : ""; }
+
+// A realisation that shares the GPU with `share` - 1 others (cafe_batch.cu):
+// its grid-stride launches are sized for its share of the SMs, and the
+// active-set compaction takes four 8-cell chunks per thread. Neither changes
+// results (every pass is order-preserving or element-wise). `graphs` = 0 keeps
+// its steps out of CUDA graphs (when several host threads drive a batch, a
+// capture in one thread must not meet another thread's device-wide calls).
+void cafe_internal_set_share(cafe_sim *s, int share, int graphs);
+// Up to max_k loop iterations at once (as many cafe_sim_step calls); *ran gets
+// the iterations run, *done the loop's end (cafe_batch.cu).
+int cafe_internal_advance(cafe_sim *s, int max_k, int *ran, int *done);
 
 struct cafe_sim {
   GridH g;
@@ -400,12 +412,30 @@ struct cafe_sim {
   int act_chunks = 1;       // 8-cell chunks per thread of the compaction
   long long nblk_pos = 0;   // position compaction blocks
   int nsm = 1;
+  int gsm = 1;              // SMs that grid-stride launches are sized for (nsm, or a share in a batch)
   // output (SetBuild / WriteToHDF1)
   bool output_due = false;
   uint8_t *gflag = nullptr;   // per-grain flags of SetBuild
   long long gflag_cap = 0;
   unsigned char *h_out = nullptr;  // pinned bounce buffer of the file writer
+  // the device work of 1, 4 or 16 consecutive steps as one CUDA graph each
+  // (see chunk_graph_launch)
+  bool use_graph = true;
+  cudaGraph_t graph[3] = {nullptr};
+  cudaGraphExec_t graph_exec[3] = {nullptr};
+  std::vector<unsigned char> graph_key[3];
+  long long graph_launch[3][CAFE_NPHASE] = {{0}};
+  long long graph_captures = 0;
 };
+
+void cafe_internal_set_share(cafe_sim *s, int share, int graphs) {
+  if (!s || share < 1) return;
+  s->use_graph = graphs != 0;
+  s->gsm = std::max(4, s->nsm / share);
+  s->act_chunks = CAFE_ACT_MAX_CHUNKS;
+  long long per_block = (long long)CAFE_CELLS_PER_BLOCK * s->act_chunks;
+  s->nblk_act = (s->K.N + per_block - 1) / per_block;
+}
 
 namespace {
 
@@ -567,7 +597,7 @@ void free_tmp(cafe_sim *s, std::vector<void *> &tmp) {
 
 int grid_blocks(long long work, int threads, cafe_sim *s) {
   long long b = (work + threads - 1) / threads;
-  long long cap = (long long)s->nsm * 16;
+  long long cap = (long long)s->gsm * 16;
   if (b > cap) b = cap;
   if (b < 1) b = 1;
   return (int)b;
@@ -656,6 +686,350 @@ int easm_field(cafe_sim *s) {
   return CAFE_OK;
 }
 
+// ---- the device work of one step
+// TempField::tInd (main1.C:64), the step parameters on the host and in device
+// memory, the EASM field when selected, and the class-map capacity.
+int step_plan(cafe_sim *s, bool may_grow, bool *need_grow);
+
+int step_prepare(cafe_sim *s) {
+  int rc = step_plan(s, true, nullptr);
+  if (rc) return rc;
+  k_put_params<<<1, 1, 0, s->stream>>>(s->D.Pd, s->P);
+  LAUNCHED(CAFE_PH_MELT, 1);
+  CUDA_TRY(cudaGetLastError());
+  return CAFE_OK;
+}
+
+// The host part of a step's preparation: TempField::tInd, the parameters into
+// s->P, the EASM field when selected, and the class-map capacity for the pool
+// box. With may_grow false a needed regrowth is reported in *need_grow
+// instead (the caller still has launches of earlier steps to issue).
+int step_plan(cafe_sim *s, bool may_grow, bool *need_grow) {
+  GridH &g = s->g;
+  s->tf_tInd = int(std::round(g.time / s->DelT));
+  if (g.isp < 0 || g.isp >= g.NpT || (std::fmod(g.isp, g.Nsd) == 0 && g.isp + 1 >= g.NpT) ||
+      (std::fmod(g.isp, g.Nsd) != 0 && g.isp < 1))
+    return fail(CAFE_E_STATE, "laser index %d outside the scan grid", g.isp);
+  make_step_params(s, s->P);
+  s->have_P = true;
+  if (s->K.easm) {
+    int rc = easm_field(s);
+    if (rc) return rc;
+  }
+  const CafeStepParams &P = s->P;
+  long long nbox = (long long)(P.hi[0] - P.lo[0]) * (P.hi[1] - P.lo[1]) * (P.hi[2] - P.lo[2]);
+  if (need_grow) *need_grow = false;
+  if (nbox > s->D.tcls_cap && !may_grow) {
+    if (need_grow) *need_grow = true;
+    return CAFE_OK;
+  }
+  if (nbox > s->D.tcls_cap) {
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    for (auto &p : s->owned)
+      if (p == (void *)s->D.tcls) {
+        cudaFree(p);
+        p = nullptr;
+      }
+    long long cap = std::max<long long>(nbox, 2 * s->D.tcls_cap);
+    cap = std::min<long long>(cap, s->K.N);
+    CUDA_TRY(cudaMalloc((void **)&s->D.tcls, cap));
+    s->owned.push_back(s->D.tcls);
+    s->D.tcls_cap = cap;
+  }
+  return CAFE_OK;
+}
+
+// SetLiquid3 + BuildjID + the class map over the pool box (k_melt). In a
+// graph the grid is fixed (the kernel strides over the box it reads).
+int launch_melt(cafe_sim *s, bool graph, const CafeStepParams *Pp) {
+  const CafeStepParams &P = s->P;
+  CUDA_TRY(cudaMemsetAsync(s->D.ctr + CTR_HOT, 0, sizeof(int), s->stream));
+  long long nbox = (long long)(P.hi[0] - P.lo[0]) * (P.hi[1] - P.lo[1]) * (P.hi[2] - P.lo[2]);
+  if (graph || nbox > 0) {
+    PhaseScope ps(s, CAFE_PH_MELT);
+    if (s->K.easm)
+      k_melt_easm<<<grid_blocks(nbox, 256, s), 256, 0, s->stream>>>(s->D, s->K, P);
+    else
+      k_melt<<<graph ? s->gsm * 16 : grid_blocks(nbox, 256, s), 256, 0, s->stream>>>(s->D, s->K, Pp);
+    LAUNCHED(CAFE_PH_MELT, 1);
+  }
+  CUDA_TRY(cudaGetLastError());
+  return CAFE_OK;
+}
+
+// End-of-scan check of TempField (TempField.C:199-216), only when the laser is
+// outside the grid box: host flags from "some cell at the liquidus".
+int end_of_scan(cafe_sim *s) {
+  GridH &g = s->g;
+  const CafeStepParams &P = s->P;
+  const int *isv = s->ispvec.data();
+  double x = g.lcoor2[2 * isv[g.isp]] - g.offset[0];
+  double y = g.lcoor2[2 * isv[g.isp] + 1] - g.offset[1];
+  if (x < g.gbox[0] || x > g.gbox[1] || y < g.gbox[2] || y > g.gbox[3]) {
+    int hot = 0;
+    if (s->K.easm) {
+      // TempField::EASM asks all_of(T >= tL) (TempField.C:123-125); cells
+      // above the laser plane hold T = 0
+      hot = (P.kabove >= g.nX[2] && !s->easm_cold) ? 1 : 0;
+    } else {
+      int rc = read_ctr(s, CTR_HOT, &hot);
+      if (rc) return rc;
+    }
+    if (hot == 0 || std::fmod(g.isp + 1, g.Nsd) == 0) g.inewscanflg = 1;
+    if (g.isp == g.NpT - 1) {
+      g.inewscanflg = 1;
+      g.inewlayerflg = 1;
+      g.isp = 0;
+      g.indlayer += 1;
+    }
+  }
+  return CAFE_OK;
+}
+
+// VoxelsCA::UpdateVoxels on the device (no host synchronisation). In a graph
+// the box kernels get fixed grids and read their boxes from the parameters.
+int launch_voxels(cafe_sim *s, bool graph, const CafeStepParams *Pp) {
+  CafeDev &D = s->D;
+  const CafeConsts &K = s->K;
+  const CafeStepParams &P = s->P;
+  cudaStream_t st = s->stream;
+  int nb = (int)s->nblk;
+  {
+    PhaseScope ps(s, CAFE_PH_CLASSIFY);
+    if (s->full_k2) {
+      k_solid2mushy_dense<<<nb, CAFE_DENSE_THREADS, 0, st>>>(D, K);
+      LAUNCHED(CAFE_PH_CLASSIFY, 1);
+      s->full_k2 = false;
+    } else {
+      long long vb = (long long)(P.hi[0] - P.lo[0] + 2) * (P.hi[1] - P.lo[1] + 2) * (P.hi[2] - P.lo[2] + 2);
+      k_solid2mushy_pbox<<<graph ? s->gsm * 16 : grid_blocks(vb, 256, s), 256, 0, st>>>(D, K, Pp, 0);
+      LAUNCHED(CAFE_PH_CLASSIFY, 1);
+      long long pb = (long long)(P.phi[0] - P.plo[0] + 2) * (P.phi[1] - P.plo[1] + 2) * (P.phi[2] - P.plo[2] + 2);
+      if (graph || (P.phi[0] > P.plo[0] && P.phi[1] > P.plo[1] && P.phi[2] > P.plo[2])) {
+        k_solid2mushy_pbox<<<graph ? s->gsm * 16 : grid_blocks(pb, 256, s), 256, 0, st>>>(D, K, Pp, 1);
+        LAUNCHED(CAFE_PH_CLASSIFY, 1);
+      }
+      k_solid2mushy_list<<<s->gsm * 4, 256, 0, st>>>(D, K);
+      LAUNCHED(CAFE_PH_CLASSIFY, 1);
+    }
+    CUDA_TRY(cudaMemsetAsync(D.ctr + CTR_NLIQ, 0, sizeof(int), st));
+    k_active_count<<<(int)s->nblk_act, CAFE_DENSE_THREADS, 0, st>>>(D, K, Pp, s->act_chunks);
+    k_scan_blocks<<<1, 1024, 0, st>>>(D.blk, s->nblk_act, D.ctr + CTR_NA);
+    k_active_scatter<<<(int)s->nblk_act, CAFE_DENSE_THREADS, 0, st>>>(D, K, Pp, s->act_chunks);
+    LAUNCHED(CAFE_PH_CLASSIFY, 3);
+  }
+  int gb = s->gsm * 8;
+  {
+    PhaseScope ps(s, CAFE_PH_GATHER);
+    k_gather<<<gb, 256, 0, st>>>(D, K, Pp);
+    int nbp = (int)s->nblk_pos;
+    k_lists_count<<<nbp, CAFE_DENSE_THREADS, 0, st>>>(D);
+    k_scan_pairs<<<1, 1024, 0, st>>>(D.blk, s->nblk_pos, D.ctr + CTR_NA, D.ctr + CTR_NVS2, D.ctr + CTR_NROWS);
+    k_lists_scatter<<<nbp, CAFE_DENSE_THREADS, 0, st>>>(D);
+    if (K.easm)  // rows grow with per-cell velocities: the exact per-event scan
+      k_set_int<<<1, 1, 0, st>>>(D.ctr + CTR_SLOW, 1);
+    else
+      CUDA_TRY(cudaMemsetAsync(D.ctr + CTR_SLOW, 0, sizeof(int), st));
+    CUDA_TRY(cudaMemsetAsync(D.ctr + CTR_NPAIRS, 0, sizeof(int), st));
+    k_rows_prep<<<s->gsm * 4, 256, 0, st>>>(D, K);
+    k_rows_geo<<<s->gsm * 8, 256, 0, st>>>(D, K);
+    k_rows_order<<<s->gsm * 4, 256, 0, st>>>(D, K);
+    LAUNCHED(CAFE_PH_GATHER, 7);
+  }
+  {
+    PhaseScope ps(s, CAFE_PH_EVENTS);
+    k_event_loop<<<1, CAFE_LOOP_THREADS, 0, st>>>(D, K, Pp, D.act_cap + 1, s->event_scan ? 0 : 1);
+    k_rows_finalize<<<s->gsm * 4, 256, 0, st>>>(D);
+    LAUNCHED(CAFE_PH_EVENTS, 2);
+  }
+  {
+    PhaseScope ps(s, CAFE_PH_WRITEBACK);
+    k_writeback<<<gb, 256, 0, st>>>(D);
+    k_mushy2solid<<<gb, 256, 0, st>>>(D, K);
+    LAUNCHED(CAFE_PH_WRITEBACK, 2);
+  }
+  CUDA_TRY(cudaGetLastError());
+  return CAFE_OK;
+}
+
+void voxels_done(cafe_sim *s) {
+  const CafeStepParams &P = s->P;
+  for (int a = 0; a < 3; ++a) {
+    s->prev_lo[a] = P.lo[a];
+    s->prev_hi[a] = P.hi[a];
+  }
+  s->have_prev_box = true;
+}
+
+// Everything the captured launches depend on besides the step parameters
+// (which they read from device memory): device pointers, constants, launch
+// shapes. A change (a regrown buffer, a new grain table) forces a new capture.
+std::vector<unsigned char> graph_key(const cafe_sim *s) {
+  std::vector<unsigned char> k(sizeof(CafeDev) + sizeof(CafeConsts) + 8 * sizeof(long long));
+  unsigned char *p = k.data();
+  std::memcpy(p, &s->D, sizeof(CafeDev));
+  p += sizeof(CafeDev);
+  std::memcpy(p, &s->K, sizeof(CafeConsts));
+  p += sizeof(CafeConsts);
+  long long v[8] = {s->gsm, s->act_chunks, s->nblk, s->nblk_act, s->nblk_pos, s->event_scan, s->nsm, 0};
+  std::memcpy(p, v, sizeof v);
+  return k;
+}
+
+// The melt pass and UpdateVoxels of 4^q consecutive steps as one graph launch
+// (step j reads its parameters from D.Pd[j]): captured once per handle and
+// size (again whenever graph_key changes) and replayed, so that a chunk of
+// steps costs two host launches (k_put_params_pack and the graph) instead of
+// about twenty-five API calls per step. Used when no phase timing is asked
+// for, the temperature is analytic and no dense solid->mushy pass is due.
+int chunk_graph_launch(cafe_sim *s, int q) {
+  const int m = 1 << (2 * q);
+  std::vector<unsigned char> key = graph_key(s);
+  if (!s->graph_exec[q] || key != s->graph_key[q]) {
+    if (s->graph_exec[q]) cudaGraphExecDestroy(s->graph_exec[q]);
+    if (s->graph[q]) cudaGraphDestroy(s->graph[q]);
+    s->graph_exec[q] = nullptr;
+    s->graph[q] = nullptr;
+    long long before[CAFE_NPHASE];
+    for (int p = 0; p < CAFE_NPHASE; ++p) before[p] = s->phase_launch[p];
+    long long tot0 = s->launches;
+    CUDA_TRY(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+    int rc = CAFE_OK;
+    for (int j = 0; j < m && !rc; ++j) {
+      rc = launch_melt(s, true, s->D.Pd + j);
+      if (!rc) rc = launch_voxels(s, true, s->D.Pd + j);
+    }
+    cudaGraph_t g = nullptr;
+    cudaError_t ce = cudaStreamEndCapture(s->stream, &g);
+    // the capture only recorded the launches: take back their counts
+    for (int p = 0; p < CAFE_NPHASE; ++p) {
+      s->graph_launch[q][p] = s->phase_launch[p] - before[p];
+      s->phase_launch[p] = before[p];
+    }
+    s->launches = tot0;
+    if (rc || ce != cudaSuccess) {
+      if (g) cudaGraphDestroy(g);
+      if (rc) return rc;
+      return fail(CAFE_E_CUDA, "step graph capture: %s", cudaGetErrorString(ce));
+    }
+    s->graph[q] = g;
+    CUDA_TRY(cudaGraphInstantiate(&s->graph_exec[q], g, 0));
+    s->graph_key[q] = key;
+    s->graph_captures++;
+  }
+  CUDA_TRY(cudaGraphLaunch(s->graph_exec[q], s->stream));
+  for (int p = 0; p < CAFE_NPHASE; ++p) {
+    s->phase_launch[p] += s->graph_launch[q][p];
+    s->launches += s->graph_launch[q][p];
+  }
+  return CAFE_OK;
+}
+
+// Issues the device work of the m planned steps pack[0..m): their parameters,
+// then graphs of 16, 4 and 1 steps.
+int launch_chunk(cafe_sim *s, const CafeStepParams *pack, int m) {
+  int off = 0;
+  for (int q = 2; q >= 0; --q) {
+    int sz = 1 << (2 * q);
+    while (m - off >= sz) {
+      CafeStepPack pk;
+      std::memset(&pk, 0, sizeof pk);
+      for (int j = 0; j < sz; ++j) pk.p[j] = pack[off + j];
+      pk.n = sz;
+      k_put_params_pack<<<1, 32, 0, s->stream>>>(s->D.Pd, pk);
+      LAUNCHED(CAFE_PH_MELT, 1);
+      CUDA_TRY(cudaGetLastError());
+      int rc = chunk_graph_launch(s, q);
+      if (rc) return rc;
+      off += sz;
+    }
+  }
+  return CAFE_OK;
+}
+
+bool graph_eligible(const cafe_sim *s) { return s->use_graph && !s->timing && !s->K.easm && !s->full_k2; }
+
+// The rest of a loop iteration after its device work (main1.C:72-93).
+int finish_after_laser(cafe_sim *s, bool bcheck, int *done) {
+  int rc;
+  if (s->g.inewlayerflg == 1 && (rc = cafe_sim_clean_layer(s))) return rc;
+  // output point (main1.C:77-84): SetBuild; WriteToHDF1 is the caller's
+  const GridH &g = s->g;
+  s->output_due = (g.outint > 0 && s->tf_tInd % g.outint == 0) || bcheck || (g.inewlayerflg == 1 && g.outNL == 0);
+  if (s->output_due && (rc = cafe_sim_set_build(s))) return rc;
+  cafe_sim_update_time(s);
+  if (s->g.inewlayerflg == 1 && (rc = cafe_sim_add_layer(s))) return rc;
+  s->steps++;
+  if (bcheck) s->done = true;
+  if (done) *done = s->done ? 1 : 0;
+  return CAFE_OK;
+}
+int finish_step(cafe_sim *s, int *done) {
+  grid_update_laser(s->g);
+  return finish_after_laser(s, s->g.indlayer > s->nlayerTot, done);
+}
+
+// Loop iterations (main1.C:62-93) in one go, with the meaning of as many
+// cafe_sim_step calls: the host parts of up to CAFE_CHUNK steps are worked out
+// first (laser state machine, parameters, counters: none of them depends on
+// device results) and the device work is issued as one chunk. A chunk ends at
+// a step whose host part needs a device result (the end-of-scan check when
+// the laser is outside the grid box), at a new layer (CleanLayer and
+// AddLayer1 follow the step's device work), at the end of the run, or before
+// a step whose pool box needs a larger class map.
+int advance_steps(cafe_sim *s, int max_k, int *ran, int *done_out) {
+  *ran = 0;
+  if (!graph_eligible(s) || max_k <= 1) {
+    int rc = cafe_sim_step(s, done_out);
+    if (!rc) *ran = 1;
+    return rc;
+  }
+  CUDA_TRY(cudaSetDevice(s->device));
+  CafeStepParams pack[CAFE_CHUNK];
+  int m = 0, rc;
+  if (max_k > CAFE_CHUNK) max_k = CAFE_CHUNK;
+  while (m < max_k) {
+    bool grow = false;
+    const int tf_prev = s->tf_tInd;
+    if ((rc = step_plan(s, m == 0, &grow))) return rc;
+    if (grow) {  // this step needs a larger class map: issue the chunk first
+      s->P = pack[m - 1];
+      s->tf_tInd = tf_prev;
+      break;
+    }
+    pack[m++] = s->P;
+    GridH &g = s->g;
+    const int *isv = s->ispvec.data();
+    double x = g.lcoor2[2 * isv[g.isp]] - g.offset[0];
+    double y = g.lcoor2[2 * isv[g.isp] + 1] - g.offset[1];
+    if (x < g.gbox[0] || x > g.gbox[1] || y < g.gbox[2] || y > g.gbox[3]) {
+      // the end-of-scan check reads this step's "some cell at the liquidus"
+      if ((rc = launch_chunk(s, pack, m))) return rc;
+      *ran = m;
+      if ((rc = end_of_scan(s))) return rc;
+      voxels_done(s);
+      return finish_step(s, done_out);
+    }
+    voxels_done(s);
+    grid_update_laser(g);
+    bool bcheck = g.indlayer > s->nlayerTot;
+    // CleanLayer, SetBuild at an output point and AddLayer1 follow the step's
+    // device work
+    if (g.inewlayerflg == 1 || bcheck || (g.outint > 0 && s->tf_tInd % g.outint == 0)) {
+      if ((rc = launch_chunk(s, pack, m))) return rc;
+      *ran = m;
+      return finish_after_laser(s, bcheck, done_out);
+    }
+    s->output_due = false;
+    cafe_sim_update_time(s);
+    s->steps++;
+  }
+  if ((rc = launch_chunk(s, pack, m))) return rc;
+  *ran = m;
+  if (done_out) *done_out = 0;
+  return CAFE_OK;
+}
+
 }  // namespace
 
 // ====================================================================== C ABI
@@ -682,6 +1056,7 @@ int cafe_sim_create(const char *deck_path, const cafe_options *opt, cafe_sim **o
     return fail(CAFE_E_CUDA, "cudaSetDevice(%d): %s", opt ? opt->device : 0, cudaGetErrorString(ce));
   }
   cudaDeviceGetAttribute(&s->nsm, cudaDevAttrMultiProcessorCount, s->device);
+  s->gsm = s->nsm;
   if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) {
     delete s;
     return fail(CAFE_E_CUDA, "cudaStreamCreate failed");
@@ -801,6 +1176,20 @@ int cafe_sim_create(const char *deck_path, const cafe_options *opt, cafe_sim **o
     s->nblk_act = (N + per_block - 1) / per_block;
   }
   s->nblk_pos = (acap + CAFE_CELLS_PER_BLOCK - 1) / CAFE_CELLS_PER_BLOCK;
+  // the class map covers the pool box of a step; with the analytic field its
+  // size is bounded by the pool extents (make_step_params), so it is sized
+  // once here rather than regrown (a regrowth would change the device
+  // pointers that the step graphs captured)
+  if (!K.easm) {
+    double A = std::max(K.bmDX0, K.a1[3]), B = std::max(K.a1[1], K.a1[4]), C = std::max(K.a1[2], K.a1[5]);
+    double ext[3] = {2 * (A + B), 2 * (A + B), 2 * C};
+    long long box = 1;
+    for (int a = 0; a < 3; ++a) {
+      double cells = ext[a] / g.dX[a] + 8;
+      box *= (long long)std::min<double>((double)g.nX[a], cells == cells ? cells : (double)g.nX[a]);
+    }
+    D.tcls_cap = std::min<long long>(std::max<long long>(box, 1), N);
+  }
   D.blk_cap = std::max(s->nblk, 2 * s->nblk_pos);
   auto &o = s->owned;
   if ((rc = dalloc(&D.state, N, o)) || (rc = dalloc(&D.gid, N, o)) || (rc = dalloc(&D.ext, N, o)) ||
@@ -825,6 +1214,7 @@ int cafe_sim_create(const char *deck_path, const cafe_options *opt, cafe_sim **o
       (rc = dalloc(&D.row_key, D.row_cap, o)) || (rc = dalloc(&D.row_bt, D.row_cap, o)) ||
       (rc = dalloc(&D.row_bruq, D.row_cap, o)) ||
       (rc = dalloc(&D.ctr, CTR_COUNT, o)) || (rc = dalloc(&D.err, 1, o)) || (rc = dalloc(&D.stat, STAT_COUNT, o)) ||
+      (rc = dalloc(&D.Pd, CAFE_CHUNK, o)) || (rc = dalloc(&D.tcls, std::max<long long>(D.tcls_cap, 1), o)) ||
       (K.easm && ((rc = dalloc(&D.temp, N, o)) || (rc = dalloc(&D.a_vh, acap, o))))) {
     cafe_sim_destroy(s);
     return rc;
@@ -866,6 +1256,10 @@ void cafe_sim_destroy(cafe_sim *s) {
   for (void *p : s->owned) cudaFree(p);
   if (s->h_pinned) cudaFreeHost(s->h_pinned);
   if (s->h_out) cudaFreeHost(s->h_out);
+  for (int q = 0; q < 3; ++q) {
+    if (s->graph_exec[q]) cudaGraphExecDestroy(s->graph_exec[q]);
+    if (s->graph[q]) cudaGraphDestroy(s->graph[q]);
+  }
   if (s->stream) cudaStreamDestroy(s->stream);
   delete s;
 }
@@ -999,135 +1393,18 @@ int cafe_sim_update_laser(cafe_sim *s) {
 int cafe_sim_temperature(cafe_sim *s) {
   if (!s || !s->initialized) return fail(CAFE_E_STATE, "temperature before initialize_voxels");
   CUDA_TRY(cudaSetDevice(s->device));
-  GridH &g = s->g;
-  s->tf_tInd = int(std::round(g.time / s->DelT));
-  if (g.isp < 0 || g.isp >= g.NpT || (std::fmod(g.isp, g.Nsd) == 0 && g.isp + 1 >= g.NpT) ||
-      (std::fmod(g.isp, g.Nsd) != 0 && g.isp < 1))
-    return fail(CAFE_E_STATE, "laser index %d outside the scan grid", g.isp);
-  make_step_params(s, s->P);
-  s->have_P = true;
-  if (s->K.easm) {
-    int rc = easm_field(s);
-    if (rc) return rc;
-  }
-  const CafeStepParams &P = s->P;
-  CUDA_TRY(cudaMemsetAsync(s->D.ctr + CTR_HOT, 0, sizeof(int), s->stream));
-  long long nbox = (long long)(P.hi[0] - P.lo[0]) * (P.hi[1] - P.lo[1]) * (P.hi[2] - P.lo[2]);
-  if (nbox > s->D.tcls_cap) {
-    CUDA_TRY(cudaStreamSynchronize(s->stream));
-    for (auto &p : s->owned)
-      if (p == (void *)s->D.tcls) {
-        cudaFree(p);
-        p = nullptr;
-      }
-    long long cap = std::max<long long>(nbox, 2 * s->D.tcls_cap);
-    cap = std::min<long long>(cap, s->K.N);
-    CUDA_TRY(cudaMalloc((void **)&s->D.tcls, cap));
-    s->owned.push_back(s->D.tcls);
-    s->D.tcls_cap = cap;
-  }
-  if (nbox > 0) {
-    PhaseScope ps(s, CAFE_PH_MELT);
-    if (s->K.easm)
-      k_melt_easm<<<grid_blocks(nbox, 256, s), 256, 0, s->stream>>>(s->D, s->K, P);
-    else
-      k_melt<<<grid_blocks(nbox, 256, s), 256, 0, s->stream>>>(s->D, s->K, P);
-    LAUNCHED(CAFE_PH_MELT, 1);
-  }
-  CUDA_TRY(cudaGetLastError());
-  // end-of-scan check (TempField.C:199-216), only when the laser is outside the grid box
-  const int *isv = s->ispvec.data();
-  double x = g.lcoor2[2 * isv[g.isp]] - g.offset[0];
-  double y = g.lcoor2[2 * isv[g.isp] + 1] - g.offset[1];
-  if (x < g.gbox[0] || x > g.gbox[1] || y < g.gbox[2] || y > g.gbox[3]) {
-    int hot = 0;
-    if (s->K.easm) {
-      // TempField::EASM asks all_of(T >= tL) (TempField.C:123-125); cells
-      // above the laser plane hold T = 0
-      hot = (P.kabove >= g.nX[2] && !s->easm_cold) ? 1 : 0;
-    } else {
-      int rc = read_ctr(s, CTR_HOT, &hot);
-      if (rc) return rc;
-    }
-    if (hot == 0 || std::fmod(g.isp + 1, g.Nsd) == 0) g.inewscanflg = 1;
-    if (g.isp == g.NpT - 1) {
-      g.inewscanflg = 1;
-      g.inewlayerflg = 1;
-      g.isp = 0;
-      g.indlayer += 1;
-    }
-  }
-  return CAFE_OK;
+  int rc = step_prepare(s);
+  if (!rc) rc = launch_melt(s, false, s->D.Pd);
+  if (!rc) rc = end_of_scan(s);
+  return rc;
 }
 
 int cafe_sim_update_voxels(cafe_sim *s) {
   if (!s || !s->have_P) return fail(CAFE_E_STATE, "update_voxels before temperature");
   CUDA_TRY(cudaSetDevice(s->device));
-  CafeDev &D = s->D;
-  const CafeConsts &K = s->K;
-  const CafeStepParams &P = s->P;
-  cudaStream_t st = s->stream;
-  int nb = (int)s->nblk;
-  {
-    PhaseScope ps(s, CAFE_PH_CLASSIFY);
-    if (s->full_k2) {
-      k_solid2mushy_dense<<<nb, CAFE_DENSE_THREADS, 0, st>>>(D, K);
-      LAUNCHED(CAFE_PH_CLASSIFY, 1);
-      s->full_k2 = false;
-    } else {
-      long long vb = (long long)(P.hi[0] - P.lo[0] + 2) * (P.hi[1] - P.lo[1] + 2) * (P.hi[2] - P.lo[2] + 2);
-      k_solid2mushy_box<<<grid_blocks(vb, 256, s), 256, 0, st>>>(D, K, P.lo[0], P.hi[0], P.lo[1], P.hi[1], P.lo[2], P.hi[2]);
-      LAUNCHED(CAFE_PH_CLASSIFY, 1);
-      long long pb = (long long)(P.phi[0] - P.plo[0] + 2) * (P.phi[1] - P.plo[1] + 2) * (P.phi[2] - P.plo[2] + 2);
-      if (P.phi[0] > P.plo[0] && P.phi[1] > P.plo[1] && P.phi[2] > P.plo[2]) {
-        k_solid2mushy_box<<<grid_blocks(pb, 256, s), 256, 0, st>>>(D, K, P.plo[0], P.phi[0], P.plo[1], P.phi[1], P.plo[2], P.phi[2]);
-        LAUNCHED(CAFE_PH_CLASSIFY, 1);
-      }
-      k_solid2mushy_list<<<s->nsm * 4, 256, 0, st>>>(D, K);
-      LAUNCHED(CAFE_PH_CLASSIFY, 1);
-    }
-    CUDA_TRY(cudaMemsetAsync(D.ctr + CTR_NLIQ, 0, sizeof(int), st));
-    k_active_count<<<(int)s->nblk_act, CAFE_DENSE_THREADS, 0, st>>>(D, K, P, s->act_chunks);
-    k_scan_blocks<<<1, 1024, 0, st>>>(D.blk, s->nblk_act, D.ctr + CTR_NA);
-    k_active_scatter<<<(int)s->nblk_act, CAFE_DENSE_THREADS, 0, st>>>(D, K, P, s->act_chunks);
-    LAUNCHED(CAFE_PH_CLASSIFY, 3);
-  }
-  int gb = s->nsm * 8;
-  {
-    PhaseScope ps(s, CAFE_PH_GATHER);
-    k_gather<<<gb, 256, 0, st>>>(D, K, P);
-    int nbp = (int)s->nblk_pos;
-    k_lists_count<<<nbp, CAFE_DENSE_THREADS, 0, st>>>(D);
-    k_scan_pairs<<<1, 1024, 0, st>>>(D.blk, s->nblk_pos, D.ctr + CTR_NA, D.ctr + CTR_NVS2, D.ctr + CTR_NROWS);
-    k_lists_scatter<<<nbp, CAFE_DENSE_THREADS, 0, st>>>(D);
-    if (K.easm)  // rows grow with per-cell velocities: the exact per-event scan
-      k_set_int<<<1, 1, 0, st>>>(D.ctr + CTR_SLOW, 1);
-    else
-      CUDA_TRY(cudaMemsetAsync(D.ctr + CTR_SLOW, 0, sizeof(int), st));
-    CUDA_TRY(cudaMemsetAsync(D.ctr + CTR_NPAIRS, 0, sizeof(int), st));
-    k_rows_prep<<<s->nsm * 4, 256, 0, st>>>(D, K);
-    k_rows_geo<<<s->nsm * 8, 256, 0, st>>>(D, K);
-    k_rows_order<<<s->nsm * 4, 256, 0, st>>>(D, K);
-    LAUNCHED(CAFE_PH_GATHER, 7);
-  }
-  {
-    PhaseScope ps(s, CAFE_PH_EVENTS);
-    k_event_loop<<<1, CAFE_LOOP_THREADS, 0, st>>>(D, K, P, D.act_cap + 1, s->event_scan ? 0 : 1);
-    k_rows_finalize<<<s->nsm * 4, 256, 0, st>>>(D);
-    LAUNCHED(CAFE_PH_EVENTS, 2);
-  }
-  {
-    PhaseScope ps(s, CAFE_PH_WRITEBACK);
-    k_writeback<<<gb, 256, 0, st>>>(D);
-    k_mushy2solid<<<gb, 256, 0, st>>>(D, K);
-    LAUNCHED(CAFE_PH_WRITEBACK, 2);
-  }
-  CUDA_TRY(cudaGetLastError());
-  for (int a = 0; a < 3; ++a) {
-    s->prev_lo[a] = P.lo[a];
-    s->prev_hi[a] = P.hi[a];
-  }
-  s->have_prev_box = true;
+  int rc = launch_voxels(s, false, s->D.Pd);
+  if (rc) return rc;
+  voxels_done(s);
   return CAFE_OK;
 }
 
@@ -1191,21 +1468,17 @@ int cafe_sim_step(cafe_sim *s, int *done) {
     return CAFE_OK;
   }
   int rc;
-  if ((rc = cafe_sim_temperature(s))) return rc;
-  if ((rc = cafe_sim_update_voxels(s))) return rc;
-  grid_update_laser(s->g);
-  bool bcheck = s->g.indlayer > s->nlayerTot;
-  if (s->g.inewlayerflg == 1 && (rc = cafe_sim_clean_layer(s))) return rc;
-  // output point (main1.C:77-84): SetBuild; WriteToHDF1 is the caller's
-  const GridH &g = s->g;
-  s->output_due = (g.outint > 0 && s->tf_tInd % g.outint == 0) || bcheck || (g.inewlayerflg == 1 && g.outNL == 0);
-  if (s->output_due && (rc = cafe_sim_set_build(s))) return rc;
-  cafe_sim_update_time(s);
-  if (s->g.inewlayerflg == 1 && (rc = cafe_sim_add_layer(s))) return rc;
-  s->steps++;
-  if (bcheck) s->done = true;
-  if (done) *done = s->done ? 1 : 0;
-  return CAFE_OK;
+  if (graph_eligible(s)) {
+    CUDA_TRY(cudaSetDevice(s->device));
+    bool grow = false;
+    if ((rc = step_plan(s, true, &grow))) return rc;
+    if ((rc = launch_chunk(s, &s->P, 1)) || (rc = end_of_scan(s))) return rc;
+    voxels_done(s);
+  } else {
+    if ((rc = cafe_sim_temperature(s))) return rc;
+    if ((rc = cafe_sim_update_voxels(s))) return rc;
+  }
+  return finish_step(s, done);
 }
 
 int cafe_sim_run(cafe_sim *s, long long max_steps, long long *steps_done) {
@@ -1213,8 +1486,10 @@ int cafe_sim_run(cafe_sim *s, long long max_steps, long long *steps_done) {
   long long n = 0;
   int done = s->done ? 1 : 0, rc;
   while (!done && (max_steps <= 0 || n < max_steps)) {
-    if ((rc = cafe_sim_step(s, &done))) return rc;
-    ++n;
+    int ran = 0;
+    long long left = max_steps > 0 ? max_steps - n : CAFE_CHUNK;
+    if ((rc = advance_steps(s, (int)std::min<long long>(left, CAFE_CHUNK), &ran, &done))) return rc;
+    n += ran;
   }
   if (done && (rc = cafe_sim_clean_layer(s))) return rc;
   if (steps_done) *steps_done = n;
@@ -1278,6 +1553,7 @@ int cafe_sim_stats(cafe_sim *s, cafe_stats *st) {
   st->cycles_select = v[STAT_CYC_SELECT];
   st->cycles_apply = v[STAT_CYC_APPLY];
   st->cycles_fill = v[STAT_CYC_FILL];
+  st->graph_captures = (unsigned long long)s->graph_captures;
 #ifdef CAFE_DETAIL_CYCLES
   fprintf(stderr, "cafe detail cycles:");
   for (int c = 0; c < 32; ++c) fprintf(stderr, " %llu", v[STAT_DETAIL + c]);
@@ -1731,3 +2007,13 @@ int cafe_sim_write_output(cafe_sim *s, const char *prefix) {
 }
 
 }  // extern "C"
+
+int cafe_internal_advance(cafe_sim *s, int max_k, int *ran, int *done) {
+  if (!s || !s->begun) return fail(CAFE_E_STATE, "step before begin");
+  if (s->done) {
+    *ran = 0;
+    if (done) *done = 1;
+    return CAFE_OK;
+  }
+  return advance_steps(s, max_k, ran, done);
+}

@@ -78,7 +78,8 @@ __device__ __forceinline__ int cafe_moore(const CafeConsts &K, int i, int j, int
 
 // ------------------------------------------------------------------ K: melt
 // Over the box where T may reach the liquidus: SetLiquid3 and BuildjID.
-__global__ void k_melt(CafeDev D, CafeConsts K, CafeStepParams P) {
+__global__ void k_melt(CafeDev D, CafeConsts K, const CafeStepParams *__restrict__ Pp) {
+  const CafeStepParams P = *Pp;
   int bx = P.hi[0] - P.lo[0], by = P.hi[1] - P.lo[1], bz = P.hi[2] - P.lo[2];
   long long nbox = (long long)bx * by * bz;
   long long iz1 = (long long)P.ilaserLoc * K.nxy;
@@ -130,7 +131,12 @@ __global__ void k_solid2mushy_dense(CafeDev D, CafeConsts K) {
   }
 }
 
-__global__ void k_solid2mushy_box(CafeDev D, CafeConsts K, int x0, int x1, int y0, int y1, int z0, int z1) {
+// ConvertSolid1(1) over this step's pool box (which = 0) or the previous one
+// (1), each dilated by one cell, read from the step parameters in device memory.
+__global__ void k_solid2mushy_pbox(CafeDev D, CafeConsts K, const CafeStepParams *__restrict__ Pp, int which) {
+  const int *lo = which ? Pp->plo : Pp->lo, *hi = which ? Pp->phi : Pp->hi;
+  int x0 = lo[0], x1 = hi[0], y0 = lo[1], y1 = hi[1], z0 = lo[2], z1 = hi[2];
+  if (which && !(x1 > x0 && y1 > y0 && z1 > z0)) return;  // no previous box
   x0 = max(x0 - 1, 0); y0 = max(y0 - 1, 0); z0 = max(z0 - 1, 0);
   x1 = min(x1 + 1, K.nx); y1 = min(y1 + 1, K.ny); z1 = min(z1 + 1, K.nz);
   if (x1 <= x0 || y1 <= y0 || z1 <= z0) return;
@@ -148,6 +154,13 @@ __global__ void k_solid2mushy_box(CafeDev D, CafeConsts K, int x0, int x1, int y
     for (int a = 0; a < n && !liq; ++a) liq = (D.state[nb[a]] == 1);
     if (liq) D.state[idx] = 2;
   }
+}
+
+// The step parameters into device memory (kernel arguments are copied at
+// launch, so the host copy may change right after).
+__global__ void k_put_params(CafeStepParams *Pd, CafeStepParams P) { *Pd = P; }
+__global__ void k_put_params_pack(CafeStepParams *Pd, CafeStepPack pack) {
+  if ((int)threadIdx.x < pack.n) Pd[threadIdx.x] = pack.p[threadIdx.x];
 }
 
 __global__ void k_solid2mushy_list(CafeDev D, CafeConsts K) {
@@ -238,7 +251,8 @@ __device__ __forceinline__ uint32_t cafe_thread_active(const CafeDev &D, const C
   return f;
 }
 
-__global__ void k_active_count(CafeDev D, CafeConsts K, CafeStepParams P, int chunks) {
+__global__ void k_active_count(CafeDev D, CafeConsts K, const CafeStepParams *__restrict__ Pp, int chunks) {
+  const CafeStepParams P = *Pp;
   __shared__ int wsum[CAFE_DENSE_THREADS / 32];
   long long base = ((long long)blockIdx.x * blockDim.x + threadIdx.x) * (CAFE_CELLS_PER_THREAD * chunks);
   int cnt = __popc(cafe_thread_active(D, K, P, base, chunks));
@@ -280,7 +294,8 @@ __global__ void k_scan_blocks(int32_t *blk, long long n, int *total) {
   }
 }
 
-__global__ void k_active_scatter(CafeDev D, CafeConsts K, CafeStepParams P, int chunks) {
+__global__ void k_active_scatter(CafeDev D, CafeConsts K, const CafeStepParams *__restrict__ Pp, int chunks) {
+  const CafeStepParams P = *Pp;
   __shared__ int wsum[CAFE_DENSE_THREADS / 32];
   long long base = ((long long)blockIdx.x * blockDim.x + threadIdx.x) * (CAFE_CELLS_PER_THREAD * chunks);
   const uint32_t flags = cafe_thread_active(D, K, P, base, chunks);
@@ -323,7 +338,8 @@ __global__ void k_active_scatter(CafeDev D, CafeConsts K, CafeStepParams P, int 
 // positions in ascending index order (-1 = not active), liquid-neighbour count,
 // all-neighbours-below-liquidus flag and the ruq offset (VoxelsCA.C:380:
 // ruq[p] = (U_p - .5) dX / 100, U_p the p-th uniform of minstd(30 tInd + seed1)).
-__global__ void k_gather(CafeDev D, CafeConsts K, CafeStepParams P) {
+__global__ void k_gather(CafeDev D, CafeConsts K, const CafeStepParams *__restrict__ Pp) {
+  const CafeStepParams P = *Pp;
   int na = D.ctr[CTR_NA];
   if (na > D.act_cap) na = (int)D.act_cap;
   uint32_t seed = cafe_minstd_seed((uint64_t)(uint32_t)(30 * P.tInd + (int)K.seed1));
@@ -1186,7 +1202,8 @@ __device__ void cafe_select_keyed(const CafeDev &D, const CafeConsts &K, int ev,
 // reference's per-event scan of every row, also the fallback when the rows
 // stop sharing one velocity) evaluates every row at every event.
 __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
-    k_event_loop(CafeDev D, CafeConsts K, CafeStepParams P, long long max_events, int allow_fast) {
+    k_event_loop(CafeDev D, CafeConsts K, const CafeStepParams *__restrict__ Pp, long long max_events, int allow_fast) {
+  const CafeStepParams P = *Pp;
   constexpr int NSEL = CAFE_LOOP_THREADS - CAFE_QUAD_THREADS;  // threads of the selecting warps
   __shared__ CafeCand red[CAFE_LOOP_THREADS / 32];
   __shared__ CafeSelShared s_sel;

@@ -42,7 +42,11 @@ WORKLOADS = {
     "c1": ("amcafe_gb300/decks/c1.in", 2000, "config 1: 512x256x128 voxels @2.5um, 4 layers, hatching 100um"),
     "c2": ("amcafe_gb300/decks/c2.in", 1200, "config 2: 1024x1024x256 voxels @2.5um, 10 layers, 67 deg rotation"),
     "c0": ("amcafe_gb300/decks/c0.in", 300, "config 0: 128x64x32 voxels @2.5um, single track"),
+    "c3": (None, 0, "config 3: ensemble of single-track realisations, sides U(96,192) voxels @2.5um, "
+                    "v U(0.5,1.5) m/s, P U(150,300) W, seeds 1..n, run batched on one GPU"),
 }
+ENSEMBLE_HOST_SEED = 20240603
+ENSEMBLE_ACTIVE_CAPACITY = 1 << 18  # active cells per step of one realisation
 FALLBACK_HBM_GBS = 6800.0
 BYTES_DENSE_PER_VOXEL = 2   # read + write of the uint8 cell state per voxel-update
 BYTES_PER_FRONT_CELL = 74   # gID 4, extents 8, centroid 24, state 1; read and written
@@ -215,6 +219,122 @@ def run_reference(args, ws, rank):
     return 0
 
 
+def _final_digest(sim):
+    import hashlib
+
+    st = sim.state()
+    h = hashlib.sha256()
+    for k in ("gID", "vState", "extents", "centroid", "buildj"):
+        h.update(st[k].tobytes())
+    h.update(sim.ctheta().tobytes())
+    return h.hexdigest()
+
+
+def run_ensemble(args, ws, rank, local):
+    """Config 3: runs/s of whole realisations (initialisation, the full loop
+    and the closing CleanLayer), batched (cafe_batch_*) against the same
+    realisations run one after another through the plain API. Each rank runs
+    its own ensemble (replicas); rank 0 prints."""
+    import torch
+
+    from amcafe_gb300 import Batch, Simulation
+    from amcafe_gb300.ensemble import make_decks
+
+    dist = init_dist(ws)
+    n = args.realisations
+    work = tempfile.mkdtemp(prefix="cafe_ens_")
+    decks = make_decks(work, n=n, sides=(96, 192), host_seed=ENSEMBLE_HOST_SEED)
+    cap = ENSEMBLE_ACTIVE_CAPACITY
+    # warm-up: context, allocator and code paths on three small realisations
+    wdecks = make_decks(os.path.join(work, "warm"), n=3, sides=(24, 32), host_seed=1)
+    for _ in range(args.warmup):
+        with Batch(wdecks, device=local, active_capacity=cap) as wb:
+            wb.run()
+    torch.cuda.synchronize(local)
+    # ---- batched (timed): all realisations in one batch
+    clocks = ClockSampler(local)
+    barrier(dist)
+    clocks.start()
+    t0 = time.time()
+    b = Batch(decks, device=local, threads=args.threads, active_capacity=cap)
+    iters = b.run()
+    torch.cuda.synchronize(local)
+    batch_s = time.time() - t0
+    clk = clocks.stop()
+    batch_s = reduce_max(dist, batch_s)
+    digests_b = [_final_digest(s) for s in b.sims]
+    nvox = [s.ncell for s in b.sims]
+    steps_each = [s.info()["steps"] for s in b.sims]
+    launches = sum(s.stats()["launches"] for s in b.sims)
+    threads = min(args.threads or min(16, os.cpu_count() or 1), n)  # as cafe_batch_create picks
+    b.close()
+    # ---- sequential plain runs of the same realisations (bounded by --seq-seconds)
+    seq_s, seq_done, same = 0.0, 0, True
+    for i, d in enumerate(decks):
+        if seq_s > args.seq_seconds:
+            break
+        t1 = time.time()
+        with Simulation(d, device=local, active_capacity=cap) as sim:
+            sim.InitializeVoxels()
+            sim.begin()
+            sim.run()
+            sim.synchronize()
+            seq_s += time.time() - t1
+            same = same and _final_digest(sim) == digests_b[i]
+        seq_done += 1
+    seq_rate = seq_done / seq_s if seq_s > 0 else None
+    # ---- CPU baseline: the oracle on realisation 1 for a bounded sample
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import cafe_oracle as orc
+
+        orc.set_budget(args.cpu_seconds)
+        st = orc.run(decks[0], "", max_steps=-1, dump_stride=0, libm=orc.LIBM_GLIBC)
+        orc.set_budget(0)
+        sec = st["loop_ns"] * 1e-9
+        frac = st["steps"] / max(1, steps_each[0])
+        cpu = {"value": frac / sec if sec > 0 else None, "unit": "runs/s", "cores": 1, "kind": "port",
+               "sample": "realisation 1 (%d voxels): %d of its %d steps in %.1f s, one thread, glibc libm; "
+                         "runs/s = completed fraction / time (initialisation excluded)"
+                         % (nvox[0], st["steps"], steps_each[0], sec)}
+    if rank == 0:
+        value = ws * n / batch_s
+        out = {
+            "metric": "runs/s",
+            "value": value,
+            "unit": "runs/s",
+            "n_gpus": ws,
+            "steps": int(iters),
+            "warmup": args.warmup,
+            "ms_per_step": 1e3 * batch_s / max(1, max(steps_each)),
+            "higher_is_better": True,
+            "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": "f64",
+            "data": "synthetic (seeded decks from amcafe_gb300.ensemble, host seed %d)" % ENSEMBLE_HOST_SEED,
+            "config": {"workload": "c3", "description": WORKLOADS["c3"][2], "realisations": n,
+                       "voxels_total": int(sum(nvox)), "voxels_min": int(min(nvox)), "voxels_max": int(max(nvox)),
+                       "host_threads": int(threads), "active_capacity": cap,
+                       "l2": "each realisation's state larger than L2 or not: timing is whole runs",
+                       "parallelism": "batch%d" % n},
+            "sequential": {"value": seq_rate, "unit": "runs/s", "runs": seq_done, "seconds": seq_s},
+            "speedup_vs_sequential": (value / ws) / seq_rate if seq_rate else None,
+            "bitexact_vs_sequential": same,
+            "voxel_updates_per_s": ws * sum(v * k for v, k in zip(nvox, steps_each)) / batch_s,
+            "e2e": {"value": value, "unit": "runs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0,
+                    "note": "whole runs from the decks: wall time of the batch including initialisation"},
+            "cpu_baseline": cpu,
+            "clocks": clk,
+            "gpu_launches": int(launches),
+            "wall_s_timed": batch_s,
+        }
+        print(json.dumps(out))
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -227,9 +347,14 @@ def main():
     ap.add_argument("--ref-seconds", type=float, default=60.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--realisations", type=int, default=64)
+    ap.add_argument("--threads", type=int, default=0)
+    ap.add_argument("--seq-seconds", type=float, default=150.0)
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     ws, rank, local = dist_env()
+    if args.workload == "c3":
+        return run_ensemble(args, ws, rank, local)
     if args.impl == "reference":
         return run_reference(args, ws, rank)
     dist = init_dist(ws)
@@ -255,8 +380,8 @@ def main():
         snapshot = (sim.info(), sim.state(), sim.ctheta())
 
     # ---- timed region: device time between two events on the engine's stream
+    # (the product path: each step is the step's CUDA graph)
     stats0 = sim.stats()
-    sim.set_timing(True)
     sim.phase_times(reset=True)
     clocks = ClockSampler(local)
     barrier(dist)
@@ -274,19 +399,34 @@ def main():
     sim.synchronize()
     wall = time.time() - t0
     clk = clocks.stop()
-    phases = sim.phase_times()
     stats1 = sim.stats()
-    sim.set_timing(False)
+    launches = int(stats1["launches"])  # counted since the reset before the timed steps
     ms = reduce_max(dist, ms)
     barrier(dist)
     value = ws * nvox * k / (ms * 1e-3)
+
+    # ---- phase breakdown: the next steps again with CUDA events around each
+    # phase (ungraphed launches), for the roofline of the dominant phase
+    kp = 0
+    if not done:
+        sim.set_timing(True)
+        sim.phase_times(reset=True)
+        statsp0 = sim.stats()
+        while kp < min(args.steps, 20) and not done:
+            done = sim.step()
+            kp += 1
+        phases = sim.phase_times()
+        statsp1 = sim.stats()
+        sim.set_timing(False)
+    if kp == 0:
+        phases, statsp0, statsp1 = {"events": (ms, k)}, stats0, stats1
 
     # ---- roofline of the dominant phase
     peak, peak_src = hbm_peak()
     dom = max(phases, key=lambda p: phases[p][0])
     dom_ms, dom_launches = phases[dom]
-    steps_done = max(1, stats1["steps"] - stats0["steps"])
-    avg_na = (stats1["sum_active"] - stats0["sum_active"]) / steps_done
+    steps_done = max(1, statsp1["steps"] - statsp0["steps"])
+    avg_na = (statsp1["sum_active"] - statsp0["sum_active"]) / steps_done
     if dom in ("events", "writeback", "gather"):
         bytes_per_launch = BYTES_PER_FRONT_CELL * avg_na
     else:
@@ -294,12 +434,14 @@ def main():
     launches_dom = max(1, dom_launches)
     per_launch_ms = dom_ms / launches_dom if dom != "events" else dom_ms / steps_done
     achieved = bytes_per_launch / (per_launch_ms * 1e-3) / 1e9
-    step_bytes = BYTES_DENSE_PER_VOXEL * nvox + BYTES_PER_FRONT_CELL * avg_na
+    avg_na_timed = (stats1["sum_active"] - stats0["sum_active"]) / max(1, stats1["steps"] - stats0["steps"])
+    step_bytes = BYTES_DENSE_PER_VOXEL * nvox + BYTES_PER_FRONT_CELL * avg_na_timed
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": committed_traffic(args.workload, dom),
                 "kernel": {"events": "k_event_loop", "classify": "k_active_count/k_active_scatter",
                            "gather": "k_gather", "melt": "k_melt", "writeback": "k_writeback"}.get(dom, dom),
                 "phase": dom, "peak_source": peak_src,
+                "phase_steps": kp,
                 "step_achieved_GBs": step_bytes * k / (ms * 1e-3) / 1e9}
 
     # ---- end to end through the C ABI with host buffers
@@ -368,7 +510,7 @@ def main():
             "roofline": roofline,
             "cpu_baseline": cpu,
             "clocks": clk,
-            "gpu_launches": int(stats1["launches"]),
+            "gpu_launches": launches,
             "events_per_step": ev / max(1, k),
             "phase_ms": {p: round(v[0], 3) for p, v in phases.items()},
             "wall_s_timed": wall,

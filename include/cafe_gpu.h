@@ -72,6 +72,7 @@ typedef struct {
   unsigned long long cycles_select;    /* event-loop SM cycles in event selection */
   unsigned long long cycles_apply;     /* ... applying the capture/nucleation */
   unsigned long long cycles_fill;      /* ... neighbour bookkeeping and new frontier rows */
+  unsigned long long graph_captures;   /* step graphs captured (1, 4 or 16 steps each) */
 } cafe_stats;
 
 /* Grid::Grid (Grid.C:15-109, deck parse Grid.C:165-318) + Partition::
@@ -177,8 +178,8 @@ int cafe_sim_write_output(cafe_sim *sim, const char *prefix);
 /* Batched ensemble (no counterpart in the reference, which runs one
  * realisation per MPI job): n independent realisations, one deck each, on
  * one device. Each is a cafe_sim handle with its own stream; `threads` host
- * threads (0: up to 16, one per hardware thread) step them round-robin so
- * that their device work overlaps. Every realisation runs exactly the calls of
+ * threads (0: one) step them round-robin so that their device work overlaps
+ * (with one thread each step is a CUDA graph launch). Every realisation runs exactly the calls of
  * a plain run (initialize_voxels, begin, step until done, the closing
  * clean_layer), so its results are bit-identical to its plain run. */
 typedef struct cafe_batch cafe_batch;

@@ -1,0 +1,52 @@
+"""Step scheduling paths give identical results: the chunked run (up to 16
+steps per CUDA graph launch, cafe_sim_run), single steps (one graph per step,
+cafe_sim_step) and the ungraphed launches (phase timing on), on a deck with
+rotated layers, new layers and output points every 7 steps."""
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+DECKS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "decks")
+
+
+def _deck(tmp_path, outint):
+    src = open(os.path.join(DECKS, "layers_rot.in")).read()
+    txt = "\n".join(l for l in src.splitlines() if not l.lower().startswith("outint")) + "\noutint %d\n" % outint
+    p = tmp_path / ("layers_rot_out%d.in" % outint)
+    p.write_text(txt)
+    return str(p)
+
+
+def _final(sim):
+    st = sim.state()
+    st["build"] = sim.build()
+    st["ctheta"] = sim.ctheta()
+    i = sim.info()
+    st["scalars"] = np.array([i["nGrain"], i["tInd"], i["isp"], i["indlayer"], i["steps"], i["tf_tInd"]])
+    return st
+
+
+@pytest.mark.parametrize("outint", [7, 1000000])
+def test_chunked_single_and_ungraphed_agree(tmp_path, outint):
+    from amcafe_gb300 import Simulation
+
+    deck = _deck(tmp_path, outint)
+    res = {}
+    for mode in ("run", "step", "timed"):
+        with Simulation(deck) as sim:
+            sim.InitializeVoxels()
+            sim.begin()
+            if mode == "run":
+                sim.run()
+            else:
+                if mode == "timed":
+                    sim.set_timing(True)
+                while not sim.step():
+                    pass
+                sim.CleanLayer()
+            res[mode] = _final(sim)
+    for mode in ("step", "timed"):
+        for k, v in res["run"].items():
+            assert np.array_equal(np.asarray(v), np.asarray(res[mode][k]), equal_nan=True), "%s: %s" % (mode, k)
