@@ -21,7 +21,6 @@
 
 void cafe_internal_set_error(const char *msg);
 void cafe_internal_set_share(cafe_sim *s, int share, int graphs);
-int cafe_internal_advance(cafe_sim *s, int max_k, int *ran, int *done);
 
 struct cafe_batch {
   std::vector<cafe_sim *> sims;
@@ -103,16 +102,13 @@ int cafe_batch_run(cafe_batch *b, long long max_steps, long long *steps_done) {
       for (int i : mine) {
         if (b->phase[i] != 1 || rcs[i]) continue;
         if (max_steps > 0 && b->steps[i] >= max_steps) continue;
-        // one loop iteration per turn: measured on GB300, 64 realisations
-        // finish sooner with one single-step graph each per turn than with
-        // chunks of 4 or 16 steps per graph
-        int done = 0, ran = 0;
-        int rc = cafe_internal_advance(b->sims[i], 1, &ran, &done);
+        int done = 0;
+        int rc = cafe_sim_step(b->sims[i], &done);
         if (rc) {
           fail(i, rc);
           continue;
         }
-        b->steps[i] += ran;
+        b->steps[i] += 1;
         if (done) {
           rc = cafe_sim_clean_layer(b->sims[i]);  // main1.C:95
           if (rc) fail(i, rc);

@@ -42,14 +42,6 @@ struct CafeStepParams {
   int any_hot_full;   // 1: evaluate T exactly everywhere below the plane
 };
 
-// Parameters of up to CAFE_CHUNK consecutive steps, passed by value to one
-// kernel that stores them in CafeDev::Pd.
-#define CAFE_CHUNK 16
-struct CafeStepPack {
-  CafeStepParams p[CAFE_CHUNK];
-  int n;
-};
-
 // Constants of the inverse-pole-figure colour triangle of
 // VoxelsCA::WriteToHDF1 (VoxelsCA.C:1597-1613), computed on the host.
 struct CafeIpfConsts {
@@ -107,8 +99,7 @@ struct CafeDev {
   uint8_t *build;
   // EASM mode: TempField::TempCurr per cell, growth velocity per active position
   double *temp, *a_vh;
-  // step parameters: slot j for the j-th step of a launched chunk of steps
-  // (the kernels of a step read them from here)
+  // this step's parameters (the kernels of a step read them from here)
   CafeStepParams *Pd;
   // liquid cells left by the previous step (cell indices)
   int32_t *liq;

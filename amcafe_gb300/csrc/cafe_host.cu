@@ -365,9 +365,6 @@ void cafe_internal_set_error(const char *msg) { g_last_error = msg ? msg : ""; }
 // its steps out of CUDA graphs (when several host threads drive a batch, a
 // capture in one thread must not meet another thread's device-wide calls).
 void cafe_internal_set_share(cafe_sim *s, int share, int graphs);
-// Up to max_k loop iterations at once (as many cafe_sim_step calls); *ran gets
-// the iterations run, *done the loop's end (cafe_batch.cu).
-int cafe_internal_advance(cafe_sim *s, int max_k, int *ran, int *done);
 
 struct cafe_sim {
   GridH g;
@@ -418,13 +415,12 @@ struct cafe_sim {
   uint8_t *gflag = nullptr;   // per-grain flags of SetBuild
   long long gflag_cap = 0;
   unsigned char *h_out = nullptr;  // pinned bounce buffer of the file writer
-  // the device work of 1, 4 or 16 consecutive steps as one CUDA graph each
-  // (see chunk_graph_launch)
+  // the device work of a step as one CUDA graph (see step_graph_launch)
   bool use_graph = true;
-  cudaGraph_t graph[3] = {nullptr};
-  cudaGraphExec_t graph_exec[3] = {nullptr};
-  std::vector<unsigned char> graph_key[3];
-  long long graph_launch[3][CAFE_NPHASE] = {{0}};
+  cudaGraph_t graph[1] = {nullptr};
+  cudaGraphExec_t graph_exec[1] = {nullptr};
+  std::vector<unsigned char> graph_key[1];
+  long long graph_launch[1][CAFE_NPHASE] = {{0}};
   long long graph_captures = 0;
 };
 
@@ -876,14 +872,15 @@ std::vector<unsigned char> graph_key(const cafe_sim *s) {
   return k;
 }
 
-// The melt pass and UpdateVoxels of 4^q consecutive steps as one graph launch
-// (step j reads its parameters from D.Pd[j]): captured once per handle and
-// size (again whenever graph_key changes) and replayed, so that a chunk of
-// steps costs two host launches (k_put_params_pack and the graph) instead of
-// about twenty-five API calls per step. Used when no phase timing is asked
-// for, the temperature is analytic and no dense solid->mushy pass is due.
-int chunk_graph_launch(cafe_sim *s, int q) {
-  const int m = 1 << (2 * q);
+// The melt pass and UpdateVoxels of a step as one graph launch (the kernels
+// read the step's parameters from D.Pd): captured once per handle (again
+// whenever graph_key changes) and replayed, so that a step costs two host
+// launches (k_put_params and the graph) instead of about twenty-five API
+// calls. Used when no phase timing is asked for, the temperature is analytic
+// and no dense solid->mushy pass is due. (Graphs of several consecutive steps
+// were measured slower on the device than one graph per step.)
+int step_graph_launch(cafe_sim *s) {
+  const int q = 0;
   std::vector<unsigned char> key = graph_key(s);
   if (!s->graph_exec[q] || key != s->graph_key[q]) {
     if (s->graph_exec[q]) cudaGraphExecDestroy(s->graph_exec[q]);
@@ -894,11 +891,8 @@ int chunk_graph_launch(cafe_sim *s, int q) {
     for (int p = 0; p < CAFE_NPHASE; ++p) before[p] = s->phase_launch[p];
     long long tot0 = s->launches;
     CUDA_TRY(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
-    int rc = CAFE_OK;
-    for (int j = 0; j < m && !rc; ++j) {
-      rc = launch_melt(s, true, s->D.Pd + j);
-      if (!rc) rc = launch_voxels(s, true, s->D.Pd + j);
-    }
+    int rc = launch_melt(s, true, s->D.Pd);
+    if (!rc) rc = launch_voxels(s, true, s->D.Pd);
     cudaGraph_t g = nullptr;
     cudaError_t ce = cudaStreamEndCapture(s->stream, &g);
     // the capture only recorded the launches: take back their counts
@@ -925,28 +919,6 @@ int chunk_graph_launch(cafe_sim *s, int q) {
   return CAFE_OK;
 }
 
-// Issues the device work of the m planned steps pack[0..m): their parameters,
-// then graphs of 16, 4 and 1 steps.
-int launch_chunk(cafe_sim *s, const CafeStepParams *pack, int m) {
-  int off = 0;
-  for (int q = 2; q >= 0; --q) {
-    int sz = 1 << (2 * q);
-    while (m - off >= sz) {
-      CafeStepPack pk;
-      std::memset(&pk, 0, sizeof pk);
-      for (int j = 0; j < sz; ++j) pk.p[j] = pack[off + j];
-      pk.n = sz;
-      k_put_params_pack<<<1, 32, 0, s->stream>>>(s->D.Pd, pk);
-      LAUNCHED(CAFE_PH_MELT, 1);
-      CUDA_TRY(cudaGetLastError());
-      int rc = chunk_graph_launch(s, q);
-      if (rc) return rc;
-      off += sz;
-    }
-  }
-  return CAFE_OK;
-}
-
 bool graph_eligible(const cafe_sim *s) { return s->use_graph && !s->timing && !s->K.easm && !s->full_k2; }
 
 // The rest of a loop iteration after its device work (main1.C:72-93).
@@ -967,67 +939,6 @@ int finish_after_laser(cafe_sim *s, bool bcheck, int *done) {
 int finish_step(cafe_sim *s, int *done) {
   grid_update_laser(s->g);
   return finish_after_laser(s, s->g.indlayer > s->nlayerTot, done);
-}
-
-// Loop iterations (main1.C:62-93) in one go, with the meaning of as many
-// cafe_sim_step calls: the host parts of up to CAFE_CHUNK steps are worked out
-// first (laser state machine, parameters, counters: none of them depends on
-// device results) and the device work is issued as one chunk. A chunk ends at
-// a step whose host part needs a device result (the end-of-scan check when
-// the laser is outside the grid box), at a new layer (CleanLayer and
-// AddLayer1 follow the step's device work), at the end of the run, or before
-// a step whose pool box needs a larger class map.
-int advance_steps(cafe_sim *s, int max_k, int *ran, int *done_out) {
-  *ran = 0;
-  if (!graph_eligible(s) || max_k <= 1) {
-    int rc = cafe_sim_step(s, done_out);
-    if (!rc) *ran = 1;
-    return rc;
-  }
-  CUDA_TRY(cudaSetDevice(s->device));
-  CafeStepParams pack[CAFE_CHUNK];
-  int m = 0, rc;
-  if (max_k > CAFE_CHUNK) max_k = CAFE_CHUNK;
-  while (m < max_k) {
-    bool grow = false;
-    const int tf_prev = s->tf_tInd;
-    if ((rc = step_plan(s, m == 0, &grow))) return rc;
-    if (grow) {  // this step needs a larger class map: issue the chunk first
-      s->P = pack[m - 1];
-      s->tf_tInd = tf_prev;
-      break;
-    }
-    pack[m++] = s->P;
-    GridH &g = s->g;
-    const int *isv = s->ispvec.data();
-    double x = g.lcoor2[2 * isv[g.isp]] - g.offset[0];
-    double y = g.lcoor2[2 * isv[g.isp] + 1] - g.offset[1];
-    if (x < g.gbox[0] || x > g.gbox[1] || y < g.gbox[2] || y > g.gbox[3]) {
-      // the end-of-scan check reads this step's "some cell at the liquidus"
-      if ((rc = launch_chunk(s, pack, m))) return rc;
-      *ran = m;
-      if ((rc = end_of_scan(s))) return rc;
-      voxels_done(s);
-      return finish_step(s, done_out);
-    }
-    voxels_done(s);
-    grid_update_laser(g);
-    bool bcheck = g.indlayer > s->nlayerTot;
-    // CleanLayer, SetBuild at an output point and AddLayer1 follow the step's
-    // device work
-    if (g.inewlayerflg == 1 || bcheck || (g.outint > 0 && s->tf_tInd % g.outint == 0)) {
-      if ((rc = launch_chunk(s, pack, m))) return rc;
-      *ran = m;
-      return finish_after_laser(s, bcheck, done_out);
-    }
-    s->output_due = false;
-    cafe_sim_update_time(s);
-    s->steps++;
-  }
-  if ((rc = launch_chunk(s, pack, m))) return rc;
-  *ran = m;
-  if (done_out) *done_out = 0;
-  return CAFE_OK;
 }
 
 }  // namespace
@@ -1214,7 +1125,7 @@ int cafe_sim_create(const char *deck_path, const cafe_options *opt, cafe_sim **o
       (rc = dalloc(&D.row_key, D.row_cap, o)) || (rc = dalloc(&D.row_bt, D.row_cap, o)) ||
       (rc = dalloc(&D.row_bruq, D.row_cap, o)) ||
       (rc = dalloc(&D.ctr, CTR_COUNT, o)) || (rc = dalloc(&D.err, 1, o)) || (rc = dalloc(&D.stat, STAT_COUNT, o)) ||
-      (rc = dalloc(&D.Pd, CAFE_CHUNK, o)) || (rc = dalloc(&D.tcls, std::max<long long>(D.tcls_cap, 1), o)) ||
+      (rc = dalloc(&D.Pd, 1, o)) || (rc = dalloc(&D.tcls, std::max<long long>(D.tcls_cap, 1), o)) ||
       (K.easm && ((rc = dalloc(&D.temp, N, o)) || (rc = dalloc(&D.a_vh, acap, o))))) {
     cafe_sim_destroy(s);
     return rc;
@@ -1256,7 +1167,7 @@ void cafe_sim_destroy(cafe_sim *s) {
   for (void *p : s->owned) cudaFree(p);
   if (s->h_pinned) cudaFreeHost(s->h_pinned);
   if (s->h_out) cudaFreeHost(s->h_out);
-  for (int q = 0; q < 3; ++q) {
+  for (int q = 0; q < 1; ++q) {
     if (s->graph_exec[q]) cudaGraphExecDestroy(s->graph_exec[q]);
     if (s->graph[q]) cudaGraphDestroy(s->graph[q]);
   }
@@ -1472,7 +1383,10 @@ int cafe_sim_step(cafe_sim *s, int *done) {
     CUDA_TRY(cudaSetDevice(s->device));
     bool grow = false;
     if ((rc = step_plan(s, true, &grow))) return rc;
-    if ((rc = launch_chunk(s, &s->P, 1)) || (rc = end_of_scan(s))) return rc;
+    k_put_params<<<1, 1, 0, s->stream>>>(s->D.Pd, s->P);
+    LAUNCHED(CAFE_PH_MELT, 1);
+    CUDA_TRY(cudaGetLastError());
+    if ((rc = step_graph_launch(s)) || (rc = end_of_scan(s))) return rc;
     voxels_done(s);
   } else {
     if ((rc = cafe_sim_temperature(s))) return rc;
@@ -1486,10 +1400,8 @@ int cafe_sim_run(cafe_sim *s, long long max_steps, long long *steps_done) {
   long long n = 0;
   int done = s->done ? 1 : 0, rc;
   while (!done && (max_steps <= 0 || n < max_steps)) {
-    int ran = 0;
-    long long left = max_steps > 0 ? max_steps - n : CAFE_CHUNK;
-    if ((rc = advance_steps(s, (int)std::min<long long>(left, CAFE_CHUNK), &ran, &done))) return rc;
-    n += ran;
+    if ((rc = cafe_sim_step(s, &done))) return rc;
+    ++n;
   }
   if (done && (rc = cafe_sim_clean_layer(s))) return rc;
   if (steps_done) *steps_done = n;
@@ -2007,13 +1919,3 @@ int cafe_sim_write_output(cafe_sim *s, const char *prefix) {
 }
 
 }  // extern "C"
-
-int cafe_internal_advance(cafe_sim *s, int max_k, int *ran, int *done) {
-  if (!s || !s->begun) return fail(CAFE_E_STATE, "step before begin");
-  if (s->done) {
-    *ran = 0;
-    if (done) *done = 1;
-    return CAFE_OK;
-  }
-  return advance_steps(s, max_k, ran, done);
-}

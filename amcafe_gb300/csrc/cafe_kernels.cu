@@ -159,9 +159,7 @@ __global__ void k_solid2mushy_pbox(CafeDev D, CafeConsts K, const CafeStepParams
 // The step parameters into device memory (kernel arguments are copied at
 // launch, so the host copy may change right after).
 __global__ void k_put_params(CafeStepParams *Pd, CafeStepParams P) { *Pd = P; }
-__global__ void k_put_params_pack(CafeStepParams *Pd, CafeStepPack pack) {
-  if ((int)threadIdx.x < pack.n) Pd[threadIdx.x] = pack.p[threadIdx.x];
-}
+
 
 __global__ void k_solid2mushy_list(CafeDev D, CafeConsts K) {
   int n = D.ctr[CTR_NLIQ];

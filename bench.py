@@ -266,7 +266,7 @@ def run_ensemble(args, ws, rank, local):
     nvox = [s.ncell for s in b.sims]
     steps_each = [s.info()["steps"] for s in b.sims]
     launches = sum(s.stats()["launches"] for s in b.sims)
-    threads = min(args.threads or min(16, os.cpu_count() or 1), n)  # as cafe_batch_create picks
+    threads = min(args.threads or 1, n)  # as cafe_batch_create picks
     b.close()
     # ---- sequential plain runs of the same realisations (bounded by --seq-seconds)
     seq_s, seq_done, same = 0.0, 0, True

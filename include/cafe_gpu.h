@@ -72,7 +72,7 @@ typedef struct {
   unsigned long long cycles_select;    /* event-loop SM cycles in event selection */
   unsigned long long cycles_apply;     /* ... applying the capture/nucleation */
   unsigned long long cycles_fill;      /* ... neighbour bookkeeping and new frontier rows */
-  unsigned long long graph_captures;   /* step graphs captured (1, 4 or 16 steps each) */
+  unsigned long long graph_captures;   /* step graphs captured (one per handle unless buffers move) */
 } cafe_stats;
 
 /* Grid::Grid (Grid.C:15-109, deck parse Grid.C:165-318) + Partition::

@@ -1,7 +1,6 @@
-"""Step scheduling paths give identical results: the chunked run (up to 16
-steps per CUDA graph launch, cafe_sim_run), single steps (one graph per step,
-cafe_sim_step) and the ungraphed launches (phase timing on), on a deck with
-rotated layers, new layers and output points every 7 steps."""
+"""The launch paths of a step give identical results: the step's CUDA graph
+(cafe_sim_run and cafe_sim_step) and the ungraphed launches (phase timing on),
+on a deck with rotated layers, new layers and output points every 7 steps."""
 import os
 
 import numpy as np
@@ -29,7 +28,7 @@ def _final(sim):
 
 
 @pytest.mark.parametrize("outint", [7, 1000000])
-def test_chunked_single_and_ungraphed_agree(tmp_path, outint):
+def test_graphed_and_ungraphed_steps_agree(tmp_path, outint):
     from amcafe_gb300 import Simulation
 
     deck = _deck(tmp_path, outint)
