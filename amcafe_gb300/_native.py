@@ -21,7 +21,7 @@ EXPORTS = (
     "cafe_sim_stream", "cafe_sim_mark", "cafe_sim_elapsed", "cafe_clean_layer_noalloc",
     "cafe_sim_set_build", "cafe_sim_download_build", "cafe_sim_download_output", "cafe_sim_write_output",
     "cafe_batch_create", "cafe_batch_run", "cafe_batch_size", "cafe_batch_sim", "cafe_batch_finished",
-    "cafe_batch_destroy",
+    "cafe_batch_destroy", "cafe_sim_checkpoint", "cafe_sim_restore",
 )
 PHASES = ("melt", "classify", "gather", "events", "writeback", "layer")
 NPHASE = 8
@@ -106,6 +106,8 @@ def load():
         "cafe_batch_sim": (P, [P, I]),
         "cafe_batch_finished": (I, [P, I]),
         "cafe_batch_destroy": (None, [P]),
+        "cafe_sim_checkpoint": (I, [P, ctypes.c_char_p]),
+        "cafe_sim_restore": (I, [P, ctypes.c_char_p]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

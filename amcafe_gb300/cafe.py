@@ -155,6 +155,16 @@ class Simulation:
         <prefix>.<dataset>.bin (prefix such as "out/run120.h5")."""
         check(self._lib.cafe_sim_write_output(self._h, os.fsencode(prefix)))
 
+    # -- checkpoint / restore --------------------------------------------------
+    def checkpoint(self, path):
+        """Writes the whole loop state to `path` (cafe_sim_checkpoint)."""
+        check(self._lib.cafe_sim_checkpoint(self._h, os.fsencode(path)))
+
+    def restore(self, path):
+        """Loads a checkpoint written from the same deck, in place of
+        InitializeVoxels + begin (cafe_sim_restore)."""
+        check(self._lib.cafe_sim_restore(self._h, os.fsencode(path)))
+
     def upload_state(self, gID, vState, extents, centroid, ctheta):
         gID = np.ascontiguousarray(gID, np.int32)
         vState = np.ascontiguousarray(vState, np.int32)

@@ -158,10 +158,10 @@ int parse_deck(const char *path, GridH &g) {
   return CAFE_OK;
 }
 
-void grid_laser_grid(GridH &g, bool init) {
+// The laser points rotated by the current gth (Grid.C:82-103).
+void grid_rotate_points(GridH &g, bool init) {
   double gmid0 = g.LX[0] / 2., gmid1 = g.LX[1] / 2.;
   double xlmin = (g.LX[0] - g.gsize[0]) / 2., ylmin = (g.LX[1] - g.gsize[1]) / 2.;
-  g.gth += g.gth0;
   for (int j2 = 0; j2 < g.Ntd; ++j2)
     for (int j1 = 0; j1 < g.Nsd; ++j1) {
       int k = g.Nsd * j2 + j1;
@@ -174,6 +174,10 @@ void grid_laser_grid(GridH &g, bool init) {
       g.lcoor2[2 * k + 1] = std::sin(g.gth) * (g.lcoor[2 * k] - gmid0) +
                             std::cos(g.gth) * (g.lcoor[2 * k + 1] - gmid1) + gmid1;
     }
+}
+void grid_laser_grid(GridH &g, bool init) {
+  g.gth += g.gth0;
+  grid_rotate_points(g, init);
 }
 
 // Grid constructor tail (Grid.C:69-108).
@@ -1916,6 +1920,163 @@ int cafe_sim_write_output(cafe_sim *s, const char *prefix) {
     if (rc) return rc;
   }
   return write_xdmf(s, prefix);
+}
+
+// ------------------------------------------------------------------ checkpoint
+namespace {
+const char kCkptMagic[8] = {'C', 'A', 'F', 'E', 'C', 'K', 'P', 'T'};
+struct CkptHeader {
+  char magic[8];
+  int32_t version, nx, ny, nz;
+  double time, gth;
+  int32_t tInd, isp, inewscanflg, inewlayerflg, indlayer, ilaserLoc, tf_tInd, nGrain, done, output_due;
+  int64_t steps;
+  uint32_t genlayer_state, pad;
+};
+// Reads `bytes` from fp into device memory dst through the pinned buffer.
+int stream_from_file(cafe_sim *s, FILE *fp, const std::string &path, long long bytes, void *dst) {
+  for (long long off = 0; off < bytes; off += CAFE_XFER_BYTES) {
+    long long n = std::min<long long>(CAFE_XFER_BYTES, bytes - off);
+    CUDA_TRY(cudaStreamSynchronize(s->stream));  // the previous chunk has left the buffer
+    if (std::fread(s->h_out, 1, n, fp) != (size_t)n) return fail(CAFE_E_IO, "'%s' is truncated", path.c_str());
+    CUDA_TRY(cudaMemcpyAsync((unsigned char *)dst + off, s->h_out, n, cudaMemcpyHostToDevice, s->stream));
+  }
+  CUDA_TRY(cudaStreamSynchronize(s->stream));
+  return CAFE_OK;
+}
+int ensure_host_buffer(cafe_sim *s) {
+  if (!s->h_out && cudaMallocHost((void **)&s->h_out, CAFE_XFER_BYTES) != cudaSuccess) {
+    s->h_out = nullptr;
+    return fail(CAFE_E_CUDA, "cudaMallocHost of the transfer buffer failed");
+  }
+  return CAFE_OK;
+}
+}  // namespace
+
+int cafe_sim_checkpoint(cafe_sim *s, const char *path) {
+  if (!s || !path) return fail(CAFE_E_ARG, "null argument");
+  if (!s->begun) return fail(CAFE_E_STATE, "checkpoint before begin");
+  CUDA_TRY(cudaSetDevice(s->device));
+  int rc = sim_sync(s);
+  if (rc || (rc = ensure_host_buffer(s)) || (rc = read_ctr(s, CTR_NGRAIN, &s->nGrain))) return rc;
+  const GridH &g = s->g;
+  CkptHeader h;
+  std::memset(&h, 0, sizeof h);
+  std::memcpy(h.magic, kCkptMagic, 8);
+  h.version = 1;
+  h.nx = g.nX[0];
+  h.ny = g.nX[1];
+  h.nz = g.nX[2];
+  h.time = g.time;
+  h.gth = g.gth;
+  h.tInd = g.tInd;
+  h.isp = g.isp;
+  h.inewscanflg = g.inewscanflg;
+  h.inewlayerflg = g.inewlayerflg;
+  h.indlayer = g.indlayer;
+  h.ilaserLoc = g.ilaserLoc;
+  h.tf_tInd = s->tf_tInd;
+  h.nGrain = s->nGrain;
+  h.done = s->done ? 1 : 0;
+  h.output_due = s->output_due ? 1 : 0;
+  h.steps = s->steps;
+  {
+    std::ostringstream os;
+    os << s->genlayer;
+    h.genlayer_state = (uint32_t)std::stoul(os.str());
+  }
+  const std::string p(path);
+  FILE *fp = std::fopen(path, "wb");
+  if (!fp) return fail(CAFE_E_IO, "cannot open '%s' for writing", path);
+  const long long N = s->K.N;
+  const CafeDev &D = s->D;
+  if (std::fwrite(&h, sizeof h, 1, fp) != 1) rc = fail(CAFE_E_IO, "write to '%s' failed", path);
+  // voxel fields in the device layout, then cTheta
+  struct Part {
+    const void *p;
+    long long bytes;
+  } parts[] = {{D.gid, N * 4}, {D.state, N}, {D.ext, N * 8}, {D.cx, N * 8}, {D.cy, N * 8},
+               {D.cz, N * 8}, {D.buildj, N}, {D.build, N}, {D.cth, 32LL * s->nGrain}};
+  for (const Part &pt : parts)
+    if (!rc) rc = stream_to_file(s, fp, p, pt.bytes, pt.p);
+  if (std::fclose(fp) != 0 && !rc) rc = fail(CAFE_E_IO, "write to '%s' failed", path);
+  return rc;
+}
+
+int cafe_sim_restore(cafe_sim *s, const char *path) {
+  if (!s || !path) return fail(CAFE_E_ARG, "null argument");
+  CUDA_TRY(cudaSetDevice(s->device));
+  int rc = sim_sync(s);
+  if (rc || (rc = ensure_host_buffer(s)) || (rc = ensure_xfer(s))) return rc;
+  FILE *fp = std::fopen(path, "rb");
+  if (!fp) return fail(CAFE_E_IO, "cannot open '%s'", path);
+  CkptHeader h;
+  GridH &g = s->g;
+  const long long N = s->K.N;
+  if (std::fread(&h, sizeof h, 1, fp) != 1 || std::memcmp(h.magic, kCkptMagic, 8) != 0 || h.version != 1) {
+    std::fclose(fp);
+    return fail(CAFE_E_ARG, "'%s' is not a checkpoint of this engine", path);
+  }
+  if (h.nx != g.nX[0] || h.ny != g.nX[1] || h.nz != g.nX[2] || h.nGrain < 0 || h.isp < 0 || h.isp >= g.NpT) {
+    std::fclose(fp);
+    return fail(CAFE_E_ARG, "checkpoint '%s' does not belong to this deck (grid %dx%dx%d)", path, h.nx, h.ny, h.nz);
+  }
+  if ((rc = grow_grains(s, (long long)h.nGrain + 1))) {
+    std::fclose(fp);
+    return rc;
+  }
+  // the state is replaced from here on: usable again only after a complete restore
+  s->initialized = false;
+  s->begun = false;
+  CafeDev &D = s->D;
+  struct Part {
+    void *p;
+    long long bytes;
+  } parts[] = {{D.gid, N * 4}, {D.state, N}, {D.ext, N * 8}, {D.cx, N * 8}, {D.cy, N * 8},
+               {D.cz, N * 8}, {D.buildj, N}, {D.build, N}, {D.cth, 32LL * h.nGrain}};
+  for (const Part &pt : parts)
+    if (!rc) rc = stream_from_file(s, fp, path, pt.bytes, pt.p);
+  if (!rc && std::fgetc(fp) != EOF) rc = fail(CAFE_E_ARG, "'%s' has trailing data", path);
+  std::fclose(fp);
+  if (rc) return rc;
+  // value checks (as cafe_sim_upload_state)
+  cudaStream_t st = s->stream;
+  CUDA_TRY(cudaMemsetAsync(s->d_bad, 0, sizeof(int), st));
+  k_check_range_i32<<<grid_blocks(N, 256, s), 256, 0, st>>>(D.gid, N, h.nGrain, s->d_bad, 2);
+  k_check_range_u8<<<grid_blocks(N, 256, s), 256, 0, st>>>(D.state, N, 3, s->d_bad, 1);
+  k_check_range_u8<<<grid_blocks(N, 256, s), 256, 0, st>>>(D.buildj, N, 1, s->d_bad, 4);
+  k_check_range_u8<<<grid_blocks(N, 256, s), 256, 0, st>>>(D.build, N, 1, s->d_bad, 4);
+  if (h.nGrain > 0) k_rot_range<<<grid_blocks(h.nGrain, 128, s), 128, 0, st>>>(D, 0, h.nGrain);
+  CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaMemcpyAsync(s->h_pinned + 3, s->d_bad, sizeof(int), cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaStreamSynchronize(st));
+  int bad = s->h_pinned[3];
+  if (bad) return fail(CAFE_E_ARG, "checkpoint '%s' holds out-of-range values (flags %d)", path, bad);
+  // host state
+  g.time = h.time;
+  g.gth = h.gth;
+  grid_rotate_points(g, false);
+  g.tInd = h.tInd;
+  g.isp = h.isp;
+  g.inewscanflg = h.inewscanflg;
+  g.inewlayerflg = h.inewlayerflg;
+  g.indlayer = h.indlayer;
+  g.ilaserLoc = h.ilaserLoc;
+  s->tf_tInd = h.tf_tInd;
+  s->genlayer.seed(h.genlayer_state);
+  s->nGrain = h.nGrain;
+  s->h_pinned[2] = h.nGrain;
+  CUDA_TRY(cudaMemcpyAsync(D.ctr + CTR_NGRAIN, s->h_pinned + 2, sizeof(int), cudaMemcpyHostToDevice, st));
+  CUDA_TRY(cudaMemsetAsync(D.ctr + CTR_NLIQ, 0, sizeof(int), st));
+  s->steps = h.steps;
+  s->done = h.done != 0;
+  s->output_due = h.output_due != 0;
+  s->have_P = false;
+  s->full_k2 = true;          // the liquid list is rebuilt by a dense pass
+  s->have_prev_box = false;
+  s->initialized = true;
+  s->begun = true;
+  return sim_sync(s);
 }
 
 }  // extern "C"

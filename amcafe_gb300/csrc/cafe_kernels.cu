@@ -2294,3 +2294,9 @@ __global__ void k_temp_copy_f(const double *T, long long off, long long n, float
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
     out[i] = (float)T[off + i];
 }
+
+// Sets bit `bit` of *bad if some v[i] > maxv.
+__global__ void k_check_range_u8(const uint8_t *v, long long n, int maxv, int *bad, int bit) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    if (v[i] > maxv) atomicOr(bad, bit);
+}

@@ -175,6 +175,18 @@ int cafe_sim_download_output(cafe_sim *sim, float *temperature, float *ipfz, flo
  * <base><tInd>.h5 corresponds to prefix "<base><tInd>.h5". */
 int cafe_sim_write_output(cafe_sim *sim, const char *prefix);
 
+/* Checkpoint of the whole loop state (no counterpart in the reference, which
+ * restarts from a deck): the Grid scalars (time, tInd, laser index, scan and
+ * layer flags, layer, laser plane, rotation), TempField::tInd,
+ * VoxelsCA::genlayer and nGrain, the loop counters, the voxel fields (gID,
+ * vState, extents, centroidOct, BuildjID, Build) and cTheta, in one binary
+ * file. cafe_sim_restore loads it into a handle created from the same deck
+ * (instead of initialize_voxels and begin); the loop then continues with
+ * cafe_sim_step and reaches the same results as the run that wrote it. A
+ * restore that fails leaves the handle unusable until a successful one. */
+int cafe_sim_checkpoint(cafe_sim *sim, const char *path);
+int cafe_sim_restore(cafe_sim *sim, const char *path);
+
 /* Batched ensemble (no counterpart in the reference, which runs one
  * realisation per MPI job): n independent realisations, one deck each, on
  * one device. Each is a cafe_sim handle with its own stream; `threads` host
