@@ -167,7 +167,7 @@ enum {
 };
 enum { STAT_EVENTS = 0, STAT_NUC, STAT_MAXNA, STAT_MAXROWS, STAT_STEPS, STAT_NEGDT, STAT_SUMNA, STAT_SUMROWS,
        STAT_SLOWSTEPS, STAT_EVALS, STAT_CYC_SELECT, STAT_CYC_APPLY, STAT_CYC_FILL, STAT_CYC_OTHER,
-       STAT_DETAIL, STAT_COUNT = STAT_DETAIL + 32 };
+       STAT_EASM_INTEGRALS, STAT_DETAIL, STAT_COUNT = STAT_DETAIL + 32 };
 
 // --------------------------------------------------------------- temperature
 // TempField::AnalyticTempCurr (TempField.C:155-190) for one cell; returns the

@@ -1470,6 +1470,7 @@ int cafe_sim_stats(cafe_sim *s, cafe_stats *st) {
   st->cycles_apply = v[STAT_CYC_APPLY];
   st->cycles_fill = v[STAT_CYC_FILL];
   st->graph_captures = (unsigned long long)s->graph_captures;
+  st->easm_integrals = v[STAT_EASM_INTEGRALS];
 #ifdef CAFE_DETAIL_CYCLES
   fprintf(stderr, "cafe detail cycles:");
   for (int c = 0; c < 32; ++c) fprintf(stderr, " %llu", v[STAT_DETAIL + c]);

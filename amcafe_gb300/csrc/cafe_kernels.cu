@@ -2199,6 +2199,7 @@ __global__ void k_easm_reset(CafeDev D) {
 __global__ void k_easm(CafeDev D, CafeConsts K, CafeStepParams P, CafeEasm E, long long ncell) {
   __shared__ double s_Lx[CAFE_EASM_NODES];
   __shared__ int s_box[6], s_cold;
+  __shared__ unsigned long long s_integrals;
   const double t = 80.0e-5;
   if (threadIdx.x < CAFE_EASM_NODES) {
     double x0 = P.lx - E.bmV * t;  // Utilities.C:243-244
@@ -2208,8 +2209,12 @@ __global__ void k_easm(CafeDev D, CafeConsts K, CafeStepParams P, CafeEasm E, lo
     s_box[threadIdx.x] = 0x7fffffff;
     s_box[3 + threadIdx.x] = -1;
   }
-  if (threadIdx.x == 0) s_cold = 0;
+  if (threadIdx.x == 0) {
+    s_cold = 0;
+    s_integrals = 0;
+  }
   __syncthreads();
+  unsigned long long nint = 0;
   for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < ncell;
        idx += (long long)gridDim.x * blockDim.x) {
     int i, j, k;
@@ -2234,6 +2239,7 @@ __global__ void k_easm(CafeDev D, CafeConsts K, CafeStepParams P, CafeEasm E, lo
         n++;
       }
       T = Tnew;
+      nint += 1 + n;
     }
     D.temp[idx] = T;
     if (T > K.tL)
@@ -2251,7 +2257,9 @@ __global__ void k_easm(CafeDev D, CafeConsts K, CafeStepParams P, CafeEasm E, lo
       s_cold = 1;
     }
   }
+  if (nint) atomicAdd(&s_integrals, nint);
   __syncthreads();
+  if (threadIdx.x == 0 && s_integrals) atomicAdd(&D.stat[STAT_EASM_INTEGRALS], s_integrals);
   if (threadIdx.x < 3 && s_box[3 + threadIdx.x] >= 0) {
     atomicMin(&D.ctr[CTR_EASM_BOX + threadIdx.x], s_box[threadIdx.x]);
     atomicMax(&D.ctr[CTR_EASM_BOX + 3 + threadIdx.x], s_box[3 + threadIdx.x]);

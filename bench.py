@@ -42,12 +42,23 @@ WORKLOADS = {
     "c1": ("amcafe_gb300/decks/c1.in", 2000, "config 1: 512x256x128 voxels @2.5um, 4 layers, hatching 100um"),
     "c2": ("amcafe_gb300/decks/c2.in", 1200, "config 2: 1024x1024x256 voxels @2.5um, 10 layers, 67 deg rotation"),
     "c0": ("amcafe_gb300/decks/c0.in", 300, "config 0: 128x64x32 voxels @2.5um, single track"),
+    "c0e": ("amcafe_gb300/decks/c0_easm.in", 100, "config 0 geometry with the EASM temperature: 128x64x32 "
+                                                   "voxels @2.5um, single track, 200 W"),
     "c3": (None, 0, "config 3: ensemble of single-track realisations, sides U(96,192) voxels @2.5um, "
                     "v U(0.5,1.5) m/s, P U(150,300) W, seeds 1..n, run batched on one GPU"),
 }
 ENSEMBLE_HOST_SEED = 20240603
 ENSEMBLE_ACTIVE_CAPACITY = 1 << 18  # active cells per step of one realisation
 FALLBACK_HBM_GBS = 6800.0
+# EASM field: FP64 operations per quadrature node of Utilities::Integral as the
+# kernel evaluates them with per-integral invariants hoisted (6 multiplies,
+# 5 adds or subtracts, 3 divisions, the weighted accumulation's multiply and
+# add, the final product, and exp counted as one), against the nominal FP64
+# rate of GB300 in instructions (1.25 TFLOP/s counts an FMA as two flops;
+# these operations are single instructions)
+EASM_OPS_PER_NODE = 18
+EASM_NODES = 25
+FP64_NOMINAL_GOPS = 625.0
 BYTES_DENSE_PER_VOXEL = 2   # read + write of the uint8 cell state per voxel-update
 BYTES_PER_FRONT_CELL = 74   # gID 4, extents 8, centroid 24, state 1; read and written
 
@@ -436,13 +447,25 @@ def main():
     achieved = bytes_per_launch / (per_launch_ms * 1e-3) / 1e9
     avg_na_timed = (stats1["sum_active"] - stats0["sum_active"]) / max(1, stats1["steps"] - stats0["steps"])
     step_bytes = BYTES_DENSE_PER_VOXEL * nvox + BYTES_PER_FRONT_CELL * avg_na_timed
-    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "traffic": committed_traffic(args.workload, dom),
-                "kernel": {"events": "k_event_loop", "classify": "k_active_count/k_active_scatter",
-                           "gather": "k_gather", "melt": "k_melt", "writeback": "k_writeback"}.get(dom, dom),
-                "phase": dom, "peak_source": peak_src,
-                "phase_steps": kp,
-                "step_achieved_GBs": step_bytes * k / (ms * 1e-3) / 1e9}
+    easm = "easm" in open(deck).read().lower()
+    if easm and dom == "melt":
+        # the EASM field (k_easm) is FP64-bound: operations per step over its time
+        integrals = (statsp1["easm_integrals"] - statsp0["easm_integrals"]) / steps_done
+        ops = integrals * EASM_NODES * EASM_OPS_PER_NODE
+        achieved = ops / (dom_ms / steps_done * 1e-3) / 1e9
+        roofline = {"bound": "fp64", "achieved": achieved, "peak": FP64_NOMINAL_GOPS, "unit": "GOP/s",
+                    "frac": achieved / FP64_NOMINAL_GOPS, "traffic": committed_traffic(args.workload, dom),
+                    "kernel": "k_easm", "phase": dom, "phase_steps": kp,
+                    "peak_source": "nominal FP64 rate in instructions (1.25 TFLOP/s with an FMA as two flops)",
+                    "integrals_per_step": integrals, "ops_per_node": EASM_OPS_PER_NODE}
+    else:
+        roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                    "frac": achieved / peak, "traffic": committed_traffic(args.workload, dom),
+                    "kernel": {"events": "k_event_loop", "classify": "k_active_count/k_active_scatter",
+                               "gather": "k_gather", "melt": "k_melt", "writeback": "k_writeback"}.get(dom, dom),
+                    "phase": dom, "peak_source": peak_src,
+                    "phase_steps": kp,
+                    "step_achieved_GBs": step_bytes * k / (ms * 1e-3) / 1e9}
 
     # ---- end to end through the C ABI with host buffers
     e2e = None

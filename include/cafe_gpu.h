@@ -73,6 +73,7 @@ typedef struct {
   unsigned long long cycles_apply;     /* ... applying the capture/nucleation */
   unsigned long long cycles_fill;      /* ... neighbour bookkeeping and new frontier rows */
   unsigned long long graph_captures;   /* step graphs captured (one per handle unless buffers move) */
+  unsigned long long easm_integrals;   /* EASM: Utilities::Integral evaluations (25 nodes each) */
 } cafe_stats;
 
 /* Grid::Grid (Grid.C:15-109, deck parse Grid.C:165-318) + Partition::
