@@ -80,6 +80,14 @@ struct CafeConsts {
 // 228-249), computed on the host: the 25-node Gauss-Legendre rule on
 // [0, 8e-4 s], t - x_i and (t - x_i)^(-1/2) per node.
 #define CAFE_EASM_NODES 25
+// A cell whose fixed point has not converged after CAFE_EASM_LANE_INTEGRALS
+// integrals in the lane-per-cell pass continues in the warp-per-cell pass.
+#define CAFE_EASM_LANE_INTEGRALS 4
+struct CafeEasmItem {
+  long long idx;
+  double Told, Tnew;
+  int n, pad;
+};
 struct CafeEasm {
   double qw[CAFE_EASM_NODES], qx[CAFE_EASM_NODES], tx[CAFE_EASM_NODES], r[CAFE_EASM_NODES];
   double bmV, Q, layerT;
@@ -99,6 +107,9 @@ struct CafeDev {
   uint8_t *build;
   // EASM mode: TempField::TempCurr per cell, growth velocity per active position
   double *temp, *a_vh;
+  // EASM cells handed from the lane-per-cell pass to the warp-per-cell pass
+  struct CafeEasmItem *easm_q;
+  long long easm_qcap;
   // this step's parameters (the kernels of a step read them from here)
   CafeStepParams *Pd;
   // liquid cells left by the previous step (cell indices)
@@ -163,8 +174,12 @@ enum {
   CTR_NPAIRS,      // (row, slot) pairs listed for the row set-up
   CTR_EASM_BOX,    // 6 slots: box of the cells at or above the liquidus (EASM)
   CTR_EASM_COLD = CTR_EASM_BOX + 6,  // 1: some cell below the liquidus (EASM)
+  CTR_EASM_CURSOR = CTR_EASM_COLD + 2,  // 2 slots, 8-byte aligned: next cell of the EASM field
+  CTR_EASM_QN = CTR_EASM_CURSOR + 2,    // cells queued for the warp-per-cell pass
+  CTR_EASM_QHEAD,                       // next queued cell to take
   CTR_COUNT
 };
+static_assert(CTR_EASM_CURSOR % 2 == 0, "64-bit cursor needs an 8-byte aligned slot");
 enum { STAT_EVENTS = 0, STAT_NUC, STAT_MAXNA, STAT_MAXROWS, STAT_STEPS, STAT_NEGDT, STAT_SUMNA, STAT_SUMROWS,
        STAT_SLOWSTEPS, STAT_EVALS, STAT_CYC_SELECT, STAT_CYC_APPLY, STAT_CYC_FILL, STAT_CYC_OTHER,
        STAT_EASM_INTEGRALS, STAT_DETAIL, STAT_COUNT = STAT_DETAIL + 32 };

@@ -666,9 +666,12 @@ int easm_field(cafe_sim *s) {
   {
     PhaseScope ps(s, CAFE_PH_MELT);
     k_easm_reset<<<1, 32, 0, s->stream>>>(s->D);
-    if (ncell > 0)
-      k_easm<<<grid_blocks(ncell, 256, s), 256, 0, s->stream>>>(s->D, K, P, s->E, ncell);
-    LAUNCHED(CAFE_PH_MELT, 2);
+    if (ncell > 0) {  // persistent: a few blocks per SM pull cells from a cursor
+      k_easm<<<(int)std::min<long long>((ncell + 255) / 256, (long long)s->nsm * 3), 256, 0, s->stream>>>(
+          s->D, K, P, s->E, ncell);
+      k_easm_long<<<s->nsm * 3, 256, 0, s->stream>>>(s->D, K, P, s->E);
+    }
+    LAUNCHED(CAFE_PH_MELT, 3);
   }
   CUDA_TRY(cudaGetLastError());
   int *h = s->h_pinned + 8;  // 7 ints: box lo, box hi, cold
@@ -1130,7 +1133,8 @@ int cafe_sim_create(const char *deck_path, const cafe_options *opt, cafe_sim **o
       (rc = dalloc(&D.row_bruq, D.row_cap, o)) ||
       (rc = dalloc(&D.ctr, CTR_COUNT, o)) || (rc = dalloc(&D.err, 1, o)) || (rc = dalloc(&D.stat, STAT_COUNT, o)) ||
       (rc = dalloc(&D.Pd, 1, o)) || (rc = dalloc(&D.tcls, std::max<long long>(D.tcls_cap, 1), o)) ||
-      (K.easm && ((rc = dalloc(&D.temp, N, o)) || (rc = dalloc(&D.a_vh, acap, o))))) {
+      (K.easm && ((rc = dalloc(&D.temp, N, o)) || (rc = dalloc(&D.a_vh, acap, o)) ||
+                  (rc = dalloc(&D.easm_q, (size_t)(D.easm_qcap = std::min<long long>(N, 1LL << 21)), o))))) {
     cafe_sim_destroy(s);
     return rc;
   }

@@ -2192,10 +2192,16 @@ __global__ void k_easm_reset(CafeDev D) {
   if (t < 3) D.ctr[CTR_EASM_BOX + t] = 0x7fffffff;
   else if (t < 6) D.ctr[CTR_EASM_BOX + t] = -1;
   else if (t == 6) D.ctr[CTR_EASM_COLD] = 0;
+  else if (t == 7) *(unsigned long long *)&D.ctr[CTR_EASM_CURSOR] = 0ULL;
+  else if (t == 8) D.ctr[CTR_EASM_QN] = 0;
+  else if (t == 9) D.ctr[CTR_EASM_QHEAD] = 0;
 }
 // Cells [0, ncell) (cells above the laser plane keep T = 0). Writes temp,
 // BuildjID, the box of the cells at or above the liquidus and the "some cell
-// below the liquidus" flag.
+// below the liquidus" flag. Cells need 2 to 100 integrals each, so each
+// thread takes the next cell from a shared cursor whenever its own has
+// converged: the lanes of a warp then run the same 25-node loop together
+// instead of idling behind the slowest cell of a fixed assignment.
 __global__ void k_easm(CafeDev D, CafeConsts K, CafeStepParams P, CafeEasm E, long long ncell) {
   __shared__ double s_Lx[CAFE_EASM_NODES];
   __shared__ int s_box[6], s_cold;
@@ -2215,48 +2221,120 @@ __global__ void k_easm(CafeDev D, CafeConsts K, CafeStepParams P, CafeEasm E, lo
   }
   __syncthreads();
   unsigned long long nint = 0;
-  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < ncell;
-       idx += (long long)gridDim.x * blockDim.x) {
-    int i, j, k;
-    cafe_cell_xyz(K, idx, i, j, k);
-    double x0 = ((double)i + .5) * K.dx[0];
-    double y0 = ((double)j + .5) * K.dx[1];
-    double zp = ((double)k + .5) * K.dx[2];
-    if (zp > P.lz) continue;
-    double xp = P.cg * (x0 - K.hLX0) + P.sg * (y0 - K.hLX1) + K.hLX0;
-    double yp = -P.sg * (x0 - K.hLX0) + P.cg * (y0 - K.hLX1) + K.hLX1;
-    double T;
-    if ((x0 > P.lx) && (zp > (P.lz - E.layerT))) {
-      T = .99 * K.T0;
-    } else {
-      double Told = 0.0;
-      double Tnew = cafe_easm_integral(E, s_Lx, xp, yp, zp, P.ly, P.lz, 0.0);
-      int n = 0;
-      while (fabs(Told - Tnew) > 10.0 && n < 100) {
-        Told = Tnew;
-        double Tt = cafe_easm_integral(E, s_Lx, xp, yp, zp, P.ly, P.lz, Told);
-        Tnew = 0.5 * (Told + Tt);
-        n++;
+  int bx0 = 0x7fffffff, by0 = 0x7fffffff, bz0 = 0x7fffffff, bx1 = -1, by1 = -1, bz1 = -1, cold = 0;
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  long long idx = -1;  // this lane's cell, -1 when it needs one
+  bool exhausted = false;
+  int ci = 0, cj = 0, ck = 0, n = 0, done_here = 0;
+  bool first = true;
+  double xp = 0, yp = 0, zp = 0, Told = 0, Tnew = 0, Tin = 0;
+  // warp-synchronous rounds: lanes without a cell take new ones together (one
+  // atomic per warp), then every lane evaluates one integral (lanes without a
+  // cell on dummy inputs, discarded), so the warp stays converged
+  while (true) {
+    bool need = idx < 0 && !exhausted;
+    unsigned needm = __ballot_sync(FULL, need);
+    if (needm) {
+      unsigned long long base = 0;
+      int leader = __ffs(needm) - 1;
+      if (lane == leader) base = atomicAdd((unsigned long long *)&D.ctr[CTR_EASM_CURSOR], (unsigned long long)__popc(needm));
+      base = __shfl_sync(FULL, base, leader);
+      if (need) {
+        long long r = (long long)(base + __popc(needm & ((1u << lane) - 1u)));
+        // from the top down: the cells just below the laser plane take the most
+        // integrals, and handing them out first keeps the end of the pass from
+        // waiting on a few long cells
+        long long c = ncell - 1 - r;
+        if (r >= ncell) {
+          exhausted = true;
+        } else {
+          cafe_cell_xyz(K, c, ci, cj, ck);
+          double x0 = ((double)ci + .5) * K.dx[0];
+          double y0 = ((double)cj + .5) * K.dx[1];
+          zp = ((double)ck + .5) * K.dx[2];
+          if (zp > P.lz) {
+            // above the laser plane: T stays 0 (TempField.C:99)
+          } else if ((x0 > P.lx) && (zp > (P.lz - E.layerT))) {
+            double T = .99 * K.T0;
+            D.temp[c] = T;
+            if (T > K.tL)
+              D.buildj[c] = 1;
+            else if (T < K.T0)
+              D.buildj[c] = 0;
+            if (T >= K.tL) {
+              bx0 = min(bx0, ci); by0 = min(by0, cj); bz0 = min(bz0, ck);
+              bx1 = max(bx1, ci); by1 = max(by1, cj); bz1 = max(bz1, ck);
+            } else {
+              cold = 1;
+            }
+          } else {
+            xp = P.cg * (x0 - K.hLX0) + P.sg * (y0 - K.hLX1) + K.hLX0;
+            yp = -P.sg * (x0 - K.hLX0) + P.cg * (y0 - K.hLX1) + K.hLX1;
+            idx = c;
+            first = true;
+            Told = 0.0;
+            Tin = 0.0;
+            n = 0;
+            done_here = 0;
+          }
+        }
       }
-      T = Tnew;
-      nint += 1 + n;
     }
+    const bool work = idx >= 0;
+    if (__all_sync(FULL, !work && exhausted)) break;
+    if (!__any_sync(FULL, work)) continue;  // only cells without integrals were taken
+    // one integral per lane; then the step of Utilities::EASM_Temp_LG's loop
+    double Tres = cafe_easm_integral(E, s_Lx, xp, yp, zp, P.ly, P.lz, Tin);
+    if (!work) continue;
+    ++nint;
+    if (first) {
+      Tnew = Tres;
+      first = false;
+    } else {
+      Tnew = 0.5 * (Told + Tres);
+      n++;
+    }
+    if (fabs(Told - Tnew) > 10.0 && n < 100) {
+      // a long fixed point goes on in the warp-per-cell pass (when the queue
+      // has room), from this point of the loop: test passed, next integral due
+      if (++done_here >= CAFE_EASM_LANE_INTEGRALS) {
+        int slot = atomicAdd(&D.ctr[CTR_EASM_QN], 1);
+        if (slot < D.easm_qcap) {
+          CafeEasmItem it;
+          it.idx = idx;
+          it.Told = Told;
+          it.Tnew = Tnew;
+          it.n = n;
+          it.pad = 0;
+          D.easm_q[slot] = it;
+          idx = -1;
+          continue;
+        }
+      }
+      Told = Tnew;
+      Tin = Told;
+      continue;
+    }
+    double T = Tnew;
     D.temp[idx] = T;
     if (T > K.tL)
       D.buildj[idx] = 1;
     else if (T < K.T0)
       D.buildj[idx] = 0;
     if (T >= K.tL) {
-      atomicMin(&s_box[0], i);
-      atomicMin(&s_box[1], j);
-      atomicMin(&s_box[2], k);
-      atomicMax(&s_box[3], i);
-      atomicMax(&s_box[4], j);
-      atomicMax(&s_box[5], k);
+      bx0 = min(bx0, ci); by0 = min(by0, cj); bz0 = min(bz0, ck);
+      bx1 = max(bx1, ci); by1 = max(by1, cj); bz1 = max(bz1, ck);
     } else {
-      s_cold = 1;
+      cold = 1;
     }
+    idx = -1;
   }
+  if (bx1 >= 0) {
+    atomicMin(&s_box[0], bx0); atomicMin(&s_box[1], by0); atomicMin(&s_box[2], bz0);
+    atomicMax(&s_box[3], bx1); atomicMax(&s_box[4], by1); atomicMax(&s_box[5], bz1);
+  }
+  if (cold) s_cold = 1;
   if (nint) atomicAdd(&s_integrals, nint);
   __syncthreads();
   if (threadIdx.x == 0 && s_integrals) atomicAdd(&D.stat[STAT_EASM_INTEGRALS], s_integrals);
@@ -2266,6 +2344,113 @@ __global__ void k_easm(CafeDev D, CafeConsts K, CafeStepParams P, CafeEasm E, lo
   }
   if (threadIdx.x == 0 && s_cold) D.ctr[CTR_EASM_COLD] = 1;
 }
+// Utilities::Integral for one cell with the 25 nodes spread over the lanes of
+// a warp; the weighted terms are added in node order on every lane, as the
+// quadrature sum does, so the result is that of cafe_easm_integral.
+__device__ __forceinline__ double cafe_easm_integral_warp(const CafeEasm &E, const double *Lx, double R0, double R1,
+                                                          double R2, double Ly, double Lz, double T, int lane) {
+  const unsigned FULL = 0xffffffffu;
+  const double sigma = 50.0e-6, eta = 0.56, pi = 3.14159265358979323846;
+  double M[4];
+  cafe_easm_materials(T, M);
+  double C = eta * E.Q / (pi * M[2] * M[0] * sqrt(4 * pi * M[3]));
+  double sig2 = sigma * sigma;
+  double dy = R1 - Ly, dz = fabs(R2 - Lz);
+  double dy2 = dy * dy, dz2 = dz * dz;
+  double p = 0.0;
+  if (lane < CAFE_EASM_NODES) {
+    int i = lane;
+    double tx = E.tx[i];
+    double dx = R0 - Lx[i];
+    double a = C * E.r[i] / (2 * M[3] * tx + sig2);
+    double arg = -1 * (dx * dx + dy2) / (4 * M[3] * tx + 2 * sig2) - dz2 / (4 * M[3] * tx);
+    double f = arg < -745.2 ? a * 0.0 : a * crm_exp(arg);
+    p = E.qw[i] * f;
+  }
+  double s = 0.0;
+#pragma unroll
+  for (int i = 0; i < CAFE_EASM_NODES; ++i) s += __shfl_sync(FULL, p, i);
+  return 300 + s;
+}
+
+// The cells queued by k_easm: one warp per cell until its fixed point ends.
+__global__ void k_easm_long(CafeDev D, CafeConsts K, CafeStepParams P, CafeEasm E) {
+  __shared__ double s_Lx[CAFE_EASM_NODES];
+  __shared__ int s_box[6], s_cold;
+  __shared__ unsigned long long s_integrals;
+  const double t = 80.0e-5;
+  if (threadIdx.x < CAFE_EASM_NODES) {
+    double x0 = P.lx - E.bmV * t;
+    s_Lx[threadIdx.x] = x0 + E.bmV * E.qx[threadIdx.x];
+  }
+  if (threadIdx.x < 3) {
+    s_box[threadIdx.x] = 0x7fffffff;
+    s_box[3 + threadIdx.x] = -1;
+  }
+  if (threadIdx.x == 0) {
+    s_cold = 0;
+    s_integrals = 0;
+  }
+  __syncthreads();
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  int nq = D.ctr[CTR_EASM_QN];
+  if (nq > D.easm_qcap) nq = (int)D.easm_qcap;
+  unsigned long long nint = 0;
+  int bx0 = 0x7fffffff, by0 = 0x7fffffff, bz0 = 0x7fffffff, bx1 = -1, by1 = -1, bz1 = -1, cold = 0;
+  while (true) {
+    int q = 0;
+    if (lane == 0) q = atomicAdd(&D.ctr[CTR_EASM_QHEAD], 1);
+    q = __shfl_sync(FULL, q, 0);
+    if (q >= nq) break;
+    CafeEasmItem it = D.easm_q[q];
+    int ci, cj, ck;
+    cafe_cell_xyz(K, it.idx, ci, cj, ck);
+    double x0 = ((double)ci + .5) * K.dx[0];
+    double y0 = ((double)cj + .5) * K.dx[1];
+    double zp = ((double)ck + .5) * K.dx[2];
+    double xp = P.cg * (x0 - K.hLX0) + P.sg * (y0 - K.hLX1) + K.hLX0;
+    double yp = -P.sg * (x0 - K.hLX0) + P.cg * (y0 - K.hLX1) + K.hLX1;
+    double Told = it.Told, Tnew = it.Tnew;
+    int n = it.n;
+    // continue Utilities::EASM_Temp_LG's loop where the lane pass left it
+    while (fabs(Told - Tnew) > 10.0 && n < 100) {
+      Told = Tnew;
+      double Tt = cafe_easm_integral_warp(E, s_Lx, xp, yp, zp, P.ly, P.lz, Told, lane);
+      Tnew = 0.5 * (Told + Tt);
+      n++;
+      ++nint;
+    }
+    if (lane == 0) {
+      double T = Tnew;
+      D.temp[it.idx] = T;
+      if (T > K.tL)
+        D.buildj[it.idx] = 1;
+      else if (T < K.T0)
+        D.buildj[it.idx] = 0;
+      if (T >= K.tL) {
+        bx0 = min(bx0, ci); by0 = min(by0, cj); bz0 = min(bz0, ck);
+        bx1 = max(bx1, ci); by1 = max(by1, cj); bz1 = max(bz1, ck);
+      } else {
+        cold = 1;
+      }
+    }
+  }
+  if (bx1 >= 0) {
+    atomicMin(&s_box[0], bx0); atomicMin(&s_box[1], by0); atomicMin(&s_box[2], bz0);
+    atomicMax(&s_box[3], bx1); atomicMax(&s_box[4], by1); atomicMax(&s_box[5], bz1);
+  }
+  if (cold) s_cold = 1;
+  if (lane == 0 && nint) atomicAdd(&s_integrals, nint);
+  __syncthreads();
+  if (threadIdx.x == 0 && s_integrals) atomicAdd(&D.stat[STAT_EASM_INTEGRALS], s_integrals);
+  if (threadIdx.x < 3 && s_box[3 + threadIdx.x] >= 0) {
+    atomicMin(&D.ctr[CTR_EASM_BOX + threadIdx.x], s_box[threadIdx.x]);
+    atomicMax(&D.ctr[CTR_EASM_BOX + 3 + threadIdx.x], s_box[3 + threadIdx.x]);
+  }
+  if (threadIdx.x == 0 && s_cold) D.ctr[CTR_EASM_COLD] = 1;
+}
+
 // SetLiquid3 (VoxelsCA.C:1098-1116) and the class map over the box of the
 // cells at or above the liquidus, from the EASM temperatures.
 __global__ void k_melt_easm(CafeDev D, CafeConsts K, CafeStepParams P) {
