@@ -21,7 +21,8 @@ EXPORTS = (
     "cafe_sim_stream", "cafe_sim_mark", "cafe_sim_elapsed", "cafe_clean_layer_noalloc",
     "cafe_sim_set_build", "cafe_sim_download_build", "cafe_sim_download_output", "cafe_sim_write_output",
     "cafe_batch_create", "cafe_batch_run", "cafe_batch_size", "cafe_batch_sim", "cafe_batch_finished",
-    "cafe_batch_destroy", "cafe_sim_checkpoint", "cafe_sim_restore",
+    "cafe_batch_destroy", "cafe_sim_checkpoint", "cafe_sim_restore", "cafe_sim_set_growth_log",
+    "cafe_sim_growth_log_count", "cafe_adjoint_pool", "cafe_adjoint_growth",
 )
 PHASES = ("melt", "classify", "gather", "events", "writeback", "layer")
 NPHASE = 8
@@ -40,6 +41,13 @@ class CafeInfo(ctypes.Structure):
                 ("nlayerTot", ctypes.c_int), ("Nzh", ctypes.c_int), ("done", ctypes.c_int),
                 ("steps", ctypes.c_longlong), ("gth", ctypes.c_double), ("genlayer_state", ctypes.c_uint),
                 ("tf_tInd", ctypes.c_int), ("output_due", ctypes.c_int)]
+
+
+class CafeAdjointSetup(ctypes.Structure):
+    _fields_ = [("k", ctypes.c_double), ("alpha", ctypes.c_double), ("T0", ctypes.c_double), ("Tl", ctypes.c_double),
+                ("tau_T", ctypes.c_double), ("x_start", ctypes.c_double), ("y_src", ctypes.c_double),
+                ("z_src", ctypes.c_double), ("dt", ctypes.c_double), ("dx", ctypes.c_double),
+                ("nx", ctypes.c_int), ("ny", ctypes.c_int), ("nz", ctypes.c_int), ("step_final", ctypes.c_int)]
 
 
 class CafeStats(ctypes.Structure):
@@ -108,6 +116,10 @@ def load():
         "cafe_batch_destroy": (None, [P]),
         "cafe_sim_checkpoint": (I, [P, ctypes.c_char_p]),
         "cafe_sim_restore": (I, [P, ctypes.c_char_p]),
+        "cafe_sim_set_growth_log": (I, [P, P, P, P, LL]),
+        "cafe_sim_growth_log_count": (I, [P, ctypes.POINTER(LL)]),
+        "cafe_adjoint_pool": (I, [ctypes.POINTER(CafeAdjointSetup), f64p, f64p, f64p, f64p, P]),
+        "cafe_adjoint_growth": (I, [ctypes.POINTER(CafeAdjointSetup), f64p, P, P, P, LL, D, f64p, f64p, P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

@@ -50,7 +50,8 @@ def build_engine(force=False, verbose=False):
     if not force and not _stale(LIB, _sources()):
         return LIB
     cmd = [_nvcc()] + NVCC_FLAGS + [os.path.join(CSRC, "cafe_host.cu"), os.path.join(CSRC, "cafe_noalloc.cu"),
-                                    os.path.join(CSRC, "cafe_batch.cu"), "-o", LIB + ".tmp"]
+                                    os.path.join(CSRC, "cafe_batch.cu"), os.path.join(CSRC, "cafe_adjoint.cu"),
+                                    "-o", LIB + ".tmp"]
     if verbose:
         print(" ".join(cmd))
     subprocess.run(cmd, check=True)

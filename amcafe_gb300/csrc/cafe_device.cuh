@@ -110,6 +110,12 @@ struct CafeDev {
   // EASM cells handed from the lane-per-cell pass to the warp-per-cell pass
   struct CafeEasmItem *easm_q;
   long long easm_qcap;
+  // growth log (cafe_sim_set_growth_log): per frontier row of each step its
+  // cell, the step's Grid::tInd and its growth time (extent gained / velocity);
+  // caller-owned device arrays, glog_cap entries, NULL when off
+  int32_t *glog_cell, *glog_step;
+  double *glog_tau;
+  long long glog_cap;
   // this step's parameters (the kernels of a step read them from here)
   CafeStepParams *Pd;
   // liquid cells left by the previous step (cell indices)
@@ -177,6 +183,8 @@ enum {
   CTR_EASM_CURSOR = CTR_EASM_COLD + 2,  // 2 slots, 8-byte aligned: next cell of the EASM field
   CTR_EASM_QN = CTR_EASM_CURSOR + 2,    // cells queued for the warp-per-cell pass
   CTR_EASM_QHEAD,                       // next queued cell to take
+  CTR_GLOG_N,                           // growth-log entries written
+  CTR_GLOG_OVER,                        // 1: the growth log ran out of room
   CTR_COUNT
 };
 static_assert(CTR_EASM_CURSOR % 2 == 0, "64-bit cursor needs an 8-byte aligned slot");

@@ -842,8 +842,17 @@ int launch_voxels(cafe_sim *s, bool graph, const CafeStepParams *Pp) {
   {
     PhaseScope ps(s, CAFE_PH_EVENTS);
     k_event_loop<<<1, CAFE_LOOP_THREADS, 0, st>>>(D, K, Pp, D.act_cap + 1, s->event_scan ? 0 : 1);
+    if (D.glog_cell) {
+      k_glog_begin<<<s->gsm * 4, 256, 0, st>>>(D, Pp);
+      LAUNCHED(CAFE_PH_EVENTS, 1);
+    }
     k_rows_finalize<<<s->gsm * 4, 256, 0, st>>>(D);
     LAUNCHED(CAFE_PH_EVENTS, 2);
+    if (D.glog_cell) {
+      k_glog_end<<<s->gsm * 4, 256, 0, st>>>(D, K);
+      k_glog_advance<<<1, 1, 0, st>>>(D);
+      LAUNCHED(CAFE_PH_EVENTS, 2);
+    }
   }
   {
     PhaseScope ps(s, CAFE_PH_WRITEBACK);
@@ -2082,6 +2091,32 @@ int cafe_sim_restore(cafe_sim *s, const char *path) {
   s->initialized = true;
   s->begun = true;
   return sim_sync(s);
+}
+
+// ------------------------------------------------------------------ growth log
+int cafe_sim_set_growth_log(cafe_sim *s, int32_t *cells, int32_t *steps, double *tau, long long cap) {
+  if (!s) return fail(CAFE_E_ARG, "null handle");
+  if ((cells || steps || tau) && (!cells || !steps || !tau || cap <= 0 || cap > 0x7fffffffLL))
+    return fail(CAFE_E_ARG, "growth log needs three device arrays and 0 < cap < 2^31");
+  CUDA_TRY(cudaSetDevice(s->device));
+  int rc = sim_sync(s);
+  if (rc) return rc;
+  s->D.glog_cell = cells;
+  s->D.glog_step = steps;
+  s->D.glog_tau = tau;
+  s->D.glog_cap = cells ? cap : 0;
+  CUDA_TRY(cudaMemsetAsync(s->D.ctr + CTR_GLOG_N, 0, 2 * sizeof(int), s->stream));
+  return sim_sync(s);
+}
+
+int cafe_sim_growth_log_count(cafe_sim *s, long long *n) {
+  if (!s || !n) return fail(CAFE_E_ARG, "null argument");
+  CUDA_TRY(cudaSetDevice(s->device));
+  int v = 0, over = 0, rc;
+  if ((rc = read_ctr(s, CTR_GLOG_N, &v)) || (rc = read_ctr(s, CTR_GLOG_OVER, &over))) return rc;
+  if (over) return fail(CAFE_E_CAPACITY, "growth log full after %d entries", v);
+  *n = v;
+  return CAFE_OK;
 }
 
 }  // extern "C"

@@ -2493,3 +2493,45 @@ __global__ void k_check_range_u8(const uint8_t *v, long long n, int maxv, int *b
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
     if (v[i] > maxv) atomicOr(bad, bit);
 }
+
+// ------------------------------------------------------------------ growth log
+// Before k_rows_finalize: every frontier row of the step (those present at
+// the start and those created by captures) gets a log entry holding its cell
+// and its extent before the step's growth (a_ext still holds it: the start
+// value, or the value set at capture). tau temporarily holds that extent.
+__global__ void k_glog_begin(CafeDev D, const CafeStepParams *__restrict__ Pp) {
+  int nrows = D.ctr[CTR_NROWS_END];
+  if (nrows > D.row_cap) nrows = (int)D.row_cap;
+  long long base = D.ctr[CTR_GLOG_N];
+  if (base + nrows > D.glog_cap) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) D.ctr[CTR_GLOG_OVER] = 1;
+    return;
+  }
+  const int tind = Pp->tInd;
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < nrows; r += gridDim.x * blockDim.x) {
+    int p = D.row_pos[r];
+    D.glog_cell[base + r] = (int32_t)D.act[p];
+    D.glog_step[base + r] = tind;
+    D.glog_tau[base + r] = D.a_ext[p];
+  }
+}
+// After k_rows_finalize: growth time = (final extent - extent before) / v
+// (0 for a row that does not grow).
+__global__ void k_glog_end(CafeDev D, CafeConsts K) {
+  int nrows = D.ctr[CTR_NROWS_END];
+  if (nrows > D.row_cap) nrows = (int)D.row_cap;
+  long long base = D.ctr[CTR_GLOG_N];
+  if (base + nrows > D.glog_cap) return;
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < nrows; r += gridDim.x * blockDim.x) {
+    int p = D.row_pos[r];
+    double v = cafe_vh(D, K, p);
+    double e0 = D.glog_tau[base + r];
+    D.glog_tau[base + r] = v > 0.0 ? (D.a_ext[p] - e0) / v : 0.0;
+  }
+}
+__global__ void k_glog_advance(CafeDev D) {
+  int nrows = D.ctr[CTR_NROWS_END];
+  if (nrows > D.row_cap) nrows = (int)D.row_cap;
+  long long base = D.ctr[CTR_GLOG_N];
+  if (base + nrows <= D.glog_cap) D.ctr[CTR_GLOG_N] = (int)(base + nrows);
+}

@@ -188,6 +188,46 @@ int cafe_sim_write_output(cafe_sim *sim, const char *prefix);
 int cafe_sim_checkpoint(cafe_sim *sim, const char *path);
 int cafe_sim_restore(cafe_sim *sim, const char *path);
 
+/* Growth log for the adjoint extension (no counterpart in the reference): with
+ * three caller-owned device arrays of `cap` entries, every step appends, for
+ * each frontier cell of the step (a mushy cell with a liquid neighbour), its
+ * cell index, the step's Grid::tInd and its growth time: the extent it gained
+ * in the step (VoxelsCA.C:511-516) over its growth velocity, i.e. the sum of
+ * the event times it grew through. NULL arrays turn the log off. Setting the
+ * arrays resets the count; a full log stops recording and makes
+ * cafe_sim_growth_log_count report CAFE_E_CAPACITY. */
+int cafe_sim_set_growth_log(cafe_sim *sim, int32_t *cells, int32_t *steps, double *tau, long long cap);
+int cafe_sim_growth_log_count(cafe_sim *sim, long long *n);
+
+/* Differentiable part of the step with hand-written adjoints (no counterpart
+ * in the reference): the Rosenthal moving point source
+ * T = T0 + eta P / (2 pi k R) exp(-v (R + xi) / (2 alpha)) on the cell
+ * centres, source at (x_start + v t, y_src, z_src) at t = step dt, parameters
+ * theta = {P, eta, v, a, n}.
+ * cafe_adjoint_pool: melt-pool length, width, depth at step_final from the
+ *   m-weighted moments of the soft melt indicator m = sigmoid((T - Tl)/tau_T)
+ *   over the cells below the source plane (sqrt(12 var_x), sqrt(12 var_y),
+ *   sqrt(3 E[depth^2])); with cot (3 values) also grad = cot . d out / d theta.
+ * cafe_adjoint_growth: over a growth log (device arrays, n entries), the
+ *   summed growth sum a (Tl - T)^n tau of the frozen event set; with grad,
+ *   also cot * dG/dtheta.
+ * Both run on `stream` (a cudaStream_t, NULL = legacy default stream) of the
+ * current device and return when done. */
+typedef struct {
+  double k, alpha, T0, Tl;      /* W/(m K), m^2/s, K, K */
+  double tau_T;                 /* width of the soft melt indicator, K */
+  double x_start, y_src, z_src; /* source position at t = 0, m */
+  double dt;                    /* time per step, s */
+  double dx;                    /* voxel size, m */
+  int nx, ny, nz;
+  int step_final;               /* step of the pool shape */
+} cafe_adjoint_setup;
+int cafe_adjoint_pool(const cafe_adjoint_setup *setup, const double theta[5], const double *cot, double out[3],
+                      double grad[5], void *stream);
+int cafe_adjoint_growth(const cafe_adjoint_setup *setup, const double theta[5], const int32_t *cells,
+                        const int32_t *steps, const double *tau, long long n, double cot, double *out,
+                        double grad[5], void *stream);
+
 /* Batched ensemble (no counterpart in the reference, which runs one
  * realisation per MPI job): n independent realisations, one deck each, on
  * one device. Each is a cafe_sim handle with its own stream; `threads` host

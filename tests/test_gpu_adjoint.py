@@ -1,0 +1,105 @@
+"""Adjoint extension: the hand-written CUDA values and vector-Jacobian products
+(csrc/cafe_adjoint.cu) against the FP64 numpy restatement (oracle/adjoint_ref.py)
+and central finite differences (h = 1e-6 relative), the segment replay from
+checkpoints against one logged run, and a calibration that recovers hidden
+parameters from a synthetic target."""
+import os
+
+import numpy as np
+import pytest
+
+import adjoint_ref as ref
+
+pytestmark = pytest.mark.gpu
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+DECK = os.path.join(ROOT, "amcafe_gb300", "decks", "c4.in")
+THETA = np.array([200.0, 0.35, 1.0, 1e-5, 2.0])
+
+
+@pytest.fixture(scope="module")
+def run():
+    from amcafe_gb300.adjoint import GrowthRun
+
+    r = GrowthRun(DECK, nsteps=192, segment=32)
+    yield r
+    r.close()
+
+
+def _rel(a, b):
+    a, b = np.asarray(a, float), np.asarray(b, float)
+    return float(np.max(np.abs(a - b) / np.maximum(np.abs(b), 1e-300)))
+
+
+def _fd(f, theta, k, h=1e-6):
+    tp, tm = theta.copy(), theta.copy()
+    tp[k] *= 1 + h
+    tm[k] *= 1 - h
+    return (f(tp) - f(tm)) / (2 * h * theta[k])
+
+
+def test_pool_matches_reference_and_fd(run):
+    cot = np.array([0.7, -1.3, 2.1])
+    out, g = run.pool(THETA, cot)
+    rout, rg = ref.pool(run.setup_dict(), THETA, cot)
+    assert _rel(out, rout) < 1e-10
+    assert _rel(g[:3], rg[:3]) < 1e-8 and np.all(g[3:] == 0)
+    for k in range(3):
+        fd = _fd(lambda th: float(cot @ run.pool(th)[0]), THETA, k)
+        assert abs(g[k] - fd) <= 1e-6 * abs(fd), (k, g[k], fd)
+
+
+def test_growth_matches_reference_and_fd(run):
+    cells, steps, tau = run.log()
+    assert len(cells) > 500 and np.all(tau >= 0) and np.any(tau > 0)
+    G, g = run.growth(THETA, cot=1.0)
+    rG, rg = ref.growth(run.setup_dict(), THETA, cells, steps, tau, cot=1.0)
+    assert _rel(G, rG) < 1e-10
+    assert _rel(g, rg) < 1e-8
+    for k in range(5):
+        fd = _fd(lambda th: run.growth(th)[0], THETA, k)
+        assert abs(g[k] - fd) <= 1e-6 * abs(fd), (k, g[k], fd)
+
+
+def test_replayed_segments_equal_one_logged_run(run):
+    """The checkpointed replay reproduces the log of an uninterrupted run."""
+    import torch
+    from amcafe_gb300 import Simulation
+
+    cells, steps, tau = run.log()
+    sim = Simulation(DECK)
+    sim.InitializeVoxels()
+    sim.begin()
+    cap = 1 << 22
+    c = torch.empty(cap, dtype=torch.int32, device="cuda")
+    s = torch.empty(cap, dtype=torch.int32, device="cuda")
+    t = torch.empty(cap, dtype=torch.float64, device="cuda")
+    sim._lib.cafe_sim_set_growth_log(sim._h, c.data_ptr(), s.data_ptr(), t.data_ptr(), cap)
+    for _ in range(run.nsteps):
+        sim.step()
+    import ctypes
+
+    n = ctypes.c_longlong(0)
+    assert sim._lib.cafe_sim_growth_log_count(sim._h, ctypes.byref(n)) == 0
+    n = n.value
+    assert np.array_equal(c[:n].cpu().numpy(), cells)
+    assert np.array_equal(s[:n].cpu().numpy(), steps)
+    assert np.array_equal(t[:n].cpu().numpy(), tau)
+    sim.close()
+
+
+def test_objective_gradient_and_calibration(run):
+    import torch
+
+    from amcafe_gb300.adjoint import Objective, calibrate
+
+    th = torch.tensor(THETA, dtype=torch.float64, requires_grad=True)
+    out = Objective.apply(th, run)
+    w = torch.tensor([1.0, 2.0, 3.0, 1e3], dtype=torch.float64)
+    (out * w).sum().backward()
+    for k in range(5):
+        fd = _fd(lambda x: float((Objective.apply(torch.tensor(x), run) * w).sum()), THETA, k)
+        assert abs(float(th.grad[k]) - fd) <= 1e-6 * abs(fd), k
+    hidden = np.array([180.0, 0.4, 1.0, 1.2e-5, 2.0])
+    target = Objective.apply(torch.tensor(hidden), run).numpy()
+    got, hist = calibrate(run, target, [220.0, 0.4, 1.0, 0.9e-5, 2.0], free=(0, 3))
+    assert abs(got[0] - 180.0) < 1e-4 * 180.0 and abs(got[3] - 1.2e-5) < 1e-4 * 1.2e-5, (got, hist[-3:])
