@@ -74,6 +74,9 @@ struct CafeConsts {
   int easm;
   double Avel;        // Grid::Avel
   int nvel_i;         // Grid::nvel (an integer when easm)
+  // Gaussian-undercooling nucleation (extension keyword "nucgauss mean sd")
+  int nuc_gauss;
+  double nuc_mean, nuc_sd;
 };
 
 // Tables of the EASM temperature (TempField.C:79-137, Utilities.C:105-140,

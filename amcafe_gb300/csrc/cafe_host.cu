@@ -61,6 +61,8 @@ struct GridH {
   int outint = 1, patternID = 1, outNL = 0;
   int EASM_Flag = 0;  // Grid::EASM_Flag (keyword "easm", see parse_deck)
   int seed = 1;       // extension keyword "seed" (1: the reference's seeds)
+  int nuc_gauss = 0;  // extension keyword "nucgauss mean sd"
+  double nuc_mean = 0, nuc_sd = 1;
   double tL = 1620, tS = 1531.5, T0 = 300, layerT = 25e-6, bpH = 0.0, mu = .01, lrate = 0;
   double meltparam[4] = {75e-6, 162.75e-6, 75e-6, 75e-6};
   double bhatch = 0, bmDelT = 0, bmV = 500e-3, bmP = 0, rNmax = .002;
@@ -142,6 +144,12 @@ int parse_deck(const char *path, GridH &g) {
     // (VoxelsCA.C:47-48) by (s - 1) * kSeedStride and seeds the BasePlate
     // engine (BasePlate.h:28, default seed 1) with s, so s = 1 is the reference
     else if (key == "seed") ok = inum(g.seed) && g.seed >= 1;
+    // extension: nucleation probability rX exp(-.5 x1^2) per capture event,
+    // x1 = ((tL - T) - mean)/sd/sqrt(2) (the form of VoxelsCA.C:2545-2548)
+    else if (key == "nucgauss") {
+      ok = num(g.nuc_mean) && num(g.nuc_sd) && g.nuc_sd > 0;
+      g.nuc_gauss = 1;
+    }
     if (!ok) return fail(CAFE_E_ARG, "deck '%s': bad value after keyword '%s'", path, key.c_str());
     in >> kw;
   }
@@ -1038,6 +1046,9 @@ int cafe_sim_create(const char *deck_path, const cafe_options *opt, cafe_sim **o
     K.gt_cls[c] = T > g.tL;
     K.vhat_cls[c] = T >= g.tL ? 0.0 : g.Avel * std::pow(g.tL - T, g.nvel);
   }
+  K.nuc_gauss = g.nuc_gauss;
+  K.nuc_mean = g.nuc_mean;
+  K.nuc_sd = g.nuc_sd;
   K.easm = g.EASM_Flag == 1;
   K.Avel = g.Avel;
   K.nvel_i = 0;

@@ -50,6 +50,17 @@ __device__ __forceinline__ double cafe_vh(const CafeDev &D, const CafeConsts &K,
   return K.easm ? D.a_vh[p] : K.vhat_cls[D.a_cls[p]];
 }
 
+// Nucleation probability of a capture event that takes active position icap
+// (VoxelsCA.C:483): rX, or with the Gaussian-undercooling extension
+// rX exp(-.5 x1^2), x1 = ((tL - T) - mean) / sd / sqrt(2), the form of
+// VoxelsCA.C:2545-2548, with T the captured cell's temperature.
+__device__ __forceinline__ double cafe_nuc_rate(const CafeDev &D, const CafeConsts &K, int icap) {
+  if (!K.nuc_gauss) return K.rX;
+  double T = K.easm ? D.temp[D.act[icap]] : K.Tcls[D.a_cls[icap]];
+  double x1 = ((K.tL - T) - K.nuc_mean) / K.nuc_sd / 1.4142135623730951;
+  return K.rX * crm_exp(-.5 * (x1 * x1));
+}
+
 __device__ __forceinline__ int cafe_hot(const CafeDev &D, const CafeConsts &K, const CafeStepParams &P,
                                         int i, int j, int k) {
   return K.hot_cls[cafe_cls(D, P, i, j, k)];
@@ -1349,7 +1360,7 @@ __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
             s_jspos = jspos;
             s_bslot = b.s;
             s_icap = D.a_nbr[(long long)jspos * CAFE_NSLOT + b.s];
-            s_nuc = U < K.rX;
+            s_nuc = U < cafe_nuc_rate(D, K, s_icap);
             s_dt = s_nuc ? 0.0 : b.t;
             if (cafe_is_neg(s_dt)) s_negdt++;
             s_ev += 1;
@@ -1575,7 +1586,7 @@ __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
           s_jspos = jspos;
           s_bslot = b.s;
           s_icap = D.a_nbr[(long long)jspos * CAFE_NSLOT + b.s];
-          s_nuc = U < K.rX;
+          s_nuc = U < cafe_nuc_rate(D, K, s_icap);
           s_dt = s_nuc ? 0.0 : b.t;
           if (s_dt < 0.0) s_negdt++;
           s_ev += 1;

@@ -114,6 +114,8 @@ struct Grid {
   double dX[3] = {1e-6, 1e-6, 1e-6};
   int outint = 1, patternID = 1, outNL = 0, nTsd = 0, EASM_Flag = 0;
   int seed = 1;  // extension keyword "seed" (1: the reference's seeds)
+  int nuc_gauss = 0;  // extension keyword "nucgauss mean sd"
+  double nuc_mean = 0, nuc_sd = 1;
   double tL = 1620, tS = 1531.5, T0 = 300, layerT = 25e-6, bpH = 0.0, mu = .01;
   double lrate = 0.0;
   bool have_lrate = false, have_bmdelt = false;
@@ -216,6 +218,11 @@ static bool read_deck(const char *path, Grid &g, std::string &err) {
       }
       if (kw == "gridtheta") next_d(g.gth0);
       if (kw == "seed") next_i(g.seed);
+      if (kw == "nucgauss") {
+        g.nuc_gauss = 1;
+        next_d(g.nuc_mean);
+        next_d(g.nuc_sd);
+      }
       if (kw == "dendritegrowth2") {
         next_d(g.Avel);
         next_d(g.nvel);
@@ -1233,7 +1240,14 @@ static void update_voxels(State &S) {
     if (DtMin >= 1e6 || js < 0) break;
     ++nev;
     int icap = nid[nptr[js] + j1s];
-    if (xrand1(g1) < rX) {
+    // extension "nucgauss": rX exp(-.5 x1^2) with the captured cell's
+    // undercooling, the form of VoxelsCA.C:2545-2548
+    double rXe = rX;
+    if (g.nuc_gauss) {
+      double x1 = ((tL - T[icap]) - g.nuc_mean) / g.nuc_sd / 1.4142135623730951;
+      rXe = rX * m_exp(-.5 * (x1 * x1));
+    }
+    if (xrand1(g1) < rXe) {
       // nucleation (VoxelsCA.C:483-505)
       std::vector<double> q;
       generate_samples(1, sdloc, q, true);

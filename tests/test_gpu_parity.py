@@ -68,7 +68,7 @@ def run_and_compare(deck, nsteps, stride, tmp_path, event_scan=0):
 
 @pytest.mark.parametrize("deck,nsteps,stride", [
     ("track_r0.in", 0, 1), ("track_nuc.in", 0, 1), ("layers_rot.in", 0, 20), ("c0_small.in", 400, 40),
-    ("track_nuc_s7.in", 0, 1)])
+    ("track_nuc_s7.in", 0, 1), ("track_nuc_ng.in", 0, 1)])
 def test_gpu_matches_oracle(tmp_path, deck, nsteps, stride):
     """Default keyed event selection with lazily replayed growth."""
     worst, stats = run_and_compare(deck, nsteps, stride, tmp_path)
@@ -76,7 +76,7 @@ def test_gpu_matches_oracle(tmp_path, deck, nsteps, stride):
     print("%s: max float rel diff %g, %s" % (deck, worst, stats))
 
 
-@pytest.mark.parametrize("deck", ["track_easm.in", "track_easm60.in"])
+@pytest.mark.parametrize("deck", ["track_easm.in", "track_easm60.in", "track_easm60_ng.in"])
 def test_gpu_easm_matches_oracle(tmp_path, deck):
     """EASM temperature (keyword easm): per-cell temperatures and velocities,
     rows evaluated with the exact per-event scan."""
