@@ -121,6 +121,9 @@ struct CafeDev {
   long long glog_cap;
   // this step's parameters (the kernels of a step read them from here)
   CafeStepParams *Pd;
+  // activity flags of the compaction, one word per thread of the counting
+  // pass (bit c: its c-th cell), reused by the scattering pass
+  uint32_t *act_flags;
   // liquid cells left by the previous step (cell indices)
   int32_t *liq;
   // grains
@@ -188,6 +191,7 @@ enum {
   CTR_EASM_QHEAD,                       // next queued cell to take
   CTR_GLOG_N,                           // growth-log entries written
   CTR_GLOG_OVER,                        // 1: the growth log ran out of room
+  CTR_ZLO, CTR_ZHI,                     // z range of the mushy and liquid cells after the last step
   CTR_COUNT
 };
 static_assert(CTR_EASM_CURSOR % 2 == 0, "64-bit cursor needs an 8-byte aligned slot");

@@ -515,6 +515,15 @@ int read_ctr(cafe_sim *s, int which, int *out) {
   return CAFE_OK;
 }
 
+// The next step's active-set compaction scans every z plane (after a state
+// that no step produced: initialisation, upload, restore).
+int full_active_range(cafe_sim *s) {
+  k_set_int<<<1, 1, 0, s->stream>>>(s->D.ctr + CTR_ZLO, 0);
+  k_set_int<<<1, 1, 0, s->stream>>>(s->D.ctr + CTR_ZHI, s->K.nz - 1);
+  CUDA_TRY(cudaGetLastError());
+  return CAFE_OK;
+}
+
 int grow_grains(cafe_sim *s, long long need) {
   if (need <= s->D.grain_cap) return CAFE_OK;
   long long cap = std::max<long long>(need * 2, (long long)s->D.grain_cap * 2);
@@ -824,9 +833,10 @@ int launch_voxels(cafe_sim *s, bool graph, const CafeStepParams *Pp) {
       LAUNCHED(CAFE_PH_CLASSIFY, 1);
     }
     CUDA_TRY(cudaMemsetAsync(D.ctr + CTR_NLIQ, 0, sizeof(int), st));
-    k_active_count<<<(int)s->nblk_act, CAFE_DENSE_THREADS, 0, st>>>(D, K, Pp, s->act_chunks);
+    const int ab = (int)std::min<long long>(s->nblk_act, (long long)s->gsm * 8);  // persistent grid
+    k_active_count<<<ab, CAFE_DENSE_THREADS, 0, st>>>(D, K, Pp, s->act_chunks, s->nblk_act);
     k_scan_blocks<<<1, 1024, 0, st>>>(D.blk, s->nblk_act, D.ctr + CTR_NA);
-    k_active_scatter<<<(int)s->nblk_act, CAFE_DENSE_THREADS, 0, st>>>(D, K, Pp, s->act_chunks);
+    k_active_scatter<<<ab, CAFE_DENSE_THREADS, 0, st>>>(D, K, Pp, s->act_chunks, s->nblk_act);
     LAUNCHED(CAFE_PH_CLASSIFY, 3);
   }
   int gb = s->gsm * 8;
@@ -864,7 +874,7 @@ int launch_voxels(cafe_sim *s, bool graph, const CafeStepParams *Pp) {
   }
   {
     PhaseScope ps(s, CAFE_PH_WRITEBACK);
-    k_writeback<<<gb, 256, 0, st>>>(D);
+    k_writeback<<<gb, 256, 0, st>>>(D, K);
     k_mushy2solid<<<gb, 256, 0, st>>>(D, K);
     LAUNCHED(CAFE_PH_WRITEBACK, 2);
   }
@@ -1152,7 +1162,8 @@ int cafe_sim_create(const char *deck_path, const cafe_options *opt, cafe_sim **o
       (rc = dalloc(&D.row_key, D.row_cap, o)) || (rc = dalloc(&D.row_bt, D.row_cap, o)) ||
       (rc = dalloc(&D.row_bruq, D.row_cap, o)) ||
       (rc = dalloc(&D.ctr, CTR_COUNT, o)) || (rc = dalloc(&D.err, 1, o)) || (rc = dalloc(&D.stat, STAT_COUNT, o)) ||
-      (rc = dalloc(&D.Pd, 1, o)) || (rc = dalloc(&D.tcls, std::max<long long>(D.tcls_cap, 1), o)) ||
+      (rc = dalloc(&D.Pd, 1, o)) ||
+      (rc = dalloc(&D.act_flags, (size_t)((N + CAFE_CELLS_PER_BLOCK - 1) / CAFE_CELLS_PER_BLOCK) * CAFE_DENSE_THREADS, o)) || (rc = dalloc(&D.tcls, std::max<long long>(D.tcls_cap, 1), o)) ||
       (K.easm && ((rc = dalloc(&D.temp, N, o)) || (rc = dalloc(&D.a_vh, acap, o)) ||
                   (rc = dalloc(&D.easm_q, (size_t)(D.easm_qcap = std::min<long long>(N, 1LL << 21)), o))))) {
     cafe_sim_destroy(s);
@@ -1238,6 +1249,7 @@ int cafe_sim_initialize_voxels(cafe_sim *s) {
   // VoxelsCA::Build of the baseplate cells (VoxelsCA.C:156-159)
   k_build_init<<<grid_blocks(K.N, 256, s), 256, 0, s->stream>>>(s->D, K);
   CUDA_TRY(cudaGetLastError());
+  if ((rc = full_active_range(s))) return rc;
   // orientations (BasePlate.C:83-96)
   std::default_random_engine g1(531231);
   unsigned int sdloc = unsigned(double(g1()) / double(g1.max()) * std::pow(2.0, 32.0));
@@ -1691,6 +1703,7 @@ int cafe_sim_upload_state(cafe_sim *s, const int32_t *gID, const int32_t *vState
   CUDA_TRY(cudaMemsetAsync(s->D.ctr + CTR_NLIQ, 0, sizeof(int), st));
   s->full_k2 = true;
   s->have_prev_box = false;
+  if ((rc = full_active_range(s))) return rc;
   s->initialized = true;
   return sim_sync(s);
 }
@@ -2099,6 +2112,7 @@ int cafe_sim_restore(cafe_sim *s, const char *path) {
   s->have_P = false;
   s->full_k2 = true;          // the liquid list is rebuilt by a dense pass
   s->have_prev_box = false;
+  if ((rc = full_active_range(s))) return rc;
   s->initialized = true;
   s->begun = true;
   return sim_sync(s);

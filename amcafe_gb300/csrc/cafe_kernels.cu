@@ -214,6 +214,34 @@ __device__ __forceinline__ bool cafe_is_active(const CafeDev &D, const CafeConst
   return false;
 }
 
+// Cell-index range that can hold active cells this step: the z planes of the
+// mushy and liquid cells left by the previous step (k_writeback) and of this
+// and the previous pool box, widened by one plane. Every active cell is mushy,
+// liquid, or at/above the liquidus (inside the pool box); a cell turns mushy
+// this step only next to a liquid cell (ConvertSolid1(1)), and liquid cells
+// are those left by the previous step or melted in the pool box; new layers
+// bring solid and powder cells only.
+__device__ __forceinline__ void cafe_active_range(const CafeDev &D, const CafeConsts &K, const CafeStepParams &P,
+                                                  long long &r0, long long &r1) {
+  int zlo = D.ctr[CTR_ZLO], zhi = D.ctr[CTR_ZHI];
+  if (P.hi[0] > P.lo[0] && P.hi[1] > P.lo[1] && P.hi[2] > P.lo[2]) {
+    zlo = min(zlo, P.lo[2]);
+    zhi = max(zhi, P.hi[2] - 1);
+  }
+  if (P.phi[0] > P.plo[0] && P.phi[1] > P.plo[1] && P.phi[2] > P.plo[2]) {
+    zlo = min(zlo, P.plo[2]);
+    zhi = max(zhi, P.phi[2] - 1);
+  }
+  zlo = max(zlo - 1, 0);
+  zhi = min(zhi + 1, K.nz - 1);
+  if (zhi < zlo) {
+    r0 = r1 = 0;
+    return;
+  }
+  r0 = (long long)zlo * K.nxy;
+  r1 = (long long)(zhi + 1) * K.nxy;
+}
+
 // Activity flags of the CAFE_CELLS_PER_THREAD (8) cells from `base` (bit c
 // for cell base + c). A cell that cannot be at or above the liquidus (outside
 // the pool box, or not below the laser plane) is active exactly when it is
@@ -252,26 +280,49 @@ __device__ __forceinline__ uint32_t cafe_chunk_active(const CafeDev &D, const Ca
 // Activity flags of this thread's `chunks` chunks (bit 8 c + j for cell
 // base + 8 c + j).
 __device__ __forceinline__ uint32_t cafe_thread_active(const CafeDev &D, const CafeConsts &K,
-                                                       const CafeStepParams &P, long long base, int chunks) {
+                                                       const CafeStepParams &P, long long base, int chunks,
+                                                       long long r0, long long r1) {
   uint32_t f = 0;
+  if (base >= r1 || base + 8LL * chunks <= r0) return 0;  // no plane that can hold active cells
 #pragma unroll
   for (int c = 0; c < CAFE_ACT_MAX_CHUNKS; ++c)
     if (c < chunks) f |= cafe_chunk_active(D, K, P, base + 8 * c) << (8 * c);
+  // cells of the range's edge chunks that lie outside it
+  for (int c = 0; c < 8 * chunks; ++c)
+    if (base + c < r0 || base + c >= r1) f &= ~(1u << c);
   return f;
 }
 
-__global__ void k_active_count(CafeDev D, CafeConsts K, const CafeStepParams *__restrict__ Pp, int chunks) {
+// The compaction runs over "virtual blocks" of CAFE_DENSE_THREADS threads x
+// `chunks` 8-cell chunks (nvb of them cover the grid); a persistent grid
+// strides over them, writes a zero count for those outside the active range
+// (cafe_active_range) without touching their cells, and counts the rest.
+__global__ void k_active_count(CafeDev D, CafeConsts K, const CafeStepParams *__restrict__ Pp, int chunks,
+                               long long nvb) {
   const CafeStepParams P = *Pp;
   __shared__ int wsum[CAFE_DENSE_THREADS / 32];
-  long long base = ((long long)blockIdx.x * blockDim.x + threadIdx.x) * (CAFE_CELLS_PER_THREAD * chunks);
-  int cnt = __popc(cafe_thread_active(D, K, P, base, chunks));
-  for (int o = 16; o > 0; o >>= 1) cnt += __shfl_down_sync(0xffffffffu, cnt, o);
-  if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = cnt;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    int s = 0;
-    for (int w = 0; w < CAFE_DENSE_THREADS / 32; ++w) s += wsum[w];
-    D.blk[blockIdx.x] = s;
+  long long r0, r1;
+  cafe_active_range(D, K, P, r0, r1);
+  const long long per_vb = (long long)CAFE_DENSE_THREADS * CAFE_CELLS_PER_THREAD * chunks;
+  for (long long vb = blockIdx.x; vb < nvb; vb += gridDim.x) {
+    long long b0 = vb * per_vb;
+    if (b0 >= r1 || b0 + per_vb <= r0) {
+      if (threadIdx.x == 0) D.blk[vb] = 0;
+      continue;
+    }
+    long long base = b0 + (long long)threadIdx.x * (CAFE_CELLS_PER_THREAD * chunks);
+    const uint32_t f = cafe_thread_active(D, K, P, base, chunks, r0, r1);
+    D.act_flags[vb * CAFE_DENSE_THREADS + threadIdx.x] = f;
+    int cnt = __popc(f);
+    for (int o = 16; o > 0; o >>= 1) cnt += __shfl_down_sync(0xffffffffu, cnt, o);
+    if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = cnt;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int sum = 0;
+      for (int w = 0; w < CAFE_DENSE_THREADS / 32; ++w) sum += wsum[w];
+      D.blk[vb] = sum;
+    }
+    __syncthreads();
   }
 }
 
@@ -303,11 +354,18 @@ __global__ void k_scan_blocks(int32_t *blk, long long n, int *total) {
   }
 }
 
-__global__ void k_active_scatter(CafeDev D, CafeConsts K, const CafeStepParams *__restrict__ Pp, int chunks) {
+__global__ void k_active_scatter(CafeDev D, CafeConsts K, const CafeStepParams *__restrict__ Pp, int chunks,
+                                 long long nvb) {
   const CafeStepParams P = *Pp;
   __shared__ int wsum[CAFE_DENSE_THREADS / 32];
-  long long base = ((long long)blockIdx.x * blockDim.x + threadIdx.x) * (CAFE_CELLS_PER_THREAD * chunks);
-  const uint32_t flags = cafe_thread_active(D, K, P, base, chunks);
+  long long r0, r1;
+  cafe_active_range(D, K, P, r0, r1);
+  const long long per_vb = (long long)CAFE_DENSE_THREADS * CAFE_CELLS_PER_THREAD * chunks;
+  long long vb_lo = r0 / per_vb, vb_hi = r1 > 0 ? (r1 - 1) / per_vb : -1;
+  if (vb_hi >= nvb) vb_hi = nvb - 1;
+  for (long long vb = vb_lo + blockIdx.x; vb <= vb_hi; vb += gridDim.x) {
+  long long base = vb * per_vb + (long long)threadIdx.x * (CAFE_CELLS_PER_THREAD * chunks);
+  const uint32_t flags = D.act_flags[vb * CAFE_DENSE_THREADS + threadIdx.x];  // from k_active_count
   const int cnt = __popc(flags);
   // block-exclusive scan of per-thread counts
   int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -328,7 +386,7 @@ __global__ void k_active_scatter(CafeDev D, CafeConsts K, const CafeStepParams *
     if (threadIdx.x < CAFE_DENSE_THREADS / 32) wsum[threadIdx.x] = inc - v;
   }
   __syncthreads();
-  long long pos = (long long)D.blk[blockIdx.x] + wsum[w] + (incl - cnt);
+  long long pos = (long long)D.blk[vb] + wsum[w] + (incl - cnt);
   for (int c = 0; c < CAFE_CELLS_PER_THREAD * chunks; ++c) {
     if (!(flags >> c & 1u)) continue;
     long long idx = base + c;
@@ -339,6 +397,8 @@ __global__ void k_active_scatter(CafeDev D, CafeConsts K, const CafeStepParams *
       atomicOr(D.err, CAFE_ERR_ACTIVE_CAP);
     }
     ++pos;
+  }
+  __syncthreads();  // wsum is reused by the next virtual block
   }
 }
 
@@ -352,6 +412,10 @@ __global__ void k_gather(CafeDev D, CafeConsts K, const CafeStepParams *__restri
   int na = D.ctr[CTR_NA];
   if (na > D.act_cap) na = (int)D.act_cap;
   uint32_t seed = cafe_minstd_seed((uint64_t)(uint32_t)(30 * P.tInd + (int)K.seed1));
+  if (blockIdx.x == 0 && threadIdx.x == 0) {  // rebuilt by k_writeback for the next step
+    D.ctr[CTR_ZLO] = 0x7fffffff;
+    D.ctr[CTR_ZHI] = -1;
+  }
   for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < na; p += gridDim.x * blockDim.x) {
     long long idx = D.act[p];
     int i, j, k;
@@ -1747,11 +1811,17 @@ __global__ void k_rows_finalize(CafeDev D) {
 }
 
 // ------------------------------------------------------------------ write back
-__global__ void k_writeback(CafeDev D) {
+__global__ void k_writeback(CafeDev D, CafeConsts K) {
   int na = D.ctr[CTR_NA];
   if (na > D.act_cap) na = (int)D.act_cap;
+  int zlo = 0x7fffffff, zhi = -1;
   for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < na; p += gridDim.x * blockDim.x) {
     long long idx = D.act[p];
+    if (D.a_state[p] == 1 || D.a_state[p] == 2) {
+      int k = (int)(idx / K.nxy);
+      zlo = min(zlo, k);
+      zhi = max(zhi, k);
+    }
     D.state[idx] = D.a_state[p];
     D.gid[idx] = D.a_gid[p];
     D.ext[idx] = D.a_ext[p];
@@ -1763,6 +1833,14 @@ __global__ void k_writeback(CafeDev D) {
       int t = atomicAdd(&D.ctr[CTR_NLIQ], 1);
       D.liq[t] = (int32_t)idx;  // t < na <= act_cap = liq capacity
     }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    zlo = min(zlo, __shfl_down_sync(0xffffffffu, zlo, o));
+    zhi = max(zhi, __shfl_down_sync(0xffffffffu, zhi, o));
+  }
+  if ((threadIdx.x & 31) == 0 && zhi >= 0) {
+    atomicMin(&D.ctr[CTR_ZLO], zlo);
+    atomicMax(&D.ctr[CTR_ZHI], zhi);
   }
 }
 
