@@ -429,10 +429,10 @@ struct cafe_sim {
   unsigned char *h_out = nullptr;  // pinned bounce buffer of the file writer
   // the device work of a step as one CUDA graph (see step_graph_launch)
   bool use_graph = true;
-  cudaGraph_t graph[1] = {nullptr};
-  cudaGraphExec_t graph_exec[1] = {nullptr};
-  std::vector<unsigned char> graph_key[1];
-  long long graph_launch[1][CAFE_NPHASE] = {{0}};
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t graph_exec = nullptr;
+  std::vector<unsigned char> graph_key;
+  long long graph_launch[CAFE_NPHASE] = {0};
   long long graph_captures = 0;
 };
 
@@ -709,10 +709,10 @@ int easm_field(cafe_sim *s) {
 // ---- the device work of one step
 // TempField::tInd (main1.C:64), the step parameters on the host and in device
 // memory, the EASM field when selected, and the class-map capacity.
-int step_plan(cafe_sim *s, bool may_grow, bool *need_grow);
+int step_plan(cafe_sim *s);
 
 int step_prepare(cafe_sim *s) {
-  int rc = step_plan(s, true, nullptr);
+  int rc = step_plan(s);
   if (rc) return rc;
   k_put_params<<<1, 1, 0, s->stream>>>(s->D.Pd, s->P);
   LAUNCHED(CAFE_PH_MELT, 1);
@@ -722,9 +722,9 @@ int step_prepare(cafe_sim *s) {
 
 // The host part of a step's preparation: TempField::tInd, the parameters into
 // s->P, the EASM field when selected, and the class-map capacity for the pool
-// box. With may_grow false a needed regrowth is reported in *need_grow
-// instead (the caller still has launches of earlier steps to issue).
-int step_plan(cafe_sim *s, bool may_grow, bool *need_grow) {
+// box (regrown only for the EASM field; the analytic pool box fits the map
+// sized at creation).
+int step_plan(cafe_sim *s) {
   GridH &g = s->g;
   s->tf_tInd = int(std::round(g.time / s->DelT));
   if (g.isp < 0 || g.isp >= g.NpT || (std::fmod(g.isp, g.Nsd) == 0 && g.isp + 1 >= g.NpT) ||
@@ -738,11 +738,6 @@ int step_plan(cafe_sim *s, bool may_grow, bool *need_grow) {
   }
   const CafeStepParams &P = s->P;
   long long nbox = (long long)(P.hi[0] - P.lo[0]) * (P.hi[1] - P.lo[1]) * (P.hi[2] - P.lo[2]);
-  if (need_grow) *need_grow = false;
-  if (nbox > s->D.tcls_cap && !may_grow) {
-    if (need_grow) *need_grow = true;
-    return CAFE_OK;
-  }
   if (nbox > s->D.tcls_cap) {
     CUDA_TRY(cudaStreamSynchronize(s->stream));
     for (auto &p : s->owned)
@@ -914,13 +909,12 @@ std::vector<unsigned char> graph_key(const cafe_sim *s) {
 // and no dense solid->mushy pass is due. (Graphs of several consecutive steps
 // were measured slower on the device than one graph per step.)
 int step_graph_launch(cafe_sim *s) {
-  const int q = 0;
   std::vector<unsigned char> key = graph_key(s);
-  if (!s->graph_exec[q] || key != s->graph_key[q]) {
-    if (s->graph_exec[q]) cudaGraphExecDestroy(s->graph_exec[q]);
-    if (s->graph[q]) cudaGraphDestroy(s->graph[q]);
-    s->graph_exec[q] = nullptr;
-    s->graph[q] = nullptr;
+  if (!s->graph_exec || key != s->graph_key) {
+    if (s->graph_exec) cudaGraphExecDestroy(s->graph_exec);
+    if (s->graph) cudaGraphDestroy(s->graph);
+    s->graph_exec = nullptr;
+    s->graph = nullptr;
     long long before[CAFE_NPHASE];
     for (int p = 0; p < CAFE_NPHASE; ++p) before[p] = s->phase_launch[p];
     long long tot0 = s->launches;
@@ -931,7 +925,7 @@ int step_graph_launch(cafe_sim *s) {
     cudaError_t ce = cudaStreamEndCapture(s->stream, &g);
     // the capture only recorded the launches: take back their counts
     for (int p = 0; p < CAFE_NPHASE; ++p) {
-      s->graph_launch[q][p] = s->phase_launch[p] - before[p];
+      s->graph_launch[p] = s->phase_launch[p] - before[p];
       s->phase_launch[p] = before[p];
     }
     s->launches = tot0;
@@ -940,15 +934,15 @@ int step_graph_launch(cafe_sim *s) {
       if (rc) return rc;
       return fail(CAFE_E_CUDA, "step graph capture: %s", cudaGetErrorString(ce));
     }
-    s->graph[q] = g;
-    CUDA_TRY(cudaGraphInstantiate(&s->graph_exec[q], g, 0));
-    s->graph_key[q] = key;
+    s->graph = g;
+    CUDA_TRY(cudaGraphInstantiate(&s->graph_exec, g, 0));
+    s->graph_key = key;
     s->graph_captures++;
   }
-  CUDA_TRY(cudaGraphLaunch(s->graph_exec[q], s->stream));
+  CUDA_TRY(cudaGraphLaunch(s->graph_exec, s->stream));
   for (int p = 0; p < CAFE_NPHASE; ++p) {
-    s->phase_launch[p] += s->graph_launch[q][p];
-    s->launches += s->graph_launch[q][p];
+    s->phase_launch[p] += s->graph_launch[p];
+    s->launches += s->graph_launch[p];
   }
   return CAFE_OK;
 }
@@ -1206,10 +1200,8 @@ void cafe_sim_destroy(cafe_sim *s) {
   for (void *p : s->owned) cudaFree(p);
   if (s->h_pinned) cudaFreeHost(s->h_pinned);
   if (s->h_out) cudaFreeHost(s->h_out);
-  for (int q = 0; q < 1; ++q) {
-    if (s->graph_exec[q]) cudaGraphExecDestroy(s->graph_exec[q]);
-    if (s->graph[q]) cudaGraphDestroy(s->graph[q]);
-  }
+  if (s->graph_exec) cudaGraphExecDestroy(s->graph_exec);
+  if (s->graph) cudaGraphDestroy(s->graph);
   if (s->stream) cudaStreamDestroy(s->stream);
   delete s;
 }
@@ -1421,8 +1413,7 @@ int cafe_sim_step(cafe_sim *s, int *done) {
   int rc;
   if (graph_eligible(s)) {
     CUDA_TRY(cudaSetDevice(s->device));
-    bool grow = false;
-    if ((rc = step_plan(s, true, &grow))) return rc;
+    if ((rc = step_plan(s))) return rc;
     k_put_params<<<1, 1, 0, s->stream>>>(s->D.Pd, s->P);
     LAUNCHED(CAFE_PH_MELT, 1);
     CUDA_TRY(cudaGetLastError());
