@@ -1007,9 +1007,25 @@ __device__ __forceinline__ void cafe_row_replay(const CafeDev &D, int r, int upt
 // events at time T.
 __device__ __forceinline__ void cafe_row_eval_live(const CafeDev &D, const CafeConsts &K, int r, int ev,
                                                    double T, uint32_t live) {
+#ifdef CAFE_DETAIL_CYCLES
+  long long rp0 = clock64();
+  int rm0 = D.row_m[r];
+#endif
   cafe_row_replay(D, r, ev);
+#ifdef CAFE_DETAIL_CYCLES
+  atomicAdd(&D.stat[STAT_DETAIL + 27], (unsigned long long)(D.row_m[r] - rm0 > 0 ? D.row_m[r] - rm0 : 0));
+  atomicAdd(&D.stat[STAT_DETAIL + 28], 1ULL);
+  atomicAdd(&D.stat[STAT_DETAIL + 29], (unsigned long long)(clock64() - rp0));
+#endif
   CafeCand b = cafe_cand_none();
+#ifdef CAFE_DETAIL_CYCLES
+  long long be0 = clock64();
+#endif
   cafe_row_best_live(D, K, r, live, b, false);
+#ifdef CAFE_DETAIL_CYCLES
+  atomicAdd(&D.stat[STAT_DETAIL + 30], (unsigned long long)(clock64() - be0));
+  atomicAdd(&D.stat[STAT_DETAIL + 31], 1ULL);
+#endif
   D.row_stamp[r] = ev + 1;
   if (b.j < 0) {
     D.row_key[r] = CAFE_KEY_NONE;
