@@ -352,7 +352,12 @@ CRM_HD int crm_atan_unit_fast(double num, double den, double *hi, double *lo) {
   double rr = (fma(-uh, bd.hi, a.hi) + alo) - uh * blo;
   double ul = rr * (double)crm_rcp_f32((float)bd.hi);
   double w = uh * uh;
-  double poly = uh * w * (-1.0 / 3 + w * (1.0 / 5 + w * (-1.0 / 7 + w * (1.0 / 9 + w * (-1.0 / 11)))));
+  // u^3 (-1/3 + w/5 - w^2/7 + w^3/9 - w^4/11), Horner with explicit fma
+  double q = fma(w, -1.0 / 11, 1.0 / 9);
+  q = fma(w, q, -1.0 / 7);
+  q = fma(w, q, 1.0 / 5);
+  q = fma(w, q, -1.0 / 3);
+  double poly = uh * w * q;
   double th = CRM_TAB(crm_atan_tab)[k][0], tlo = CRM_TAB(crm_atan_tab)[k][1];
   crm_dd sm = crm_two_sum(th, uh);
   *hi = sm.hi;
@@ -399,20 +404,26 @@ CRM_HD void crm_sc_core(double rh, double rl, int want_sin, double *h, double *l
   double c = (double)j * (1.0 / CRM_SC_STEPS);
   double sh0 = rh - c;  // exact (Sterbenz)
   double w = sh0 * sh0;
-  double sm = sh0 * w * (-1.0 / 6 + w * (1.0 / 120 + w * (-1.0 / 5040)));            // sin s - s
-  double cm = w * (-0.5 + w * (1.0 / 24 + w * (-1.0 / 720 + w * (1.0 / 40320)))) - sh0 * rl;  // cos s - 1
+  // Horner with explicit fma
+  double qs = fma(w, -1.0 / 5040, 1.0 / 120);
+  qs = fma(w, qs, -1.0 / 6);
+  double sm = sh0 * w * qs;  // sin s - s
+  double qc = fma(w, 1.0 / 40320, -1.0 / 720);
+  qc = fma(w, qc, 1.0 / 24);
+  qc = fma(w, qc, -0.5);
+  double cm = fma(w, qc, -(sh0 * rl));  // cos s - 1
   double sc = CRM_TAB(crm_sincos_tab)[j][0], scl = CRM_TAB(crm_sincos_tab)[j][1];
   double cc = CRM_TAB(crm_sincos_tab)[j][2], ccl = CRM_TAB(crm_sincos_tab)[j][3];
   if (want_sin) {
     crm_dd p = crm_two_prod(cc, sh0);
     crm_dd t = crm_two_sum(sc, p.hi);
     *h = t.hi;
-    *l = t.lo + (scl + (p.lo + (cc * rl + (ccl * sh0 + (cc * sm + sc * cm)))));
+    *l = t.lo + (scl + (p.lo + fma(cc, rl, fma(ccl, sh0, fma(cc, sm, sc * cm)))));
   } else {
     crm_dd p2 = crm_two_prod(sc, sh0);
     crm_dd t2 = crm_two_sum(cc, -p2.hi);
     *h = t2.hi;
-    *l = t2.lo + (ccl + (-p2.lo + (-sc * rl + (-scl * sh0 + (-sc * sm + cc * cm)))));
+    *l = t2.lo + (ccl + (-p2.lo + fma(-sc, rl, fma(-scl, sh0, fma(-sc, sm, cc * cm)))));
   }
 }
 
