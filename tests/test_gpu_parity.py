@@ -68,7 +68,7 @@ def run_and_compare(deck, nsteps, stride, tmp_path, event_scan=0):
 
 @pytest.mark.parametrize("deck,nsteps,stride", [
     ("track_r0.in", 0, 1), ("track_nuc.in", 0, 1), ("layers_rot.in", 0, 20), ("c0_small.in", 400, 40),
-    ("track_nuc_s7.in", 0, 1), ("track_nuc_ng.in", 0, 1)])
+    ("track_nuc_s7.in", 0, 1), ("track_nuc_ng.in", 0, 1), ("odd_dims.in", 0, 3)])
 def test_gpu_matches_oracle(tmp_path, deck, nsteps, stride):
     """Default keyed event selection with lazily replayed growth."""
     worst, stats = run_and_compare(deck, nsteps, stride, tmp_path)

@@ -19,7 +19,7 @@ import pytest
 import cafe_oracle as orc
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-DECKS = ["track_r0", "track_nuc", "layers_rot", "c0_small", "track_easm", "track_easm60"]
+DECKS = ["track_r0", "track_nuc", "layers_rot", "c0_small", "track_easm", "track_easm60", "odd_dims"]
 
 
 def _digest(a):
@@ -65,9 +65,32 @@ def test_oracle_glibc_reproduces_reference(name, tmp_path):
     _check(name, orc.LIBM_GLIBC, tmp_path, check_floats=True)
 
 
-@pytest.mark.parametrize("name", DECKS)
+# odd_dims is not among these: with correctly rounded libm its extents differ
+# from the reference's in the last bits from step 4 on (glibc rounds some
+# capture-geometry result differently) and a capture decision flips at step 32;
+# test_correctly_rounded_libm_diverges_late_on_odd_dims records that.
+CR_DECKS = [d for d in DECKS if d != "odd_dims"]
+
+
+@pytest.mark.parametrize("name", CR_DECKS)
 def test_oracle_correctly_rounded_libm_keeps_reference_integers(name, tmp_path):
     _check(name, orc.LIBM_CR, tmp_path, check_floats=False)
+
+
+def test_correctly_rounded_libm_diverges_late_on_odd_dims(tmp_path):
+    """The limit of the parity anchor: correctly rounded math reproduces the
+    reference's grain IDs and states on odd_dims.in for its first 31 steps
+    (records 0-10 at stride 3), extents within 1e-14 relative, and differs
+    after a capture decision that glibc's rounding changes."""
+    g = np.load(os.path.join(HERE, "golden", "odd_dims.npz"))
+    dump = str(tmp_path / "o.bin")
+    orc.run(os.path.join(HERE, "golden", "decks", "odd_dims.in"), dump, max_steps=int(g["nsteps"]),
+            dump_stride=int(g["stride"]), libm=orc.LIBM_CR)
+    recs = orc.read_dump(dump)
+    for j in range(11):
+        for f in ("gID", "vState"):
+            assert _digest(recs[j][f]) == str(g["sha_" + f][j]), (j, f)
+    assert any(_digest(r["gID"]) != str(d) for r, d in zip(recs, g["sha_gID"]))
 
 
 @pytest.mark.parametrize("libm", [orc.LIBM_GLIBC, orc.LIBM_CR])
