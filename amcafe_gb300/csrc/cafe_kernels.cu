@@ -692,7 +692,8 @@ __device__ unsigned long long cafe_row_finish_warp(const CafeDev &D, const CafeC
       cand = !cafe_is_nan(t);
     }
     // lexicographic (t, ruqs, slot) minimum over the warp (VoxelsCA.C:427-440)
-    unsigned long long tk = cand ? cafe_key_canon(t) : CAFE_KEY_NONE;
+    const unsigned long long tk0 = cand ? cafe_key_canon(t) : CAFE_KEY_NONE;
+    unsigned long long tk = tk0;
     unsigned long long rk = cand ? cafe_key_canon(ruqs) : CAFE_KEY_NONE;
     int sl = cand ? lane : 255;
     for (int o = 16; o > 0; o >>= 1) {
@@ -705,6 +706,10 @@ __device__ unsigned long long cafe_row_finish_warp(const CafeDev &D, const CafeC
         sl = sl2;
       }
     }
+    // the smallest time of the other candidates (the row's time once slot sl
+    // is captured by another row)
+    unsigned long long k2 = lane == sl ? CAFE_KEY_NONE : tk0;
+    for (int o = 16; o > 0; o >>= 1) k2 = min(k2, cafe_shfl_u64_xor(k2, o));
     double bt = __shfl_sync(FULL, t, sl & 31);
     double bruq = __shfl_sync(FULL, ruqs, sl & 31);
     if (lane == 0) {
@@ -715,7 +720,9 @@ __device__ unsigned long long cafe_row_finish_warp(const CafeDev &D, const CafeC
         D.row_bt[r] = bt;
         D.row_bruq[r] = bruq;
         D.row_bslot[r] = sl;
-        D.row_key[r] = cafe_key(T + bt);
+        const unsigned long long key = cafe_key(T + bt);
+        D.row_key[r] = key;
+        D.row_key2[r] = k2 == CAFE_KEY_NONE ? key : cafe_key(T + cafe_unkey(k2));
       }
     }
   }
@@ -912,7 +919,8 @@ __device__ __forceinline__ CafeCand cafe_warp_best(CafeCand best) {
 // minimum; otherwise every live slot is evaluated. `bounded` applies the
 // reference's acceptance limit t <= 1e6 (VoxelsCA.C:383, 427).
 __device__ __forceinline__ void cafe_row_best_live(const CafeDev &D, const CafeConsts &K, long long r,
-                                                   uint32_t live, CafeCand &best, bool bounded) {
+                                                   uint32_t live, CafeCand &best, bool bounded,
+                                                   unsigned long long *k2out = nullptr) {
   int p = D.row_pos[r];
   if (!live) return;
   double E = D.row_E[r];
@@ -926,6 +934,9 @@ __device__ __forceinline__ void cafe_row_best_live(const CafeDev &D, const CafeC
   double ruq_p = D.a_ruq[p];
   bool have = false;
   unsigned long long tfirst = 0;
+  // with k2out (best enters empty): the smallest time key of the candidates
+  // other than the best one; in g order the slot that ends the visit has it
+  unsigned long long k2 = CAFE_KEY_NONE;
   for (int k = 0; k < nn; ++k) {
     int s = mono ? ord[k] : k;
     if (!(live >> s & 1u)) continue;
@@ -937,7 +948,10 @@ __device__ __forceinline__ void cafe_row_best_live(const CafeDev &D, const CafeC
       if (mono) break;
       continue;
     }
-    if (mono && have && tk > tfirst) break;
+    if (mono && have && tk > tfirst) {
+      k2 = min(k2, tk);
+      break;
+    }
     int q = D.a_nbr[(long long)p * CAFE_NSLOT + s];
     CafeCand c;
     c.t = t;
@@ -946,12 +960,18 @@ __device__ __forceinline__ void cafe_row_best_live(const CafeDev &D, const CafeC
     c.rk = cafe_key_canon(c.ruqs);
     c.j = jrow;
     c.s = s;
-    if (cafe_cand_better(c, best)) best = c;
+    if (cafe_cand_better(c, best)) {
+      if (have) k2 = min(k2, best.tk);
+      best = c;
+    } else {
+      k2 = min(k2, tk);
+    }
     if (!have) {
       have = true;
       tfirst = tk;
     }
   }
+  if (k2out) *k2out = k2;
 }
 __device__ __forceinline__ void cafe_row_best(const CafeDev &D, const CafeConsts &K, long long r,
                                               CafeCand &best, bool bounded = true) {
@@ -1021,7 +1041,8 @@ __device__ __forceinline__ void cafe_row_eval_live(const CafeDev &D, const CafeC
 #ifdef CAFE_DETAIL_CYCLES
   long long be0 = clock64();
 #endif
-  cafe_row_best_live(D, K, r, live, b, false);
+  unsigned long long k2;
+  cafe_row_best_live(D, K, r, live, b, false, &k2);
 #ifdef CAFE_DETAIL_CYCLES
   atomicAdd(&D.stat[STAT_DETAIL + 30], (unsigned long long)(clock64() - be0));
   atomicAdd(&D.stat[STAT_DETAIL + 31], 1ULL);
@@ -1034,7 +1055,9 @@ __device__ __forceinline__ void cafe_row_eval_live(const CafeDev &D, const CafeC
   D.row_bt[r] = b.t;
   D.row_bruq[r] = b.ruqs;
   D.row_bslot[r] = b.s;
-  D.row_key[r] = cafe_key(T + b.t);
+  const unsigned long long key = cafe_key(T + b.t);
+  D.row_key[r] = key;
+  D.row_key2[r] = k2 == CAFE_KEY_NONE ? key : cafe_key(T + cafe_unkey(k2));
 }
 __device__ __forceinline__ void cafe_row_eval(const CafeDev &D, const CafeConsts &K, int r, int ev,
                                               double T) {
@@ -1176,7 +1199,17 @@ __device__ void cafe_select_keyed(const CafeDev &D, const CafeConsts &K, int ev,
   if (dirty[gtid]) {
     dirty[gtid] = 0;
     unsigned long long m = CAFE_KEY_NONE;
-    for (int r = gtid; r < nrows; r += gn) m = min(m, D.row_key[r]);
+    // batches of eight loads in flight together
+    for (int r0 = gtid; r0 < nrows; r0 += 8 * gn) {
+      unsigned long long kk[8];
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        const int r = r0 + i * gn;
+        kk[i] = r < nrows ? D.row_key[r] : CAFE_KEY_NONE;
+      }
+#pragma unroll
+      for (int i = 0; i < 8; ++i) m = min(m, kk[i]);
+    }
     my_min = m;
   }
   CafeCand best;
@@ -1226,16 +1259,67 @@ __device__ void cafe_select_keyed(const CafeDev &D, const CafeConsts &K, int ev,
 #endif
     const unsigned long long kthr = S.kthr;
     int again = 0;
+#ifdef CAFE_DETAIL_CYCLES
+    long long eval_cyc = 0, phase_a = 0;
+    int n_mark = 0;
+#endif
     best = cafe_cand_none();
     if (kthr != CAFE_KEY_NONE && (my_min <= kthr || my_forced)) {
       unsigned long long m = CAFE_KEY_NONE;
-      for (int r = gtid; r < nrows; r += gn) {
-        unsigned long long k = D.row_key[r];
-        if (k <= kthr || my_forced) {
+      // this thread's rows r = r0 + i gn, 32 at a time: first their keys,
+      // loaded together, mark the rows at or below the threshold (and, when
+      // forced, the rows stamped -1); then only the marked rows are visited
+      for (int r0 = gtid; r0 < nrows; r0 += 32 * gn) {
+        uint32_t mark = 0;
+#ifdef CAFE_DETAIL_CYCLES
+        long long pa0 = cafe_clock_ordered();
+#endif
+        // (branch-free batches of eight loads, so that they are in flight
+        // together)
+#pragma unroll
+        for (int b = 0; b < 32; b += 8) {
+          if (r0 + b * gn >= nrows) break;
+          unsigned long long kk[8];
+#pragma unroll
+          for (int i = 0; i < 8; ++i) {
+            const int r = r0 + (b + i) * gn;
+            kk[i] = r < nrows ? D.row_key[r] : CAFE_KEY_NONE;
+          }
+          uint32_t fm = 0;  // rows stamped -1, visited whatever their key
+          if (my_forced) {
+#pragma unroll
+            for (int i = 0; i < 8; ++i) {
+              const int r = r0 + (b + i) * gn;
+              fm |= (r < nrows && D.row_stamp[r] == -1) ? 1u << i : 0u;
+            }
+          }
+#pragma unroll
+          for (int i = 0; i < 8; ++i) {
+            // a visited row's key enters the minimum after its visit
+            if (kk[i] <= kthr || (fm >> i & 1u))
+              mark |= 1u << (b + i);
+            else
+              m = min(m, kk[i]);
+          }
+        }
+#ifdef CAFE_DETAIL_CYCLES
+        phase_a += cafe_clock_ordered() - pa0;
+        n_mark += __popc(mark);
+#endif
+        while (mark) {
+          const int r = r0 + (__ffs(mark) - 1) * gn;
+          mark &= mark - 1;
+          unsigned long long k = D.row_key[r];
           int stamp = D.row_stamp[r];
           // stamp -1: forced after a possible clamp of the row's extent
           if ((k <= kthr && stamp != ev + 1) || (stamp == -1 && D.row_alive[r])) {
+#ifdef CAFE_DETAIL_CYCLES
+            long long ev0 = cafe_clock_ordered();
+#endif
             cafe_row_eval(D, K, r, ev, T);
+#ifdef CAFE_DETAIL_CYCLES
+            eval_cyc += cafe_clock_ordered() - ev0;
+#endif
             k = D.row_key[r];
             again = 1;
           }
@@ -1249,12 +1333,22 @@ __device__ void cafe_select_keyed(const CafeDev &D, const CafeConsts &K, int ev,
             c.s = D.row_bslot[r];
             if (cafe_cand_better(c, best)) best = c;
           }
+          m = min(m, k);
         }
-        m = min(m, k);
       }
       my_min = m;
       my_forced = false;
     }
+#ifdef CAFE_DETAIL_CYCLES
+    if (again) {
+      // scan time of the evaluating threads apart from their evaluations
+      atomicAdd(&D.stat[STAT_DETAIL + 10], (unsigned long long)(cafe_clock_ordered() - sr1 - eval_cyc));
+      atomicAdd(&D.stat[STAT_DETAIL + 11], 1ULL);
+      atomicAdd(&D.stat[STAT_DETAIL + 12], (unsigned long long)eval_cyc);
+      atomicAdd(&D.stat[STAT_DETAIL + 14], (unsigned long long)phase_a);
+      atomicAdd(&D.stat[STAT_DETAIL + 15], (unsigned long long)n_mark);
+    }
+#endif
 #ifdef CAFE_DETAIL_CYCLES
     long long sr2 = cafe_clock_ordered();
     if (gtid == 0) S.cyc[2] += sr2 - sr1;  // scan and evaluations (this thread)
@@ -1519,6 +1613,15 @@ __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
               D.row_death[r] = e;  // it grew at this event too
               D.row_key[r] = CAFE_KEY_NONE;
               s_dirty[r % NSEL] = 1;
+            } else if (sl >= 0 && sl == D.row_bslot[r]) {
+              // the row's best candidate is gone: its key rises to that of
+              // its next candidate at the same evaluation, which bounds the
+              // row's exact value from below as the old key did
+              const unsigned long long k2 = D.row_key2[r];
+              if (k2 > D.row_key[r]) {
+                D.row_key[r] = k2;
+                s_dirty[r % NSEL] = 1;
+              }
             }
           }
         }
