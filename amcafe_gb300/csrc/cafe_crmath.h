@@ -32,6 +32,9 @@
 
 #if defined(__CUDACC__)
 #define CRM_HD __host__ __device__ __forceinline__
+// the double-double paths, taken rarely: one out-of-line copy each keeps the
+// inlined fast paths compact
+#define CRM_COLD __host__ __device__ __noinline__
 #ifdef __CUDA_ARCH__
 #define CRM_TAB(name) name##_d
 #else
@@ -39,6 +42,7 @@
 #endif
 #else
 #define CRM_HD static inline
+#define CRM_COLD static inline
 #define CRM_TAB(name) name##_h
 #endif
 
@@ -197,7 +201,7 @@ CRM_HD double crm_atan2_dd(crm_dd ay, crm_dd ax, int y_neg, int x_neg) {
   return y_neg ? -v : v;
 }
 
-CRM_HD double crm_atan2_acc(double y, double x) {
+CRM_COLD double crm_atan2_acc(double y, double x) {
   if (y != y || x != x) return y + x;
   int yn = signbit(y) ? 1 : 0, xn = signbit(x) ? 1 : 0;
   double ay = fabs(y), ax = fabs(x);
@@ -221,7 +225,7 @@ CRM_HD double crm_atan2_acc(double y, double x) {
 }
 
 // Cody-Waite reduction x = k pi/2 + r for |x| < 2^20, r in double-double.
-CRM_HD crm_dd crm_reduce_pio2(double x, int *quadrant) {
+CRM_COLD crm_dd crm_reduce_pio2(double x, int *quadrant) {
   double kd = x * CRM_TWO_OVER_PI;
   kd = (kd >= 0.0) ? (double)(long long)(kd + 0.5) : -(double)(long long)(-kd + 0.5);
   crm_dd a = crm_two_prod(kd, CRM_PIO2_1);  // exact
@@ -266,7 +270,7 @@ CRM_HD void crm_sincos_small(crm_dd r, crm_dd *sn, crm_dd *cs) {
 
 // Supported domain |x| < 2^20 (the CA evaluates arguments in [-2 pi, 2 pi]);
 // outside it the result is NaN.
-CRM_HD double crm_sin_acc(double x) {
+CRM_COLD double crm_sin_acc(double x) {
   if (!(fabs(x) < 1048576.0)) return NAN;
   if (x == 0.0) return x;
   int q;
@@ -280,7 +284,7 @@ CRM_HD double crm_sin_acc(double x) {
     default: return -crm_dd_round(c);
   }
 }
-CRM_HD double crm_cos_acc(double x) {
+CRM_COLD double crm_cos_acc(double x) {
   if (!(fabs(x) < 1048576.0)) return NAN;
   int q;
   crm_dd r = crm_reduce_pio2(x, &q);
@@ -592,7 +596,7 @@ CRM_HD int crm_exp_finish(double s, double lo, double err, int m, int force, dou
   return crm_round_scaled_sub(s, lo, err, m, force, out);
 }
 
-CRM_HD double crm_exp_acc(double x) {
+CRM_COLD double crm_exp_acc(double x) {
   long long k;
   double rh, rl;
   crm_exp_reduce(x, &k, &rh, &rl);

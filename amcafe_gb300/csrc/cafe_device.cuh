@@ -153,11 +153,12 @@ struct CafeDev {
   // including the growth of events 1..row_m, copied back to a_ext afterwards;
   // a row grows at the events (birth, row_death]; row_key orders the rows by
   // estimated absolute capture time; row_b* hold the exact best candidate of
-  // the iteration row_stamp; row_key2 is the key of the row's smallest
-  // candidate time apart from slot row_bslot at that evaluation, the row's
-  // key once that slot is captured by another row
+  // the iteration row_stamp (row_bq: the position that slot captures);
+  // row_key2 is the key of the row's smallest candidate time apart from slot
+  // row_bslot at that evaluation, the row's key once that slot is captured
+  // by another row
   double *row_E;
-  int32_t *row_m, *row_death, *row_stamp, *row_bslot;
+  int32_t *row_m, *row_death, *row_stamp, *row_bslot, *row_bq;
   unsigned long long *row_key, *row_key2;
   double *row_bt, *row_bruq;
   // per-event growth: ev_vd[e] = fl(v * DtMin_e) (+0 for a nucleation),

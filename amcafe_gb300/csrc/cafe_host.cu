@@ -1153,6 +1153,7 @@ int cafe_sim_create(const char *deck_path, const cafe_options *opt, cafe_sim **o
       (rc = dalloc(&D.row_m, D.row_cap, o)) || (rc = dalloc(&D.ev_vd, D.ev_cap, o)) ||
       (rc = dalloc(&D.ev_vs, D.ev_cap, o)) ||
       (rc = dalloc(&D.row_stamp, D.row_cap, o)) || (rc = dalloc(&D.row_bslot, D.row_cap, o)) ||
+      (rc = dalloc(&D.row_bq, D.row_cap, o)) ||
       (rc = dalloc(&D.row_key, D.row_cap, o)) || (rc = dalloc(&D.row_key2, D.row_cap, o)) ||
       (rc = dalloc(&D.row_bt, D.row_cap, o)) ||
       (rc = dalloc(&D.row_bruq, D.row_cap, o)) ||

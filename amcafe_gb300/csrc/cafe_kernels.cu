@@ -44,6 +44,10 @@ __device__ __forceinline__ long long cafe_clock_ordered() {
 #endif
 
 // ------------------------------------------------------------------ helpers
+// Hint: bring the line holding *a into this SM's L1 (no effect on results).
+__device__ __forceinline__ void cafe_prefetch_l1(const void *a) {
+  asm volatile("prefetch.global.L1 [%0];" ::"l"(a));
+}
 // Growth velocity of active position p (VoxelsCA.C:405): per temperature class
 // with the analytic field, per cell with the EASM field.
 __device__ __forceinline__ double cafe_vh(const CafeDev &D, const CafeConsts &K, int p) {
@@ -647,10 +651,16 @@ __device__ __forceinline__ int cafe_exp_lb(double x) {
 // `eval`, the row's exact best candidate at iteration `ev` and time T is stored
 // (what cafe_row_best computes, one slot per lane). Returns, in every lane, the
 // order key of the largest finite |g| of the live slots, or 0 when none.
+// `parts` selects the row order (CAFE_FIN_ORDER) and the rest (CAFE_FIN_BEST:
+// row_live, the best candidate, the largest |g|), so that two warps holding
+// the same slots can share the work.
+#define CAFE_FIN_ORDER 1
+#define CAFE_FIN_BEST 2
 __device__ unsigned long long cafe_row_finish_warp(const CafeDev &D, const CafeConsts &K, long long r, int p,
                                                    int nn, bool liv, double gv, int q, bool eval, int ev,
                                                    double T, bool have_t = false, double t_pre = 0.0,
-                                                   double ruqs_pre = 0.0) {
+                                                   double ruqs_pre = 0.0,
+                                                   int parts = CAFE_FIN_ORDER | CAFE_FIN_BEST) {
   const unsigned FULL = 0xffffffffu;
   int lane = threadIdx.x & 31;
   uint32_t live = __ballot_sync(FULL, liv);
@@ -659,17 +669,23 @@ __device__ unsigned long long cafe_row_finish_warp(const CafeDev &D, const CafeC
   long long fz0 = clock64();
 #endif
   const bool gfin = !cafe_is_nan(gv);
-  unsigned long long key = (liv && gfin) ? cafe_key_canon(gv) : CAFE_KEY_NONE;
-  int rank = liv ? 0 : __popc(live);
-  for (int t = 0; t < nn; ++t) {
-    unsigned long long kt = cafe_shfl_u64(key, t);
-    bool lt = (live >> t) & 1u;
-    if (liv)
-      rank += lt && (kt < key || (kt == key && t < lane));
-    else
-      rank += !lt && t < lane;
+  if (parts & CAFE_FIN_ORDER) {
+    unsigned long long key = (liv && gfin) ? cafe_key_canon(gv) : CAFE_KEY_NONE;
+    int rank = liv ? 0 : __popc(live);
+    // (every slot position, so that the shuffles are independent; the bits of
+    // live above nn are clear)
+#pragma unroll
+    for (int t = 0; t < CAFE_NSLOT; ++t) {
+      unsigned long long kt = cafe_shfl_u64(key, t);
+      bool lt = (live >> t) & 1u;
+      if (liv)
+        rank += lt && (kt < key || (kt == key && t < lane));
+      else
+        rank += !lt && t < nn && t < lane;
+    }
+    if (lane < nn) D.row_ord[r * CAFE_NSLOT + rank] = (uint8_t)lane;
   }
-  if (lane < nn) D.row_ord[r * CAFE_NSLOT + rank] = (uint8_t)lane;
+  if (!(parts & CAFE_FIN_BEST)) return 0ULL;
   if (lane == 0) D.row_live[r] = live;
 #ifdef CAFE_DETAIL_CYCLES
   long long fz1 = clock64();
@@ -712,6 +728,7 @@ __device__ unsigned long long cafe_row_finish_warp(const CafeDev &D, const CafeC
     for (int o = 16; o > 0; o >>= 1) k2 = min(k2, cafe_shfl_u64_xor(k2, o));
     double bt = __shfl_sync(FULL, t, sl & 31);
     double bruq = __shfl_sync(FULL, ruqs, sl & 31);
+    int bq = __shfl_sync(FULL, q, sl & 31);
     if (lane == 0) {
       D.row_stamp[r] = ev + 1;
       if (sl == 255) {
@@ -720,6 +737,7 @@ __device__ unsigned long long cafe_row_finish_warp(const CafeDev &D, const CafeC
         D.row_bt[r] = bt;
         D.row_bruq[r] = bruq;
         D.row_bslot[r] = sl;
+        D.row_bq[r] = bq;
         const unsigned long long key = cafe_key(T + bt);
         D.row_key[r] = key;
         D.row_key2[r] = k2 == CAFE_KEY_NONE ? key : cafe_key(T + cafe_unkey(k2));
@@ -743,6 +761,12 @@ __device__ unsigned long long cafe_row_finish_warp(const CafeDev &D, const CafeC
   return ak;
 }
 
+// The captured cell's grain, centre and extent as the capture section just
+// stored them, handed to the fill through shared memory.
+struct CafeNewCell {
+  double c[3], ext;
+  int gid;
+};
 // Per-slot partial results passed between the four warps of cafe_row_fill_quad.
 struct CafeQuadScratch {
   double cth[32], sph[32], l[32], d1I[32], dI2[32], d1J[32], dJ3[32], g[32], t[32], ruqs[32];
@@ -764,13 +788,14 @@ __device__ __forceinline__ void cafe_bar_quad() { asm volatile("bar.sync 1, 128;
 //           centre.
 // Warp 0 finishes the row; the return value is valid in warp 0.
 __device__ unsigned long long cafe_row_fill_quad(const CafeDev &D, const CafeConsts &K, long long r, int p,
-                                                 bool eval, int ev, double T, CafeQuadScratch &S) {
+                                                 bool eval, int ev, double T, CafeQuadScratch &S,
+                                                 const CafeNewCell *nc = nullptr) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
 #ifdef CAFE_DETAIL_CYCLES
   long long fq0 = clock64();
 #endif
   int nn = D.a_nn[p];
-  int gp = D.a_gid[p];
+  int gp = nc ? nc->gid : D.a_gid[p];
   bool grain_ok = gp >= 1 && gp <= D.grain_cap;
   bool liv = false;
   int q = 0;
@@ -787,9 +812,9 @@ __device__ unsigned long long cafe_row_fill_quad(const CafeDev &D, const CafeCon
   if (work) {
     cafe_cell_xyz(K, D.act[q], ci, cj, ck);
     cafe_cell_xyz(K, D.act[p], si, sj, sk);
-    cs[0] = D.a_cx[p];
-    cs[1] = D.a_cy[p];
-    cs[2] = D.a_cz[p];
+    cs[0] = nc ? nc->c[0] : D.a_cx[p];
+    cs[1] = nc ? nc->c[1] : D.a_cy[p];
+    cs[2] = nc ? nc->c[2] : D.a_cz[p];
     cafe_geo_dn(K, ci, cj, ck, cs, dn);
     if (w == 0) {
       S.cth[lane] = cafe_geo_costh(dn);
@@ -803,7 +828,7 @@ __device__ unsigned long long cafe_row_fill_quad(const CafeDev &D, const CafeCon
       s0i = cafe_geo_corners(loc, dr, pk);
       if (w == 2) {
         if (eval) {
-          E2 = D.a_ext[p];
+          E2 = nc ? nc->ext : D.a_ext[p];
           v2 = cafe_vh(D, K, p);
         }
         cafe_geo_edge(loc, pk[0], pk[1], &S.d1I[lane], &S.dI2[lane]);
@@ -850,7 +875,11 @@ __device__ unsigned long long cafe_row_fill_quad(const CafeDev &D, const CafeCon
     if (work) gv = S.g[lane];
     if (liv) D.row_g[r * CAFE_NSLOT + lane] = gv;
     ak = cafe_row_finish_warp(D, K, r, p, nn, liv, gv, q, eval, ev, T, true, work ? S.t[lane] : (double)NAN,
-                              work ? S.ruqs[lane] : 0.0);
+                              work ? S.ruqs[lane] : 0.0, CAFE_FIN_BEST);
+  } else if (w == 1) {
+    // the slot order, beside warp 0 (read only by later evaluations)
+    if (work) gv = S.g[lane];
+    cafe_row_finish_warp(D, K, r, p, nn, liv, gv, q, false, ev, T, false, 0.0, 0.0, CAFE_FIN_ORDER);
   }
 #ifdef CAFE_DETAIL_CYCLES
   if (lane == 0) {
@@ -873,6 +902,7 @@ struct CafeCand {
   unsigned long long tk, rk;
   double t, ruqs;
   int j, s;  // vs2 index and neighbour slot of the capturing cell; j < 0 = none
+  int r, p, q;  // (not compared) its row, its active position and the captured position
 };
 __device__ __forceinline__ CafeCand cafe_cand_none() {
   CafeCand c;
@@ -880,6 +910,7 @@ __device__ __forceinline__ CafeCand cafe_cand_none() {
   c.t = c.ruqs = 0.0;
   c.j = -1;
   c.s = 0;
+  c.r = c.p = c.q = 0;
   return c;
 }
 __device__ __forceinline__ bool cafe_cand_better(const CafeCand &a, const CafeCand &b) {
@@ -900,6 +931,9 @@ __device__ __forceinline__ CafeCand cafe_shfl_cand(const CafeCand &c, int o) {
   r.ruqs = __shfl_xor_sync(0xffffffffu, c.ruqs, o);
   r.j = __shfl_xor_sync(0xffffffffu, c.j, o);
   r.s = __shfl_xor_sync(0xffffffffu, c.s, o);
+  r.r = __shfl_xor_sync(0xffffffffu, c.r, o);
+  r.p = __shfl_xor_sync(0xffffffffu, c.p, o);
+  r.q = __shfl_xor_sync(0xffffffffu, c.q, o);
   return r;
 }
 // Best candidate of the warp, in every lane.
@@ -960,6 +994,9 @@ __device__ __forceinline__ void cafe_row_best_live(const CafeDev &D, const CafeC
     c.rk = cafe_key_canon(c.ruqs);
     c.j = jrow;
     c.s = s;
+    c.r = (int)r;
+    c.p = p;
+    c.q = q;
     if (cafe_cand_better(c, best)) {
       if (have) k2 = min(k2, best.tk);
       best = c;
@@ -1055,6 +1092,7 @@ __device__ __forceinline__ void cafe_row_eval_live(const CafeDev &D, const CafeC
   D.row_bt[r] = b.t;
   D.row_bruq[r] = b.ruqs;
   D.row_bslot[r] = b.s;
+  D.row_bq[r] = b.q;
   const unsigned long long key = cafe_key(T + b.t);
   D.row_key[r] = key;
   D.row_key2[r] = k2 == CAFE_KEY_NONE ? key : cafe_key(T + cafe_unkey(k2));
@@ -1331,6 +1369,9 @@ __device__ void cafe_select_keyed(const CafeDev &D, const CafeConsts &K, int ev,
             c.rk = cafe_key_canon(c.ruqs);
             c.j = D.row_j[r];
             c.s = D.row_bslot[r];
+            c.r = r;
+            c.p = D.row_pos[r];
+            c.q = D.row_bq[r];
             if (cafe_cand_better(c, best)) best = c;
           }
           m = min(m, k);
@@ -1392,11 +1433,13 @@ __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
   __shared__ CafeSelShared s_sel;
   __shared__ CafeCand s_best;  // winner of the next event (keyed mode)
   __shared__ double s_tinc, s_dt, s_dsum, s_gmax, s_emax, s_vd, s_vs;
-  __shared__ int s_nvs2, s_countS, s_nrows, s_ngrain, s_done, s_nuc, s_icap, s_jspos, s_bslot, s_na, s_slow,
-      s_ev, s_switch, s_newrow;
+  __shared__ int s_nvs2, s_countS, s_nrows, s_ngrain, s_done, s_nuc, s_icap, s_jspos, s_bslot, s_brow, s_na,
+      s_slow, s_ev, s_switch, s_newrow;
   __shared__ unsigned char s_dirty[NSEL];   // a row of selecting thread i changed its key elsewhere
   __shared__ unsigned char s_forced[NSEL];  // a row of selecting thread i was stamped -1
-  __shared__ uint32_t s_rng;
+  __shared__ uint32_t s_rng, s_rng_next;  // stream state after the consumed draws, after the next one
+  __shared__ double s_unext;               // the next event's draw (VoxelsCA.C:483)
+  __shared__ CafeNewCell s_nc;
   __shared__ unsigned int s_sdloc;
   __shared__ long long s_nnuc, s_negdt;
   __shared__ long long s_cyc[4];  // winner, capture + bookkeeping, new row || selection, merge
@@ -1442,6 +1485,13 @@ __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
     s_ngrain = D.ctr[CTR_NGRAIN];
     uint32_t seed = cafe_minstd_seed((uint64_t)(uint32_t)(30 * P.tInd + (int)K.seed1));
     s_rng = cafe_minstd_skip(seed, 2ULL * (uint64_t)s_na);
+    {
+      // the first event's draw; later draws are made one event ahead
+      cafe_uniform_stream st;
+      st.x = s_rng;
+      s_unext = cafe_uniform_next(&st);
+      s_rng_next = st.x;
+    }
     s_sdloc = K.seed0 + 32u * (unsigned int)P.tInd + 64u * (unsigned int)s_ngrain;
     s_tinc = 0.0;
     s_dsum = 0.0;
@@ -1526,14 +1576,15 @@ __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
             if (b.j >= 0 && b.tk < CAFE_KEY_1E6) atomicOr(D.err, CAFE_ERR_ITER_CAP);
             s_done = 1;
           } else {
-            cafe_uniform_stream st;
-            st.x = s_rng;
-            double U = cafe_uniform_next(&st);
-            s_rng = st.x;
-            int jspos = D.vs2[b.j];
-            s_jspos = jspos;
+            // the draw made one event ahead from the current stream state
+            const double U = s_unext;
+            s_rng = s_rng_next;
+            // (the candidate carries vs2[j], its row and the captured
+            // position a_nbr[vs2[j], s])
+            s_jspos = b.p;
             s_bslot = b.s;
-            s_icap = D.a_nbr[(long long)jspos * CAFE_NSLOT + b.s];
+            s_brow = b.r;
+            s_icap = b.q;
             s_nuc = U < cafe_nuc_rate(D, K, s_icap);
             s_dt = s_nuc ? 0.0 : b.t;
             if (cafe_is_neg(s_dt)) s_negdt++;
@@ -1583,48 +1634,72 @@ __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
           }
           s_ngrain += 1;
           D.a_gid[icap] = s_ngrain;
-          D.a_cx[icap] = ((double)ci + .5) * K.dx[0];
-          D.a_cy[icap] = ((double)cj + .5) * K.dx[1];
-          D.a_cz[icap] = ((double)ck + .5) * K.dx[2];
+          s_nc.gid = s_ngrain;
+          D.a_cx[icap] = s_nc.c[0] = ((double)ci + .5) * K.dx[0];
+          D.a_cy[icap] = s_nc.c[1] = ((double)cj + .5) * K.dx[1];
+          D.a_cz[icap] = s_nc.c[2] = ((double)ck + .5) * K.dx[2];
           s_sdloc += 10u;
-          D.a_ext[icap] = 0.0;
+          D.a_ext[icap] = s_nc.ext = 0.0;
           s_nnuc++;
         } else {
           // the capture result of this slot, computed when the row was filled
-          D.a_gid[icap] = D.a_gid[js];
-          const double *gq = D.row_geo + ((long long)D.a_frow[js] * CAFE_NSLOT + s_bslot) * 4;
-          D.a_ext[icap] = gq[0];
-          D.a_cx[icap] = gq[1];
-          D.a_cy[icap] = gq[2];
-          D.a_cz[icap] = gq[3];
+          const int gcap = D.a_gid[js];
+          if (gcap >= 1 && gcap <= D.grain_cap) {
+            // the grain's rotation, read by the new row's fill
+            cafe_prefetch_l1(D.rot + 9LL * (gcap - 1));
+            cafe_prefetch_l1(D.rot + 9LL * (gcap - 1) + 8);
+          }
+          cafe_prefetch_l1(D.act + icap);
+          D.a_gid[icap] = s_nc.gid = gcap;
+          const double *gq = D.row_geo + ((long long)s_brow * CAFE_NSLOT + s_bslot) * 4;
+          D.a_ext[icap] = s_nc.ext = gq[0];
+          D.a_cx[icap] = s_nc.c[0] = gq[1];
+          D.a_cy[icap] = s_nc.c[1] = gq[2];
+          D.a_cz[icap] = s_nc.c[2] = gq[3];
         }
       } else if (warp == 1) {
         // neighbours of the captured cell lose one liquid neighbour
         const int nn = D.a_nn[icap];
         if (lane < nn) {
           int q = D.a_nbr[(long long)icap * CAFE_NSLOT + lane];
-          int left = --D.a_liq[q];
-          int r = D.a_frow[q];
-          if (r >= 0 && D.row_alive[r]) {
-            int sl = cafe_find_slot(D, q, icap);
-            if (sl >= 0) D.row_live[r] &= ~(1u << sl);
+          // the new row's fill reads these next (nothing writes them here)
+          cafe_prefetch_l1(D.a_state + q);
+          cafe_prefetch_l1(D.act + q);
+          // every load before the stores, so that the loads of one chain
+          // level are in flight together
+          const int liq = D.a_liq[q];
+          const int r = D.a_frow[q];
+          const int sl = cafe_find_slot(D, q, icap);
+          const int rr = r >= 0 ? r : 0;
+          const bool alive = r >= 0 && D.row_alive[rr];
+          const uint32_t lv = D.row_live[rr];
+          const int bs = D.row_bslot[rr];
+          const unsigned long long k1 = D.row_key[rr], k2 = D.row_key2[rr];
+          const int left = liq - 1;
+          D.a_liq[q] = left;
+          if (alive) {
+            if (sl >= 0) D.row_live[r] = lv & ~(1u << sl);
             if (left <= 0) {
               D.row_alive[r] = 0;
               D.row_death[r] = e;  // it grew at this event too
               D.row_key[r] = CAFE_KEY_NONE;
               s_dirty[r % NSEL] = 1;
-            } else if (sl >= 0 && sl == D.row_bslot[r]) {
+            } else if (sl >= 0 && sl == bs && k2 > k1) {
               // the row's best candidate is gone: its key rises to that of
               // its next candidate at the same evaluation, which bounds the
               // row's exact value from below as the old key did
-              const unsigned long long k2 = D.row_key2[r];
-              if (k2 > D.row_key[r]) {
-                D.row_key[r] = k2;
-                s_dirty[r % NSEL] = 1;
-              }
+              D.row_key[r] = k2;
+              s_dirty[r % NSEL] = 1;
             }
           }
         }
+      } else if (tid == 64) {
+        // the next event's draw, off the winner section's chain (the stream
+        // advances by two engine outputs per event whatever the event)
+        cafe_uniform_stream st;
+        st.x = s_rng;
+        s_unext = cafe_uniform_next(&st);
+        s_rng_next = st.x;
       } else if (hid >= 0 && !s_nuc && cafe_is_neg(s_dt)) {
         // a negative event may clamp a small extent at zero (VoxelsCA.C:515),
         // which breaks the key bound of that row: mark the rows whose
@@ -1665,7 +1740,7 @@ __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
               D.row_m[r] = e;
             }
             const bool same_v = D.a_cls[icap] == 1;
-            unsigned long long gk = cafe_row_fill_quad(D, K, r, icap, same_v, e, s_tinc, s_quad);
+            unsigned long long gk = cafe_row_fill_quad(D, K, r, icap, same_v, e, s_tinc, s_quad, &s_nc);
             if (tid == 0) {
               if (!same_v) {
                 s_switch = 1;
@@ -1709,6 +1784,9 @@ __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
             c.rk = cafe_key_canon(c.ruqs);
             c.j = D.row_j[r];
             c.s = D.row_bslot[r];
+            c.r = r;
+            c.p = D.row_pos[r];
+            c.q = D.row_bq[r];
             if (cafe_cand_better(c, b)) b = c;
           }
         }
