@@ -769,7 +769,7 @@ struct CafeNewCell {
 };
 // Per-slot partial results passed between the four warps of cafe_row_fill_quad.
 struct CafeQuadScratch {
-  double cth[32], sph[32], l[32], d1I[32], dI2[32], d1J[32], dJ3[32], g[32], t[32], ruqs[32];
+  double cth[32], sph[32], l[32], d1I[32], dI2[32], d1J[32], dJ3[32], dr[32], ruqs[32];
 };
 #define CAFE_QUAD_THREADS 128
 __device__ __forceinline__ void cafe_bar_quad() { asm volatile("bar.sync 1, 128;" ::: "memory"); }
@@ -780,13 +780,14 @@ __device__ __forceinline__ void cafe_bar_quad() { asm volatile("bar.sync 1, 128;
 // ordered and, with `eval`, the row's exact best candidate at iteration `ev`
 // and time T is stored. A warp issues one FP64 instruction at a time whatever its
 // active lanes, so the independent chains of each slot's geometry run in
-// different warps, lane s of each warp on slot s:
+// different warps, lane s of each warp on slot s. First stage:
 //   warp 0: cos th and the cell distance l; warp 1: sin ph;
-//   warp 2: the projection on edge p0-p1, then g, the extent and (with
-//           eval) the capture time t = (g - ExtA)/v;
-//   warp 3: the projection on edge p0-p2 and the tie-break ruqs, then the new
-//           centre.
-// Warp 0 finishes the row; the return value is valid in warp 0.
+//   warp 2: |R^T dn|_1 and the projection on edge p0-p1;
+//   warp 3: the projection on edge p0-p2 and the tie-break ruqs.
+// Second stage, after one barrier: warps 0 and 1 form g; warp 0 the capture
+// time t = (g - ExtA)/v (with eval) and the row's best candidate, warp 1 the
+// slot order; warp 2 the extent and warp 3 the centre a capture from this row
+// gives. The return value is valid in warp 0.
 __device__ unsigned long long cafe_row_fill_quad(const CafeDev &D, const CafeConsts &K, long long r, int p,
                                                  bool eval, int ev, double T, CafeQuadScratch &S,
                                                  const CafeNewCell *nc = nullptr) {
@@ -807,7 +808,7 @@ __device__ unsigned long long cafe_row_fill_quad(const CafeDev &D, const CafeCon
   }
   const bool work = liv && grain_ok;
   double R[9], loc[3], dr = 0.0, pk[3][3];
-  double E2 = 0.0, v2 = 1.0;  // warp 2: the row's extent and velocity for t
+  double E0 = 0.0, v0 = 1.0;  // warp 0: the row's extent and velocity for t
   int s0i = 0;
   if (work) {
     cafe_cell_xyz(K, D.act[q], ci, cj, ck);
@@ -817,6 +818,10 @@ __device__ unsigned long long cafe_row_fill_quad(const CafeDev &D, const CafeCon
     cs[2] = nc ? nc->c[2] : D.a_cz[p];
     cafe_geo_dn(K, ci, cj, ck, cs, dn);
     if (w == 0) {
+      if (eval) {
+        E0 = nc ? nc->ext : D.a_ext[p];
+        v0 = cafe_vh(D, K, p);
+      }
       S.cth[lane] = cafe_geo_costh(dn);
       S.l[lane] = cafe_geo_l(K, ci, cj, ck, si, sj, sk);
     } else if (w == 1) {
@@ -827,10 +832,7 @@ __device__ unsigned long long cafe_row_fill_quad(const CafeDev &D, const CafeCon
       dr = cafe_geo_loc(R, dn, loc);
       s0i = cafe_geo_corners(loc, dr, pk);
       if (w == 2) {
-        if (eval) {
-          E2 = nc ? nc->ext : D.a_ext[p];
-          v2 = cafe_vh(D, K, p);
-        }
+        S.dr[lane] = dr;
         cafe_geo_edge(loc, pk[0], pk[1], &S.d1I[lane], &S.dI2[lane]);
       } else {
         cafe_geo_edge(loc, pk[0], pk[2], &S.d1J[lane], &S.dJ3[lane]);
@@ -845,19 +847,40 @@ __device__ unsigned long long cafe_row_fill_quad(const CafeDev &D, const CafeCon
 #ifdef CAFE_DETAIL_CYCLES
   long long fq2 = clock64();
 #endif
+  // second stage, no barrier after it: warp 0 forms g and the capture time
+  // and takes the row's best candidate, warp 1 forms g and orders the slots,
+  // warps 2 and 3 finish the capture geometry (extent, centre), which only a
+  // later capture by this row reads
   double gv = liv ? NAN : 0.0;  // a capturing cell without a grain never captures
-  if (work && w >= 2) {
+  unsigned long long ak = 0ULL;
+#ifdef CAFE_DETAIL_CYCLES
+  long long fq3 = clock64();
+#endif
+  if (w <= 1) {
+    double f = 0.0;
+    if (work) {
+      f = crm_pow_half(S.cth[lane] * S.sph[lane]);
+      gv = f * S.dr[lane];
+    }
+    if (w == 0) {
+      double t = NAN;
+      if (work && eval) {
+        double dr2 = gv - E0;
+        t = dr2 / v0;
+      }
+      if (liv) D.row_g[r * CAFE_NSLOT + lane] = gv;
+      ak = cafe_row_finish_warp(D, K, r, p, nn, liv, gv, q, eval, ev, T, true, t, work ? S.ruqs[lane] : 0.0,
+                                CAFE_FIN_BEST);
+    } else {
+      // the slot order (read only by later evaluations)
+      cafe_row_finish_warp(D, K, r, p, nn, liv, gv, q, false, ev, T, false, 0.0, 0.0, CAFE_FIN_ORDER);
+    }
+  } else if (work) {
     double Lmud = cafe_geo_lmud(K, S.l[lane], S.d1I[lane], S.dI2[lane], S.d1J[lane], S.dJ3[lane]);
     double *o = D.row_geo + (r * CAFE_NSLOT + lane) * 4;
     if (w == 2) {
       double f = crm_pow_half(S.cth[lane] * S.sph[lane]);
-      gv = f * dr;
-      S.g[lane] = gv;
       o[0] = f * Lmud * 1.0;
-      if (eval) {
-        double dr2 = gv - E2;
-        S.t[lane] = dr2 / v2;
-      }
     } else {
       double cn[3];
       cafe_geo_centre(R, cs, pk[0], s0i, Lmud, cn);
@@ -867,25 +890,10 @@ __device__ unsigned long long cafe_row_fill_quad(const CafeDev &D, const CafeCon
     }
   }
 #ifdef CAFE_DETAIL_CYCLES
-  long long fq3 = clock64();
-#endif
-  cafe_bar_quad();
-  unsigned long long ak = 0ULL;
-  if (w == 0) {
-    if (work) gv = S.g[lane];
-    if (liv) D.row_g[r * CAFE_NSLOT + lane] = gv;
-    ak = cafe_row_finish_warp(D, K, r, p, nn, liv, gv, q, eval, ev, T, true, work ? S.t[lane] : (double)NAN,
-                              work ? S.ruqs[lane] : 0.0, CAFE_FIN_BEST);
-  } else if (w == 1) {
-    // the slot order, beside warp 0 (read only by later evaluations)
-    if (work) gv = S.g[lane];
-    cafe_row_finish_warp(D, K, r, p, nn, liv, gv, q, false, ev, T, false, 0.0, 0.0, CAFE_FIN_ORDER);
-  }
-#ifdef CAFE_DETAIL_CYCLES
   if (lane == 0) {
     long long fq4 = clock64();
     atomicAdd(&D.stat[STAT_DETAIL + 16 + w], (unsigned long long)(fq1 - fq0));
-    if (w >= 2) atomicAdd(&D.stat[STAT_DETAIL + 18 + w], (unsigned long long)(fq3 - fq2));
+    if (w >= 2) atomicAdd(&D.stat[STAT_DETAIL + 18 + w], (unsigned long long)(fq4 - fq3));
     if (w == 0) {
       atomicAdd(&D.stat[STAT_DETAIL + 22], (unsigned long long)(fq4 - fq3));
       atomicAdd(&D.stat[STAT_DETAIL + 23], 1ULL);
