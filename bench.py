@@ -13,8 +13,11 @@ timed steps. The voxel state (about 700 MB for config 1) is larger than L2.
 
 Printed keys beyond the common contract:
   e2e        the same metric through the C ABI with host buffers: the state is
-             uploaded from host memory before the steps and downloaded after,
-             and every step reads its summary (nGrain, flags) back to the host;
+             uploaded from pinned host memory before the steps and downloaded
+             after, and every step reads its summary (nGrain, flags) back to the
+             host; up to E2E_REWIND_MAX cells the run is first restored from a
+             checkpoint taken at the start of the timed window, so that the
+             end-to-end steps are the timed steps;
   roofline   for the phase with the largest device time in the timed region,
              its algorithmic bytes per launch over its mean launch time
              (CUDA events on the engine's stream), against the measured HBM
@@ -56,6 +59,10 @@ FALLBACK_HBM_GBS = 6800.0
 # add, the final product, and exp counted as one), against the nominal FP64
 # rate of GB300 in instructions (1.25 TFLOP/s counts an FMA as two flops;
 # these operations are single instructions)
+# the end-to-end run repeats the timed window from a checkpoint up to this
+# many cells (config 1: 16.8 M, a 0.7 GB checkpoint); larger boxes time the
+# steps that follow the timed window instead
+E2E_REWIND_MAX = 64 << 20
 EASM_OPS_PER_NODE = 18
 EASM_NODES = 25
 FP64_NOMINAL_GOPS = 625.0
@@ -386,9 +393,29 @@ def main():
     setup_s = time.time() - t_setup
     info0 = sim.info()
     nvox = info0["nx"] * info0["ny"] * info0["nz"]
+    # the state at the start of the timed window, in pinned host memory (the
+    # end-to-end run uploads it) and, up to E2E_REWIND_MAX cells, a checkpoint
+    # there, so that the end-to-end run repeats the timed window's steps
+    st_host = cth_host = ckpt = None
+    if not args.no_e2e or (rank == 0 and not args.no_cpu):
+        import torch
+
+        def pinned(n, dt):
+            return torch.empty(n, dtype=dt, pin_memory=True).numpy()
+
+        ncell = sim.ncell
+        st_host = sim.state(out=dict(gID=pinned(ncell, torch.int32), vState=pinned(ncell, torch.int32),
+                                     extents=pinned(ncell, torch.float64),
+                                     centroid=pinned(3 * ncell, torch.float64),
+                                     buildj=pinned(ncell, torch.int32)))
+        cth_host = sim.ctheta()
+    if not args.no_e2e and nvox <= E2E_REWIND_MAX:
+        fd, ckpt = tempfile.mkstemp(suffix=".ckpt")
+        os.close(fd)
+        sim.checkpoint(ckpt)
     snapshot = None
     if rank == 0 and not args.no_cpu:
-        snapshot = (sim.info(), sim.state(), sim.ctheta())
+        snapshot = (info0, st_host, cth_host)
 
     # ---- timed region: device time between two events on the engine's stream
     # (the product path: each step is the step's CUDA graph)
@@ -467,27 +494,30 @@ def main():
                     "phase_steps": kp,
                     "step_achieved_GBs": step_bytes * k / (ms * 1e-3) / 1e9}
 
+    cpu = None
+    if snapshot is not None:
+        cpu = cpu_baseline(deck, snapshot[0], snapshot[1], snapshot[2], nvox, args.cpu_seconds)
+
     # ---- end to end through the C ABI with host buffers
     e2e = None
-    if not args.no_e2e and not done:
-        # host buffers in pinned memory, as a host program driving the engine
-        # would keep them
-        import torch
-
-        def pinned(n, dt):
-            return torch.empty(n, dtype=dt, pin_memory=True).numpy()
-
-        ncell = sim.ncell
-        st_host = sim.state(out=dict(gID=pinned(ncell, torch.int32), vState=pinned(ncell, torch.int32),
-                                     extents=pinned(ncell, torch.float64),
-                                     centroid=pinned(3 * ncell, torch.float64),
-                                     buildj=pinned(ncell, torch.int32)))
-        cth_host = sim.ctheta()
+    if not args.no_e2e and (ckpt is not None or not done):
+        rewound = ckpt is not None
+        if rewound:
+            # back to the start of the timed window (untimed): the same steps
+            sim.restore(ckpt)
+            os.unlink(ckpt)
+        else:
+            # too large to checkpoint here: the steps after the timed ones,
+            # from the state reached there
+            st_host = sim.state(out=st_host)
+            cth_host = sim.ctheta()
         h2d = sum(a.nbytes for a in (st_host["gID"], st_host["vState"], st_host["extents"], st_host["centroid"])) \
             + cth_host.nbytes
         d2h = h2d - cth_host.nbytes + st_host["buildj"].nbytes
         ke = args.steps
         sim.synchronize()
+        e2e_start = sim.info()["steps"]
+        ev_e0 = sim.stats()["events"]
         barrier(dist)
         te0 = time.time()
         sim.upload_state(st_host["gID"], st_host["vState"], st_host["extents"], st_host["centroid"], cth_host)
@@ -504,12 +534,13 @@ def main():
         e2e = {"value": ws * nvox * n_e / te, "unit": "voxel-updates/s",
                "h2d_bytes_per_step": int(h2d / max(1, n_e)),
                "d2h_bytes_per_step": int(d2h / max(1, n_e) + per_step_d2h / max(1, n_e)),
-               "steps": n_e}
+               "steps": n_e, "window_start_step": e2e_start,
+               "window": "the timed window again (restored from a checkpoint)" if rewound
+               else "the steps after the timed and phase-timing steps",
+               "events_per_step": (sim.stats()["events"] - ev_e0) / max(1, n_e)}
         del out_state, inf
-
-    cpu = None
-    if snapshot is not None:
-        cpu = cpu_baseline(deck, snapshot[0], snapshot[1], snapshot[2], nvox, args.cpu_seconds)
+    if ckpt is not None and os.path.exists(ckpt):
+        os.unlink(ckpt)
     if rank == 0:
         ev = stats1["events"] - stats0["events"]
         out = {
