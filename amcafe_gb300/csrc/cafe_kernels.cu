@@ -1259,6 +1259,11 @@ __device__ void cafe_select_keyed(const CafeDev &D, const CafeConsts &K, int ev,
     my_min = m;
   }
   CafeCand best;
+  // this thread's last scan in this selection: marked rows, smallest key of
+  // the others
+  bool sc_have = false;
+  uint32_t sc_mark = 0;
+  unsigned long long sc_u = CAFE_KEY_NONE;
 #ifdef CAFE_DETAIL_CYCLES
   long long sc1 = cafe_clock_ordered();
   if (gtid == 0) S.cyc[0] += sc1 - sc0;  // dirty rescan
@@ -1314,44 +1319,59 @@ __device__ void cafe_select_keyed(const CafeDev &D, const CafeConsts &K, int ev,
       unsigned long long m = CAFE_KEY_NONE;
       // this thread's rows r = r0 + i gn, 32 at a time: first their keys,
       // loaded together, mark the rows at or below the threshold (and, when
-      // forced, the rows stamped -1); then only the marked rows are visited
+      // forced, the rows stamped -1); then only the marked rows are visited.
+      // Within one selection only this thread changes its rows, and only
+      // marked ones: with its rows in one chunk, a later round whose
+      // threshold lies below the smallest unmarked key of the last scan
+      // visits the same marked rows again without loading the other keys.
+      const bool one_chunk = nrows <= 32 * gn;
       for (int r0 = gtid; r0 < nrows; r0 += 32 * gn) {
         uint32_t mark = 0;
+        if (one_chunk && sc_have && !my_forced && sc_u > kthr) {
+          mark = sc_mark;
+          m = sc_u;
+        } else {
 #ifdef CAFE_DETAIL_CYCLES
-        long long pa0 = cafe_clock_ordered();
+          long long pa0 = cafe_clock_ordered();
 #endif
-        // (branch-free batches of eight loads, so that they are in flight
-        // together)
+          // (branch-free batches of eight loads, so that they are in flight
+          // together)
 #pragma unroll
-        for (int b = 0; b < 32; b += 8) {
-          if (r0 + b * gn >= nrows) break;
-          unsigned long long kk[8];
-#pragma unroll
-          for (int i = 0; i < 8; ++i) {
-            const int r = r0 + (b + i) * gn;
-            kk[i] = r < nrows ? D.row_key[r] : CAFE_KEY_NONE;
-          }
-          uint32_t fm = 0;  // rows stamped -1, visited whatever their key
-          if (my_forced) {
+          for (int b = 0; b < 32; b += 8) {
+            if (r0 + b * gn >= nrows) break;
+            unsigned long long kk[8];
 #pragma unroll
             for (int i = 0; i < 8; ++i) {
               const int r = r0 + (b + i) * gn;
-              fm |= (r < nrows && D.row_stamp[r] == -1) ? 1u << i : 0u;
+              kk[i] = r < nrows ? D.row_key[r] : CAFE_KEY_NONE;
+            }
+            uint32_t fm = 0;  // rows stamped -1, visited whatever their key
+            if (my_forced) {
+#pragma unroll
+              for (int i = 0; i < 8; ++i) {
+                const int r = r0 + (b + i) * gn;
+                fm |= (r < nrows && D.row_stamp[r] == -1) ? 1u << i : 0u;
+              }
+            }
+#pragma unroll
+            for (int i = 0; i < 8; ++i) {
+              // a visited row's key enters the minimum after its visit
+              if (kk[i] <= kthr || (fm >> i & 1u))
+                mark |= 1u << (b + i);
+              else
+                m = min(m, kk[i]);
             }
           }
-#pragma unroll
-          for (int i = 0; i < 8; ++i) {
-            // a visited row's key enters the minimum after its visit
-            if (kk[i] <= kthr || (fm >> i & 1u))
-              mark |= 1u << (b + i);
-            else
-              m = min(m, kk[i]);
+#ifdef CAFE_DETAIL_CYCLES
+          phase_a += cafe_clock_ordered() - pa0;
+          n_mark += __popc(mark);
+#endif
+          if (one_chunk) {
+            sc_have = true;
+            sc_mark = mark;
+            sc_u = m;
           }
         }
-#ifdef CAFE_DETAIL_CYCLES
-        phase_a += cafe_clock_ordered() - pa0;
-        n_mark += __popc(mark);
-#endif
         while (mark) {
           const int r = r0 + (__ffs(mark) - 1) * gn;
           mark &= mark - 1;
