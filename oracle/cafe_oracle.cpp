@@ -553,6 +553,7 @@ struct State {
   double DelT = 0, bmDX0 = 0, a1[6];
   // statistics
   long long n_events = 0, n_nuc = 0, max_na = 0, max_front = 0, n_steps = 0;
+  long long n_negdt = 0, n_clamp = 0;  // events with DtMin < 0; extents clamped at 0 by them
   int tf_tInd = 0;  // TempField::tInd, set at the start of each step (main1.C:64)
 };
 
@@ -1266,10 +1267,12 @@ static void update_voxels(State &S) {
       S.n_nuc++;
     } else {
       // growth of every mushy cell in the list (VoxelsCA.C:511-516)
+      if (DtMin < 0.0) S.n_negdt++;
       if (std::isfinite(DtMin)) {
         for (size_t f = 0; f < nfr; ++f) {
           int i1 = vs2ind[fr[f]];
           ExtA[i1] += vh[i1] * DtMin;
+          if (ExtA[i1] < 0.0) S.n_clamp++;
           ExtA[i1] = smax(ExtA[i1], 0.0);
         }
       } else {
@@ -1547,8 +1550,9 @@ void cafe_oracle_set_output(const char *dir, long every) {
 
 // Runs the whole main1.C time loop on deck `deck`. dump_stride: 0 = write only
 // the initial and final records, k > 0 = also every k-th step. max_steps > 0
-// stops early. stats (may be NULL) receives
-// {steps, events, nucleations, max active-list size, max frontier, nGrain, N}.
+// stops early. stats (may be NULL, else 10 entries) receives
+// {steps, events, nucleations, max active-list size, max frontier, nGrain, N,
+// loop nanoseconds, events with DtMin < 0, extents those clamped at 0}.
 int cafe_oracle_run(const char *deck, const char *dump_path, long max_steps, int dump_stride,
                     int libm_mode, double perturb_p, unsigned long long perturb_seed,
                     long long *stats) {
@@ -1610,6 +1614,8 @@ int cafe_oracle_run(const char *deck, const char *dump_path, long max_steps, int
     stats[5] = S.nGrain;
     stats[6] = S.N;
     stats[7] = (long long)((t1.tv_sec - t0.tv_sec) * 1000000000LL + (t1.tv_nsec - t0.tv_nsec));
+    stats[8] = S.n_negdt;
+    stats[9] = S.n_clamp;
   }
   return 0;
 }
@@ -1625,7 +1631,9 @@ struct cafe_oracle_window {
 // Runs `nsteps` loop iterations of `deck` starting from the given state (the
 // arrays have N = nx*ny*nz entries; centroid holds x,y,z per cell), without
 // the initial baseplate/layer construction. Wall seconds of the loop go to
-// *seconds. The final state is written back into the arrays (if non-NULL).
+// *seconds. The final state is written back into the arrays (if non-NULL);
+// stats (may be NULL, else 10 entries) as for cafe_oracle_run, without the
+// loop nanoseconds (entry 7).
 int cafe_oracle_run_window(const char *deck, const cafe_oracle_window *w, int32_t *gID, int32_t *vState,
                            double *ext, double *cen, int32_t *buildj, double *cth, long nsteps,
                            int libm_mode, double *seconds, long long *stats, int *ngrain_out) {
@@ -1700,6 +1708,8 @@ int cafe_oracle_run_window(const char *deck, const cafe_oracle_window *w, int32_
     stats[4] = S.max_front;
     stats[5] = S.nGrain;
     stats[6] = S.N;
+    stats[8] = S.n_negdt;
+    stats[9] = S.n_clamp;
   }
   if (ngrain_out) *ngrain_out = S.nGrain;
   std::memcpy(gID, S.gID.data(), S.N * sizeof(int32_t));

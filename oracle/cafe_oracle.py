@@ -58,7 +58,7 @@ def run_window(deck, info, state, ctheta, nsteps, libm=LIBM_CR):
     st = {k: np.array(v, copy=True) for k, v in state.items()}
     cth = np.ascontiguousarray(ctheta, np.float64)
     sec = ctypes.c_double(0)
-    stats = (ctypes.c_longlong * 8)()
+    stats = (ctypes.c_longlong * 10)()
     ng = ctypes.c_int(0)
     rc = f(str(deck).encode(), ctypes.byref(w), st["gID"].ctypes.data_as(i32p), st["vState"].ctypes.data_as(i32p),
            st["extents"].ctypes.data_as(f64p), st["centroid"].ctypes.data_as(f64p), st["buildj"].ctypes.data_as(i32p),
@@ -66,18 +66,21 @@ def run_window(deck, info, state, ctheta, nsteps, libm=LIBM_CR):
     if rc != 0:
         raise RuntimeError("oracle window run failed")
     keys = ("steps", "events", "nucleations", "max_active", "max_front", "nGrain", "ncell")
-    return st, sec.value, dict(zip(keys, list(stats)[:7]))
+    out = dict(zip(keys, list(stats)[:7]))
+    out["negative_dt"], out["clamped"] = stats[8], stats[9]
+    return st, sec.value, out
 
 
 def run(deck, dump_path="", max_steps=-1, dump_stride=1, libm=LIBM_GLIBC, perturb_p=0.0, perturb_seed=0):
     """Runs the main1.C loop on `deck`; returns a stats dict."""
-    st = (ctypes.c_longlong * 8)()
+    st = (ctypes.c_longlong * 10)()
     rc = load().cafe_oracle_run(str(deck).encode(), str(dump_path).encode(), max_steps, dump_stride, libm,
                                 perturb_p, perturb_seed, st)
     if rc != 0:
         raise RuntimeError("oracle run failed on %s" % deck)
-    keys = ("steps", "events", "nucleations", "max_active", "max_front", "nGrain", "ncell", "loop_ns")
-    return dict(zip(keys, list(st)[:8]))
+    keys = ("steps", "events", "nucleations", "max_active", "max_front", "nGrain", "ncell", "loop_ns",
+            "negative_dt", "clamped")
+    return dict(zip(keys, list(st)[:10]))
 
 
 def set_output(out_dir, every=1):

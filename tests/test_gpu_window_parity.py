@@ -4,8 +4,11 @@ The oracle cannot run config 1 from the start in test time, so the GPU state at
 a step (fields, grain table, laser and layer counters, genlayer engine state)
 is handed to the oracle, both advance the same number of steps, and the
 results must agree: integer fields bit-exact, floats within 1e-12 relative.
-Windows: in the first track (step 300) and at the benchmark's window (step
-2000, four tracks into the first layers).
+Windows: in the first track (step 300), around the run's first capture event
+with a negative time (steps 341-344: the event at step 343 shrinks the front's
+extents and clamps 11 of them at zero, VoxelsCA.C:511-516, which the keyed
+event loop handles by forcing exact evaluations) and at the benchmark's window
+(step 2000, four tracks into the first layers).
 """
 import os
 
@@ -21,17 +24,20 @@ C1 = os.path.join(ROOT, "amcafe_gb300", "decks", "c1.in")
 WINDOW = 6
 
 
-def _compare_window(sim, where):
+def _compare_window(sim, where, n=WINDOW):
     info = sim.info()
     st = sim.state()
     cth = sim.ctheta()
-    ost, _, ostats = orc.run_window(C1, info, st, cth, WINDOW, libm=orc.LIBM_CR)
-    for _ in range(WINDOW):
+    neg0 = sim.stats()["negative_dt"]
+    ost, _, ostats = orc.run_window(C1, info, st, cth, n, libm=orc.LIBM_CR)
+    for _ in range(n):
         sim.step()
     got = sim.state()
     compare_states(got, ost, where=where)
-    assert ostats["steps"] == WINDOW, ostats
+    assert ostats["steps"] == n, ostats
     assert sim.info()["nGrain"] == ostats["nGrain"], where
+    assert sim.stats()["negative_dt"] - neg0 == ostats["negative_dt"], where
+    return ostats
 
 
 def test_config1_windows_match_oracle():
@@ -42,7 +48,10 @@ def test_config1_windows_match_oracle():
     sim.begin()
     sim.run(300)
     _compare_window(sim, "config 1, steps 300-%d" % (300 + WINDOW))
-    sim.run(2000 - 300 - WINDOW)
+    sim.run(341 - 300 - WINDOW)
+    ostats = _compare_window(sim, "config 1, steps 341-344", n=3)
+    assert ostats["negative_dt"] >= 1 and ostats["clamped"] >= 1, ostats
+    sim.run(2000 - 344)
     _compare_window(sim, "config 1, steps 2000-%d" % (2000 + WINDOW))
     stats = sim.stats()
     assert stats["exact_scan_steps"] == 0
