@@ -412,7 +412,12 @@ def main():
     if not args.no_e2e and nvox <= E2E_REWIND_MAX:
         fd, ckpt = tempfile.mkstemp(suffix=".ckpt")
         os.close(fd)
-        sim.checkpoint(ckpt)
+        try:
+            sim.checkpoint(ckpt)
+        except Exception as exc:  # e.g. no room for the file: time the following steps instead
+            print("bench: no checkpoint for the end-to-end run (%s)" % exc, file=sys.stderr)
+            os.unlink(ckpt)
+            ckpt = None
     snapshot = None
     if rank == 0 and not args.no_cpu:
         snapshot = (info0, st_host, cth_host)
