@@ -1045,7 +1045,10 @@ __device__ __forceinline__ int cafe_find_slot(const CafeDev &D, int q, int targe
 // evaluated exactly. Between evaluations the key is within a small rounding
 // bound of the row's exact current value (or below it once a candidate was
 // captured by someone else), so the event needs exact times only for the rows
-// whose key lies within twice that bound of the smallest key. An extent that a
+// whose key lies within twice that bound of the smallest key. When the row's
+// best candidate is the one captured elsewhere, the key becomes row_key2, the
+// key of the row's next candidate at the same evaluation, which bounds the
+// row's exact value the same way. An extent that a
 // negative event may clamp at zero (VoxelsCA.C:515) breaks the bound; such rows
 // are stamped -1 and evaluated again. The growth is logged once per event and
 // replayed per row when the row is evaluated, and for every row at the end of
