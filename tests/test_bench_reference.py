@@ -1,0 +1,34 @@
+"""bench.py's reference arm on the CPU: the JSON line the driver reads.
+
+`--impl reference` times the CPU restatement of the reference (the oracle,
+single thread) on the workload's deck; its line carries the common keys plus
+`impl`, a `cpu_baseline` describing the run and an `e2e` object with no
+transfers. Config 0's small deck keeps the run to a few seconds.
+"""
+import json
+import os
+import subprocess
+import sys
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def test_reference_arm_json_line():
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--workload", "c0",
+                        "--steps", "2", "--warmup", "3"], capture_output=True, text=True, timeout=600, cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [l for l in r.stdout.splitlines() if l.startswith("{")]
+    assert len(lines) == 1, r.stdout
+    d = json.loads(lines[0])
+    for k in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better",
+              "scaling", "vs_baseline", "dtype", "data", "config", "cpu_baseline", "e2e"):
+        assert k in d, k
+    assert d["impl"] == "reference"
+    assert d["metric"] == "voxel-updates/s" and d["unit"] == "voxel-updates/s"
+    assert d["higher_is_better"] is True
+    assert d["value"] > 0 and d["steps"] == 5
+    assert d["config"]["workload"] == "c0"
+    cb = d["cpu_baseline"]
+    assert cb["value"] == d["value"] and cb["cores"] == 1 and cb["kind"] in ("port", "reference")
+    assert d["e2e"]["value"] == d["value"]
+    assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["d2h_bytes_per_step"] == 0
