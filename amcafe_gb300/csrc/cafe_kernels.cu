@@ -1453,9 +1453,16 @@ __device__ void cafe_select_keyed(const CafeDev &D, const CafeConsts &K, int ev,
 // select the best capture of event e+1 among the other rows. The winner of
 // e+1 is the better of that selection and the new row's own exact best
 // candidate: a row not evaluated by the selection has a key above the
-// threshold, so its exact time is above the selected one. Exact mode (the
-// reference's per-event scan of every row, also the fallback when the rows
-// stop sharing one velocity) evaluates every row at every event.
+// threshold, so its exact time is above the selected one. Per event: (1)
+// thread 0 settles the winner (its candidate carries the row and both cells)
+// with the draw made one event ahead and logs the growth; (2) thread 0 applies
+// the capture or nucleation, warp 1 updates the captured cell's neighbours and
+// their rows (row deaths, second-key promotions), thread 64 draws the next
+// event's uniform, and on a negative event the selecting threads flag the rows
+// whose extent may clamp; (3) the new-row fill beside the next selection; (4)
+// thread 0 merges the two. Exact mode (the reference's per-event scan of every
+// row, also the fallback when the rows stop sharing one velocity) evaluates
+// every row at every event.
 __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
     k_event_loop(CafeDev D, CafeConsts K, const CafeStepParams *__restrict__ Pp, long long max_events, int allow_fast) {
   const CafeStepParams P = *Pp;
