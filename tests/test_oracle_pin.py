@@ -19,7 +19,7 @@ import pytest
 import cafe_oracle as orc
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-DECKS = ["track_r0", "track_nuc", "layers_rot", "c0_small", "track_easm", "track_easm60", "odd_dims"]
+DECKS = ["track_r0", "track_nuc", "layers_rot", "c0_small", "track_easm", "track_easm60", "odd_dims", "track_p0"]
 
 
 def _digest(a):
