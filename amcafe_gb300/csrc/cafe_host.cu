@@ -128,6 +128,7 @@ int parse_deck(const char *path, GridH &g) {
     else if (key == "bph") ok = num(g.bpH);
     else if (key == "lrate") { ok = num(g.lrate); g.set_lrate = true; }
     else if (key == "outnl") ok = inum(g.outNL);
+    // ntsd only sets Utilities::nTTemp (Utilities.C:163), which nothing reads
     else if (key == "ntsd") { int dummy; ok = inum(dummy); }
     else if (key == "offset") ok = num(g.offset[0]) && num(g.offset[1]) && num(g.offset[2]);
     else if (key == "meltparam")
