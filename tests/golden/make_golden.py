@@ -70,7 +70,8 @@ def main(only=()):
 
 # Output of VoxelsCA::WriteToHDF1 (through the ADIOS2 shim's raw files) on
 # three decks: deck, every k-th output point (outint is 1 in these decks).
-OUTPUT_DECKS = [("track_r0", 10), ("track_nuc", 10), ("layers_rot", 40)]
+OUTPUT_DECKS = [("track_r0", 10), ("track_nuc", 10), ("layers_rot", 40), ("layers_out_nl0", 1),
+                ("layers_out_nl1", 1)]
 
 
 def output_digests():

@@ -2,7 +2,7 @@
 
 tests/golden/output_digests.npz holds the SHA-256 of every dataset file that
 the reference (oracle/_ref, built from AMCAFE's sources) wrote at the output
-points of three decks (tests/golden/make_golden.py). Here the same decks run
+points of its decks (tests/golden/make_golden.py). Here three of them run
 through the C ABI: cafe_sim_step calls SetBuild at each output point, and at
 every k-th step (the fixture's stride) and after the closing CleanLayer the
 datasets are written with cafe_sim_write_output. Every file must be
