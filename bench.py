@@ -30,6 +30,7 @@ initial state (the reference's own CPU code path; no GPU work).
 """
 import argparse
 import json
+import shutil
 import os
 import statistics
 import subprocess
@@ -300,6 +301,74 @@ def _final_digest(sim):
     return h.hexdigest()
 
 
+def _track_steps(deck):
+    """Loop iterations of a one-layer single-track deck: its Nsd laser points
+    (Grid.C:83) less the one the first UpdateLaser takes before the time loop
+    (main1.C:61); on the 64 decks of config 3 their sum equals the engine's
+    38,643 iterations."""
+    import math
+
+    g = {}
+    for line in open(deck):
+        f = line.split("#")[0].split()
+        if f:
+            g[f[0].lower()] = f[1:]
+    gs, v, dt = float(g["gridsize"][0]), float(g["bmv"][0]), float(g["bmdelt"][0])
+    return int(math.ceil(gs / (v * dt)))
+
+
+def run_reference_ensemble(args, ws, rank):
+    """Config 3 on the CPU restatement: one copy per host core (within the
+    memory cap), copy i running realisation i+1 from its deck for a bounded
+    sample; runs/s is the sum over copies of completed fraction / loop time."""
+    if rank != 0:
+        return 0
+    from amcafe_gb300.ensemble import make_decks
+
+    t_wall0 = time.time()
+    work = tempfile.mkdtemp(prefix="cafe_ens_ref_")
+    n = args.realisations
+    decks = make_decks(work, n=n, sides=(96, 192), host_seed=ENSEMBLE_HOST_SEED)
+    ncopy = _ref_copies(max(_deck_cells(d) for d in decks), getattr(args, "ref_copies", 0))
+    jobs = [(decks[i % n], -1, args.ref_seconds) for i in range(ncopy)]
+    if ncopy == 1:
+        res = [_ref_sample(jobs[0])]
+    else:
+        import multiprocessing as mp
+
+        with mp.get_context("spawn").Pool(ncopy) as pool:
+            res = pool.map(_ref_sample, jobs)
+    rates = [(r[0] / _track_steps(j[0])) / r[1] for r, j in zip(res, jobs) if r[1] > 0]
+    value = sum(rates) if rates else None
+    steps_done = sum(r[0] for r in res)
+    out = {
+        "impl": "reference",
+        "metric": "runs/s",
+        "value": value,
+        "unit": "runs/s",
+        "n_gpus": ws,
+        "steps": steps_done,
+        "warmup": 0,
+        "ms_per_step": 1e3 * sum(r[1] / max(1, r[0]) for r in res) / len(res),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic (seeded decks from amcafe_gb300.ensemble, host seed %d)" % ENSEMBLE_HOST_SEED,
+        "config": {"workload": "c3", "description": WORKLOADS["c3"][2], "realisations": n},
+        "cpu_baseline": {"value": value, "unit": "runs/s", "cores": ncopy, "kind": "port",
+                         "sample": "realisations 1..%d, one single-thread copy each at once (one per host core "
+                                   "within half the free memory), glibc libm, up to %.1f s loop time each "
+                                   "(initialisation excluded); runs/s = the copies' summed completed fraction / "
+                                   "time" % (ncopy, max(r[1] for r in res))},
+        "e2e": {"value": value, "unit": "runs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "wall_s": time.time() - t_wall0,
+    }
+    print(json.dumps(out))
+    shutil.rmtree(work, ignore_errors=True)
+    return 0
+
+
 def run_ensemble(args, ws, rank, local):
     """Config 3: runs/s of whole realisations (initialisation, the full loop
     and the closing CleanLayer), batched (cafe_batch_*) against the same
@@ -425,6 +494,8 @@ def main():
     args.warmup = max(3, args.warmup)
     ws, rank, local = dist_env()
     if args.workload == "c3":
+        if args.impl == "reference":
+            return run_reference_ensemble(args, ws, rank)
         return run_ensemble(args, ws, rank, local)
     if args.impl == "reference":
         return run_reference(args, ws, rank)
