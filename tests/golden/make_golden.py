@@ -25,7 +25,8 @@ REF = os.path.join(ROOT, "oracle", "_ref", "cafe_ref_dump")
 # *easm* run the EASM temperature (CAFE_REF_EASM=1: the reference's parser
 # cannot select it from a deck).
 DECKS = [("track_r0", -1, 1), ("track_nuc", -1, 1), ("layers_rot", -1, 5), ("c0_small", 160, 10),
-         ("track_easm", -1, 1), ("track_easm60", -1, 1), ("odd_dims", -1, 3), ("track_p0", -1, 1)]
+         ("track_easm", -1, 1), ("track_easm60", -1, 1), ("odd_dims", -1, 3), ("track_p0", -1, 1),
+         ("layers_easm", 260, 5)]
 
 
 def digest(a):

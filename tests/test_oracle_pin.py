@@ -6,7 +6,8 @@ make_golden.py). The oracle restatement with glibc libm must reproduce every
 dumped record: integer fields bit for bit (SHA-256), float fields to 1e-12
 relative (bit-exact on the machine that made the fixtures).
 The correctly-rounded-libm mode (the arithmetic the GPU uses) must reproduce
-the integer fields too on these decks. The two track_easm decks run the EASM
+the integer fields too on these decks (on two of them only for their first
+steps, see CR_LATE). The track_easm and layers_easm decks run the EASM
 temperature (TempField::EASM, Utilities.C), which the reference reaches only
 with the CAFE_REF_EASM switch of its driver (its parser cannot select it).
 """
@@ -19,7 +20,8 @@ import pytest
 import cafe_oracle as orc
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-DECKS = ["track_r0", "track_nuc", "layers_rot", "c0_small", "track_easm", "track_easm60", "odd_dims", "track_p0"]
+DECKS = ["track_r0", "track_nuc", "layers_rot", "c0_small", "track_easm", "track_easm60", "odd_dims", "track_p0",
+         "layers_easm"]
 
 
 def _digest(a):
@@ -65,11 +67,13 @@ def test_oracle_glibc_reproduces_reference(name, tmp_path):
     _check(name, orc.LIBM_GLIBC, tmp_path, check_floats=True)
 
 
-# odd_dims is not among these: with correctly rounded libm its extents differ
-# from the reference's in the last bits from step 4 on (glibc rounds some
-# capture-geometry result differently) and a capture decision flips at step 32;
-# test_correctly_rounded_libm_diverges_late_on_odd_dims records that.
-CR_DECKS = [d for d in DECKS if d != "odd_dims"]
+# odd_dims and layers_easm are not among these: with correctly rounded libm
+# their extents differ from the reference's in the last bits after a few steps
+# (glibc rounds some capture-geometry or EASM value differently) and a capture
+# decision flips later (steps 32 and 108); test_correctly_rounded_libm_diverges_late
+# records that.
+CR_LATE = {"odd_dims": 11, "layers_easm": 22}  # leading records whose integers agree
+CR_DECKS = [d for d in DECKS if d not in CR_LATE]
 
 
 @pytest.mark.parametrize("name", CR_DECKS)
@@ -77,17 +81,21 @@ def test_oracle_correctly_rounded_libm_keeps_reference_integers(name, tmp_path):
     _check(name, orc.LIBM_CR, tmp_path, check_floats=False)
 
 
-def test_correctly_rounded_libm_diverges_late_on_odd_dims(tmp_path):
+@pytest.mark.parametrize("name", sorted(CR_LATE))
+def test_correctly_rounded_libm_diverges_late(name, tmp_path):
     """The limit of the parity anchor: correctly rounded math reproduces the
     reference's grain IDs and states on odd_dims.in for its first 31 steps
-    (records 0-10 at stride 3), extents within 1e-14 relative, and differs
-    after a capture decision that glibc's rounding changes."""
-    g = np.load(os.path.join(HERE, "golden", "odd_dims.npz"))
+    (records 0-10 at stride 3) and on layers_easm.in for its first 105 steps
+    (records 0-21 at stride 5; its EASM temperatures differ in the last bits
+    from step 1 and its extents from step 9, within 2e-15 relative), and
+    differs after a capture decision that glibc's rounding changes (steps 32
+    and 108)."""
+    g = np.load(os.path.join(HERE, "golden", name + ".npz"))
     dump = str(tmp_path / "o.bin")
-    orc.run(os.path.join(HERE, "golden", "decks", "odd_dims.in"), dump, max_steps=int(g["nsteps"]),
+    orc.run(os.path.join(HERE, "golden", "decks", name + ".in"), dump, max_steps=int(g["nsteps"]),
             dump_stride=int(g["stride"]), libm=orc.LIBM_CR)
     recs = orc.read_dump(dump)
-    for j in range(11):
+    for j in range(CR_LATE[name]):
         for f in ("gID", "vState"):
             assert _digest(recs[j][f]) == str(g["sha_" + f][j]), (j, f)
     assert any(_digest(r["gID"]) != str(d) for r, d in zip(recs, g["sha_gID"]))
