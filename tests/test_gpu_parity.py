@@ -68,7 +68,7 @@ def run_and_compare(deck, nsteps, stride, tmp_path, event_scan=0):
 
 @pytest.mark.parametrize("deck,nsteps,stride", [
     ("track_r0.in", 0, 1), ("track_nuc.in", 0, 1), ("layers_rot.in", 0, 20), ("c0_small.in", 400, 40),
-    ("track_nuc_s7.in", 0, 1), ("track_nuc_ng.in", 0, 1), ("odd_dims.in", 0, 3)])
+    ("track_nuc_s7.in", 0, 1), ("track_nuc_ng.in", 0, 1), ("odd_dims.in", 0, 3), ("track_p0.in", 0, 1)])
 def test_gpu_matches_oracle(tmp_path, deck, nsteps, stride):
     """Default keyed event selection with lazily replayed growth."""
     worst, stats = run_and_compare(deck, nsteps, stride, tmp_path)
@@ -76,11 +76,13 @@ def test_gpu_matches_oracle(tmp_path, deck, nsteps, stride):
     print("%s: max float rel diff %g, %s" % (deck, worst, stats))
 
 
-@pytest.mark.parametrize("deck", ["track_easm.in", "track_easm60.in", "track_easm60_ng.in"])
-def test_gpu_easm_matches_oracle(tmp_path, deck):
+@pytest.mark.parametrize("deck,nsteps,stride", [("track_easm.in", 0, 1), ("track_easm60.in", 0, 1),
+                                                ("track_easm60_ng.in", 0, 1), ("layers_easm.in", 100, 10)])
+def test_gpu_easm_matches_oracle(tmp_path, deck, nsteps, stride):
     """EASM temperature (keyword easm): per-cell temperatures and velocities,
-    rows evaluated with the exact per-event scan."""
-    worst, stats = run_and_compare(deck, 0, 1, tmp_path)
+    rows evaluated with the exact per-event scan (layers_easm: the first 100
+    steps of three rotated layers)."""
+    worst, stats = run_and_compare(deck, nsteps, stride, tmp_path)
     assert stats["exact_scan_steps"] == stats["steps"]
     print("%s: max float rel diff %g, %s" % (deck, worst, stats))
 
@@ -91,3 +93,16 @@ def test_gpu_full_scan_matches_oracle(tmp_path, deck, nsteps, stride):
     worst, stats = run_and_compare(deck, nsteps, stride, tmp_path, event_scan=1)
     assert stats["exact_scan_steps"] == stats["steps"]
     print("%s full scan: max float rel diff %g, %s" % (deck, worst, stats))
+
+
+@pytest.mark.parametrize("deck,pattern,stride", [("track_nuc.in", 3, 1), ("layers_rot.in", 4, 20)])
+def test_gpu_scan_patterns_3_and_4(tmp_path, deck, pattern, stride):
+    """Scan patterns 3 and 4 order the laser points as 1 and 2 do
+    (TempField.C:34-50); the decks switched to them run as the oracle does."""
+    import re
+
+    src = open(os.path.join(DECKS, deck)).read()
+    p = tmp_path / ("p%d_%s" % (pattern, deck))
+    p.write_text(re.sub(r"(?mi)^patternID\s+\d+", "patternID %d" % pattern, src))
+    worst, stats = run_and_compare(str(p), 0, stride, tmp_path)
+    assert stats["exact_scan_steps"] == 0
