@@ -172,7 +172,9 @@ def hbm_peak():
 
 
 def committed_traffic(workload, phase):
-    """DRAM bytes per launch of `phase` from a committed ncu summary, or None."""
+    """A figure from the committed ncu summaries (profiles/traffic.json), or
+    None: under a phase's name its DRAM bytes per launch, under
+    "<phase>_fp64_issue_frac" its FP64 issue rate on the SM it runs on."""
     path = os.path.join(ROOT, "profiles", "traffic.json")
     try:
         d = json.load(open(path))
@@ -622,6 +624,11 @@ def main():
                     "phase": dom, "peak_source": peak_src,
                     "phase_steps": kp,
                     "step_achieved_GBs": step_bytes * k / (ms * 1e-3) / 1e9}
+        fp64 = committed_traffic(args.workload, dom + "_fp64_issue_frac")
+        if fp64 is not None:
+            # the serial loop runs on one SM: its FP64 issue rate there against
+            # that SM's peak (ncu, sm__inst_executed_pipe_fp64, profiles/)
+            roofline["sm_fp64_issue_frac_ncu"] = fp64
 
     cpu = None
     if snapshot is not None:
