@@ -19,7 +19,9 @@ LIB_DIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(LIB_DIR, "libcafe_gpu.so")
 ORACLE_DIR = os.path.join(ROOT, "oracle")
 ORACLE_LIB = os.path.join(ORACLE_DIR, "_build", "libcafe_oracle.so")
-REF_SRC = os.environ.get("CAFE_REF_SRC", "/root/reference/src/src-mpi")
+# the reference checkout's src/src-mpi: CAFE_REF_SRC, else a checkout named
+# "reference" beside the repository
+REF_SRC = os.environ.get("CAFE_REF_SRC") or os.path.normpath(os.path.join(ROOT, "..", "reference", "src", "src-mpi"))
 
 NVCC_FLAGS = ["-std=c++17", "-O3", "--fmad=false", "-lineinfo",
               "-gencode", "arch=compute_103a,code=sm_103a",

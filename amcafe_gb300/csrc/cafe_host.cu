@@ -392,6 +392,7 @@ struct cafe_sim {
   std::default_random_engine bp_generator;  // BasePlate.h:28 (default seed)
   std::default_random_engine genlayer;      // VoxelsCA.h:129
   bool initialized = false, begun = false, done = false;
+  bool closed = false;  // the closing CleanLayer of main1.C:95 has been applied
   long long steps = 0;
   // device
   CafeConsts K;
@@ -1360,15 +1361,23 @@ int cafe_sim_clean_layer(cafe_sim *s) {
   int rc = read_ctr(s, CTR_NGRAIN, &s->nGrain);
   if (rc) return rc;
   int ng = s->nGrain;
-  int32_t *cnt, *newid;
-  double *cth2, *rot2;
-  std::vector<void *> tmp;
+  int32_t *cnt = nullptr, *newid = nullptr;
+  double *cth2 = nullptr, *rot2 = nullptr;
+  // every temporary is freed on every return; the new grain tables leave the
+  // list only once the handle owns them
+  struct Temps {
+    cafe_sim *s;
+    std::vector<void *> p;
+    ~Temps() { free_tmp(s, p); }
+  } tmp{s, {}};
   CUDA_TRY(cudaMalloc((void **)&cnt, std::max(1, ng) * sizeof(int32_t)));
-  tmp.push_back(cnt);
+  tmp.p.push_back(cnt);
   CUDA_TRY(cudaMalloc((void **)&newid, std::max(1, ng) * sizeof(int32_t)));
-  tmp.push_back(newid);
+  tmp.p.push_back(newid);
   CUDA_TRY(cudaMalloc((void **)&cth2, (size_t)s->D.grain_cap * 4 * sizeof(double)));
+  tmp.p.push_back(cth2);
   CUDA_TRY(cudaMalloc((void **)&rot2, (size_t)s->D.grain_cap * 9 * sizeof(double)));
+  tmp.p.push_back(rot2);
   CUDA_TRY(cudaMemsetAsync(cnt, 0, std::max(1, ng) * sizeof(int32_t), s->stream));
   LAUNCHED(CAFE_PH_LAYER, 3);
   k_grain_count<<<grid_blocks(s->K.N, 256, s), 256, 0, s->stream>>>(s->D, s->K, cnt);
@@ -1381,12 +1390,13 @@ int cafe_sim_clean_layer(cafe_sim *s) {
     if (p == (void *)s->D.cth) { cudaFree(p); p = (void *)cth2; }
     else if (p == (void *)s->D.rot) { cudaFree(p); p = (void *)rot2; }
   }
+  tmp.p.resize(2);  // cth2 and rot2 now belong to the handle
   s->D.cth = cth2;
   s->D.rot = rot2;
   s->nGrain = nnew;
   s->h_pinned[2] = nnew;
   CUDA_TRY(cudaMemcpyAsync(s->D.ctr + CTR_NGRAIN, s->h_pinned + 2, sizeof(int), cudaMemcpyHostToDevice, s->stream));
-  free_tmp(s, tmp);
+  free_tmp(s, tmp.p);
   return sim_sync(s);
 }
 
@@ -1437,7 +1447,10 @@ int cafe_sim_run(cafe_sim *s, long long max_steps, long long *steps_done) {
     if ((rc = cafe_sim_step(s, &done))) return rc;
     ++n;
   }
-  if (done && (rc = cafe_sim_clean_layer(s))) return rc;
+  if (done && !s->closed) {  // main1.C:95 runs once, after the loop
+    if ((rc = cafe_sim_clean_layer(s))) return rc;
+    s->closed = true;
+  }
   if (steps_done) *steps_done = n;
   return sim_sync(s);
 }
@@ -2102,6 +2115,7 @@ int cafe_sim_restore(cafe_sim *s, const char *path) {
   CUDA_TRY(cudaMemsetAsync(D.ctr + CTR_NLIQ, 0, sizeof(int), st));
   s->steps = h.steps;
   s->done = h.done != 0;
+  s->closed = false;
   s->output_due = h.output_due != 0;
   s->have_P = false;
   s->full_k2 = true;          // the liquid list is rebuilt by a dense pass

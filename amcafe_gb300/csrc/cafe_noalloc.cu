@@ -24,7 +24,8 @@
 
 // Largest grain count a call accepts; the scratch holds, per grain, a volume
 // count (int32), the new grain number (int32) and the compacted orientation
-// (4 doubles), plus one int32 for the new grain count.
+// (4 doubles), plus two int32 words: the new grain count and an input-error
+// flag (set when a cell holds a grain ID outside 0..ngrain).
 #define NOALLOC_SCRATCH_INTS (2 * CAFE_NOALLOC_MAX_GRAINS + 64)
 #define NOALLOC_SCRATCH_BYTES (NOALLOC_SCRATCH_INTS * 4 + 4 * 8 * (size_t)CAFE_NOALLOC_MAX_GRAINS)
 
@@ -41,7 +42,8 @@ std::mutex g_scratch_mu;
 struct ScratchView {
   int32_t *count;   // [CAFE_NOALLOC_MAX_GRAINS] cells per grain
   int32_t *newid;   // [CAFE_NOALLOC_MAX_GRAINS] new 1-based number, 0 = dropped
-  int32_t *nnew;    // [1] grains kept
+  int32_t *nnew;    // [2] grains kept, then the input-error flag
+  int32_t *bad;     // == nnew + 1
   double *cth;      // [4 * CAFE_NOALLOC_MAX_GRAINS] compacted orientations
 };
 
@@ -51,23 +53,32 @@ ScratchView view_of(void *base) {
   v.count = ip;
   v.newid = ip + CAFE_NOALLOC_MAX_GRAINS;
   v.nnew = ip + 2 * CAFE_NOALLOC_MAX_GRAINS;
+  v.bad = v.nnew + 1;
   v.cth = (double *)((unsigned char *)base + (size_t)NOALLOC_SCRATCH_INTS * 4);
   return v;
 }
 
-__global__ void na_count(const int32_t *gid, long long ncell, int32_t *count) {
+// The caller's gid[] is not trusted: a grain ID outside 0..ngrain would index
+// outside the caller's grain table (and past the scratch), so such a cell is
+// skipped and the call's error flag is raised; the later kernels then change
+// nothing.
+__global__ void na_count(const int32_t *gid, long long ncell, int ngrain, int32_t *count, int32_t *bad) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < ncell;
        i += (long long)gridDim.x * blockDim.x) {
     int g = gid[i];
-    if (g > 0) atomicAdd(&count[g - 1], 1);
+    if (g > 0 && g <= ngrain)
+      atomicAdd(&count[g - 1], 1);
+    else if (g != 0)
+      *bad = 1;
   }
 }
 
 // One block: grains with cells keep their order and are renumbered 1..k;
 // their orientations are packed into the scratch.
-__global__ void na_renumber(const int32_t *count, int32_t *newid, int32_t *nnew, const double *cth_in,
-                            double *cth_out, int ngrain) {
+__global__ void na_renumber(const int32_t *count, int32_t *newid, int32_t *nnew, const int32_t *bad,
+                            const double *cth_in, double *cth_out, int ngrain) {
   __shared__ int part[1024];
+  if (*bad) return;
   int per = (ngrain + blockDim.x - 1) / blockDim.x;
   int b0 = threadIdx.x * per, b1 = min(b0 + per, ngrain);
   int s = 0;
@@ -96,15 +107,17 @@ __global__ void na_renumber(const int32_t *count, int32_t *newid, int32_t *nnew,
   }
 }
 
-__global__ void na_remap(int32_t *gid, long long ncell, const int32_t *newid) {
+__global__ void na_remap(int32_t *gid, long long ncell, int ngrain, const int32_t *newid, const int32_t *bad) {
+  if (*bad) return;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < ncell;
        i += (long long)gridDim.x * blockDim.x) {
     int g = gid[i];
-    if (g != 0) gid[i] = newid[g - 1];
+    if (g > 0 && g <= ngrain) gid[i] = newid[g - 1];
   }
 }
 
-__global__ void na_copy_back(const int32_t *nnew, const double *cth_in, double *cth_out) {
+__global__ void na_copy_back(const int32_t *nnew, const int32_t *bad, const double *cth_in, double *cth_out) {
+  if (*bad) return;
   long long n = 4LL * *nnew;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
     cth_out[i] = cth_in[i];
@@ -150,30 +163,52 @@ extern "C" int cafe_clean_layer_noalloc(int32_t *gid, long long ncell, double *c
   int nsm = 1;
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   int blocks = nsm * 8;
+  // an error left by the caller's own earlier work is not this call's failure
+  (void)cudaGetLastError();
   if (ngrain > 0) {
     if (cudaMemsetAsync(v.count, 0, (size_t)ngrain * sizeof(int32_t), st) != cudaSuccess) {
       cafe_internal_set_error("cafe_clean_layer_noalloc: clearing the scratch failed");
       return CAFE_E_CUDA;
     }
   }
-  if (cudaMemsetAsync(v.nnew, 0, sizeof(int32_t), st) != cudaSuccess) {
+  // the grain count and the input-error flag start at zero
+  if (cudaMemsetAsync(v.nnew, 0, 2 * sizeof(int32_t), st) != cudaSuccess) {
     cafe_internal_set_error("cafe_clean_layer_noalloc: clearing the scratch failed");
     return CAFE_E_CUDA;
   }
+  cudaError_t e = cudaSuccess;
   if (ngrain > 0) {
-    na_count<<<blocks, 256, 0, st>>>(gid, ncell, v.count);
-    na_renumber<<<1, 1024, 0, st>>>(v.count, v.newid, v.nnew, ctheta, v.cth, ngrain);
-    na_remap<<<blocks, 256, 0, st>>>(gid, ncell, v.newid);
-    na_copy_back<<<blocks, 256, 0, st>>>(v.nnew, v.cth, ctheta);
+    na_count<<<blocks, 256, 0, st>>>(gid, ncell, ngrain, v.count, v.bad);
+    e = cudaGetLastError();
+    if (e == cudaSuccess) {
+      na_renumber<<<1, 1024, 0, st>>>(v.count, v.newid, v.nnew, v.bad, ctheta, v.cth, ngrain);
+      e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) {
+      na_remap<<<blocks, 256, 0, st>>>(gid, ncell, ngrain, v.newid, v.bad);
+      e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) {
+      na_copy_back<<<blocks, 256, 0, st>>>(v.nnew, v.bad, v.cth, ctheta);
+      e = cudaGetLastError();
+    }
+  } else if (ncell > 0) {
+    // no grain table: every cell must be 0
+    na_count<<<blocks, 256, 0, st>>>(gid, ncell, 0, v.count, v.bad);
+    e = cudaGetLastError();
   }
-  int32_t n = 0;
-  cudaError_t e = cudaGetLastError();
-  if (e == cudaSuccess) e = cudaMemcpyAsync(&n, v.nnew, sizeof(int32_t), cudaMemcpyDeviceToHost, st);
+  int32_t res[2] = {0, 0};
+  if (e == cudaSuccess) e = cudaMemcpyAsync(res, v.nnew, sizeof(res), cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) {
     cafe_internal_set_error(cudaGetErrorString(e));
     return CAFE_E_CUDA;
   }
-  *ngrain_out = n;
+  if (res[1]) {
+    cafe_internal_set_error("cafe_clean_layer_noalloc: gid holds a grain ID outside 0..ngrain; "
+                            "gid and ctheta were left unchanged");
+    return CAFE_E_ARG;
+  }
+  *ngrain_out = res[0];
   return CAFE_OK;
 }

@@ -259,10 +259,13 @@ void cafe_batch_destroy(cafe_batch *b);
  * no cudaMalloc/cudaFree: its scratch is one file-scope device array sized for
  * CAFE_NOALLOC_MAX_GRAINS grains (about 10.5 MB, held by every GPU that loads
  * the library until exit); larger ngrain is rejected with CAFE_E_CAPACITY. The
- * first call on a device looks up that array's device address, so make the
- * first call outside any stream capture. All calls share the scratch: calls
- * whose GPU work overlaps race and must be serialised by the caller. The call
- * waits for its own work before returning. */
+ * first call on a device looks up that array's device address. Every call
+ * ends by synchronising `stream`, so no call may be made while that stream is
+ * being captured into a graph. All calls share the scratch: calls whose GPU
+ * work overlaps race and must be serialised by the caller. gid[] is checked:
+ * a grain ID outside 0..ngrain makes the call return CAFE_E_ARG with gid and
+ * ctheta unchanged. After a CAFE_E_CUDA return the contents of gid and ctheta
+ * are undefined. */
 #define CAFE_NOALLOC_MAX_GRAINS (1 << 18)
 int cafe_clean_layer_noalloc(int32_t *gid, long long ncell, double *ctheta, int ngrain,
                              int *ngrain_out, void *stream);

@@ -73,3 +73,34 @@ def test_noalloc_rejects_oversized_grain_table():
                                       (1 << 18) + 1, ctypes.byref(out), None)
     assert rc == 3  # CAFE_E_CAPACITY
     assert b"CAFE_NOALLOC_MAX_GRAINS" in lib.cafe_last_error()
+
+
+def test_noalloc_rejects_grain_ids_outside_the_table():
+    """A grain ID above ngrain or below zero would index outside the caller's
+    grain table; the call must refuse it and change neither array."""
+    import torch
+
+    from amcafe_gb300._native import load
+
+    lib = load()
+    ngrain = 3
+    gid_host = np.array([1, 2, 0, ngrain + 1, 3, -1, 2, 1], dtype=np.int32)
+    cth_host = np.arange(4 * ngrain, dtype=np.float64) + 0.5
+    gid = torch.from_numpy(gid_host.copy()).cuda()
+    cth = torch.from_numpy(cth_host.copy()).cuda()
+    out = ctypes.c_int(-1)
+    torch.cuda.synchronize()
+    rc = lib.cafe_clean_layer_noalloc(ctypes.c_void_p(gid.data_ptr()), gid.numel(), ctypes.c_void_p(cth.data_ptr()),
+                                      ngrain, ctypes.byref(out), None)
+    assert rc == 1  # CAFE_E_ARG
+    assert b"outside 0..ngrain" in lib.cafe_last_error()
+    assert out.value == -1
+    assert np.array_equal(gid.cpu().numpy(), gid_host)
+    assert np.array_equal(cth.cpu().numpy(), cth_host)
+    # a valid call right after it still gives the handle-free renumbering
+    gid_ok = torch.from_numpy(np.array([0, 3, 3, 1, 0, 1], dtype=np.int32)).cuda()
+    check = lib.cafe_clean_layer_noalloc(ctypes.c_void_p(gid_ok.data_ptr()), gid_ok.numel(),
+                                         ctypes.c_void_p(cth.data_ptr()), ngrain, ctypes.byref(out), None)
+    assert check == 0 and out.value == 2
+    assert np.array_equal(gid_ok.cpu().numpy(), np.array([0, 2, 2, 1, 0, 1], dtype=np.int32))
+    assert np.array_equal(cth.cpu().numpy()[:8], np.concatenate([cth_host[0:4], cth_host[8:12]]))
