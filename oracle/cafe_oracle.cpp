@@ -1538,6 +1538,11 @@ static double g_max_seconds = 0.0;
 extern "C" {
 
 void cafe_oracle_set_budget(double seconds) { g_max_seconds = seconds; }
+// 0: cafe_oracle_run_window leaves its input arrays untouched (they may be
+// read-only mappings shared by several processes); 1 (default): the state
+// reached is copied back into them.
+static int g_window_writeback = 1;
+void cafe_oracle_set_window_writeback(int on) { g_window_writeback = on != 0; }
 
 // Output of the following cafe_oracle_run calls: the datasets of
 // VoxelsCA::WriteToHDF1 as raw files <dir>/out<tInd>.h5.<name>.bin at every
@@ -1712,6 +1717,7 @@ int cafe_oracle_run_window(const char *deck, const cafe_oracle_window *w, int32_
     stats[9] = S.n_clamp;
   }
   if (ngrain_out) *ngrain_out = S.nGrain;
+  if (!g_window_writeback) return 0;
   std::memcpy(gID, S.gID.data(), S.N * sizeof(int32_t));
   std::memcpy(vState, S.vState.data(), S.N * sizeof(int32_t));
   std::memcpy(buildj, S.buildj.data(), S.N * sizeof(int32_t));

@@ -42,20 +42,27 @@ class Window(ctypes.Structure):
                 ("ngrain", ctypes.c_int)]
 
 
-def run_window(deck, info, state, ctheta, nsteps, libm=LIBM_CR):
+def run_window(deck, info, state, ctheta, nsteps, libm=LIBM_CR, copy=True):
     """Resumes the loop from a GPU state (info from Simulation.info(), state
     from Simulation.state()); returns (new_state, seconds, stats). The arrays
-    in `state` are copied, not modified."""
+    in `state` are copied, not modified. With copy=False the arrays are passed
+    as they are (they may be read-only memory maps) and new_state is None: the
+    run is only timed and counted."""
     import numpy as np
 
     lib = load()
+    lib.cafe_oracle_set_window_writeback.argtypes = [ctypes.c_int]
+    lib.cafe_oracle_set_window_writeback(1 if copy else 0)
     f = lib.cafe_oracle_run_window
     i32p, f64p = ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_double)
     f.argtypes = [ctypes.c_char_p, ctypes.POINTER(Window), i32p, i32p, f64p, f64p, i32p, f64p, ctypes.c_long,
                   ctypes.c_int, f64p, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_int)]
     w = Window(info["isp"], info["inewscanflg"], info["inewlayerflg"], info["indlayer"], info["ilaserLoc"],
                info["tInd"], info["time"], info["gth"], info["genlayer_state"], info["nGrain"])
-    st = {k: np.array(v, copy=True) for k, v in state.items()}
+    if copy:
+        st = {k: np.array(v, copy=True) for k, v in state.items()}
+    else:
+        st = {k: np.ascontiguousarray(v) for k, v in state.items()}
     cth = np.ascontiguousarray(ctheta, np.float64)
     sec = ctypes.c_double(0)
     stats = (ctypes.c_longlong * 10)()
@@ -63,12 +70,13 @@ def run_window(deck, info, state, ctheta, nsteps, libm=LIBM_CR):
     rc = f(str(deck).encode(), ctypes.byref(w), st["gID"].ctypes.data_as(i32p), st["vState"].ctypes.data_as(i32p),
            st["extents"].ctypes.data_as(f64p), st["centroid"].ctypes.data_as(f64p), st["buildj"].ctypes.data_as(i32p),
            cth.ctypes.data_as(f64p), int(nsteps), libm, ctypes.byref(sec), stats, ctypes.byref(ng))
+    lib.cafe_oracle_set_window_writeback(1)
     if rc != 0:
         raise RuntimeError("oracle window run failed")
     keys = ("steps", "events", "nucleations", "max_active", "max_front", "nGrain", "ncell")
     out = dict(zip(keys, list(stats)[:7]))
     out["negative_dt"], out["clamped"] = stats[8], stats[9]
-    return st, sec.value, out
+    return (st if copy else None), sec.value, out
 
 
 def run(deck, dump_path="", max_steps=-1, dump_stride=1, libm=LIBM_GLIBC, perturb_p=0.0, perturb_seed=0):

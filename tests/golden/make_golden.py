@@ -6,6 +6,8 @@ dumped record, SHA-256 digests of the integer fields and sums of the float
 fields, plus the complete arrays of the last record. Needs the reference
 checkout (to build oracle/_ref); run from the repository root:
     make -C oracle ref && python tests/golden/make_golden.py [deck ...]
+The *_crlibm.npz fixtures come from the same driver linked with the engine's
+libm routing (oracle/_ref/cafe_ref_dump_cr).
 """
 import hashlib
 import os
@@ -21,12 +23,21 @@ sys.path.insert(0, os.path.join(ROOT, "oracle"))
 from cafe_dump import read_dump  # noqa: E402
 
 REF = os.path.join(ROOT, "oracle", "_ref", "cafe_ref_dump")
+# the reference with its libm calls routed as the engine evaluates them
+# (oracle/ref_shims/cr_route.cpp): correctly rounded in the capture geometry,
+# orientation sampling and EASM, glibc elsewhere -> <deck>_crlibm.npz
+REF_CR = os.path.join(ROOT, "oracle", "_ref", "cafe_ref_dump_cr")
 # deck, max steps (-1 = whole run), keep every k-th record. Decks named
 # *easm* run the EASM temperature (CAFE_REF_EASM=1: the reference's parser
 # cannot select it from a deck).
 DECKS = [("track_r0", -1, 1), ("track_nuc", -1, 1), ("layers_rot", -1, 5), ("c0_small", 160, 10),
          ("track_easm", -1, 1), ("track_easm60", -1, 1), ("odd_dims", -1, 3), ("track_p0", -1, 1),
          ("layers_easm", 260, 5)]
+
+
+# decks whose grain IDs under glibc's libm differ from those under correctly
+# rounded libm (a capture decision flips at steps 32 and 108)
+CR_DECKS = [("odd_dims", -1, 3), ("layers_easm", 260, 5)]
 
 
 def digest(a):
@@ -48,25 +59,27 @@ def summarize(recs, stride):
     return out
 
 
-def main(only=()):
-    if not os.path.exists(REF):
+def main(only=(), cr=False):
+    ref = REF_CR if cr else REF
+    if not os.path.exists(ref):
         sys.exit("build the reference first: make -C oracle ref")
-    for name, nsteps, stride in DECKS:
+    for name, nsteps, stride in (CR_DECKS if cr else DECKS):
         if only and name not in only:
             continue
         deck = os.path.join(HERE, "decks", name + ".in")
         env = dict(os.environ, CAFE_REF_EASM="1" if "easm" in name else "0")
         with tempfile.TemporaryDirectory() as td:
             dump = os.path.join(td, "ref.bin")
-            cmd = [REF, deck, dump] + ([str(nsteps)] if nsteps > 0 else [])
+            cmd = [ref, deck, dump] + ([str(nsteps)] if nsteps > 0 else [])
             subprocess.run(cmd, check=True, stdout=subprocess.DEVNULL, env=env)
             recs = read_dump(dump)
         data = summarize(recs, stride)
         data["nsteps"] = np.array(nsteps)
         data["stride"] = np.array(stride)
         data["nrec"] = np.array(len(recs))
-        np.savez_compressed(os.path.join(HERE, name + ".npz"), **data)
-        print(name, len(recs), "records")
+        out = name + ("_crlibm" if cr else "") + ".npz"
+        np.savez_compressed(os.path.join(HERE, out), **data)
+        print(out, len(recs), "records")
 
 
 # Output of VoxelsCA::WriteToHDF1 (through the ADIOS2 shim's raw files) on
@@ -96,7 +109,9 @@ def output_digests():
 
 
 if __name__ == "__main__":
-    # optional arguments: deck names to regenerate (default: all, and the output digests)
+    # optional arguments: deck names to regenerate (default: all, the
+    # routed-libm fixtures and the output digests)
     main(tuple(sys.argv[1:]))
+    main(tuple(sys.argv[1:]), cr=True)
     if len(sys.argv) == 1:
         output_digests()

@@ -2,8 +2,9 @@
 
 tests/golden/output_digests.npz holds the SHA-256 of every dataset file that
 the reference (oracle/_ref, built from AMCAFE's sources) wrote at the output
-points of its decks (tests/golden/make_golden.py). Here three of them run
-through the C ABI: cafe_sim_step calls SetBuild at each output point, and at
+points of its decks (tests/golden/make_golden.py). Here all five run through
+the C ABI (two of them, layers_out_nl0/1, write every 20th step, and at each
+layer change only when outnl is 0, main1.C:77-84): cafe_sim_step calls SetBuild at each output point, and at
 every k-th step (the fixture's stride) and after the closing CleanLayer the
 datasets are written with cafe_sim_write_output. Every file must be
 byte-identical to the reference's: gID, vState, Build, the float temperature,
@@ -47,7 +48,7 @@ def _run_deck(name, every, out):
     return sim, written
 
 
-@pytest.mark.parametrize("name", ["track_r0", "track_nuc", "layers_rot"])
+@pytest.mark.parametrize("name", ["track_r0", "track_nuc", "layers_rot", "layers_out_nl0", "layers_out_nl1"])
 def test_output_files_match_reference(name, tmp_path):
     d = np.load(os.path.join(HERE, "golden", "output_digests.npz"))
     every = int(d[name + "/every"])

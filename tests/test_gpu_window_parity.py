@@ -57,3 +57,37 @@ def test_config1_windows_match_oracle():
     assert stats["exact_scan_steps"] == 0
     assert stats["events"] > 0 and stats["nucleations"] > 0, stats
     sim.close()
+
+
+def test_config1_window_across_the_first_layer_change():
+    """The oracle and the GPU both step through config 1's first layer change
+    (UpdateLaser wraps to the next layer, CleanLayer renumbers the grains,
+    AddLayer1 draws the new layer's Voronoi sites and orientations from
+    genlayer, main1.C:75-88) from the same state a few steps before it."""
+    from amcafe_gb300 import Simulation
+
+    chunk = 10
+    sim = Simulation(C1, device=0)
+    sim.InitializeVoxels()
+    sim.begin()
+    layer0 = sim.info()["indlayer"]
+    done = 0
+    while sim.info()["indlayer"] == layer0:
+        assert done < 40000, "no layer change in config 1's first 40,000 steps"
+        sim.run(chunk)
+        done += chunk
+    sim.close()
+    # the change happened within steps done-chunk+1 .. done
+    sim = Simulation(C1, device=0)
+    sim.InitializeVoxels()
+    sim.begin()
+    start = done - chunk - 2
+    sim.run(start)
+    assert sim.info()["indlayer"] == layer0
+    ng0 = sim.info()["nGrain"]
+    _compare_window(sim, "config 1, steps %d-%d (first layer change)" % (start + 1, start + chunk + 4),
+                    n=chunk + 4)
+    info = sim.info()
+    assert info["indlayer"] == layer0 + 1
+    assert info["nGrain"] != ng0
+    sim.close()

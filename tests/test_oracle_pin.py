@@ -33,8 +33,8 @@ def _rel(a, b):
     return 0.0 if a == b else abs(a - b) / max(abs(b), 1e-300)
 
 
-def _check(name, libm, tmp_path, check_floats, deck=None):
-    g = np.load(os.path.join(HERE, "golden", name + ".npz"))
+def _check(name, libm, tmp_path, check_floats, deck=None, fixture=None):
+    g = np.load(os.path.join(HERE, "golden", (fixture or name) + ".npz"))
     nsteps, stride = int(g["nsteps"]), int(g["stride"])
     dump = str(tmp_path / (name + ".bin"))
     orc.run(deck or os.path.join(HERE, "golden", "decks", name + ".in"), dump, max_steps=nsteps, dump_stride=stride,
@@ -99,6 +99,18 @@ def test_correctly_rounded_libm_diverges_late(name, tmp_path):
         for f in ("gID", "vState"):
             assert _digest(recs[j][f]) == str(g["sha_" + f][j]), (j, f)
     assert any(_digest(r["gID"]) != str(d) for r, d in zip(recs, g["sha_gID"]))
+
+
+@pytest.mark.parametrize("name", sorted(CR_LATE))
+def test_oracle_correctly_rounded_reproduces_reference_with_routed_libm(name, tmp_path):
+    """On the two decks where glibc's rounding changes a capture decision, the
+    reference's own code linked with the engine's libm routing (correctly
+    rounded inside UpdateVoxels and EASM, glibc elsewhere;
+    oracle/ref_shims/cr_route.cpp) produced tests/golden/<deck>_crlibm.npz.
+    The correctly rounded oracle reproduces every record of it, floats
+    included, to the end of the run: the restatement and the reference differ
+    in nothing but libm's last bits."""
+    _check(name, orc.LIBM_CR, tmp_path, check_floats=True, fixture=name + "_crlibm")
 
 
 @pytest.mark.parametrize("libm", [orc.LIBM_GLIBC, orc.LIBM_CR])
