@@ -22,7 +22,8 @@ EXPORTS = (
     "cafe_sim_set_build", "cafe_sim_download_build", "cafe_sim_download_output", "cafe_sim_write_output",
     "cafe_batch_create", "cafe_batch_run", "cafe_batch_size", "cafe_batch_sim", "cafe_batch_finished",
     "cafe_batch_destroy", "cafe_sim_checkpoint", "cafe_sim_restore", "cafe_sim_set_growth_log",
-    "cafe_sim_growth_log_count", "cafe_adjoint_pool", "cafe_adjoint_growth",
+    "cafe_sim_growth_log_count", "cafe_adjoint_pool", "cafe_adjoint_growth", "cafe_sim_grid",
+    "cafe_generate_samples",
 )
 PHASES = ("melt", "classify", "gather", "events", "writeback", "layer")
 NPHASE = 8
@@ -31,6 +32,19 @@ NPHASE = 8
 class CafeOptions(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int), ("active_capacity", ctypes.c_longlong),
                 ("grain_capacity", ctypes.c_longlong), ("event_scan", ctypes.c_int)]
+
+
+class CafeGrid(ctypes.Structure):
+    _fields_ = [("nX", ctypes.c_int * 3), ("dX", ctypes.c_double * 3), ("LX", ctypes.c_double * 3),
+                ("offset", ctypes.c_double * 3), ("meltparam", ctypes.c_double * 4), ("gbox", ctypes.c_double * 4),
+                ("gsize", ctypes.c_double * 2)] + [
+        (n, ctypes.c_double) for n in ("bmV", "bmP", "bmDelT", "bhatch", "tL", "tS", "T0", "layerT", "bpH", "mu",
+                                       "lrate", "rNmax", "Avel", "nvel", "gth0", "gth", "time", "DelT")] + [
+        (n, ctypes.c_int) for n in ("outint", "patternID", "outNL", "EASM_Flag", "nZlayer", "Nzhg", "Nsd", "Ntd",
+                                    "NpT", "isp", "inewscanflg", "inewlayerflg", "indlayer", "ilaserLoc", "tInd",
+                                    "tf_tInd", "Nzh", "nlayerTot", "seed", "tmodel")] + [
+        ("ros_eta", ctypes.c_double), ("ros_k", ctypes.c_double), ("ros_alpha", ctypes.c_double),
+        ("laser", ctypes.c_double * 3), ("dirp", ctypes.c_double)]
 
 
 class CafeInfo(ctypes.Structure):
@@ -91,6 +105,8 @@ def load():
         "cafe_sim_run": (I, [P, LL, ctypes.POINTER(LL)]),
         "cafe_sim_synchronize": (I, [P]),
         "cafe_sim_info": (I, [P, ctypes.POINTER(CafeInfo)]),
+        "cafe_sim_grid": (I, [P, ctypes.POINTER(CafeGrid)]),
+        "cafe_generate_samples": (I, [I, ctypes.c_uint, P]),
         "cafe_sim_stats": (I, [P, ctypes.POINTER(CafeStats)]),
         "cafe_sim_download_state": (I, [P, i32p, i32p, f64p, f64p, i32p]),
         "cafe_sim_download_temperature": (I, [P, f64p]),

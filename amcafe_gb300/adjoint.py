@@ -2,22 +2,28 @@
 
 With the capture and nucleation events held fixed, the CA's growth is the
 time integral of the octahedron growth v = a dT^n of each frontier cell over
-the event times it grew through (VoxelsCA.C:405, 511-516). `GrowthRun` runs
-the CA once with the deck's physics, keeping a checkpoint (cafe_sim_checkpoint)
-every `segment` steps; evaluating the summed growth or its gradient replays one
-segment at a time from its checkpoint with the growth log on
-(cafe_sim_set_growth_log), so only one segment's log is held at a time. The
-temperature of the smooth model is the Rosenthal moving point source with
-parameters theta = (P, eta, v, a, n); the melt-pool length, width and depth
-come from the moments of its soft melt indicator (cafe_adjoint_pool). Values
-and vector-Jacobian products are hand-written CUDA kernels
-(csrc/cafe_adjoint.cu); `Objective` exposes them to torch.autograd.
+the event times it grew through (VoxelsCA.C:405, 511-516). The CA itself runs
+under the Rosenthal moving point source (deck keyword "rosenthal"), so the
+temperature field the adjoint differentiates is the one that decided the
+events. `GrowthRun` runs the CA once at given parameters theta = (P, eta, v,
+a, n) (written into the deck: bmP, the rosenthal absorptivity, bmV,
+dendritegrowth2), keeping a checkpoint (cafe_sim_checkpoint) every `segment`
+steps; evaluating the summed growth or its gradient replays one segment at a
+time from its checkpoint with the growth log on (cafe_sim_set_growth_log), so
+only one segment's log is held at a time. The melt-pool length, width and
+depth come from the moments of the soft melt indicator of the same field
+(cafe_adjoint_pool). Values and vector-Jacobian products are hand-written CUDA
+kernels (csrc/cafe_adjoint.cu); `Objective` exposes them to torch.autograd.
 
-Only eta P enters the temperature, so P and eta are not separately
-identifiable from these outputs; `calibrate` recovers P (eta fixed) and a.
+`ca_target` gives the outputs of a CA run at hidden parameters and
+`calibrate_ca` recovers them: an outer loop re-runs the CA at the current
+estimate (new event set) and an inner L-BFGS fits the parameters with that
+event set frozen. Only eta P enters the temperature, so P and eta are not
+separately identifiable from these outputs; P (eta fixed) and a are fitted.
 """
 import ctypes
 import os
+import re
 import shutil
 import tempfile
 
@@ -27,25 +33,52 @@ import torch
 from ._native import CafeAdjointSetup, check, load
 from .cafe import Simulation
 
-MATERIAL = dict(k=20.0, alpha=5e-6, T0=300.0)  # W/(m K), m^2/s, K (config 0's physics)
-
 
 def _f64p(a):
     return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
 
 
-class GrowthRun:
-    """The CA run of `deck` over `nsteps` steps with checkpoints every `segment`."""
+def deck_with_theta(deck, theta, path):
+    """Writes `deck` with theta = (P, eta, v, a, n) as bmP, the absorptivity
+    of the rosenthal keyword, bmV and dendritegrowth2 into `path`."""
+    P, eta, v, a, n = (float(x) for x in theta)
+    src = open(deck).read()
+    if not re.search(r"(?mi)^\s*rosenthal\s", src):
+        raise ValueError("%s: the adjoint needs the Rosenthal temperature (deck keyword rosenthal)" % deck)
 
-    def __init__(self, deck, nsteps, segment=32, device=0, tau_T=10.0, log_capacity=1 << 22, workdir=None):
-        self.deck, self.segment, self.device = str(deck), int(segment), device
+    def sub(key, repl, text):
+        out, k = re.subn(r"(?mi)^(\s*%s)\s+[^\n#]*" % key, lambda m: m.group(1) + " " + repl, text)
+        if k != 1:
+            raise ValueError("%s: keyword %s must appear once" % (deck, key))
+        return out
+
+    src = sub("bmP", repr(P), src)
+    src = sub("bmV", repr(v), src)
+    src = sub("dendritegrowth2", "%r %r" % (a, n), src)
+    m = re.search(r"(?mi)^\s*rosenthal\s+(\S+)\s+(\S+)\s+(\S+)", src)
+    src = sub("rosenthal", "%r %s %s" % (eta, m.group(2), m.group(3)), src)
+    with open(path, "w") as f:
+        f.write(src if src.endswith("\n") else src + "\n")
+    return path
+
+
+class GrowthRun:
+    """The CA run of `deck` at theta (default: the deck's own parameters) over
+    `nsteps` steps with checkpoints every `segment`."""
+
+    def __init__(self, deck, nsteps, segment=32, device=0, tau_T=10.0, log_capacity=1 << 22, workdir=None,
+                 theta=None):
+        self.segment, self.device = int(segment), device
         self._lib = load()
         self._dir = tempfile.mkdtemp(prefix="cafe_adj_", dir=workdir)
+        self.deck = str(deck)
+        if theta is not None:
+            self.deck = deck_with_theta(deck, theta, os.path.join(self._dir, "theta.in"))
         self.checkpoints = []  # (path, steps in the segment)
         sim = Simulation(self.deck, device=device)
         sim.InitializeVoxels()
         sim.begin()
-        info = sim.info()
+        g0 = sim.grid()
         done, k = False, 0
         while k < nsteps and not done:
             path = os.path.join(self._dir, "seg%05d.ckpt" % len(self.checkpoints))
@@ -58,36 +91,35 @@ class GrowthRun:
             self.checkpoints.append((path, m))
         self.nsteps = k
         self.step_final = sim.info()["tInd"] - 1
+        self.stats = sim.stats()
         sim.close()
+        self.theta = np.array([g0["bmP"], g0["ros_eta"], g0["bmV"], g0["Avel"], g0["nvel"]])
         self._sim = Simulation(self.deck, device=device)  # replays segments
         dev = torch.device("cuda", device)
         self._cells = torch.empty(log_capacity, dtype=torch.int32, device=dev)
         self._steps = torch.empty(log_capacity, dtype=torch.int32, device=dev)
         self._tau = torch.empty(log_capacity, dtype=torch.float64, device=dev)
         self._cap = log_capacity
-        self.setup = self._make_setup(info, tau_T)
+        self.setup = self._make_setup(g0, tau_T)
 
-    def _make_setup(self, info, tau_T):
-        # the deck's laser: one track along x (patternID 1, gridsize Lx 0)
-        g = {}
-        for line in open(self.deck):
-            f = line.split("#")[0].split()
-            if f:
-                g[f[0].lower()] = f[1:]
-        dx = float(g["dx"][0])
-        nx, ny, nz = (int(v) for v in g["nx"])
-        gs = [float(v) for v in g.get("gridsize", ["0", "0"])]
-        off = [float(v) for v in g.get("offset", ["0", "0", "0"])]
+    def _make_setup(self, g, tau_T):
+        """The adjoint's source path from the engine's own laser state at the
+        first step: a track along +x of an unrotated laser frame, source at
+        laser + (v t, 0, 0) at t = tInd dt."""
+        if g["tmodel"] != 2:
+            raise ValueError("the adjoint needs the Rosenthal temperature (deck keyword rosenthal)")
+        if g["gth"] != 0.0 or not g["dirp"] > 0:
+            raise ValueError("the adjoint's source path is a track along +x of an unrotated laser frame")
         s = CafeAdjointSetup()
-        s.k, s.alpha, s.T0 = MATERIAL["k"], MATERIAL["alpha"], MATERIAL["T0"]
-        s.Tl = float(g.get("tl", ["1620"])[0])
+        s.k, s.alpha, s.T0 = g["ros_k"], g["ros_alpha"], g["T0"]
+        s.Tl = g["tL"]
         s.tau_T = tau_T
-        s.x_start = (nx * dx - gs[0]) / 2 - off[0]
-        s.y_src = (ny * dx - gs[1]) / 2 - off[1]
-        s.z_src = info["ilaserLoc"] * dx - off[2]
-        s.dt = float(g["bmdelt"][0])
-        s.dx = dx
-        s.nx, s.ny, s.nz = nx, ny, nz
+        s.dt = g["DelT"]
+        s.x_start = g["laser"][0] - g["bmV"] * (g["tInd"] * s.dt)
+        s.y_src = g["laser"][1]
+        s.z_src = g["laser"][2]
+        s.dx = g["dX"][0]
+        s.nx, s.ny, s.nz = g["nX"]
         s.step_final = self.step_final
         return s
 
@@ -203,3 +235,38 @@ def calibrate(run, target, theta0, free=(0, 3), iters=30):
     th = theta0.clone()
     th[list(free)] = torch.exp(logp.detach())
     return th.numpy(), hist
+
+
+def ca_target(deck, nsteps, theta, segment=32, device=0):
+    """Outputs (length, width, depth, G) of a CA run at theta: the pool of its
+    own temperature field at the last step and the summed growth over its own
+    event set."""
+    run = GrowthRun(deck, nsteps, segment=segment, device=device, theta=theta)
+    try:
+        pool, _ = run.pool(run.theta)
+        G, _ = run.growth(run.theta)
+        return np.array([pool[0], pool[1], pool[2], G]), run.stats
+    finally:
+        run.close()
+
+
+def calibrate_ca(deck, nsteps, target, theta0, free=(0, 3), outer=6, iters=30, segment=32, device=0, rtol=1e-9):
+    """Recovers the parameters `free` from CA outputs: each outer iteration runs
+    the CA at the current estimate and fits the parameters with that run's
+    event set frozen (calibrate); stops when a CA run reproduces the target to
+    rtol or after `outer` runs. Returns (theta, history of (theta, loss))."""
+    th = np.asarray(theta0, np.float64).copy()
+    hist = []
+    tgt = np.asarray(target, np.float64)
+    for _ in range(outer):
+        run = GrowthRun(deck, nsteps, segment=segment, device=device, theta=th)
+        try:
+            out = Objective.apply(torch.tensor(run.theta), run).numpy()
+            loss = float(np.sum(((out - tgt) / tgt) ** 2))
+            hist.append((th.copy(), loss))
+            if loss <= rtol * rtol:
+                break
+            th, _ = calibrate(run, tgt, run.theta, free=free, iters=iters)
+        finally:
+            run.close()
+    return th, hist

@@ -25,7 +25,7 @@ import os
 
 import numpy as np
 
-from ._native import NPHASE, PHASES, CafeInfo, CafeOptions, CafeStats, check, load
+from ._native import NPHASE, PHASES, CafeGrid, CafeInfo, CafeOptions, CafeStats, check, load
 
 
 def _ptr(a, ct):
@@ -91,6 +91,18 @@ class Simulation:
         i = CafeInfo()
         check(self._lib.cafe_sim_info(self._h, ctypes.byref(i)))
         return {f: getattr(i, f) for f, _ in CafeInfo._fields_}
+
+    def grid(self):
+        """Grid's public scalars (cafe_sim_grid): deck values, derived laser
+        grid, clock and laser state, the temperature model, and the source
+        position and scan direction of the next temperature call."""
+        g = CafeGrid()
+        check(self._lib.cafe_sim_grid(self._h, ctypes.byref(g)))
+        out = {}
+        for f, t in CafeGrid._fields_:
+            v = getattr(g, f)
+            out[f] = list(v) if hasattr(v, "__len__") else v
+        return out
 
     def stats(self):
         s = CafeStats()

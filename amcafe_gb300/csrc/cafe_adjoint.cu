@@ -3,8 +3,10 @@
 //
 // Temperature: the Rosenthal point source moving along +x over a half space,
 //   T = T0 + q / R exp(-v (R + xi) / (2 alpha)),  q = eta P / (2 pi k),
-// xi = x - (x_start + v t), R = |(xi, y - y_src, z - z_src)|, t = step dt.
-// Parameters theta = (P, eta, v, a, n).
+// xi = x - (x_start + v t), R = |(xi, y - y_src, z - z_src)| clamped below at
+// half a voxel, t = step dt: the field the CA steps under the deck keyword
+// "rosenthal" (csrc/cafe_device.cuh, cafe_rosenthal_T) for a track along +x
+// of an unrotated laser frame. Parameters theta = (P, eta, v, a, n).
 //
 // Melt-pool shape at one step from the soft melt indicator
 // m = 1 / (1 + exp(-(T - T_liq) / tau_T)) over the cells: with the m-weighted
@@ -42,13 +44,18 @@ __device__ __forceinline__ void adj_temp(const cafe_adjoint_setup &S, const AdjT
   double xi = x - (S.x_start + th.v * t);
   double dy = y - S.y_src, dz = z - S.z_src;
   double R = sqrt(xi * xi + dy * dy + dz * dz);
+  const bool clamped = R < 0.5 * S.dx;  // R fixed at half a voxel: no dependence on v through R
+  if (clamped) R = 0.5 * S.dx;
   double q = th.eta * th.P / (2 * pi * S.k);
   double E = exp(-th.v * (R + xi) / (2 * S.alpha));
   double U = q / R * E;  // T - T0
   T = S.T0 + U;
   dT[0] = U / th.P;
   dT[1] = U / th.eta;
-  dT[2] = U * (-(R + xi) / (2 * S.alpha) + th.v * t * (1 + xi / R) / (2 * S.alpha) + xi * t / (R * R));
+  if (clamped)
+    dT[2] = U * (-(R + xi) / (2 * S.alpha) + th.v * t / (2 * S.alpha));
+  else
+    dT[2] = U * (-(R + xi) / (2 * S.alpha) + th.v * t * (1 + xi / R) / (2 * S.alpha) + xi * t / (R * R));
 }
 
 __device__ __forceinline__ void block_sum(double *v, int n, double *out) {

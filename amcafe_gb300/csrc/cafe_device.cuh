@@ -69,9 +69,13 @@ struct CafeConsts {
   // SampleOrientation constants (SampleOrientation.C:15-22)
   double so_R1, so_a, so_aprime, so_beta, so_s2, so_s2q, so_s6pi, so_spi, so_s24, so_coeffA[7];
   double s3, s23;     // pow(3,.5), pow(2/3,.5) (VoxelsCA.C:583-585)
-  // EASM temperature (TempField::EASM): per-cell temperatures in CafeDev::temp
-  // and per-cell growth velocities in CafeDev::a_vh
+  // a per-cell temperature field (EASM, TempField::EASM, or the Rosenthal
+  // extension): temperatures in CafeDev::temp, per-cell growth velocities in
+  // CafeDev::a_vh; tmodel 1 = EASM, 2 = Rosenthal (0 = the analytic field)
   int easm;
+  int tmodel;
+  // Rosenthal extension: T = T0 + ros_q / R exp(-ros_c (R + xi)), R >= ros_rmin
+  double ros_q, ros_c, ros_rmin;
   double Avel;        // Grid::Avel
   int nvel_i;         // Grid::nvel (an integer when easm)
   // Gaussian-undercooling nucleation (extension keyword "nucgauss mean sd")
@@ -228,6 +232,27 @@ __device__ __forceinline__ int cafe_temp_class_exact(const CafeConsts &K, const 
     in = dsq < 1.0;
   }
   return in ? 2 : 1;
+}
+
+// Extension "rosenthal eta k alpha": the Rosenthal moving point source at the
+// laser point (laser frame of the analytic field, TempField.C:155-166), xi the
+// distance ahead of it along the scan direction (the sign of dirp), R clamped
+// below at half a voxel; cells above the laser plane keep T0. The operation
+// order is the oracle's (no contraction).
+__device__ __forceinline__ double cafe_rosenthal_T(const CafeConsts &K, const CafeStepParams &P, int i, int j,
+                                                   int k) {
+  double zp = ((double)k + .5) * K.dx[2];
+  if (zp > P.lz) return K.T0;
+  double x0 = ((double)i + .5) * K.dx[0];
+  double y0 = ((double)j + .5) * K.dx[1];
+  double xp = P.cg * (x0 - K.hLX0) + P.sg * (y0 - K.hLX1) + K.hLX0;
+  double yp = -P.sg * (x0 - K.hLX0) + P.cg * (y0 - K.hLX1) + K.hLX1;
+  double r0 = xp - P.lx, r1 = yp - P.ly, r2 = zp - P.lz;
+  double R = sqrt(r0 * r0 + r1 * r1 + r2 * r2);
+  if (R < K.ros_rmin) R = K.ros_rmin;
+  double sd = P.dirp > 0 ? 1.0 : (P.dirp < 0 ? -1.0 : 0.0);
+  double xi = sd * r0;
+  return K.T0 + K.ros_q / R * crm_exp(-(K.ros_c * (R + xi)));
 }
 
 __device__ __forceinline__ void cafe_cell_xyz(const CafeConsts &K, long long idx, int &i, int &j,

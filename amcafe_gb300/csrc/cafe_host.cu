@@ -63,6 +63,8 @@ struct GridH {
   int seed = 1;       // extension keyword "seed" (1: the reference's seeds)
   int nuc_gauss = 0;  // extension keyword "nucgauss mean sd"
   double nuc_mean = 0, nuc_sd = 1;
+  int rosenthal = 0;  // extension keyword "rosenthal eta k alpha"
+  double ros_eta = 0.35, ros_k = 20.0, ros_alpha = 5e-6;
   double tL = 1620, tS = 1531.5, T0 = 300, layerT = 25e-6, bpH = 0.0, mu = .01, lrate = 0;
   double meltparam[4] = {75e-6, 162.75e-6, 75e-6, 75e-6};
   double bhatch = 0, bmDelT = 0, bmV = 500e-3, bmP = 0, rNmax = .002;
@@ -150,6 +152,12 @@ int parse_deck(const char *path, GridH &g) {
     else if (key == "nucgauss") {
       ok = num(g.nuc_mean) && num(g.nuc_sd) && g.nuc_sd > 0;
       g.nuc_gauss = 1;
+    }
+    // extension: the Rosenthal moving point source (absorptivity,
+    // conductivity W/(m K), diffusivity m^2/s) with power bmP and speed bmV
+    else if (key == "rosenthal") {
+      ok = num(g.ros_eta) && num(g.ros_k) && num(g.ros_alpha) && g.ros_eta > 0 && g.ros_k > 0 && g.ros_alpha > 0;
+      g.rosenthal = 1;
     }
     if (!ok) return fail(CAFE_E_ARG, "deck '%s': bad value after keyword '%s'", path, key.c_str());
     in >> kw;
@@ -685,12 +693,18 @@ int easm_field(cafe_sim *s) {
   {
     PhaseScope ps(s, CAFE_PH_MELT);
     k_easm_reset<<<1, 32, 0, s->stream>>>(s->D);
-    if (ncell > 0) {  // persistent: a few blocks per SM pull cells from a cursor
-      k_easm<<<(int)std::min<long long>((ncell + 255) / 256, (long long)s->nsm * 3), 256, 0, s->stream>>>(
-          s->D, K, P, s->E, ncell);
-      k_easm_long<<<s->nsm * 3, 256, 0, s->stream>>>(s->D, K, P, s->E);
+    if (K.tmodel == 2) {
+      if (ncell > 0)
+        k_rosenthal<<<grid_blocks(ncell, 256, s), 256, 0, s->stream>>>(s->D, K, P, ncell);
+      LAUNCHED(CAFE_PH_MELT, 2);
+    } else {
+      if (ncell > 0) {  // persistent: a few blocks per SM pull cells from a cursor
+        k_easm<<<(int)std::min<long long>((ncell + 255) / 256, (long long)s->nsm * 3), 256, 0, s->stream>>>(
+            s->D, K, P, s->E, ncell);
+        k_easm_long<<<s->nsm * 3, 256, 0, s->stream>>>(s->D, K, P, s->E);
+      }
+      LAUNCHED(CAFE_PH_MELT, 3);
     }
-    LAUNCHED(CAFE_PH_MELT, 3);
   }
   CUDA_TRY(cudaGetLastError());
   int *h = s->h_pinned + 8;  // 7 ints: box lo, box hi, cold
@@ -784,7 +798,7 @@ int end_of_scan(cafe_sim *s) {
   double y = g.lcoor2[2 * isv[g.isp] + 1] - g.offset[1];
   if (x < g.gbox[0] || x > g.gbox[1] || y < g.gbox[2] || y > g.gbox[3]) {
     int hot = 0;
-    if (s->K.easm) {
+    if (s->K.tmodel == 1) {
       // TempField::EASM asks all_of(T >= tL) (TempField.C:123-125); cells
       // above the laser plane hold T = 0
       hot = (P.kabove >= g.nX[2] && !s->easm_cold) ? 1 : 0;
@@ -1055,17 +1069,31 @@ int cafe_sim_create(const char *deck_path, const cafe_options *opt, cafe_sim **o
   K.nuc_gauss = g.nuc_gauss;
   K.nuc_mean = g.nuc_mean;
   K.nuc_sd = g.nuc_sd;
-  K.easm = g.EASM_Flag == 1;
+  if (g.EASM_Flag == 1 && g.rosenthal) {
+    cafe_sim_destroy(s);
+    return fail(CAFE_E_ARG, "a deck selects either the EASM or the Rosenthal temperature, not both");
+  }
+  K.tmodel = g.EASM_Flag == 1 ? 1 : (g.rosenthal ? 2 : 0);
+  K.easm = K.tmodel != 0;
   K.Avel = g.Avel;
   K.nvel_i = 0;
+  {
+    const double pi = 3.14159265358979323846;
+    K.ros_q = g.ros_eta * g.bmP / (2.0 * pi * g.ros_k);
+    K.ros_c = g.bmV / (2.0 * g.ros_alpha);
+    K.ros_rmin = 0.5 * std::min(g.dX[0], std::min(g.dX[1], g.dX[2]));
+  }
   if (K.easm) {
     // per-cell velocities Avel pow(tL - T, nvel) are evaluated on the device
     // as correctly rounded integer powers
     if (!(g.nvel >= 1 && g.nvel <= 64 && g.nvel == (double)(int)g.nvel)) {
       cafe_sim_destroy(s);
-      return fail(CAFE_E_ARG, "EASM temperature needs an integer growth exponent in 1..64 (dendritegrowth2)");
+      return fail(CAFE_E_ARG, "EASM and Rosenthal temperatures need an integer growth exponent in 1..64 "
+                              "(dendritegrowth2)");
     }
     K.nvel_i = (int)g.nvel;
+  }
+  if (K.tmodel == 1) {
     CafeEasm &E = s->E;
     const double t = 80.0e-5;
     cafe_gauss_legendre(CAFE_EASM_NODES, 0.0, t, E.qx, E.qw);
@@ -1179,7 +1207,9 @@ int cafe_sim_create(const char *deck_path, const cafe_options *opt, cafe_sim **o
   cudaMemsetAsync(D.cz, 0, N * sizeof(double), s->stream);
   cudaMemsetAsync(D.buildj, 0, N, s->stream);
   cudaMemsetAsync(D.build, 0, N, s->stream);
-  if (K.easm) cudaMemsetAsync(D.temp, 0, N * sizeof(double), s->stream);
+  if (K.tmodel == 1) cudaMemsetAsync(D.temp, 0, N * sizeof(double), s->stream);
+  // the Rosenthal field leaves cells above the laser plane at T0
+  if (K.tmodel == 2) k_fill_f64<<<grid_blocks(N, 256, s), 256, 0, s->stream>>>(D.temp, N, K.T0);
   cudaMemsetAsync(D.pos_of, 0xff, N * sizeof(int32_t), s->stream);
   cudaMemsetAsync(D.ctr, 0, CTR_COUNT * sizeof(int), s->stream);
   cudaMemsetAsync(D.err, 0, sizeof(int), s->stream);
@@ -1490,6 +1520,83 @@ int cafe_sim_info(cafe_sim *s, cafe_info *info) {
   }
   info->tf_tInd = s->tf_tInd;
   info->output_due = s->output_due ? 1 : 0;
+  return CAFE_OK;
+}
+
+int cafe_generate_samples(int n, unsigned int seed, double *axis_angle) {
+  if (n < 0 || (n > 0 && !axis_angle)) return fail(CAFE_E_ARG, "cafe_generate_samples: bad argument");
+  std::vector<double> v;
+  host_generate_samples(n, seed, v);
+  std::copy(v.begin(), v.end(), axis_angle);
+  return CAFE_OK;
+}
+
+int cafe_sim_grid(cafe_sim *s, cafe_grid *out) {
+  if (!s || !out) return fail(CAFE_E_ARG, "null argument");
+  const GridH &g = s->g;
+  for (int a = 0; a < 3; ++a) {
+    out->nX[a] = g.nX[a];
+    out->dX[a] = g.dX[a];
+    out->LX[a] = g.LX[a];
+    out->offset[a] = g.offset[a];
+  }
+  for (int a = 0; a < 4; ++a) {
+    out->meltparam[a] = g.meltparam[a];
+    out->gbox[a] = g.gbox[a];
+  }
+  out->gsize[0] = g.gsize[0];
+  out->gsize[1] = g.gsize[1];
+  out->bmV = g.bmV;
+  out->bmP = g.bmP;
+  out->bmDelT = g.bmDelT;
+  out->bhatch = g.bhatch;
+  out->tL = g.tL;
+  out->tS = g.tS;
+  out->T0 = g.T0;
+  out->layerT = g.layerT;
+  out->bpH = g.bpH;
+  out->mu = g.mu;
+  out->lrate = g.lrate;
+  out->rNmax = g.rNmax;
+  out->Avel = g.Avel;
+  out->nvel = g.nvel;
+  out->gth0 = g.gth0;
+  out->gth = g.gth;
+  out->time = g.time;
+  out->DelT = s->DelT;
+  out->outint = g.outint;
+  out->patternID = g.patternID;
+  out->outNL = g.outNL;
+  out->EASM_Flag = g.EASM_Flag;
+  out->nZlayer = g.nZlayer;
+  out->Nzhg = g.Nzhg;
+  out->Nsd = g.Nsd;
+  out->Ntd = g.Ntd;
+  out->NpT = g.NpT;
+  out->isp = g.isp;
+  out->inewscanflg = g.inewscanflg;
+  out->inewlayerflg = g.inewlayerflg;
+  out->indlayer = g.indlayer;
+  out->ilaserLoc = g.ilaserLoc;
+  out->tInd = g.tInd;
+  out->tf_tInd = s->tf_tInd;
+  out->Nzh = s->Nzh;
+  out->nlayerTot = s->nlayerTot;
+  out->seed = g.seed;
+  out->tmodel = s->K.tmodel;
+  out->ros_eta = g.ros_eta;
+  out->ros_k = g.ros_k;
+  out->ros_alpha = g.ros_alpha;
+  out->laser[0] = out->laser[1] = out->laser[2] = out->dirp = 0.0;
+  if (g.isp >= 0 && g.isp < g.NpT && g.Nsd > 0 && !((std::fmod(g.isp, g.Nsd) == 0 && g.isp + 1 >= g.NpT) ||
+                                                    (std::fmod(g.isp, g.Nsd) != 0 && g.isp < 1))) {
+    CafeStepParams P;
+    make_step_params(s, P);
+    out->laser[0] = P.lx;
+    out->laser[1] = P.ly;
+    out->laser[2] = P.lz;
+    out->dirp = P.dirp;
+  }
   return CAFE_OK;
 }
 

@@ -2777,6 +2777,52 @@ __global__ void k_easm_long(CafeDev D, CafeConsts K, CafeStepParams P, CafeEasm 
 
 // SetLiquid3 (VoxelsCA.C:1098-1116) and the class map over the box of the
 // cells at or above the liquidus, from the EASM temperatures.
+// The Rosenthal field (extension) over cells [0, ncell): temp, BuildjID as
+// AnalyticTempCurr sets it (TempField.C:180-185), the box of the cells at or
+// above the liquidus and the "some cell below the liquidus" flag, in the slots
+// the EASM field uses.
+__global__ void k_rosenthal(CafeDev D, CafeConsts K, CafeStepParams P, long long ncell) {
+  __shared__ int s_box[6], s_cold;
+  if (threadIdx.x < 3) {
+    s_box[threadIdx.x] = 0x7fffffff;
+    s_box[3 + threadIdx.x] = -1;
+  }
+  if (threadIdx.x == 0) s_cold = 0;
+  __syncthreads();
+  int bx0 = 0x7fffffff, by0 = 0x7fffffff, bz0 = 0x7fffffff, bx1 = -1, by1 = -1, bz1 = -1, cold = 0;
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < ncell;
+       c += (long long)gridDim.x * blockDim.x) {
+    int ci, cj, ck;
+    cafe_cell_xyz(K, c, ci, cj, ck);
+    double T = cafe_rosenthal_T(K, P, ci, cj, ck);
+    D.temp[c] = T;
+    if (T > K.tL)
+      D.buildj[c] = 1;
+    else if (T < K.T0)
+      D.buildj[c] = 0;
+    if (T >= K.tL) {
+      bx0 = min(bx0, ci); by0 = min(by0, cj); bz0 = min(bz0, ck);
+      bx1 = max(bx1, ci); by1 = max(by1, cj); bz1 = max(bz1, ck);
+    } else {
+      cold = 1;
+    }
+  }
+  if (bx1 >= 0) {
+    atomicMin(&s_box[0], bx0); atomicMin(&s_box[1], by0); atomicMin(&s_box[2], bz0);
+    atomicMax(&s_box[3], bx1); atomicMax(&s_box[4], by1); atomicMax(&s_box[5], bz1);
+  }
+  if (cold) s_cold = 1;
+  __syncthreads();
+  if (threadIdx.x < 3 && s_box[3 + threadIdx.x] >= 0) {
+    atomicMin(&D.ctr[CTR_EASM_BOX + threadIdx.x], s_box[threadIdx.x]);
+    atomicMax(&D.ctr[CTR_EASM_BOX + 3 + threadIdx.x], s_box[3 + threadIdx.x]);
+  }
+  if (threadIdx.x == 0 && s_cold) D.ctr[CTR_EASM_COLD] = 1;
+}
+__global__ void k_fill_f64(double *p, long long n, double v) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    p[i] = v;
+}
 __global__ void k_melt_easm(CafeDev D, CafeConsts K, CafeStepParams P) {
   int bx = P.hi[0] - P.lo[0], by = P.hi[1] - P.lo[1], bz = P.hi[2] - P.lo[2];
   long long nbox = (long long)bx * by * bz;

@@ -117,6 +117,36 @@ int cafe_sim_synchronize(cafe_sim *sim);
 
 int cafe_sim_info(cafe_sim *sim, cafe_info *info);
 
+/* The public scalars of the handle's Grid (Grid.h:48-93: deck values and the
+ * quantities Grid::Grid derives from them, Grid.C:15-109, plus the laser
+ * state that UpdateLaser and the temperature's end-of-scan check change),
+ * TempField::DelT and tInd, BasePlate::Nzh and main1.C's nlayerTot. The
+ * drop-in classes of include/amcafe/ mirror their public fields from it. */
+typedef struct {
+  int nX[3];
+  double dX[3], LX[3], offset[3];
+  double meltparam[4], gbox[4], gsize[2];
+  double bmV, bmP, bmDelT, bhatch, tL, tS, T0, layerT, bpH, mu, lrate, rNmax, Avel, nvel;
+  double gth0, gth, time;
+  double DelT;  /* TempField::DelT */
+  int outint, patternID, outNL, EASM_Flag, nZlayer, Nzhg, Nsd, Ntd, NpT;
+  int isp, inewscanflg, inewlayerflg, indlayer, ilaserLoc, tInd;
+  int tf_tInd;  /* TempField::tInd */
+  int Nzh;      /* BasePlate::Nzh */
+  int nlayerTot;
+  int seed;     /* extension keyword "seed" (1: the reference's seeds) */
+  int tmodel;   /* temperature: 0 analytic, 1 EASM ("easm 1"), 2 Rosenthal ("rosenthal eta k alpha") */
+  double ros_eta, ros_k, ros_alpha; /* Rosenthal: absorptivity, W/(m K), m^2/s */
+  double laser[3]; /* source of the next temperature call in the laser frame (TempField.C:145-154) */
+  double dirp;     /* its scan direction term (TempField.C:167-171): > 0 along +x of that frame */
+} cafe_grid;
+int cafe_sim_grid(cafe_sim *sim, cafe_grid *grid);
+/* SampleOrientation::GenerateSamples(n, seed, axisAngle)
+ * (SampleOrientation.C:124-161) on the host with the host's libm, as the
+ * engine draws baseplate and layer orientations: n uniformly distributed
+ * orientations as (angle, axis x, y, z), 4 doubles each, into axis_angle. */
+int cafe_generate_samples(int n, unsigned int seed, double *axis_angle);
+
 /* Device-time accounting, for profiling: phases of one step, each bracketed
  * by CUDA events on the handle's stream when timing is on. */
 enum {

@@ -1,7 +1,9 @@
 """FP64 CPU reference of the adjoint extension (test infrastructure only).
 
 Restates in numpy the melt-pool moments and the summed growth that
-amcafe_gb300/csrc/cafe_adjoint.cu evaluates (Rosenthal point source, soft
+amcafe_gb300/csrc/cafe_adjoint.cu evaluates (Rosenthal point source with R
+clamped below at half a voxel, as the CA's field under the deck keyword
+"rosenthal", soft
 melt indicator, growth a (T_liq - T)^n tau over a growth log) together with
 their gradients with respect to theta = (P, eta, v, a, n), written out by hand
 from the formulas; tests compare the GPU kernels with it and with central
@@ -15,11 +17,13 @@ def temperature(setup, theta, x, y, z, t):
     xi = x - (setup["x_start"] + v * t)
     dy, dz = y - setup["y_src"], z - setup["z_src"]
     R = np.sqrt(xi * xi + dy * dy + dz * dz)
+    clamped = R < 0.5 * setup["dx"]  # the forward field clamps R at half a voxel
+    R = np.where(clamped, 0.5 * setup["dx"], R)
     q = eta * P / (2 * np.pi * setup["k"])
     U = q / R * np.exp(-v * (R + xi) / (2 * setup["alpha"]))
-    dT = np.stack([U / P, U / eta,
-                   U * (-(R + xi) / (2 * setup["alpha"]) + v * t * (1 + xi / R) / (2 * setup["alpha"])
-                        + xi * t / (R * R))])
+    dv = np.where(clamped, -(R + xi) / (2 * setup["alpha"]) + v * t / (2 * setup["alpha"]),
+                  -(R + xi) / (2 * setup["alpha"]) + v * t * (1 + xi / R) / (2 * setup["alpha"]) + xi * t / (R * R))
+    dT = np.stack([U / P, U / eta, U * dv])
     return setup["T0"] + U, dT
 
 

@@ -116,6 +116,11 @@ struct Grid {
   int seed = 1;  // extension keyword "seed" (1: the reference's seeds)
   int nuc_gauss = 0;  // extension keyword "nucgauss mean sd"
   double nuc_mean = 0, nuc_sd = 1;
+  // extension keyword "rosenthal eta k alpha": the Rosenthal moving point
+  // source (absorptivity, conductivity W/(m K), diffusivity m^2/s) in place
+  // of the analytic field
+  int rosenthal = 0;
+  double ros_eta = 0.35, ros_k = 20.0, ros_alpha = 5e-6;
   double tL = 1620, tS = 1531.5, T0 = 300, layerT = 25e-6, bpH = 0.0, mu = .01;
   double lrate = 0.0;
   bool have_lrate = false, have_bmdelt = false;
@@ -222,6 +227,12 @@ static bool read_deck(const char *path, Grid &g, std::string &err) {
         g.nuc_gauss = 1;
         next_d(g.nuc_mean);
         next_d(g.nuc_sd);
+      }
+      if (kw == "rosenthal") {
+        g.rosenthal = 1;
+        next_d(g.ros_eta);
+        next_d(g.ros_k);
+        next_d(g.ros_alpha);
       }
       if (kw == "dendritegrowth2") {
         next_d(g.Avel);
@@ -944,10 +955,79 @@ static void easm_temp(State &S) {
     }
   }
 }
-// main1.C:65-70: EASM when Grid::EASM_Flag is 1, else the analytic field
+// Extension "rosenthal eta k alpha" (no reference code): the Rosenthal
+// solution for a point source of power eta P moving at v over a half space,
+//   T = T0 + q / R exp(-c (R + xi)),  q = eta P / (2 pi k),  c = v / (2 alpha),
+// in the laser frame of the analytic field (cell centres rotated by gth about
+// the box centre, TempField.C:155-166), source at the laser point on the laser
+// plane, xi the distance ahead of the source along the scan direction (the
+// sign of the analytic field's dirp, TempField.C:167-171), R clamped below at
+// half a voxel. Cells above the plane stay at T0. BuildjID and the
+// end-of-scan check follow AnalyticTempCurr (TempField.C:180-216).
+static void rosenthal_temp(State &S) {
+  Grid &g = S.g;
+  std::fill(S.temp.begin(), S.temp.end(), g.T0);
+  const double pi = 3.14159265358979323846;
+  const double q = g.ros_eta * g.bmP / (2.0 * pi * g.ros_k);
+  const double c = g.bmV / (2.0 * g.ros_alpha);
+  const double rmin = 0.5 * std::min(g.dX[0], std::min(g.dX[1], g.dX[2]));
+  const int *isv = S.ispvec.data();
+  double x = g.lcoor[2 * isv[g.isp]] - g.offset[0];
+  double y = g.lcoor[2 * isv[g.isp] + 1] - g.offset[1];
+  double z = g.ilaserLoc * g.dX[2] - g.offset[2];
+  double cg = std::cos(g.gth), sg = std::sin(g.gth);
+  double dirp;
+  if (std::fmod(g.isp, g.Nsd) == 0)
+    dirp = (g.lcoor[2 * isv[g.isp + 1]] - g.lcoor[2 * isv[g.isp]]);
+  else
+    dirp = (g.lcoor[2 * isv[g.isp]] - g.lcoor[2 * isv[g.isp - 1]]);
+  const double sd = dirp > 0 ? 1.0 : (dirp < 0 ? -1.0 : 0.0);
+  for (int j = 0; j < S.N; ++j) {
+    int cc[3];
+    cell_xyz(S, j, cc);
+    double x0 = (double(cc[0]) + .5) * (g.dX[0]);
+    double y0 = (double(cc[1]) + .5) * (g.dX[1]);
+    double zp = (double(cc[2]) + .5) * (g.dX[2]);
+    if (zp > z) continue;
+    double xp = cg * (x0 - g.LX[0] / 2.) + sg * (y0 - g.LX[1] / 2.) + g.LX[0] / 2.;
+    double yp = -sg * (x0 - g.LX[0] / 2.) + cg * (y0 - g.LX[1] / 2.) + g.LX[1] / 2.;
+    double r0 = xp - x, r1 = yp - y, r2 = zp - z;
+    double R = std::sqrt(r0 * r0 + r1 * r1 + r2 * r2);
+    if (R < rmin) R = rmin;
+    double xi = sd * r0;
+    double T = g.T0 + q / R * m_exp(-(c * (R + xi)));
+    S.temp[j] = T;
+    if (T > g.tL)
+      S.buildj[j] = 1;
+    else if (T < g.T0)
+      S.buildj[j] = 0;
+  }
+  double lx = g.lcoor2[2 * isv[g.isp]] - g.offset[0];
+  double ly = g.lcoor2[2 * isv[g.isp] + 1] - g.offset[1];
+  if (lx < g.gbox[0] || lx > g.gbox[1] || ly < g.gbox[2] || ly > g.gbox[3]) {
+    int icheck = 0;
+    for (int j = 0; j < S.N; ++j)
+      if (S.temp[j] >= g.tL) {
+        icheck = 1;
+        break;
+      }
+    if (icheck == 0 || std::fmod(g.isp + 1, g.Nsd) == 0) g.inewscanflg = 1;
+    if (g.isp == (g.NpT - 1)) {
+      g.inewscanflg = 1;
+      g.inewlayerflg = 1;
+      g.isp = 0;
+      g.indlayer += 1;
+    }
+  }
+}
+
+// main1.C:65-70: EASM when Grid::EASM_Flag is 1, else the analytic field (or
+// the Rosenthal extension)
 static void temperature(State &S) {
   if (S.g.EASM_Flag == 1)
     easm_temp(S);
+  else if (S.g.rosenthal)
+    rosenthal_temp(S);
   else
     analytic_temp(S);
 }
@@ -1178,9 +1258,10 @@ static void update_voxels(State &S) {
       if (!(T[nid[t]] < tL)) cold[p] = 0;
     }
   // per-position growth velocity (VoxelsCA.C:405)
-  // (the device evaluates the per-cell velocities of the EASM field as
-  // correctly rounded integer powers)
-  const bool cr_pow = g_libm.mode == 1 && g.EASM_Flag == 1 && g.nvel >= 1 && g.nvel <= 64 && g.nvel == (int)g.nvel;
+  // (the device evaluates the per-cell velocities of the EASM and Rosenthal
+  // fields as correctly rounded integer powers)
+  const bool cr_pow = g_libm.mode == 1 && (g.EASM_Flag == 1 || g.rosenthal) && g.nvel >= 1 && g.nvel <= 64 &&
+                      g.nvel == (int)g.nvel;
   auto vhat_of = [&](int p) {
     if (T[p] >= tL) return 0.0;
     return g.Avel * (cr_pow ? crm_pow_int(tL - T[p], (int)g.nvel) : std::pow(tL - T[p], g.nvel));

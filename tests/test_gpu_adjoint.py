@@ -1,8 +1,9 @@
 """Adjoint extension: the hand-written CUDA values and vector-Jacobian products
 (csrc/cafe_adjoint.cu) against the FP64 numpy restatement (oracle/adjoint_ref.py)
-and central finite differences (h = 1e-6 relative), the segment replay from
-checkpoints against one logged run, and a calibration that recovers hidden
-parameters from a synthetic target."""
+and central finite differences (h = 1e-6 relative), the adjoint's temperature
+against the field the CA stepped under (deck keyword rosenthal), the segment
+replay from checkpoints against one logged run, and a calibration that
+recovers hidden parameters from the outputs of a CA run at those parameters."""
 import os
 
 import numpy as np
@@ -20,7 +21,7 @@ THETA = np.array([200.0, 0.35, 1.0, 1e-5, 2.0])
 def run():
     from amcafe_gb300.adjoint import GrowthRun
 
-    r = GrowthRun(DECK, nsteps=192, segment=32)
+    r = GrowthRun(DECK, nsteps=192, segment=32, theta=THETA)
     yield r
     r.close()
 
@@ -87,10 +88,28 @@ def test_replayed_segments_equal_one_logged_run(run):
     sim.close()
 
 
-def test_objective_gradient_and_calibration(run):
+def test_adjoint_temperature_is_the_cas_field(run):
+    """The temperature the adjoint differentiates is the one the CA stepped
+    under: at the last step, for every cell below the source plane, the FP64
+    restatement of the adjoint's field equals the engine's TempCurr to 1e-12
+    relative (the same formula, evaluated in another operation order)."""
+    run.log()  # replays every segment: the replaying handle ends at the last step
+    T_ca = run._sim.temperature()
+    su = run.setup_dict()
+    nx, ny, nz, dx = su["nx"], su["ny"], su["nz"], su["dx"]
+    k, j, i = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+    x, y, z = (i.ravel() + .5) * dx, (j.ravel() + .5) * dx, (k.ravel() + .5) * dx
+    below = z <= su["z_src"]
+    T_adj, _ = ref.temperature(su, run.theta, x[below], y[below], z[below], su["step_final"] * su["dt"])
+    assert _rel(T_adj, T_ca[below]) < 1e-12
+    assert np.all(T_ca[~below] == su["T0"])
+    assert np.sum(T_ca >= su["Tl"]) > 1000  # a melt pool of some thousand cells
+
+
+def test_objective_gradient(run):
     import torch
 
-    from amcafe_gb300.adjoint import Objective, calibrate
+    from amcafe_gb300.adjoint import Objective
 
     th = torch.tensor(THETA, dtype=torch.float64, requires_grad=True)
     out = Objective.apply(th, run)
@@ -99,7 +118,19 @@ def test_objective_gradient_and_calibration(run):
     for k in range(5):
         fd = _fd(lambda x: float((Objective.apply(torch.tensor(x), run) * w).sum()), THETA, k)
         assert abs(float(th.grad[k]) - fd) <= 1e-6 * abs(fd), k
+
+
+def test_calibration_recovers_parameters_from_a_ca_run():
+    """The target is the output of a CA run at the hidden parameters (its own
+    event set and temperature field); starting 10 % away, the calibration
+    re-runs the CA at each estimate and fits P and a with that run's events
+    frozen, until a CA run reproduces the target."""
+    from amcafe_gb300.adjoint import ca_target, calibrate_ca
+
     hidden = np.array([180.0, 0.4, 1.0, 1.2e-5, 2.0])
-    target = Objective.apply(torch.tensor(hidden), run).numpy()
-    got, hist = calibrate(run, target, [220.0, 0.4, 1.0, 0.9e-5, 2.0], free=(0, 3))
-    assert abs(got[0] - 180.0) < 1e-4 * 180.0 and abs(got[3] - 1.2e-5) < 1e-4 * 1.2e-5, (got, hist[-3:])
+    target, stats = ca_target(DECK, 96, hidden)
+    assert stats["events"] > 1000
+    got, hist = calibrate_ca(DECK, 96, target, [200.0, 0.4, 1.0, 1.1e-5, 2.0], free=(0, 3), outer=6)
+    print("calibration history:", [(list(h[0][[0, 3]]), h[1]) for h in hist])
+    assert abs(got[0] - 180.0) < 1e-4 * 180.0, (got, hist)
+    assert abs(got[3] - 1.2e-5) < 1e-3 * 1.2e-5, (got, hist)

@@ -87,6 +87,17 @@ def test_gpu_easm_matches_oracle(tmp_path, deck, nsteps, stride):
     print("%s: max float rel diff %g, %s" % (deck, worst, stats))
 
 
+def test_gpu_rosenthal_matches_oracle(tmp_path):
+    """Rosenthal moving point source (extension keyword rosenthal) with
+    Gaussian-undercooling nucleation: per-cell temperatures (correctly rounded
+    exp) and velocities, rows evaluated with the exact per-event scan; every
+    8th step and the final state compared, temperatures included."""
+    worst, stats = run_and_compare("track_ros.in", 0, 8, tmp_path)
+    assert stats["exact_scan_steps"] == stats["steps"]
+    assert stats["nucleations"] > 0 and stats["negative_dt"] > 0
+    print("track_ros.in: max float rel diff %g, %s" % (worst, stats))
+
+
 @pytest.mark.parametrize("deck,nsteps,stride", [("track_nuc.in", 0, 1), ("layers_rot.in", 0, 20)])
 def test_gpu_full_scan_matches_oracle(tmp_path, deck, nsteps, stride):
     """The reference's per-event scan of every frontier cell (event_scan=1)."""
