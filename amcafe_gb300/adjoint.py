@@ -63,11 +63,12 @@ def deck_with_theta(deck, theta, path):
 
 
 class GrowthRun:
-    """The CA run of `deck` at theta (default: the deck's own parameters) over
-    `nsteps` steps with checkpoints every `segment`."""
+    """The CA run of `deck` at theta (default: the deck's own parameters): after
+    `spinup` steps (run, not logged), a window of `nsteps` steps with
+    checkpoints every `segment`, whose event set the adjoint holds fixed."""
 
     def __init__(self, deck, nsteps, segment=32, device=0, tau_T=10.0, log_capacity=1 << 22, workdir=None,
-                 theta=None):
+                 theta=None, spinup=0):
         self.segment, self.device = int(segment), device
         self._lib = load()
         self._dir = tempfile.mkdtemp(prefix="cafe_adj_", dir=workdir)
@@ -79,7 +80,10 @@ class GrowthRun:
         sim.InitializeVoxels()
         sim.begin()
         g0 = sim.grid()
-        done, k = False, 0
+        if spinup > 0:
+            sim.run(int(spinup))
+        self.spinup = sim.info()["steps"]
+        done, k = sim.info()["done"] != 0, 0
         while k < nsteps and not done:
             path = os.path.join(self._dir, "seg%05d.ckpt" % len(self.checkpoints))
             sim.checkpoint(path)
@@ -237,11 +241,11 @@ def calibrate(run, target, theta0, free=(0, 3), iters=30):
     return th.numpy(), hist
 
 
-def ca_target(deck, nsteps, theta, segment=32, device=0):
+def ca_target(deck, nsteps, theta, segment=32, device=0, spinup=0):
     """Outputs (length, width, depth, G) of a CA run at theta: the pool of its
     own temperature field at the last step and the summed growth over its own
-    event set."""
-    run = GrowthRun(deck, nsteps, segment=segment, device=device, theta=theta)
+    event set in the window after `spinup` steps."""
+    run = GrowthRun(deck, nsteps, segment=segment, device=device, theta=theta, spinup=spinup)
     try:
         pool, _ = run.pool(run.theta)
         G, _ = run.growth(run.theta)
@@ -250,7 +254,8 @@ def ca_target(deck, nsteps, theta, segment=32, device=0):
         run.close()
 
 
-def calibrate_ca(deck, nsteps, target, theta0, free=(0, 3), outer=6, iters=30, segment=32, device=0, rtol=1e-9):
+def calibrate_ca(deck, nsteps, target, theta0, free=(0, 3), outer=6, iters=30, segment=32, device=0, rtol=1e-9,
+                 spinup=0):
     """Recovers the parameters `free` from CA outputs: each outer iteration runs
     the CA at the current estimate and fits the parameters with that run's
     event set frozen (calibrate); stops when a CA run reproduces the target to
@@ -259,7 +264,7 @@ def calibrate_ca(deck, nsteps, target, theta0, free=(0, 3), outer=6, iters=30, s
     hist = []
     tgt = np.asarray(target, np.float64)
     for _ in range(outer):
-        run = GrowthRun(deck, nsteps, segment=segment, device=device, theta=th)
+        run = GrowthRun(deck, nsteps, segment=segment, device=device, theta=th, spinup=spinup)
         try:
             out = Objective.apply(torch.tensor(run.theta), run).numpy()
             loss = float(np.sum(((out - tgt) / tgt) ** 2))

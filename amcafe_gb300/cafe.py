@@ -241,7 +241,9 @@ def run_deck(deck, max_steps=0, device=0, **kw):
 
 class Batch:
     """Independent realisations (one deck each) stepped concurrently on one GPU
-    (cafe_batch_*). `sims[i]` reads realisation i like a Simulation."""
+    (cafe_batch_*): threads=0 launches every step kernel once for all of them
+    (autotuned launch shapes), threads>=1 steps them round-robin from that many
+    host threads. `sims[i]` reads realisation i like a Simulation."""
 
     def __init__(self, decks, device=0, threads=0, active_capacity=0, grain_capacity=0, event_scan=0):
         self._lib = load()
@@ -260,6 +262,17 @@ class Batch:
 
     def finished(self, i):
         return self._lib.cafe_batch_finished(self._h, i) == 1
+
+    def report(self):
+        """Batched launches: kernel launches and batch steps so far, and the
+        autotuner's candidates and choice (cafe_batch_report)."""
+        import json
+
+        la, st = ctypes.c_longlong(0), ctypes.c_longlong(0)
+        buf = ctypes.create_string_buffer(4096)
+        check(self._lib.cafe_batch_report(self._h, ctypes.byref(la), ctypes.byref(st), buf, len(buf)))
+        txt = buf.value.decode()
+        return {"launches": la.value, "batch_steps": st.value, "tuning": json.loads(txt) if txt else None}
 
     def close(self):
         if self._h:

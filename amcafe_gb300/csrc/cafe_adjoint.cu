@@ -58,12 +58,32 @@ __device__ __forceinline__ void adj_temp(const cafe_adjoint_setup &S, const AdjT
     dT[2] = U * (-(R + xi) / (2 * S.alpha) + th.v * t * (1 + xi / R) / (2 * S.alpha) + xi * t / (R * R));
 }
 
-__device__ __forceinline__ void block_sum(double *v, int n, double *out) {
-  // warp shuffles then one atomic per warp and value
+// Per-block partial sums of n values (n <= 16, 256 threads) in a fixed order:
+// warp shuffles, then warp 0 adds the warps' sums in warp order and writes
+// the block's partials to part[blockIdx.x * n + j]; k_adj_total adds the
+// blocks' partials in block order. The sums are thus the same at every call
+// (no atomics), which keeps finite differences of the outputs clean.
+__device__ __forceinline__ void block_sum(double *v, int n, double *part) {
+  __shared__ double ws[8][16];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   for (int j = 0; j < n; ++j) {
     double x = v[j];
     for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-    if ((threadIdx.x & 31) == 0 && x != 0.0) atomicAdd(&out[j], x);
+    if (lane == 0) ws[w][j] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x < n) {
+    double t = 0.0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) t += ws[q][threadIdx.x];
+    part[(long long)blockIdx.x * n + threadIdx.x] = t;
+  }
+}
+
+__global__ void k_adj_total(const double *part, int nblocks, int n, double *out) {
+  if (threadIdx.x < n) {
+    double t = 0.0;
+    for (int b = 0; b < nblocks; ++b) t += part[(long long)b * n + threadIdx.x];
+    out[threadIdx.x] = t;
   }
 }
 
@@ -145,18 +165,21 @@ int cafe_adjoint_pool(const cafe_adjoint_setup *S, const double theta[5], const 
     return adj_fail(CAFE_E_ARG, "cafe_adjoint_pool: bad setup");
   cudaStream_t st = (cudaStream_t)stream;
   AdjTheta th = {theta[0], theta[1], theta[2], theta[3], theta[4]};
-  double *d = nullptr;
-  if (cudaMalloc((void **)&d, 16 * sizeof(double)) != cudaSuccess)
-    return adj_fail(CAFE_E_CUDA, "cafe_adjoint_pool: cudaMalloc failed");
-  double h[16] = {0};
-  int rc = CAFE_OK;
   int dev = 0, nsm = 1;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  const int nb = nsm * 8;
+  double *d = nullptr;  // [16] totals and cotangents, then [nb][9] block partials
+  if (cudaMalloc((void **)&d, (16 + (size_t)nb * 9) * sizeof(double)) != cudaSuccess)
+    return adj_fail(CAFE_E_CUDA, "cafe_adjoint_pool: cudaMalloc failed");
+  double *part = d + 16;
+  double h[16] = {0};
+  int rc = CAFE_OK;
   // forward sums
   if (cudaMemsetAsync(d, 0, 16 * sizeof(double), st) != cudaSuccess) rc = CAFE_E_CUDA;
   if (!rc) {
-    k_adj_pool<<<nsm * 8, 256, 0, st>>>(*S, th, 0, d + 9, d);
+    k_adj_pool<<<nb, 256, 0, st>>>(*S, th, 0, d + 9, part);
+    k_adj_total<<<1, 32, 0, st>>>(part, nb, 9, d);
     if (cudaMemcpyAsync(h, d, 9 * sizeof(double), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
         cudaStreamSynchronize(st) != cudaSuccess)
       rc = CAFE_E_CUDA;
@@ -187,7 +210,8 @@ int cafe_adjoint_pool(const cafe_adjoint_setup *S, const double theta[5], const 
           cudaMemcpyAsync(d + 9, w, 6 * sizeof(double), cudaMemcpyHostToDevice, st) != cudaSuccess)
         rc = CAFE_E_CUDA;
       if (!rc) {
-        k_adj_pool<<<nsm * 8, 256, 0, st>>>(*S, th, 1, d + 9, d);
+        k_adj_pool<<<nb, 256, 0, st>>>(*S, th, 1, d + 9, part);
+        k_adj_total<<<1, 32, 0, st>>>(part, nb, 9, d);
         if (cudaMemcpyAsync(h, d, 9 * sizeof(double), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
             cudaStreamSynchronize(st) != cudaSuccess)
           rc = CAFE_E_CUDA;
@@ -213,16 +237,20 @@ int cafe_adjoint_growth(const cafe_adjoint_setup *S, const double theta[5], cons
     return adj_fail(CAFE_E_ARG, "cafe_adjoint_growth: null argument");
   cudaStream_t st = (cudaStream_t)stream;
   AdjTheta th = {theta[0], theta[1], theta[2], theta[3], theta[4]};
-  double *d = nullptr;
-  if (cudaMalloc((void **)&d, 8 * sizeof(double)) != cudaSuccess)
-    return adj_fail(CAFE_E_CUDA, "cafe_adjoint_growth: cudaMalloc failed");
-  double h[8] = {0};
-  int rc = CAFE_OK;
   int dev = 0, nsm = 1;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  const int nb = nsm * 8;
+  double *d = nullptr;  // [8] totals, then [nb][6] block partials
+  if (cudaMalloc((void **)&d, (8 + (size_t)nb * 6) * sizeof(double)) != cudaSuccess)
+    return adj_fail(CAFE_E_CUDA, "cafe_adjoint_growth: cudaMalloc failed");
+  double h[8] = {0};
+  int rc = CAFE_OK;
   if (cudaMemsetAsync(d, 0, 8 * sizeof(double), st) != cudaSuccess) rc = CAFE_E_CUDA;
-  if (!rc && n > 0) k_adj_growth<<<nsm * 8, 256, 0, st>>>(*S, th, cells, steps, tau, n, cot, d);
+  if (!rc && n > 0) {
+    k_adj_growth<<<nb, 256, 0, st>>>(*S, th, cells, steps, tau, n, cot, d + 8);
+    k_adj_total<<<1, 32, 0, st>>>(d + 8, nb, 6, d);
+  }
   if (!rc && (cudaGetLastError() != cudaSuccess ||
               cudaMemcpyAsync(h, d, 6 * sizeof(double), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
               cudaStreamSynchronize(st) != cudaSuccess))

@@ -27,6 +27,7 @@
 
 #include "../../include/cafe_gpu.h"
 #include "cafe_kernels.cu"
+#include "cafe_batch_kernels.cuh"
 #include "cafe_quadrature.h"
 
 namespace {
@@ -386,6 +387,11 @@ void cafe_internal_set_error(const char *msg) { g_last_error = msg ? msg : ""; }
 // its steps out of CUDA graphs (when several host threads drive a batch, a
 // capture in one thread must not meet another thread's device-wide calls).
 void cafe_internal_set_share(cafe_sim *s, int share, int graphs);
+// the batched step engine (end of this file), driven by cafe_batch.cu
+struct CafeBatchEngine;
+CafeBatchEngine *cafe_internal_batch_engine_create(cafe_sim *const *sims, int n, int tune, int *rc);
+void cafe_internal_batch_engine_destroy(CafeBatchEngine *E);
+int cafe_internal_batch_engine_step(CafeBatchEngine *E, int *phase, long long *steps, int *stepped);
 
 struct cafe_sim {
   GridH g;
@@ -401,6 +407,10 @@ struct cafe_sim {
   std::default_random_engine genlayer;      // VoxelsCA.h:129
   bool initialized = false, begun = false, done = false;
   bool closed = false;  // the closing CleanLayer of main1.C:95 has been applied
+  // the last cafe_sim_step ended at an output point that is also a layer
+  // change: its AddLayer1 (main1.C:88) waits until the caller has written the
+  // output (main1.C:78-83 comes first) and runs at the next continuing call
+  bool pending_layer = false;
   long long steps = 0;
   // device
   CafeConsts K;
@@ -789,8 +799,9 @@ int launch_melt(cafe_sim *s, bool graph, const CafeStepParams *Pp) {
 }
 
 // End-of-scan check of TempField (TempField.C:199-216), only when the laser is
-// outside the grid box: host flags from "some cell at the liquidus".
-int end_of_scan(cafe_sim *s) {
+// outside the grid box: host flags from "some cell at the liquidus" (read from
+// the device, or `hot_known` when the caller has read it already).
+int end_of_scan(cafe_sim *s, const int *hot_known = nullptr) {
   GridH &g = s->g;
   const CafeStepParams &P = s->P;
   const int *isv = s->ispvec.data();
@@ -802,6 +813,8 @@ int end_of_scan(cafe_sim *s) {
       // TempField::EASM asks all_of(T >= tL) (TempField.C:123-125); cells
       // above the laser plane hold T = 0
       hot = (P.kabove >= g.nX[2] && !s->easm_cold) ? 1 : 0;
+    } else if (hot_known) {
+      hot = *hot_known;
     } else {
       int rc = read_ctr(s, CTR_HOT, &hot);
       if (rc) return rc;
@@ -966,6 +979,13 @@ int step_graph_launch(cafe_sim *s) {
 bool graph_eligible(const cafe_sim *s) { return s->use_graph && !s->timing && !s->K.easm && !s->full_k2; }
 
 // The rest of a loop iteration after its device work (main1.C:72-93).
+// The AddLayer1 that the last step left for after its output point.
+int apply_pending_layer(cafe_sim *s) {
+  if (!s->pending_layer) return CAFE_OK;
+  s->pending_layer = false;
+  return cafe_sim_add_layer(s);
+}
+
 int finish_after_laser(cafe_sim *s, bool bcheck, int *done) {
   int rc;
   if (s->g.inewlayerflg == 1 && (rc = cafe_sim_clean_layer(s))) return rc;
@@ -974,7 +994,12 @@ int finish_after_laser(cafe_sim *s, bool bcheck, int *done) {
   s->output_due = (g.outint > 0 && s->tf_tInd % g.outint == 0) || bcheck || (g.inewlayerflg == 1 && g.outNL == 0);
   if (s->output_due && (rc = cafe_sim_set_build(s))) return rc;
   cafe_sim_update_time(s);
-  if (s->g.inewlayerflg == 1 && (rc = cafe_sim_add_layer(s))) return rc;
+  if (s->g.inewlayerflg == 1) {
+    if (s->output_due)
+      s->pending_layer = true;
+    else if ((rc = cafe_sim_add_layer(s)))
+      return rc;
+  }
   s->steps++;
   if (bcheck) s->done = true;
   if (done) *done = s->done ? 1 : 0;
@@ -1388,8 +1413,8 @@ int cafe_sim_update_voxels(cafe_sim *s) {
 int cafe_sim_clean_layer(cafe_sim *s) {
   if (!s || !s->initialized) return fail(CAFE_E_STATE, "clean_layer before initialize_voxels");
   CUDA_TRY(cudaSetDevice(s->device));
-  int rc = read_ctr(s, CTR_NGRAIN, &s->nGrain);
-  if (rc) return rc;
+  int rc = apply_pending_layer(s);
+  if (rc || (rc = read_ctr(s, CTR_NGRAIN, &s->nGrain))) return rc;
   int ng = s->nGrain;
   int32_t *cnt = nullptr, *newid = nullptr;
   double *cth2 = nullptr, *rot2 = nullptr;
@@ -1449,11 +1474,12 @@ int cafe_sim_begin(cafe_sim *s) {
 
 int cafe_sim_step(cafe_sim *s, int *done) {
   if (!s || !s->begun) return fail(CAFE_E_STATE, "step before begin");
+  int rc;
+  if ((rc = apply_pending_layer(s))) return rc;
   if (s->done) {
     if (done) *done = 1;
     return CAFE_OK;
   }
-  int rc;
   if (graph_eligible(s)) {
     CUDA_TRY(cudaSetDevice(s->device));
     if ((rc = step_plan(s))) return rc;
@@ -1473,6 +1499,7 @@ int cafe_sim_run(cafe_sim *s, long long max_steps, long long *steps_done) {
   if (!s || !s->begun) return fail(CAFE_E_STATE, "run before begin");
   long long n = 0;
   int done = s->done ? 1 : 0, rc;
+  if ((rc = apply_pending_layer(s))) return rc;
   while (!done && (max_steps <= 0 || n < max_steps)) {
     if ((rc = cafe_sim_step(s, &done))) return rc;
     ++n;
@@ -2109,7 +2136,8 @@ int cafe_sim_checkpoint(cafe_sim *s, const char *path) {
   if (!s || !path) return fail(CAFE_E_ARG, "null argument");
   if (!s->begun) return fail(CAFE_E_STATE, "checkpoint before begin");
   CUDA_TRY(cudaSetDevice(s->device));
-  int rc = sim_sync(s);
+  int rc = apply_pending_layer(s);  // the checkpoint holds whole steps
+  if (!rc) rc = sim_sync(s);
   if (rc || (rc = ensure_host_buffer(s)) || (rc = read_ctr(s, CTR_NGRAIN, &s->nGrain))) return rc;
   const GridH &g = s->g;
   CkptHeader h;
@@ -2223,6 +2251,7 @@ int cafe_sim_restore(cafe_sim *s, const char *path) {
   s->steps = h.steps;
   s->done = h.done != 0;
   s->closed = false;
+  s->pending_layer = false;
   s->output_due = h.output_due != 0;
   s->have_P = false;
   s->full_k2 = true;          // the liquid list is rebuilt by a dense pass
@@ -2260,3 +2289,368 @@ int cafe_sim_growth_log_count(cafe_sim *s, long long *n) {
 }
 
 }  // extern "C"
+
+// ====================================================================== batched steps
+// One launch per step kernel for all realisations of a batch (the kernels of
+// cafe_batch_kernels.cuh), captured once as a CUDA graph and replayed every
+// batch step. The host keeps each realisation's own loop logic (laser state
+// machine, end-of-scan check, layer changes, output points): per batch step it
+// plans every looping realisation's step, uploads all step parameters at once,
+// launches the graph, and reads back every realisation's "some cell at the
+// liquidus" flag and error word at once. Realisations whose step cannot take
+// the graphed path (EASM or Rosenthal field, a dense pass after an upload)
+// take a plain cafe_sim_step on their own stream that batch step. Launch
+// shapes (grid share per realisation, 8-cell chunks of the compaction) are
+// picked by timing candidates on the first batch steps; neither changes any
+// result, so a batched realisation ends bit-identical to its plain run.
+struct CafeBatchEngine {
+  std::vector<cafe_sim *> sims;
+  int n = 0, device = 0, nsm = 1;
+  cudaStream_t stream = nullptr;
+  CafeBatchReal *dR = nullptr;
+  std::vector<CafeBatchReal> hR;
+  std::vector<char> hR_valid;
+  int *dStart = nullptr;
+  int *dActive = nullptr, *hActive = nullptr;
+  CafeStepParams *dP = nullptr, *hP = nullptr;
+  int *dReport = nullptr, *hReport = nullptr;
+  int total[BK_COUNT] = {0};
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  std::vector<cudaEvent_t> ev_plain;
+  int share = 4, chunks = 1;      // launch shape in use
+  bool tuned = false;
+  int tune_steps = 6;             // batch steps timed per candidate
+  std::vector<std::pair<std::pair<int, int>, double>> trials;  // ((share, chunks), ms per batch step)
+  size_t trial = 0;
+  int trial_steps = 0;
+  double trial_ms = 0;
+  long long launches = 0, batch_steps = 0;
+  std::string log;
+};
+
+namespace {
+
+const int kBatchThreads[BK_COUNT] = {32, 256, 256, 256, 256, 32, CAFE_DENSE_THREADS, 1024, CAFE_DENSE_THREADS, 256,
+                                     CAFE_DENSE_THREADS, 1024, CAFE_DENSE_THREADS, 32, 256, 256, 256,
+                                     CAFE_LOOP_THREADS, 256, 256, 256, 32};
+
+// blocks of realisation s in a batched launch of `kind` (its plain graphed
+// step's grid, cafe_sim launch_melt / launch_voxels)
+long long batch_blocks(const cafe_sim *s, int kind) {
+  const long long g = s->gsm;
+  switch (kind) {
+    case BK_MELT: case BK_PBOX0: case BK_PBOX1: return g * 16;
+    case BK_LIST: case BK_PREP: case BK_ORDER: case BK_FINAL: return g * 4;
+    case BK_ACOUNT: case BK_ASCATTER: return std::max<long long>(1, std::min<long long>(s->nblk_act, g * 8));
+    case BK_GATHER: case BK_GEO: case BK_WB: case BK_M2S: return g * 8;
+    case BK_LCOUNT: case BK_LSCATTER: return std::max<long long>(1, s->nblk_pos);
+    default: return 1;  // resets, scans, the event loop, the report
+  }
+}
+
+void batch_set_shape(CafeBatchEngine *E, int gsm, int chunks) {
+  E->share = gsm;
+  E->chunks = chunks;
+  for (cafe_sim *s : E->sims) {
+    s->gsm = gsm;
+    s->act_chunks = chunks;
+    long long per_block = (long long)CAFE_CELLS_PER_BLOCK * chunks;
+    s->nblk_act = (s->K.N + per_block - 1) / per_block;
+  }
+  std::fill(E->hR_valid.begin(), E->hR_valid.end(), 0);
+}
+
+int batch_capture(CafeBatchEngine *E) {
+  if (E->exec) cudaGraphExecDestroy(E->exec);
+  if (E->graph) cudaGraphDestroy(E->graph);
+  E->exec = nullptr;
+  E->graph = nullptr;
+  const int n = E->n;
+  std::vector<int> start((size_t)BK_COUNT * (n + 1));
+  for (int k = 0; k < BK_COUNT; ++k) {
+    long long acc = 0;
+    for (int r = 0; r < n; ++r) {
+      start[(size_t)k * (n + 1) + r] = (int)acc;
+      acc += batch_blocks(E->sims[r], k);
+    }
+    if (acc > 0x7fffffffLL) return fail(CAFE_E_CAPACITY, "batch: too many blocks in one launch");
+    start[(size_t)k * (n + 1) + n] = (int)acc;
+    E->total[k] = (int)acc;
+  }
+  CUDA_TRY(cudaMemcpyAsync(E->dStart, start.data(), start.size() * sizeof(int), cudaMemcpyHostToDevice, E->stream));
+  CafeBatchArgs A;
+  A.R = E->dR;
+  A.start = E->dStart;
+  A.active = E->dActive;
+  A.report = E->dReport;
+  A.n = n;
+  const int *T = kBatchThreads;
+  cudaStream_t st = E->stream;
+  CUDA_TRY(cudaStreamSynchronize(st));
+  CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+  kb_reset_a<<<E->total[BK_RESET_A], T[BK_RESET_A], 0, st>>>(A);
+  kb_melt<<<E->total[BK_MELT], T[BK_MELT], 0, st>>>(A);
+  kb_solid2mushy_pbox0<<<E->total[BK_PBOX0], T[BK_PBOX0], 0, st>>>(A);
+  kb_solid2mushy_pbox1<<<E->total[BK_PBOX1], T[BK_PBOX1], 0, st>>>(A);
+  kb_solid2mushy_list<<<E->total[BK_LIST], T[BK_LIST], 0, st>>>(A);
+  kb_reset_b<<<E->total[BK_RESET_B], T[BK_RESET_B], 0, st>>>(A);
+  kb_active_count<<<E->total[BK_ACOUNT], T[BK_ACOUNT], 0, st>>>(A);
+  kb_scan_blocks<<<E->total[BK_SCAN], T[BK_SCAN], 0, st>>>(A);
+  kb_active_scatter<<<E->total[BK_ASCATTER], T[BK_ASCATTER], 0, st>>>(A);
+  kb_gather<<<E->total[BK_GATHER], T[BK_GATHER], 0, st>>>(A);
+  kb_lists_count<<<E->total[BK_LCOUNT], T[BK_LCOUNT], 0, st>>>(A);
+  kb_scan_pairs<<<E->total[BK_SCANP], T[BK_SCANP], 0, st>>>(A);
+  kb_lists_scatter<<<E->total[BK_LSCATTER], T[BK_LSCATTER], 0, st>>>(A);
+  kb_reset_c<<<E->total[BK_RESET_C], T[BK_RESET_C], 0, st>>>(A);
+  kb_rows_prep<<<E->total[BK_PREP], T[BK_PREP], 0, st>>>(A);
+  kb_rows_geo<<<E->total[BK_GEO], T[BK_GEO], 0, st>>>(A);
+  kb_rows_order<<<E->total[BK_ORDER], T[BK_ORDER], 0, st>>>(A);
+  kb_event_loop<<<E->total[BK_LOOP], T[BK_LOOP], 0, st>>>(A);
+  kb_rows_finalize<<<E->total[BK_FINAL], T[BK_FINAL], 0, st>>>(A);
+  kb_writeback<<<E->total[BK_WB], T[BK_WB], 0, st>>>(A);
+  kb_mushy2solid<<<E->total[BK_M2S], T[BK_M2S], 0, st>>>(A);
+  kb_report<<<E->total[BK_REPORT], T[BK_REPORT], 0, st>>>(A);
+  cudaMemcpyAsync(E->hReport, E->dReport, 2 * (size_t)n * sizeof(int), cudaMemcpyDeviceToHost, st);
+  cudaGraph_t g = nullptr;
+  cudaError_t le = cudaGetLastError();
+  cudaError_t ce = cudaStreamEndCapture(st, &g);
+  if (le != cudaSuccess || ce != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    return fail(CAFE_E_CUDA, "batch graph capture: %s", cudaGetErrorString(le != cudaSuccess ? le : ce));
+  }
+  E->graph = g;
+  CUDA_TRY(cudaGraphInstantiate(&E->exec, g, 0));
+  return CAFE_OK;
+}
+
+// A realisation's step takes the batched path unless it needs the plain one.
+bool batch_eligible(const cafe_sim *s) { return !s->K.easm && !s->full_k2 && !s->timing; }
+
+// The autotuner: candidates (grid share per realisation, compaction chunks)
+// in turn for tune_steps batch steps each, then the fastest.
+int batch_tune_next(CafeBatchEngine *E, double ms) {
+  if (E->tuned) return CAFE_OK;
+  E->trial_ms += ms;
+  if (++E->trial_steps < E->tune_steps) return CAFE_OK;
+  E->trials[E->trial].second = E->trial_ms / E->trial_steps;
+  E->trial_ms = 0;
+  E->trial_steps = 0;
+  ++E->trial;
+  int rc;
+  if (E->trial < E->trials.size()) {
+    batch_set_shape(E, E->trials[E->trial].first.first, E->trials[E->trial].first.second);
+    return batch_capture(E);
+  }
+  size_t best = 0;
+  for (size_t i = 1; i < E->trials.size(); ++i)
+    if (E->trials[i].second < E->trials[best].second) best = i;
+  char buf[256];
+  std::string s = "{\"candidates\": [";
+  for (size_t i = 0; i < E->trials.size(); ++i) {
+    snprintf(buf, sizeof buf, "%s{\"grid_share_sms\": %d, \"compaction_chunks\": %d, \"ms_per_batch_step\": %.4f}",
+             i ? ", " : "", E->trials[i].first.first, E->trials[i].first.second, E->trials[i].second);
+    s += buf;
+  }
+  snprintf(buf, sizeof buf, "], \"chosen\": {\"grid_share_sms\": %d, \"compaction_chunks\": %d}, \"steps_each\": %d}",
+           E->trials[best].first.first, E->trials[best].first.second, E->tune_steps);
+  s += buf;
+  E->log = s;
+  E->tuned = true;
+  batch_set_shape(E, E->trials[best].first.first, E->trials[best].first.second);
+  if ((rc = batch_capture(E))) return rc;
+  return CAFE_OK;
+}
+
+}  // namespace
+
+CafeBatchEngine *cafe_internal_batch_engine_create(cafe_sim *const *sims, int n, int tune, int *rc_out) {
+  CafeBatchEngine *E = new CafeBatchEngine;
+  auto bail = [&](int rc) {
+    *rc_out = rc;
+    return (CafeBatchEngine *)nullptr;
+  };
+  E->sims.assign(sims, sims + n);
+  E->n = n;
+  E->device = sims[0]->device;
+  for (int r = 0; r < n; ++r)
+    if (sims[r]->device != E->device) {
+      delete E;
+      return bail(fail(CAFE_E_ARG, "batch: realisations on different devices"));
+    }
+  int rc = CAFE_OK;
+  auto cu = [&](cudaError_t e, const char *what) {
+    if (e != cudaSuccess && rc == CAFE_OK) rc = fail(CAFE_E_CUDA, "batch: %s: %s", what, cudaGetErrorString(e));
+  };
+  cu(cudaSetDevice(E->device), "cudaSetDevice");
+  E->nsm = sims[0]->nsm;
+  cu(cudaStreamCreateWithFlags(&E->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+  cu(cudaMalloc((void **)&E->dR, (size_t)n * sizeof(CafeBatchReal)), "cudaMalloc");
+  cu(cudaMalloc((void **)&E->dStart, (size_t)BK_COUNT * (n + 1) * sizeof(int)), "cudaMalloc");
+  cu(cudaMalloc((void **)&E->dActive, (size_t)n * sizeof(int)), "cudaMalloc");
+  cu(cudaMalloc((void **)&E->dP, (size_t)n * sizeof(CafeStepParams)), "cudaMalloc");
+  cu(cudaMalloc((void **)&E->dReport, 2 * (size_t)n * sizeof(int)), "cudaMalloc");
+  cu(cudaMallocHost((void **)&E->hActive, (size_t)n * sizeof(int)), "cudaMallocHost");
+  cu(cudaMallocHost((void **)&E->hP, (size_t)n * sizeof(CafeStepParams)), "cudaMallocHost");
+  cu(cudaMallocHost((void **)&E->hReport, 2 * (size_t)n * sizeof(int)), "cudaMallocHost");
+  cu(cudaEventCreate(&E->ev0), "cudaEventCreate");
+  cu(cudaEventCreate(&E->ev1), "cudaEventCreate");
+  E->ev_plain.assign(n, nullptr);
+  for (int r = 0; r < n && rc == CAFE_OK; ++r) cu(cudaEventCreateWithFlags(&E->ev_plain[r], cudaEventDisableTiming), "cudaEventCreate");
+  if (rc) {
+    cafe_internal_batch_engine_destroy(E);
+    return bail(rc);
+  }
+  E->hR.resize(n);
+  E->hR_valid.assign(n, 0);
+  // every realisation reads its step parameters from its slot of dP
+  for (int r = 0; r < n; ++r) {
+    cafe_sim *s = sims[r];
+    cudaStreamSynchronize(s->stream);
+    s->D.Pd = E->dP + r;
+  }
+  const int base = std::max(2, E->nsm / std::max(1, n));
+  if (tune) {
+    for (int g : {base, 2 * base, 4 * base})
+      for (int c : {1, CAFE_ACT_MAX_CHUNKS}) E->trials.push_back({{g, c}, 0.0});
+    batch_set_shape(E, E->trials[0].first.first, E->trials[0].first.second);
+  } else {
+    E->tuned = true;
+    batch_set_shape(E, 2 * base, CAFE_ACT_MAX_CHUNKS);
+    char buf[128];
+    snprintf(buf, sizeof buf, "{\"chosen\": {\"grid_share_sms\": %d, \"compaction_chunks\": %d}, \"tuned\": false}",
+             2 * base, CAFE_ACT_MAX_CHUNKS);
+    E->log = buf;
+  }
+  if ((rc = batch_capture(E))) {
+    cafe_internal_batch_engine_destroy(E);
+    return bail(rc);
+  }
+  *rc_out = CAFE_OK;
+  return E;
+}
+
+void cafe_internal_batch_engine_destroy(CafeBatchEngine *E) {
+  if (!E) return;
+  cudaSetDevice(E->device);
+  if (E->stream) cudaStreamSynchronize(E->stream);
+  if (E->exec) cudaGraphExecDestroy(E->exec);
+  if (E->graph) cudaGraphDestroy(E->graph);
+  if (E->ev0) cudaEventDestroy(E->ev0);
+  if (E->ev1) cudaEventDestroy(E->ev1);
+  for (cudaEvent_t e : E->ev_plain)
+    if (e) cudaEventDestroy(e);
+  cudaFree(E->dR);
+  cudaFree(E->dStart);
+  cudaFree(E->dActive);
+  cudaFree(E->dP);
+  cudaFree(E->dReport);
+  cudaFreeHost(E->hActive);
+  cudaFreeHost(E->hP);
+  cudaFreeHost(E->hReport);
+  if (E->stream) cudaStreamDestroy(E->stream);
+  delete E;
+}
+
+const char *cafe_internal_batch_engine_log(const CafeBatchEngine *E) { return E ? E->log.c_str() : ""; }
+long long cafe_internal_batch_engine_launches(const CafeBatchEngine *E) { return E ? E->launches : 0; }
+long long cafe_internal_batch_engine_steps(const CafeBatchEngine *E) { return E ? E->batch_steps : 0; }
+
+// One batch step for every realisation with phase[r] == 1 (looping); a
+// realisation whose loop ends gets its closing CleanLayer (main1.C:95) and
+// phase 2. *stepped counts the realisations that took a step. Returns the
+// first error (with the realisation in the message).
+int cafe_internal_batch_engine_step(CafeBatchEngine *E, int *phase, long long *steps, int *stepped) {
+  CUDA_TRY(cudaSetDevice(E->device));
+  const int n = E->n;
+  int rc;
+  int nact = 0, nplain = 0;
+  *stepped = 0;
+  // plan: the batched realisations' step parameters; plain steps for the rest
+  for (int r = 0; r < n; ++r) {
+    cafe_sim *s = E->sims[r];
+    E->hActive[r] = 0;
+    if (phase[r] != 1) continue;
+    if (!batch_eligible(s)) {
+      int done = 0;
+      if ((rc = cafe_sim_step(s, &done))) return fail(rc, "realisation %d: %s", r, g_last_error.c_str());
+      ++steps[r];
+      ++*stepped;
+      ++nplain;
+      if (done) {
+        if ((rc = cafe_sim_clean_layer(s))) return fail(rc, "realisation %d: %s", r, g_last_error.c_str());
+        s->closed = true;
+        phase[r] = 2;
+      }
+      CUDA_TRY(cudaEventRecord(E->ev_plain[r], s->stream));
+      CUDA_TRY(cudaStreamWaitEvent(E->stream, E->ev_plain[r], 0));
+      continue;
+    }
+    if (s->pending_layer) {
+      // the last step's AddLayer1, on the handle's stream, before this step
+      if ((rc = apply_pending_layer(s))) return fail(rc, "realisation %d: %s", r, g_last_error.c_str());
+      CUDA_TRY(cudaEventRecord(E->ev_plain[r], s->stream));
+      CUDA_TRY(cudaStreamWaitEvent(E->stream, E->ev_plain[r], 0));
+    }
+    if ((rc = step_plan(s))) return fail(rc, "realisation %d: %s", r, g_last_error.c_str());
+    E->hP[r] = s->P;
+    E->hActive[r] = 1;
+    ++nact;
+    // the realisation's descriptor, uploaded again when a device buffer,
+    // constant or launch shape of it changed (a regrown grain table, say)
+    CafeBatchReal x;
+    std::memset(&x, 0, sizeof x);
+    x.D = s->D;
+    x.K = s->K;
+    x.act_chunks = s->act_chunks;
+    x.allow_fast = s->event_scan ? 0 : 1;
+    x.nblk_act = s->nblk_act;
+    x.nblk_pos = s->nblk_pos;
+    if (!E->hR_valid[r] || std::memcmp(&x, &E->hR[r], sizeof x) != 0) {
+      E->hR[r] = x;
+      E->hR_valid[r] = 1;
+      CUDA_TRY(cudaMemcpyAsync(E->dR + r, &E->hR[r], sizeof x, cudaMemcpyHostToDevice, E->stream));
+    }
+  }
+  (void)nplain;
+  if (nact == 0) return CAFE_OK;
+  CUDA_TRY(cudaMemcpyAsync(E->dP, E->hP, (size_t)n * sizeof(CafeStepParams), cudaMemcpyHostToDevice, E->stream));
+  CUDA_TRY(cudaMemcpyAsync(E->dActive, E->hActive, (size_t)n * sizeof(int), cudaMemcpyHostToDevice, E->stream));
+  CUDA_TRY(cudaEventRecord(E->ev0, E->stream));
+  CUDA_TRY(cudaGraphLaunch(E->exec, E->stream));
+  CUDA_TRY(cudaEventRecord(E->ev1, E->stream));
+  CUDA_TRY(cudaStreamSynchronize(E->stream));
+  E->launches += BK_COUNT;
+  E->batch_steps++;
+  float ms = 0;
+  cudaEventElapsedTime(&ms, E->ev0, E->ev1);
+  // each batched realisation's host side of the step, as cafe_sim_step does it
+  for (int r = 0; r < n; ++r) {
+    if (!E->hActive[r]) continue;
+    cafe_sim *s = E->sims[r];
+    if (E->hReport[2 * r + 1])
+      return fail(CAFE_E_CAPACITY,
+                  "realisation %d: device capacity exceeded (flags 0x%x: 1 active list, 2 frontier rows, 4 grain "
+                  "table, 8 mushy list, 16 event cap)",
+                  r, E->hReport[2 * r + 1]);
+    int hot = E->hReport[2 * r];
+    if ((rc = end_of_scan(s, &hot))) return fail(rc, "realisation %d: %s", r, g_last_error.c_str());
+    voxels_done(s);
+    const bool layer = s->g.inewlayerflg == 1;
+    int done = 0;
+    if ((rc = finish_step(s, &done))) return fail(rc, "realisation %d: %s", r, g_last_error.c_str());
+    ++steps[r];
+    ++*stepped;
+    if (done) {
+      if ((rc = cafe_sim_clean_layer(s))) return fail(rc, "realisation %d: %s", r, g_last_error.c_str());
+      s->closed = true;
+      phase[r] = 2;
+    } else if (layer || s->output_due) {
+      // layer changes and output points queue work on the handle's stream
+      CUDA_TRY(cudaEventRecord(E->ev_plain[r], s->stream));
+      CUDA_TRY(cudaStreamWaitEvent(E->stream, E->ev_plain[r], 0));
+    }
+  }
+  return batch_tune_next(E, ms);
+}

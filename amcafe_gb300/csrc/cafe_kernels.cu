@@ -93,14 +93,14 @@ __device__ __forceinline__ int cafe_moore(const CafeConsts &K, int i, int j, int
 
 // ------------------------------------------------------------------ K: melt
 // Over the box where T may reach the liquidus: SetLiquid3 and BuildjID.
-__global__ void k_melt(CafeDev D, CafeConsts K, const CafeStepParams *__restrict__ Pp) {
+__device__ __forceinline__ void d_melt(const CafeDev &D, const CafeConsts &K, const CafeStepParams *__restrict__ Pp, const int cafe_bid, const int cafe_nblk) {
   const CafeStepParams P = *Pp;
   int bx = P.hi[0] - P.lo[0], by = P.hi[1] - P.lo[1], bz = P.hi[2] - P.lo[2];
   long long nbox = (long long)bx * by * bz;
   long long iz1 = (long long)P.ilaserLoc * K.nxy;
   int any = 0;
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < nbox;
-       t += (long long)gridDim.x * blockDim.x) {
+  for (long long t = cafe_bid * (long long)blockDim.x + threadIdx.x; t < nbox;
+       t += (long long)cafe_nblk * blockDim.x) {
     int i = P.lo[0] + (int)(t % bx);
     long long r = t / bx;
     int j = P.lo[1] + (int)(r % by);
@@ -121,6 +121,9 @@ __global__ void k_melt(CafeDev D, CafeConsts K, const CafeStepParams *__restrict
     }
   }
   if (__syncthreads_or(any) && threadIdx.x == 0) atomicOr(&D.ctr[CTR_HOT], 1);
+}
+__global__ void k_melt(CafeDev D, CafeConsts K, const CafeStepParams *__restrict__ Pp) {
+  d_melt(D, K, Pp, blockIdx.x, gridDim.x);
 }
 
 // ------------------------------------------------------------------ K: solid -> mushy
@@ -148,7 +151,7 @@ __global__ void k_solid2mushy_dense(CafeDev D, CafeConsts K) {
 
 // ConvertSolid1(1) over this step's pool box (which = 0) or the previous one
 // (1), each dilated by one cell, read from the step parameters in device memory.
-__global__ void k_solid2mushy_pbox(CafeDev D, CafeConsts K, const CafeStepParams *__restrict__ Pp, int which) {
+__device__ __forceinline__ void d_solid2mushy_pbox(const CafeDev &D, const CafeConsts &K, const CafeStepParams *__restrict__ Pp, int which, const int cafe_bid, const int cafe_nblk) {
   const int *lo = which ? Pp->plo : Pp->lo, *hi = which ? Pp->phi : Pp->hi;
   int x0 = lo[0], x1 = hi[0], y0 = lo[1], y1 = hi[1], z0 = lo[2], z1 = hi[2];
   if (which && !(x1 > x0 && y1 > y0 && z1 > z0)) return;  // no previous box
@@ -156,8 +159,8 @@ __global__ void k_solid2mushy_pbox(CafeDev D, CafeConsts K, const CafeStepParams
   x1 = min(x1 + 1, K.nx); y1 = min(y1 + 1, K.ny); z1 = min(z1 + 1, K.nz);
   if (x1 <= x0 || y1 <= y0 || z1 <= z0) return;
   long long bx = x1 - x0, by = y1 - y0, nbox = bx * by * (z1 - z0);
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < nbox;
-       t += (long long)gridDim.x * blockDim.x) {
+  for (long long t = cafe_bid * (long long)blockDim.x + threadIdx.x; t < nbox;
+       t += (long long)cafe_nblk * blockDim.x) {
     int i = x0 + (int)(t % bx);
     long long r = t / bx;
     int j = y0 + (int)(r % by), k = z0 + (int)(r / by);
@@ -170,15 +173,18 @@ __global__ void k_solid2mushy_pbox(CafeDev D, CafeConsts K, const CafeStepParams
     if (liq) D.state[idx] = 2;
   }
 }
+__global__ void k_solid2mushy_pbox(CafeDev D, CafeConsts K, const CafeStepParams *__restrict__ Pp, int which) {
+  d_solid2mushy_pbox(D, K, Pp, which, blockIdx.x, gridDim.x);
+}
 
 // The step parameters into device memory (kernel arguments are copied at
 // launch, so the host copy may change right after).
 __global__ void k_put_params(CafeStepParams *Pd, CafeStepParams P) { *Pd = P; }
 
 
-__global__ void k_solid2mushy_list(CafeDev D, CafeConsts K) {
+__device__ __forceinline__ void d_solid2mushy_list(const CafeDev &D, const CafeConsts &K, const int cafe_bid, const int cafe_nblk) {
   int n = D.ctr[CTR_NLIQ];
-  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+  for (int t = cafe_bid * blockDim.x + threadIdx.x; t < n; t += cafe_nblk * blockDim.x) {
     long long idx = D.liq[t];
     if (D.state[idx] != 1) continue;
     int i, j, k;
@@ -188,6 +194,9 @@ __global__ void k_solid2mushy_list(CafeDev D, CafeConsts K) {
     for (int a = 0; a < m; ++a)
       if (D.state[nb[a]] == 3) D.state[nb[a]] = 2;
   }
+}
+__global__ void k_solid2mushy_list(CafeDev D, CafeConsts K) {
+  d_solid2mushy_list(D, K, blockIdx.x, gridDim.x);
 }
 
 // ------------------------------------------------------------------ active set
@@ -301,14 +310,13 @@ __device__ __forceinline__ uint32_t cafe_thread_active(const CafeDev &D, const C
 // `chunks` 8-cell chunks (nvb of them cover the grid); a persistent grid
 // strides over them, writes a zero count for those outside the active range
 // (cafe_active_range) without touching their cells, and counts the rest.
-__global__ void k_active_count(CafeDev D, CafeConsts K, const CafeStepParams *__restrict__ Pp, int chunks,
-                               long long nvb) {
+__device__ __forceinline__ void d_active_count(const CafeDev &D, const CafeConsts &K, const CafeStepParams *__restrict__ Pp, int chunks, long long nvb, const int cafe_bid, const int cafe_nblk) {
   const CafeStepParams P = *Pp;
   __shared__ int wsum[CAFE_DENSE_THREADS / 32];
   long long r0, r1;
   cafe_active_range(D, K, P, r0, r1);
   const long long per_vb = (long long)CAFE_DENSE_THREADS * CAFE_CELLS_PER_THREAD * chunks;
-  for (long long vb = blockIdx.x; vb < nvb; vb += gridDim.x) {
+  for (long long vb = cafe_bid; vb < nvb; vb += cafe_nblk) {
     long long b0 = vb * per_vb;
     if (b0 >= r1 || b0 + per_vb <= r0) {
       if (threadIdx.x == 0) D.blk[vb] = 0;
@@ -329,9 +337,12 @@ __global__ void k_active_count(CafeDev D, CafeConsts K, const CafeStepParams *__
     __syncthreads();
   }
 }
+__global__ void k_active_count(CafeDev D, CafeConsts K, const CafeStepParams *__restrict__ Pp, int chunks, long long nvb) {
+  d_active_count(D, K, Pp, chunks, nvb, blockIdx.x, gridDim.x);
+}
 
 // Exclusive scan of n block counts in place; writes the total to *total.
-__global__ void k_scan_blocks(int32_t *blk, long long n, int *total) {
+__device__ __forceinline__ void d_scan_blocks(int32_t *blk, long long n, int *total, const int cafe_bid, const int cafe_nblk) {
   __shared__ long long part[1024];
   long long per = (n + blockDim.x - 1) / blockDim.x;
   long long b0 = threadIdx.x * per, b1 = b0 + per < n ? b0 + per : n;
@@ -357,9 +368,11 @@ __global__ void k_scan_blocks(int32_t *blk, long long n, int *total) {
     acc += v;
   }
 }
+__global__ void k_scan_blocks(int32_t *blk, long long n, int *total) {
+  d_scan_blocks(blk, n, total, blockIdx.x, gridDim.x);
+}
 
-__global__ void k_active_scatter(CafeDev D, CafeConsts K, const CafeStepParams *__restrict__ Pp, int chunks,
-                                 long long nvb) {
+__device__ __forceinline__ void d_active_scatter(const CafeDev &D, const CafeConsts &K, const CafeStepParams *__restrict__ Pp, int chunks, long long nvb, const int cafe_bid, const int cafe_nblk) {
   const CafeStepParams P = *Pp;
   __shared__ int wsum[CAFE_DENSE_THREADS / 32];
   long long r0, r1;
@@ -367,7 +380,7 @@ __global__ void k_active_scatter(CafeDev D, CafeConsts K, const CafeStepParams *
   const long long per_vb = (long long)CAFE_DENSE_THREADS * CAFE_CELLS_PER_THREAD * chunks;
   long long vb_lo = r0 / per_vb, vb_hi = r1 > 0 ? (r1 - 1) / per_vb : -1;
   if (vb_hi >= nvb) vb_hi = nvb - 1;
-  for (long long vb = vb_lo + blockIdx.x; vb <= vb_hi; vb += gridDim.x) {
+  for (long long vb = vb_lo + cafe_bid; vb <= vb_hi; vb += cafe_nblk) {
   long long base = vb * per_vb + (long long)threadIdx.x * (CAFE_CELLS_PER_THREAD * chunks);
   const uint32_t flags = D.act_flags[vb * CAFE_DENSE_THREADS + threadIdx.x];  // from k_active_count
   const int cnt = __popc(flags);
@@ -405,22 +418,25 @@ __global__ void k_active_scatter(CafeDev D, CafeConsts K, const CafeStepParams *
   __syncthreads();  // wsum is reused by the next virtual block
   }
 }
+__global__ void k_active_scatter(CafeDev D, CafeConsts K, const CafeStepParams *__restrict__ Pp, int chunks, long long nvb) {
+  d_active_scatter(D, K, Pp, chunks, nvb, blockIdx.x, gridDim.x);
+}
 
 // ------------------------------------------------------------------ gather
 // Per active position: copies of the cell data, temperature class, neighbour
 // positions in ascending index order (-1 = not active), liquid-neighbour count,
 // all-neighbours-below-liquidus flag and the ruq offset (VoxelsCA.C:380:
 // ruq[p] = (U_p - .5) dX / 100, U_p the p-th uniform of minstd(30 tInd + seed1)).
-__global__ void k_gather(CafeDev D, CafeConsts K, const CafeStepParams *__restrict__ Pp) {
+__device__ __forceinline__ void d_gather(const CafeDev &D, const CafeConsts &K, const CafeStepParams *__restrict__ Pp, const int cafe_bid, const int cafe_nblk) {
   const CafeStepParams P = *Pp;
   int na = D.ctr[CTR_NA];
   if (na > D.act_cap) na = (int)D.act_cap;
   uint32_t seed = cafe_minstd_seed((uint64_t)(uint32_t)(30 * P.tInd + (int)K.seed1));
-  if (blockIdx.x == 0 && threadIdx.x == 0) {  // rebuilt by k_writeback for the next step
+  if (cafe_bid == 0 && threadIdx.x == 0) {  // rebuilt by k_writeback for the next step
     D.ctr[CTR_ZLO] = 0x7fffffff;
     D.ctr[CTR_ZHI] = -1;
   }
-  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < na; p += gridDim.x * blockDim.x) {
+  for (int p = cafe_bid * blockDim.x + threadIdx.x; p < na; p += cafe_nblk * blockDim.x) {
     long long idx = D.act[p];
     int i, j, k;
     cafe_cell_xyz(K, idx, i, j, k);
@@ -457,16 +473,19 @@ __global__ void k_gather(CafeDev D, CafeConsts K, const CafeStepParams *__restri
     D.a_ruq[p] = (U - .5) * K.ruq_dx / 100.;
   }
 }
+__global__ void k_gather(CafeDev D, CafeConsts K, const CafeStepParams *__restrict__ Pp) {
+  d_gather(D, K, Pp, blockIdx.x, gridDim.x);
+}
 
 // ------------------------------------------------------------------ vs2ind + frontier rows
 // Two order-preserving compactions over positions: mushy positions (vs2ind,
 // VoxelsCA.C:346-353) and, among them, those with a liquid neighbour and no
 // neighbour at the liquidus (the cells that can capture, VoxelsCA.C:396-397).
-__global__ void k_lists_count(CafeDev D) {
+__device__ __forceinline__ void d_lists_count(const CafeDev &D, const int cafe_bid, const int cafe_nblk) {
   __shared__ int ws[2][CAFE_DENSE_THREADS / 32];
   int na = D.ctr[CTR_NA];
   if (na > D.act_cap) na = (int)D.act_cap;
-  long long base = ((long long)blockIdx.x * blockDim.x + threadIdx.x) * CAFE_CELLS_PER_THREAD;
+  long long base = ((long long)cafe_bid * blockDim.x + threadIdx.x) * CAFE_CELLS_PER_THREAD;
   int c2 = 0, cf = 0;
   for (int c = 0; c < CAFE_CELLS_PER_THREAD; ++c) {
     long long p = base + c;
@@ -491,15 +510,18 @@ __global__ void k_lists_count(CafeDev D) {
       s2 += ws[0][w];
       sf += ws[1][w];
     }
-    D.blk[2 * blockIdx.x] = s2;
-    D.blk[2 * blockIdx.x + 1] = sf;
+    D.blk[2 * cafe_bid] = s2;
+    D.blk[2 * cafe_bid + 1] = sf;
   }
+}
+__global__ void k_lists_count(CafeDev D) {
+  d_lists_count(D, blockIdx.x, gridDim.x);
 }
 
 // Exclusive scan of interleaved pairs (blk[2b], blk[2b+1]), b < n, one block.
 // Exclusive scan of the (mushy, frontier) count pairs of the position blocks
 // that hold active positions (na from *na_ptr); totals to *tot0, *tot1.
-__global__ void k_scan_pairs(int32_t *blk, long long n, const int *na_ptr, int *tot0, int *tot1) {
+__device__ __forceinline__ void d_scan_pairs(int32_t *blk, long long n, const int *na_ptr, int *tot0, int *tot1, const int cafe_bid, const int cafe_nblk) {
   __shared__ long long part[2][1024];
   {
     long long used = ((long long)*na_ptr + CAFE_CELLS_PER_BLOCK - 1) / CAFE_CELLS_PER_BLOCK;
@@ -538,12 +560,15 @@ __global__ void k_scan_pairs(int32_t *blk, long long n, const int *na_ptr, int *
     a1 += v1;
   }
 }
+__global__ void k_scan_pairs(int32_t *blk, long long n, const int *na_ptr, int *tot0, int *tot1) {
+  d_scan_pairs(blk, n, na_ptr, tot0, tot1, blockIdx.x, gridDim.x);
+}
 
-__global__ void k_lists_scatter(CafeDev D) {
+__device__ __forceinline__ void d_lists_scatter(const CafeDev &D, const int cafe_bid, const int cafe_nblk) {
   __shared__ int ws[2][CAFE_DENSE_THREADS / 32];
   int na = D.ctr[CTR_NA];
   if (na > D.act_cap) na = (int)D.act_cap;
-  long long base = ((long long)blockIdx.x * blockDim.x + threadIdx.x) * CAFE_CELLS_PER_THREAD;
+  long long base = ((long long)cafe_bid * blockDim.x + threadIdx.x) * CAFE_CELLS_PER_THREAD;
   int c2 = 0, cf = 0;
   for (int c = 0; c < CAFE_CELLS_PER_THREAD; ++c) {
     long long p = base + c;
@@ -578,8 +603,8 @@ __global__ void k_lists_scatter(CafeDev D) {
     }
   }
   __syncthreads();
-  long long j2 = (long long)D.blk[2 * blockIdx.x] + ws[0][w] + (i2 - c2);
-  long long jf = (long long)D.blk[2 * blockIdx.x + 1] + ws[1][w] + (i_f - cf);
+  long long j2 = (long long)D.blk[2 * cafe_bid] + ws[0][w] + (i2 - c2);
+  long long jf = (long long)D.blk[2 * cafe_bid + 1] + ws[1][w] + (i_f - cf);
   for (int c = 0; c < CAFE_CELLS_PER_THREAD; ++c) {
     long long p = base + c;
     if (p >= na) break;
@@ -601,6 +626,9 @@ __global__ void k_lists_scatter(CafeDev D) {
     }
     ++j2;
   }
+}
+__global__ void k_lists_scatter(CafeDev D) {
+  d_lists_scatter(D, blockIdx.x, gridDim.x);
 }
 
 // ------------------------------------------------------------------ frontier rows
@@ -1120,11 +1148,11 @@ __device__ __forceinline__ void cafe_row_eval(const CafeDev &D, const CafeConsts
 // k_rows_geo evaluates the listed pairs; k_rows_order (one warp per row)
 // orders each row's slots and, when every row grows with the same velocity,
 // takes its exact best candidate and key.
-__global__ void k_rows_prep(CafeDev D, CafeConsts K) {
+__device__ __forceinline__ void d_rows_prep(const CafeDev &D, const CafeConsts &K, const int cafe_bid, const int cafe_nblk) {
   int nrows = D.ctr[CTR_NROWS];
   if (nrows > D.row_cap) nrows = (int)D.row_cap;
-  const int warps = (gridDim.x * blockDim.x) >> 5;
-  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int warps = (cafe_nblk * blockDim.x) >> 5;
+  const int w = (cafe_bid * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   const unsigned FULL = 0xffffffffu;
   const double V = K.vhat_cls[1];
@@ -1149,12 +1177,15 @@ __global__ void k_rows_prep(CafeDev D, CafeConsts K) {
     }
   }
 }
+__global__ void k_rows_prep(CafeDev D, CafeConsts K) {
+  d_rows_prep(D, K, blockIdx.x, gridDim.x);
+}
 
-__global__ void k_rows_geo(CafeDev D, CafeConsts K) {
+__device__ __forceinline__ void d_rows_geo(const CafeDev &D, const CafeConsts &K, const int cafe_bid, const int cafe_nblk) {
   int n = D.ctr[CTR_NPAIRS];
   const long long cap = D.row_cap * CAFE_NSLOT;
   if (n > cap) n = (int)cap;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+  for (int i = cafe_bid * blockDim.x + threadIdx.x; i < n; i += cafe_nblk * blockDim.x) {
     int v = D.row_pairs[i];
     int r = v >> 5, sl = v & 31;
     int p = D.row_pos[r];
@@ -1177,12 +1208,15 @@ __global__ void k_rows_geo(CafeDev D, CafeConsts K) {
     og[3] = cn[2];
   }
 }
+__global__ void k_rows_geo(CafeDev D, CafeConsts K) {
+  d_rows_geo(D, K, blockIdx.x, gridDim.x);
+}
 
-__global__ void k_rows_order(CafeDev D, CafeConsts K) {
+__device__ __forceinline__ void d_rows_order(const CafeDev &D, const CafeConsts &K, const int cafe_bid, const int cafe_nblk) {
   int nrows = D.ctr[CTR_NROWS];
   if (nrows > D.row_cap) nrows = (int)D.row_cap;
-  const int warps = (gridDim.x * blockDim.x) >> 5;
-  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int warps = (cafe_nblk * blockDim.x) >> 5;
+  const int w = (cafe_bid * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   for (int r = w; r < nrows; r += warps) {
     int p = D.row_pos[r];
@@ -1197,6 +1231,9 @@ __global__ void k_rows_order(CafeDev D, CafeConsts K) {
     }
     cafe_row_finish_warp(D, K, r, p, nn, liv, gv, q, true, 0, 0.0);
   }
+}
+__global__ void k_rows_order(CafeDev D, CafeConsts K) {
+  d_rows_order(D, K, blockIdx.x, gridDim.x);
 }
 
 // ---- event selection by a group of warps ------------------------------------
@@ -1463,8 +1500,7 @@ __device__ void cafe_select_keyed(const CafeDev &D, const CafeConsts &K, int ev,
 // thread 0 merges the two. Exact mode (the reference's per-event scan of every
 // row, also the fallback when the rows stop sharing one velocity) evaluates
 // every row at every event.
-__global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
-    k_event_loop(CafeDev D, CafeConsts K, const CafeStepParams *__restrict__ Pp, long long max_events, int allow_fast) {
+__device__ __forceinline__ void d_event_loop(const CafeDev &D, const CafeConsts &K, const CafeStepParams *__restrict__ Pp, long long max_events, int allow_fast, const int cafe_bid, const int cafe_nblk) {
   const CafeStepParams P = *Pp;
   constexpr int NSEL = CAFE_LOOP_THREADS - CAFE_QUAD_THREADS;  // threads of the selecting warps
   __shared__ CafeCand red[CAFE_LOOP_THREADS / 32];
@@ -2031,26 +2067,33 @@ __global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
   }
 #undef CAFE_DCYC
 }
+__global__ void __launch_bounds__(CAFE_LOOP_THREADS, 1)
+    k_event_loop(CafeDev D, CafeConsts K, const CafeStepParams *__restrict__ Pp, long long max_events, int allow_fast) {
+  d_event_loop(D, K, Pp, max_events, allow_fast, blockIdx.x, gridDim.x);
+}
 
 // Brings every row's extent up to the end of the step (the lazily applied
 // growth of VoxelsCA.C:511-516), spread over the whole GPU, and copies it back
 // to the row cell's active-list position.
-__global__ void k_rows_finalize(CafeDev D) {
+__device__ __forceinline__ void d_rows_finalize(const CafeDev &D, const int cafe_bid, const int cafe_nblk) {
   int nrows = D.ctr[CTR_NROWS_END];
   if (nrows > D.row_cap) nrows = (int)D.row_cap;
   int nev = D.ctr[CTR_NEV];
-  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < nrows; r += gridDim.x * blockDim.x) {
+  for (int r = cafe_bid * blockDim.x + threadIdx.x; r < nrows; r += cafe_nblk * blockDim.x) {
     cafe_row_replay(D, r, nev);
     D.a_ext[D.row_pos[r]] = D.row_E[r];
   }
 }
+__global__ void k_rows_finalize(CafeDev D) {
+  d_rows_finalize(D, blockIdx.x, gridDim.x);
+}
 
 // ------------------------------------------------------------------ write back
-__global__ void k_writeback(CafeDev D, CafeConsts K) {
+__device__ __forceinline__ void d_writeback(const CafeDev &D, const CafeConsts &K, const int cafe_bid, const int cafe_nblk) {
   int na = D.ctr[CTR_NA];
   if (na > D.act_cap) na = (int)D.act_cap;
   int zlo = 0x7fffffff, zhi = -1;
-  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < na; p += gridDim.x * blockDim.x) {
+  for (int p = cafe_bid * blockDim.x + threadIdx.x; p < na; p += cafe_nblk * blockDim.x) {
     long long idx = D.act[p];
     if (D.a_state[p] == 1 || D.a_state[p] == 2) {
       int k = (int)(idx / K.nxy);
@@ -2078,14 +2121,17 @@ __global__ void k_writeback(CafeDev D, CafeConsts K) {
     atomicMax(&D.ctr[CTR_ZHI], zhi);
   }
 }
+__global__ void k_writeback(CafeDev D, CafeConsts K) {
+  d_writeback(D, K, blockIdx.x, gridDim.x);
+}
 
 // ConvertSolid1(0): mushy cells whose neighbours are all mushy or solid become
 // solid with zero extent. Every mushy cell is in this step's active list. In
 // place is equivalent to collect-then-apply: 2 -> 3 keeps "neighbour >= 2".
-__global__ void k_mushy2solid(CafeDev D, CafeConsts K) {
+__device__ __forceinline__ void d_mushy2solid(const CafeDev &D, const CafeConsts &K, const int cafe_bid, const int cafe_nblk) {
   int na = D.ctr[CTR_NA];
   if (na > D.act_cap) na = (int)D.act_cap;
-  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < na; p += gridDim.x * blockDim.x) {
+  for (int p = cafe_bid * blockDim.x + threadIdx.x; p < na; p += cafe_nblk * blockDim.x) {
     if (D.a_state[p] != 2) continue;
     long long idx = D.act[p];
     int i, j, k;
@@ -2099,6 +2145,9 @@ __global__ void k_mushy2solid(CafeDev D, CafeConsts K) {
       D.ext[idx] = 0.0;
     }
   }
+}
+__global__ void k_mushy2solid(CafeDev D, CafeConsts K) {
+  d_mushy2solid(D, K, blockIdx.x, gridDim.x);
 }
 
 // ------------------------------------------------------------------ grains

@@ -187,6 +187,15 @@ def committed_traffic(workload, phase):
         return None
 
 
+def committed_traffic_source(workload):
+    """Where the committed figures of `workload` come from: the capture's
+    command, the commit it measured and its date (profiles/traffic.json)."""
+    src = committed_traffic(workload, "_source")
+    if src is None:
+        return None
+    return dict(src, note="from a committed ncu capture, not measured in this run")
+
+
 def cpu_baseline(deck, info, state, ctheta, nvox, seconds):
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import cafe_oracle as orc
@@ -731,6 +740,7 @@ def main():
     else:
         roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                     "frac": achieved / peak, "traffic": committed_traffic(args.workload, dom),
+                    "traffic_source": committed_traffic_source(args.workload),
                     "kernel": {"events": "k_event_loop", "classify": "k_active_count/k_active_scatter",
                                "gather": "k_gather", "melt": "k_melt", "writeback": "k_writeback"}.get(dom, dom),
                     "phase": dom, "peak_source": peak_src,

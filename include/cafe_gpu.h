@@ -54,7 +54,12 @@ typedef struct {
   int tf_tInd;     /* TempField::tInd of the last step (main1.C:64) */
   int output_due;  /* 1 when the last cafe_sim_step reached an output point of
                       main1.C:77-78 (it called SetBuild there; the reference
-                      writes WriteToHDF1("<base>" + tf_tInd) at this point) */
+                      writes WriteToHDF1("<base>" + tf_tInd) at this point).
+                      When that point is also a layer change, the step's
+                      AddLayer1 (main1.C:88) waits until the next
+                      cafe_sim_step, cafe_sim_run, cafe_sim_clean_layer or
+                      cafe_sim_checkpoint, so that the state read or written
+                      now is the one main1.C writes */
 } cafe_info;
 
 typedef struct {
@@ -260,11 +265,17 @@ int cafe_adjoint_growth(const cafe_adjoint_setup *setup, const double theta[5], 
 
 /* Batched ensemble (no counterpart in the reference, which runs one
  * realisation per MPI job): n independent realisations, one deck each, on
- * one device. Each is a cafe_sim handle with its own stream; `threads` host
- * threads (0: one) step them round-robin so that their device work overlaps
- * (with one thread each step is a CUDA graph launch). Every realisation runs exactly the calls of
- * a plain run (initialize_voxels, begin, step until done, the closing
- * clean_layer), so its results are bit-identical to its plain run. */
+ * one device, each a cafe_sim handle. threads <= 0 (the default): batched
+ * launches, every step kernel launched once for all realisations (the event
+ * loop one thread block per realisation), the launches of a batch step one
+ * CUDA graph replayed every batch step, launch shapes chosen by timing
+ * candidates on the first batch steps (cafe_batch_report gives the choice);
+ * a realisation whose step cannot take the graphed path (EASM or Rosenthal
+ * field) takes its plain step that batch step. threads >= 1: the realisations
+ * step round-robin on their own streams from that many host threads. Either
+ * way every realisation runs exactly the calls of a plain run
+ * (initialize_voxels, begin, step until done, the closing clean_layer), so
+ * its results are bit-identical to its plain run. */
 typedef struct cafe_batch cafe_batch;
 int cafe_batch_create(const char *const *decks, int n, const cafe_options *opt, int threads, cafe_batch **out);
 /* Initialises every realisation that is new and runs each loop to its end, or
@@ -276,6 +287,10 @@ int cafe_batch_size(const cafe_batch *b);
 cafe_sim *cafe_batch_sim(cafe_batch *b, int i);
 /* 1 when realisation i has finished its loop (closing CleanLayer applied). */
 int cafe_batch_finished(const cafe_batch *b, int i);
+/* Batched launches: kernels launched and batch steps taken so far, and the
+ * autotuner's candidates and choice as a JSON object (empty for the
+ * round-robin engine or before the first run); tuning may be NULL. */
+int cafe_batch_report(const cafe_batch *b, long long *launches, long long *batch_steps, char *tuning, int cap);
 void cafe_batch_destroy(cafe_batch *b);
 
 /* Allocation-free CleanLayer renumbering on caller-owned device arrays. No
