@@ -59,34 +59,41 @@ def test_config1_windows_match_oracle():
     sim.close()
 
 
-def test_config1_window_across_the_first_layer_change():
+def test_config1_window_across_the_first_layer_change(tmp_path):
     """The oracle and the GPU both step through config 1's first layer change
     (UpdateLaser wraps to the next layer, CleanLayer renumbers the grains,
     AddLayer1 draws the new layer's Voronoi sites and orientations from
-    genlayer, main1.C:75-88) from the same state a few steps before it."""
+    genlayer, main1.C:75-88) from the same state a few steps before it. The
+    step of the change is found by running in chunks from checkpoints."""
     from amcafe_gb300 import Simulation
 
-    chunk = 10
+    chunk = 1000
+    ck = str(tmp_path / "c1.ckpt")
     sim = Simulation(C1, device=0)
     sim.InitializeVoxels()
     sim.begin()
     layer0 = sim.info()["indlayer"]
-    done = 0
-    while sim.info()["indlayer"] == layer0:
-        assert done < 40000, "no layer change in config 1's first 40,000 steps"
+    start = 0
+    while True:
+        sim.checkpoint(ck)
         sim.run(chunk)
-        done += chunk
-    sim.close()
-    # the change happened within steps done-chunk+1 .. done
-    sim = Simulation(C1, device=0)
-    sim.InitializeVoxels()
-    sim.begin()
-    start = done - chunk - 2
-    sim.run(start)
+        if sim.info()["indlayer"] != layer0:
+            break
+        start += chunk
+        assert start < 40000, "no layer change in config 1's first 40,000 steps"
+    # back to the chunk's start, find the step that changes the layer
+    sim.restore(ck)
+    k = start
+    while sim.info()["indlayer"] == layer0:
+        sim.step()
+        k += 1
+    # and back again, to four steps before it
+    sim.restore(ck)
+    if k - 4 > start:
+        sim.run(k - 4 - start)
     assert sim.info()["indlayer"] == layer0
     ng0 = sim.info()["nGrain"]
-    _compare_window(sim, "config 1, steps %d-%d (first layer change)" % (start + 1, start + chunk + 4),
-                    n=chunk + 4)
+    _compare_window(sim, "config 1, steps %d-%d (layer change at step %d)" % (k - 3, k + 4, k), n=8)
     info = sim.info()
     assert info["indlayer"] == layer0 + 1
     assert info["nGrain"] != ng0
