@@ -67,7 +67,7 @@ def test_config1_window_across_the_first_layer_change(tmp_path):
     step of the change is found by running in chunks from checkpoints."""
     from amcafe_gb300 import Simulation
 
-    chunk = 1000
+    chunk = 3000
     ck = str(tmp_path / "c1.ckpt")
     sim = Simulation(C1, device=0)
     sim.InitializeVoxels()
