@@ -27,6 +27,17 @@ enum {
   CAFE_ERR_GRAIN_CAP = 4,
   CAFE_ERR_MUSHY_CAP = 8,
   CAFE_ERR_ITER_CAP = 16,
+  CAFE_ERR_SYNC = 32,  // a bounded wait between the event loop's two blocks ran out
+};
+
+// The new-row fill that the event loop's main block hands to its helper
+// block (k_event_loop with two blocks): the row, the captured cell's active
+// position, the event, the cell's grain, centre and extent, the time, and
+// the helper's result (the order key of the row's largest |g|).
+struct CafeFillReq {
+  int r, p, e, gid;
+  double c[3], ext, T;
+  unsigned long long gk;
 };
 
 // Scalars that change every step (computed on the host from Grid/TempField).
@@ -172,6 +183,10 @@ struct CafeDev {
   // scan scratch
   int32_t *blk;       // per-block counts / offsets
   long long blk_cap;
+  // the event loop's fill hand-off: the request, and two sequence numbers
+  // (posted by the main block, done by the helper; zeroed before each launch)
+  CafeFillReq *fill;
+  int *fill_seq;
   // device scalars
   int *ctr;           // see CTR_* below
   int *err;

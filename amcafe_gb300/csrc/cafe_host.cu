@@ -423,6 +423,7 @@ struct cafe_sim {
   int prev_lo[3] = {0, 0, 0}, prev_hi[3] = {0, 0, 0};
   bool full_k2 = false;   // next solid->mushy pass must scan the whole box
   int event_scan = 0;     // 1: evaluate every frontier row at every event
+  bool event_helper = true;  // the event loop's new-row fills run in a second block
   std::vector<void *> owned;
   int *h_pinned = nullptr;  // pinned host mirror of ctr + err
   // staging for host transfers (allocated on first use)
@@ -521,7 +522,8 @@ int sim_sync(cafe_sim *s) {
   if (err) {
     return fail(CAFE_E_CAPACITY,
                 "device capacity exceeded (flags 0x%x: 1 active list, 2 frontier rows, 4 grain "
-                "table, 8 mushy list, 16 event cap); recreate with larger capacities",
+                "table, 8 mushy list, 16 event cap; 32: the event loop's two blocks timed out "
+                "waiting for each other); recreate with larger capacities",
                 err);
   }
   return CAFE_OK;
@@ -830,6 +832,34 @@ int end_of_scan(cafe_sim *s, const int *hot_known = nullptr) {
   return CAFE_OK;
 }
 
+// The event loop: one block, or with the fill helper two blocks launched
+// cooperatively (both resident at once, which the hand-off between them
+// needs). The hand-off's sequence words start at zero.
+int launch_event_loop(cafe_sim *s, const CafeStepParams *Pp) {
+  cudaStream_t st = s->stream;
+  const CafeDev &D = s->D;
+  const long long max_ev = D.act_cap + 1;
+  const int allow_fast = s->event_scan ? 0 : 1;
+  if (!s->event_helper) {
+    k_event_loop<<<1, CAFE_LOOP_THREADS, 0, st>>>(s->D, s->K, Pp, max_ev, allow_fast);
+    CUDA_TRY(cudaGetLastError());
+    return CAFE_OK;
+  }
+  CUDA_TRY(cudaMemsetAsync(D.fill_seq, 0, 2 * sizeof(int), st));
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(2);
+  cfg.blockDim = dim3(CAFE_LOOP_THREADS);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  CUDA_TRY(cudaLaunchKernelEx(&cfg, k_event_loop, s->D, s->K, Pp, max_ev, allow_fast));
+  return CAFE_OK;
+}
+
 // VoxelsCA::UpdateVoxels on the device (no host synchronisation). In a graph
 // the box kernels get fixed grids and read their boxes from the parameters.
 int launch_voxels(cafe_sim *s, bool graph, const CafeStepParams *Pp) {
@@ -883,7 +913,8 @@ int launch_voxels(cafe_sim *s, bool graph, const CafeStepParams *Pp) {
   }
   {
     PhaseScope ps(s, CAFE_PH_EVENTS);
-    k_event_loop<<<1, CAFE_LOOP_THREADS, 0, st>>>(D, K, Pp, D.act_cap + 1, s->event_scan ? 0 : 1);
+    int rc = launch_event_loop(s, Pp);
+    if (rc) return rc;
     if (D.glog_cell) {
       k_glog_begin<<<s->gsm * 4, 256, 0, st>>>(D, Pp);
       LAUNCHED(CAFE_PH_EVENTS, 1);
@@ -1030,12 +1061,18 @@ int cafe_sim_create(const char *deck_path, const cafe_options *opt, cafe_sim **o
   GridH &g = s->g;
   s->device = opt ? opt->device : 0;
   s->event_scan = opt ? opt->event_scan : 0;
+  s->event_helper = !(opt && opt->event_single_block);
   cudaError_t ce = cudaSetDevice(s->device);
   if (ce != cudaSuccess) {
     delete s;
     return fail(CAFE_E_CUDA, "cudaSetDevice(%d): %s", opt ? opt->device : 0, cudaGetErrorString(ce));
   }
   cudaDeviceGetAttribute(&s->nsm, cudaDevAttrMultiProcessorCount, s->device);
+  {
+    int coop = 0;
+    cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, s->device);
+    if (!coop || s->nsm < 2) s->event_helper = false;
+  }
   s->gsm = s->nsm;
   if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) {
     delete s;
@@ -1213,7 +1250,7 @@ int cafe_sim_create(const char *deck_path, const cafe_options *opt, cafe_sim **o
       (rc = dalloc(&D.row_bt, D.row_cap, o)) ||
       (rc = dalloc(&D.row_bruq, D.row_cap, o)) ||
       (rc = dalloc(&D.ctr, CTR_COUNT, o)) || (rc = dalloc(&D.err, 1, o)) || (rc = dalloc(&D.stat, STAT_COUNT, o)) ||
-      (rc = dalloc(&D.Pd, 1, o)) ||
+      (rc = dalloc(&D.Pd, 1, o)) || (rc = dalloc(&D.fill, 1, o)) || (rc = dalloc(&D.fill_seq, 2, o)) ||
       (rc = dalloc(&D.act_flags, (size_t)((N + CAFE_CELLS_PER_BLOCK - 1) / CAFE_CELLS_PER_BLOCK) * CAFE_DENSE_THREADS, o)) || (rc = dalloc(&D.tcls, std::max<long long>(D.tcls_cap, 1), o)) ||
       (K.easm && ((rc = dalloc(&D.temp, N, o)) || (rc = dalloc(&D.a_vh, acap, o)) ||
                   (rc = dalloc(&D.easm_q, (size_t)(D.easm_qcap = std::min<long long>(N, 1LL << 21)), o))))) {

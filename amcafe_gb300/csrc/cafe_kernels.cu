@@ -1500,6 +1500,76 @@ __device__ void cafe_select_keyed(const CafeDev &D, const CafeConsts &K, int ev,
 // thread 0 merges the two. Exact mode (the reference's per-event scan of every
 // row, also the fallback when the rows stop sharing one velocity) evaluates
 // every row at every event.
+// ---- the fill helper: a second block of the event loop -----------------------
+// A warp issues one FP64 instruction per ~64 cycles and each SM sub-partition
+// completes one FP64 warp-instruction per ~64 cycles, so the new row's fill
+// (its four warps' chains, ~20k cycles) saturates the FP64 pipes of the SM it
+// runs on and slows the next event's selection there. With two blocks
+// (cooperative launch: both resident), the main block posts the fill of each
+// new row as soon as the event's winner is known, and the helper block, on
+// another SM, fills the row while the main block applies the capture and
+// selects the next event; the main block takes the result at the merge.
+// Both sides wait with a wall-clock limit; a wait that runs out sets
+// CAFE_ERR_SYNC and ends the step.
+#define CAFE_SYNC_WAIT_NS 2000000000ULL
+__device__ __forceinline__ unsigned long long cafe_globaltimer() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+__device__ __forceinline__ int cafe_ld_acquire(const int *p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void cafe_st_release(int *p, int v) {
+  asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+// Thread 0: waits until *p != last (or == want when want >= 0); returns the
+// value seen, or INT_MIN when the wait ran out (error bit set).
+__device__ __forceinline__ int cafe_wait_seq(const CafeDev &D, const int *p, int last, int want) {
+  const unsigned long long t0 = cafe_globaltimer();
+  unsigned int spins = 0;
+  while (true) {
+    int v = cafe_ld_acquire(p);
+    if (want >= 0 ? v == want : v != last) return v;
+    if ((++spins & 255u) == 0 && cafe_globaltimer() - t0 > CAFE_SYNC_WAIT_NS) {
+      atomicOr(D.err, CAFE_ERR_SYNC);
+      return (int)0x80000000;
+    }
+  }
+}
+
+__device__ __noinline__ void cafe_fill_helper(const CafeDev &D, const CafeConsts &K, CafeQuadScratch &S) {
+  __shared__ int s_cmd;
+  __shared__ CafeFillReq s_req;
+  const int tid = threadIdx.x;
+  int last = 0;
+  while (true) {
+    if (tid == 0) {
+      const int v = cafe_wait_seq(D, D.fill_seq, last, -1);
+      s_cmd = v;
+      if (v > 0) s_req = *D.fill;  // after the acquire: the main block's request
+    }
+    __syncthreads();
+    const int v = s_cmd;
+    if (v <= 0) return;  // -1: the main block left the keyed loop; INT_MIN: time-out
+    last = v;
+    if (tid < CAFE_QUAD_THREADS) {
+      CafeNewCell nc;
+      nc.c[0] = s_req.c[0];
+      nc.c[1] = s_req.c[1];
+      nc.c[2] = s_req.c[2];
+      nc.ext = s_req.ext;
+      nc.gid = s_req.gid;
+      unsigned long long gk = cafe_row_fill_quad(D, K, s_req.r, s_req.p, true, s_req.e, s_req.T, S, &nc);
+      if (tid == 0) D.fill->gk = gk;
+    }
+    __syncthreads();
+    if (tid == 0) cafe_st_release(D.fill_seq + 1, v);  // orders the row's stores before it
+  }
+}
+
 __device__ __forceinline__ void d_event_loop(const CafeDev &D, const CafeConsts &K, const CafeStepParams *__restrict__ Pp, long long max_events, int allow_fast, const int cafe_bid, const int cafe_nblk) {
   const CafeStepParams P = *Pp;
   constexpr int NSEL = CAFE_LOOP_THREADS - CAFE_QUAD_THREADS;  // threads of the selecting warps
@@ -1545,6 +1615,12 @@ __device__ __forceinline__ void d_event_loop(const CafeDev &D, const CafeConsts 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int nthr = blockDim.x, nwarp = blockDim.x >> 5;
   const int hid = tid - CAFE_QUAD_THREADS;  // index among the selecting warps (>= 0 there)
+  if (cafe_bid == 1) {  // the fill helper (two-block launch)
+    cafe_fill_helper(D, K, s_quad);
+    return;
+  }
+  const bool use_helper = cafe_nblk == 2;
+  __shared__ int s_post, s_seq;  // this event's fill went to the helper; requests posted
   const double V = K.vhat_cls[1];
   unsigned long long my_min = CAFE_KEY_NONE;  // smallest key of this selecting thread's rows
   bool my_forced = false;                     // one of them is stamped -1
@@ -1581,6 +1657,8 @@ __device__ __forceinline__ void d_event_loop(const CafeDev &D, const CafeConsts 
     s_ev = 0;
     s_switch = 0;
     s_newrow = -1;
+    s_post = 0;
+    s_seq = 0;
     s_cyc[0] = s_cyc[1] = s_cyc[2] = s_cyc[3] = 0;
     D.ev_vd[0] = 0.0;
     D.ev_vs[0] = 0.0;
@@ -1670,6 +1748,29 @@ __device__ __forceinline__ void d_event_loop(const CafeDev &D, const CafeConsts 
             D.ev_vs[s_ev] = s_vs;
             s_dsum += fabs(s_dt);
             s_tinc += s_dt;
+            // hand the new row's fill to the helper block now when the
+            // captured cell will start a row of the shared velocity class
+            // (the condition phase 3 tests; the capture changes neither the
+            // cell's liquid count nor its neighbours' states)
+            s_post = 0;
+            const int icp = s_icap;
+            if (use_helper && !s_nuc && s_nrows < D.row_cap && D.a_liq[icp] > 0 && D.a_cold[icp] &&
+                D.a_cls[icp] == 1) {
+              CafeFillReq *F = D.fill;
+              const double *gq = D.row_geo + ((long long)s_brow * CAFE_NSLOT + s_bslot) * 4;
+              F->r = s_nrows;
+              F->p = icp;
+              F->e = s_ev;
+              F->gid = D.a_gid[s_jspos];
+              F->ext = gq[0];
+              F->c[0] = gq[1];
+              F->c[1] = gq[2];
+              F->c[2] = gq[3];
+              F->T = s_tinc;
+              s_seq += 1;
+              cafe_st_release(D.fill_seq, s_seq);
+              s_post = 1;
+            }
           }
         }
         long long tn = clock64();
@@ -1801,7 +1902,19 @@ __device__ __forceinline__ void d_event_loop(const CafeDev &D, const CafeConsts 
       }
       // ---- (3) the new row (warps 0-3) || selection of the next event (the rest)
       if (warp < CAFE_QUAD_THREADS / 32) {
-        if (D.a_liq[icap] > 0 && D.a_cold[icap] && !s_done) {
+        if (s_post) {
+          // the helper fills this row: its bookkeeping here, its result at (4)
+          if (tid == 0) {
+            const int r = nrows_ev;
+            D.row_pos[r] = icap;
+            D.row_j[r] = s_nvs2 - 1;
+            D.row_alive[r] = 1;
+            D.a_frow[icap] = r;
+            D.row_death[r] = CAFE_ALIVE;
+            D.row_E[r] = D.a_ext[icap];
+            D.row_m[r] = e;
+          }
+        } else if (D.a_liq[icap] > 0 && D.a_cold[icap] && !s_done) {
           int r = nrows_ev;
           if (r < D.row_cap) {
             if (tid == 0) {
@@ -1845,6 +1958,25 @@ __device__ __forceinline__ void d_event_loop(const CafeDev &D, const CafeConsts 
         long long tn = clock64();
         s_cyc[2] += tn - s_t0;
         s_t0 = tn;
+        if (s_post) {
+          // the helper's fill of this event's new row (bounded wait)
+          const int got = cafe_wait_seq(D, D.fill_seq + 1, 0, s_seq);
+          if (got != s_seq) {
+            s_done = 1;
+          } else {
+            const int r = nrows_ev;
+            const unsigned long long gk = D.fill->gk;
+            if (gk != 0ULL) {
+              double gm = cafe_unkey(gk);
+              if (gm > s_gmax) s_gmax = gm;
+            }
+            double ea = fabs(D.a_ext[icap]);
+            if (ea > s_emax) s_emax = ea;
+            s_nrows = r + 1;
+            s_newrow = r;
+          }
+          s_post = 0;
+        }
         CafeCand b = s_sel.red[0];
         const int r = s_newrow;
         if (r >= 0) {
@@ -1889,6 +2021,9 @@ __device__ __forceinline__ void d_event_loop(const CafeDev &D, const CafeConsts 
     for (int r = tid; r < s_nrows; r += nthr) D.row_m[r] = CAFE_M_DONE;
     __syncthreads();
   }
+  // the helper block leaves (no request is outstanding here: every posted
+  // fill is taken at (4) of its own event)
+  if (use_helper && tid == 0) cafe_st_release(D.fill_seq, -1);
   // ======================================================== exact scan
   while (s_slow && !s_done) {
     if (tid == 0) {

@@ -57,11 +57,8 @@ class Grid {
   // Grid::Grid (Grid.C:15-109): reads the deck and derives the laser grid;
   // here cafe_sim_create, which also allocates the device state.
   Grid(std::string &filIn, int &myidIn, int &nprocsIn) : filInput(filIn), myid(myidIn), nprocs(nprocsIn) {
-    cafe_options o;
+    cafe_options o = cafe_options();
     o.device = amcafe_dropin::device_from_env();
-    o.active_capacity = 0;
-    o.grain_capacity = 0;
-    o.event_scan = 0;
     amcafe_dropin::check(cafe_sim_create(filIn.c_str(), &o, &sim_), "Grid::Grid");
     Refresh();
   }

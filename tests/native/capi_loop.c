@@ -17,7 +17,7 @@ static void check(int rc, const char *what) {
 }
 
 int main(int argc, char **argv) {
-  cafe_options opt = {0, 0, 0, 0};
+  cafe_options opt = {0, 0, 0, 0, 0};
   cafe_sim *sim = NULL;
   cafe_info info;
   char path[4096];

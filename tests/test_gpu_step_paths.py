@@ -49,3 +49,25 @@ def test_graphed_and_ungraphed_steps_agree(tmp_path, outint):
     for mode in ("step", "timed"):
         for k, v in res["run"].items():
             assert np.array_equal(np.asarray(v), np.asarray(res[mode][k]), equal_nan=True), "%s: %s" % (mode, k)
+
+
+@pytest.mark.parametrize("deck,steps", [("layers_rot.in", 0), ("odd_dims.in", 0)])
+def test_fill_helper_block_changes_nothing(deck, steps):
+    """The event loop with its new-row fills handed to a second block (the
+    default) and with one block doing everything end in identical states."""
+    from amcafe_gb300 import Simulation
+
+    out = []
+    for single in (0, 1):
+        with Simulation(os.path.join(DECKS, deck), event_single_block=single) as sim:
+            sim.InitializeVoxels()
+            sim.begin()
+            sim.run(steps)
+            st = sim.state()
+            st["ctheta"] = sim.ctheta()
+            st["events"] = sim.stats()["events"]
+            out.append(st)
+    for k in out[0]:
+        a, b = np.asarray(out[0][k]), np.asarray(out[1][k])
+        assert np.array_equal(a, b) or (a.dtype.kind == "f" and np.array_equal(np.isnan(a), np.isnan(b)) and
+                                         np.array_equal(a[~np.isnan(a)], b[~np.isnan(b)])), k
