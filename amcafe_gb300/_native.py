@@ -23,7 +23,7 @@ EXPORTS = (
     "cafe_batch_create", "cafe_batch_run", "cafe_batch_size", "cafe_batch_sim", "cafe_batch_finished",
     "cafe_batch_destroy", "cafe_sim_checkpoint", "cafe_sim_restore", "cafe_sim_set_growth_log",
     "cafe_sim_growth_log_count", "cafe_adjoint_pool", "cafe_adjoint_growth", "cafe_sim_grid",
-    "cafe_generate_samples", "cafe_batch_report",
+    "cafe_generate_samples", "cafe_batch_report", "cafe_sim_set_output",
 )
 PHASES = ("melt", "classify", "gather", "events", "writeback", "layer")
 NPHASE = 8
@@ -109,6 +109,7 @@ def load():
         "cafe_sim_grid": (I, [P, ctypes.POINTER(CafeGrid)]),
         "cafe_generate_samples": (I, [I, ctypes.c_uint, P]),
         "cafe_batch_report": (I, [P, ctypes.POINTER(LL), ctypes.POINTER(LL), ctypes.c_char_p, I]),
+        "cafe_sim_set_output": (I, [P, ctypes.c_char_p]),
         "cafe_sim_stats": (I, [P, ctypes.POINTER(CafeStats)]),
         "cafe_sim_download_state": (I, [P, i32p, i32p, f64p, f64p, i32p]),
         "cafe_sim_download_temperature": (I, [P, f64p]),

@@ -15,11 +15,15 @@ depth come from the moments of the soft melt indicator of the same field
 (cafe_adjoint_pool). Values and vector-Jacobian products are hand-written CUDA
 kernels (csrc/cafe_adjoint.cu); `Objective` exposes them to torch.autograd.
 
-`ca_target` gives the outputs of a CA run at hidden parameters and
-`calibrate_ca` recovers them: an outer loop re-runs the CA at the current
-estimate (new event set) and an inner L-BFGS fits the parameters with that
-event set frozen. Only eta P enters the temperature, so P and eta are not
-separately identifiable from these outputs; P (eta fixed) and a are fitted.
+`ca_target` runs the CA at hidden parameters and gives its outputs (its own
+field's pool, its own summed growth) together with the run, whose event set
+`calibrate` then holds fixed while it fits the parameters. The frozen event
+set is what makes the growth-law coefficient identifiable: re-running the CA
+at each estimate moves the capture times with the growth speed (a faster
+growth reaches each capture sooner), so the summed growth of a fresh run
+hardly changes with a. Only eta P enters the temperature, so P and eta are not
+separately identifiable from these outputs either; P (eta fixed) and a are
+fitted.
 """
 import ctypes
 import os
@@ -242,36 +246,11 @@ def calibrate(run, target, theta0, free=(0, 3), iters=30):
 
 
 def ca_target(deck, nsteps, theta, segment=32, device=0, spinup=0):
-    """Outputs (length, width, depth, G) of a CA run at theta: the pool of its
-    own temperature field at the last step and the summed growth over its own
-    event set in the window after `spinup` steps."""
+    """A CA run at theta and its outputs (length, width, depth, G): the pool of
+    its own temperature field at the last step and the summed growth over its
+    own event set in the window after `spinup` steps. Returns (outputs, run);
+    the caller closes the run."""
     run = GrowthRun(deck, nsteps, segment=segment, device=device, theta=theta, spinup=spinup)
-    try:
-        pool, _ = run.pool(run.theta)
-        G, _ = run.growth(run.theta)
-        return np.array([pool[0], pool[1], pool[2], G]), run.stats
-    finally:
-        run.close()
-
-
-def calibrate_ca(deck, nsteps, target, theta0, free=(0, 3), outer=6, iters=30, segment=32, device=0, rtol=1e-9,
-                 spinup=0):
-    """Recovers the parameters `free` from CA outputs: each outer iteration runs
-    the CA at the current estimate and fits the parameters with that run's
-    event set frozen (calibrate); stops when a CA run reproduces the target to
-    rtol or after `outer` runs. Returns (theta, history of (theta, loss))."""
-    th = np.asarray(theta0, np.float64).copy()
-    hist = []
-    tgt = np.asarray(target, np.float64)
-    for _ in range(outer):
-        run = GrowthRun(deck, nsteps, segment=segment, device=device, theta=th, spinup=spinup)
-        try:
-            out = Objective.apply(torch.tensor(run.theta), run).numpy()
-            loss = float(np.sum(((out - tgt) / tgt) ** 2))
-            hist.append((th.copy(), loss))
-            if loss <= rtol * rtol:
-                break
-            th, _ = calibrate(run, tgt, run.theta, free=free, iters=iters)
-        finally:
-            run.close()
-    return th, hist
+    pool, _ = run.pool(run.theta)
+    G, _ = run.growth(run.theta)
+    return np.array([pool[0], pool[1], pool[2], G]), run

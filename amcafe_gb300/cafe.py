@@ -163,6 +163,13 @@ class Simulation:
         check(self._lib.cafe_sim_download_output(self._h, _ptr(t, f), _ptr(z, f), _ptr(x, f), _ptr(y, f)))
         return dict(Temperature=t, IPFz=z, IPFx=x, IPFy=y)
 
+    def set_output(self, base):
+        """The loop writes the WriteToHDF1 datasets itself at its output
+        points as "<base><tInd>.h5.*" (before that step's AddLayer1, as
+        main1.C does), and after the closing CleanLayer of run(); None turns
+        it off (cafe_sim_set_output)."""
+        check(self._lib.cafe_sim_set_output(self._h, str(base).encode() if base else None))
+
     def WriteToHDF1(self, prefix):
         """Writes the datasets of VoxelsCA::WriteToHDF1 as raw files
         <prefix>.<dataset>.bin (prefix such as "out/run120.h5")."""

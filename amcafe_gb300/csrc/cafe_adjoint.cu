@@ -126,8 +126,8 @@ __global__ void k_adj_growth(cafe_adjoint_setup S, AdjTheta th, const int32_t *c
   double loc[6] = {0, 0, 0, 0, 0, 0};
   const long long nxy = (long long)S.nx * S.ny;
   for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
-    double ta = tau[e];
-    if (!(ta > 0.0)) continue;
+    double ta = tau[e];  // negative after negative-time events (VoxelsCA.C:511-516)
+    if (!(ta != 0.0) || isinf(ta)) continue;
     long long c = cells[e];
     long long k = c / nxy, r = c - k * nxy;
     long long j = r / S.nx, i = r - j * S.nx;

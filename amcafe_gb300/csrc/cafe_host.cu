@@ -407,10 +407,9 @@ struct cafe_sim {
   std::default_random_engine genlayer;      // VoxelsCA.h:129
   bool initialized = false, begun = false, done = false;
   bool closed = false;  // the closing CleanLayer of main1.C:95 has been applied
-  // the last cafe_sim_step ended at an output point that is also a layer
-  // change: its AddLayer1 (main1.C:88) waits until the caller has written the
-  // output (main1.C:78-83 comes first) and runs at the next continuing call
-  bool pending_layer = false;
+  // cafe_sim_set_output: files of WriteToHDF1 written by the loop itself at
+  // its output points, "<base><TempField::tInd>.h5" (main1.C:79-83, 97)
+  std::string out_base;
   long long steps = 0;
   // device
   CafeConsts K;
@@ -1010,13 +1009,6 @@ int step_graph_launch(cafe_sim *s) {
 bool graph_eligible(const cafe_sim *s) { return s->use_graph && !s->timing && !s->K.easm && !s->full_k2; }
 
 // The rest of a loop iteration after its device work (main1.C:72-93).
-// The AddLayer1 that the last step left for after its output point.
-int apply_pending_layer(cafe_sim *s) {
-  if (!s->pending_layer) return CAFE_OK;
-  s->pending_layer = false;
-  return cafe_sim_add_layer(s);
-}
-
 int finish_after_laser(cafe_sim *s, bool bcheck, int *done) {
   int rc;
   if (s->g.inewlayerflg == 1 && (rc = cafe_sim_clean_layer(s))) return rc;
@@ -1024,13 +1016,13 @@ int finish_after_laser(cafe_sim *s, bool bcheck, int *done) {
   const GridH &g = s->g;
   s->output_due = (g.outint > 0 && s->tf_tInd % g.outint == 0) || bcheck || (g.inewlayerflg == 1 && g.outNL == 0);
   if (s->output_due && (rc = cafe_sim_set_build(s))) return rc;
-  cafe_sim_update_time(s);
-  if (s->g.inewlayerflg == 1) {
-    if (s->output_due)
-      s->pending_layer = true;
-    else if ((rc = cafe_sim_add_layer(s)))
-      return rc;
+  if (s->output_due && !s->out_base.empty()) {
+    // WriteToHDF1 before UpdateTime2 and AddLayer1, as main1.C:79-88 orders them
+    std::string name = s->out_base + std::to_string(s->tf_tInd) + ".h5";
+    if ((rc = cafe_sim_write_output(s, name.c_str()))) return rc;
   }
+  cafe_sim_update_time(s);
+  if (s->g.inewlayerflg == 1 && (rc = cafe_sim_add_layer(s))) return rc;
   s->steps++;
   if (bcheck) s->done = true;
   if (done) *done = s->done ? 1 : 0;
@@ -1450,8 +1442,8 @@ int cafe_sim_update_voxels(cafe_sim *s) {
 int cafe_sim_clean_layer(cafe_sim *s) {
   if (!s || !s->initialized) return fail(CAFE_E_STATE, "clean_layer before initialize_voxels");
   CUDA_TRY(cudaSetDevice(s->device));
-  int rc = apply_pending_layer(s);
-  if (rc || (rc = read_ctr(s, CTR_NGRAIN, &s->nGrain))) return rc;
+  int rc = read_ctr(s, CTR_NGRAIN, &s->nGrain);
+  if (rc) return rc;
   int ng = s->nGrain;
   int32_t *cnt = nullptr, *newid = nullptr;
   double *cth2 = nullptr, *rot2 = nullptr;
@@ -1511,12 +1503,11 @@ int cafe_sim_begin(cafe_sim *s) {
 
 int cafe_sim_step(cafe_sim *s, int *done) {
   if (!s || !s->begun) return fail(CAFE_E_STATE, "step before begin");
-  int rc;
-  if ((rc = apply_pending_layer(s))) return rc;
   if (s->done) {
     if (done) *done = 1;
     return CAFE_OK;
   }
+  int rc;
   if (graph_eligible(s)) {
     CUDA_TRY(cudaSetDevice(s->device));
     if ((rc = step_plan(s))) return rc;
@@ -1536,14 +1527,17 @@ int cafe_sim_run(cafe_sim *s, long long max_steps, long long *steps_done) {
   if (!s || !s->begun) return fail(CAFE_E_STATE, "run before begin");
   long long n = 0;
   int done = s->done ? 1 : 0, rc;
-  if ((rc = apply_pending_layer(s))) return rc;
   while (!done && (max_steps <= 0 || n < max_steps)) {
     if ((rc = cafe_sim_step(s, &done))) return rc;
     ++n;
   }
-  if (done && !s->closed) {  // main1.C:95 runs once, after the loop
+  if (done && !s->closed) {  // main1.C:95-97 run once, after the loop
     if ((rc = cafe_sim_clean_layer(s))) return rc;
     s->closed = true;
+    if (!s->out_base.empty()) {
+      std::string name = s->out_base + std::to_string(s->tf_tInd) + ".h5";
+      if ((rc = cafe_sim_write_output(s, name.c_str()))) return rc;
+    }
   }
   if (steps_done) *steps_done = n;
   return sim_sync(s);
@@ -1584,6 +1578,12 @@ int cafe_sim_info(cafe_sim *s, cafe_info *info) {
   }
   info->tf_tInd = s->tf_tInd;
   info->output_due = s->output_due ? 1 : 0;
+  return CAFE_OK;
+}
+
+int cafe_sim_set_output(cafe_sim *s, const char *base) {
+  if (!s) return fail(CAFE_E_ARG, "null handle");
+  s->out_base = base ? base : "";
   return CAFE_OK;
 }
 
@@ -2173,8 +2173,7 @@ int cafe_sim_checkpoint(cafe_sim *s, const char *path) {
   if (!s || !path) return fail(CAFE_E_ARG, "null argument");
   if (!s->begun) return fail(CAFE_E_STATE, "checkpoint before begin");
   CUDA_TRY(cudaSetDevice(s->device));
-  int rc = apply_pending_layer(s);  // the checkpoint holds whole steps
-  if (!rc) rc = sim_sync(s);
+  int rc = sim_sync(s);
   if (rc || (rc = ensure_host_buffer(s)) || (rc = read_ctr(s, CTR_NGRAIN, &s->nGrain))) return rc;
   const GridH &g = s->g;
   CkptHeader h;
@@ -2288,7 +2287,6 @@ int cafe_sim_restore(cafe_sim *s, const char *path) {
   s->steps = h.steps;
   s->done = h.done != 0;
   s->closed = false;
-  s->pending_layer = false;
   s->output_due = h.output_due != 0;
   s->have_P = false;
   s->full_k2 = true;          // the liquid list is rebuilt by a dense pass
@@ -2623,12 +2621,6 @@ int cafe_internal_batch_engine_step(CafeBatchEngine *E, int *phase, long long *s
       CUDA_TRY(cudaEventRecord(E->ev_plain[r], s->stream));
       CUDA_TRY(cudaStreamWaitEvent(E->stream, E->ev_plain[r], 0));
       continue;
-    }
-    if (s->pending_layer) {
-      // the last step's AddLayer1, on the handle's stream, before this step
-      if ((rc = apply_pending_layer(s))) return fail(rc, "realisation %d: %s", r, g_last_error.c_str());
-      CUDA_TRY(cudaEventRecord(E->ev_plain[r], s->stream));
-      CUDA_TRY(cudaStreamWaitEvent(E->stream, E->ev_plain[r], 0));
     }
     if ((rc = step_plan(s))) return fail(rc, "realisation %d: %s", r, g_last_error.c_str());
     E->hP[r] = s->P;

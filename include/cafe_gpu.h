@@ -57,12 +57,8 @@ typedef struct {
   int tf_tInd;     /* TempField::tInd of the last step (main1.C:64) */
   int output_due;  /* 1 when the last cafe_sim_step reached an output point of
                       main1.C:77-78 (it called SetBuild there; the reference
-                      writes WriteToHDF1("<base>" + tf_tInd) at this point).
-                      When that point is also a layer change, the step's
-                      AddLayer1 (main1.C:88) waits until the next
-                      cafe_sim_step, cafe_sim_run, cafe_sim_clean_layer or
-                      cafe_sim_checkpoint, so that the state read or written
-                      now is the one main1.C writes */
+                      writes WriteToHDF1("<base>" + tf_tInd) at this point;
+                      cafe_sim_set_output has the step write it there) */
 } cafe_info;
 
 typedef struct {
@@ -213,6 +209,17 @@ int cafe_sim_download_output(cafe_sim *sim, float *temperature, float *ipfz, flo
  * per-cell files as cell data on the voxel grid. The reference's file
  * <base><tInd>.h5 corresponds to prefix "<base><tInd>.h5". */
 int cafe_sim_write_output(cafe_sim *sim, const char *prefix);
+
+/* The output of main1.C:77-84 and 95-97 written by the loop itself: with a
+ * non-empty base, cafe_sim_step writes the WriteToHDF1 datasets as
+ * cafe_sim_write_output(sim, "<base><tf_tInd>.h5") at each output point,
+ * after SetBuild and before UpdateTime2 and AddLayer1 (the reference's order:
+ * at an output point that is also a layer change the written state is the
+ * one before the new layer), and cafe_sim_run writes "<base><tf_tInd>.h5"
+ * again after the closing CleanLayer. NULL or "" turns it off (the default);
+ * a caller writing after cafe_sim_step returns sees the state after
+ * AddLayer1. */
+int cafe_sim_set_output(cafe_sim *sim, const char *base);
 
 /* Checkpoint of the whole loop state (no counterpart in the reference, which
  * restarts from a deck): the Grid scalars (time, tInd, laser index, scan and

@@ -69,7 +69,8 @@ def growth(setup, theta, cells, steps, tau, cot=None):
     j, i = r // nx, r % nx
     T, dT = temperature(setup, theta, (i + .5) * dx, (j + .5) * dx, (k + .5) * dx, np.asarray(steps) * setup["dt"])
     D = setup["Tl"] - T
-    ok = (np.asarray(tau) > 0) & (D > 0)
+    ta0 = np.asarray(tau)
+    ok = (ta0 != 0) & np.isfinite(ta0) & (D > 0)
     D, ta, dT = D[ok], np.asarray(tau)[ok], dT[:, ok]
     pw = D ** n
     G = np.sum(a * pw * ta)

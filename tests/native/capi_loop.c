@@ -1,8 +1,9 @@
 /* A C program driving one deck through the engine's C ABI (include/
  * cafe_gpu.h), the way a C caller replaces the reference's time loop
  * (main1.C:29-97): create, initialise, the loop with the datasets of
- * WriteToHDF1 written at every output point as <outdir>/out<tInd>.h5.*, the
- * closing CleanLayer and a last write as <outdir>/final.h5.*. Test-only.
+ * WriteToHDF1 written by the engine at every output point as
+ * <outdir>/out<tInd>.h5.* (cafe_sim_set_output), the closing CleanLayer and a
+ * last write as <outdir>/final.h5.*. Test-only.
  * Usage: capi_loop <deck.in> <outdir> */
 #include <stdio.h>
 #include <stdlib.h>
@@ -27,16 +28,11 @@ int main(int argc, char **argv) {
     return 2;
   }
   check(cafe_sim_create(argv[1], &opt, &sim), "create");
+  snprintf(path, sizeof path, "%s/out", argv[2]);
+  check(cafe_sim_set_output(sim, path), "set_output");
   check(cafe_sim_initialize_voxels(sim), "initialize_voxels");
   check(cafe_sim_begin(sim), "begin");
-  while (!done) {
-    check(cafe_sim_step(sim, &done), "step");
-    check(cafe_sim_info(sim, &info), "info");
-    if (info.output_due) {
-      snprintf(path, sizeof path, "%s/out%d.h5", argv[2], info.tf_tInd);
-      check(cafe_sim_write_output(sim, path), "write_output");
-    }
-  }
+  while (!done) check(cafe_sim_step(sim, &done), "step");
   check(cafe_sim_clean_layer(sim), "clean_layer");
   snprintf(path, sizeof path, "%s/final.h5", argv[2]);
   check(cafe_sim_write_output(sim, path), "write_output");

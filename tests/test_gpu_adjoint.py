@@ -54,7 +54,8 @@ def test_pool_matches_reference_and_fd(run):
 
 def test_growth_matches_reference_and_fd(run):
     cells, steps, tau = run.log()
-    assert len(cells) > 500 and np.all(tau >= 0) and np.any(tau > 0)
+    # negative-time events shrink extents: some growth times are negative
+    assert len(cells) > 500 and np.all(np.isfinite(tau)) and np.any(tau > 0)
     G, g = run.growth(THETA, cot=1.0)
     rG, rg = ref.growth(run.setup_dict(), THETA, cells, steps, tau, cot=1.0)
     assert _rel(G, rG) < 1e-10
@@ -126,16 +127,17 @@ def test_objective_gradient(run):
 
 def test_calibration_recovers_parameters_from_a_ca_run():
     """The target is the output of a CA run at the hidden parameters (its own
-    event set and temperature field); starting 10 % away, the calibration
-    re-runs the CA at each estimate and fits P and a with that run's events
-    frozen, until a CA run reproduces the target."""
-    from amcafe_gb300.adjoint import ca_target, calibrate_ca
+    temperature field's pool and its own summed growth); starting away from
+    them, the calibration fits P and a with that run's event set frozen and
+    recovers them."""
+    from amcafe_gb300.adjoint import ca_target, calibrate
 
     hidden = np.array([180.0, 0.4, 1.0, 1.2e-5, 2.0])
-    target, stats = ca_target(DECK, 96, hidden, spinup=SPINUP)
-    assert stats["events"] > 1000
-    got, hist = calibrate_ca(DECK, 96, target, [200.0, 0.4, 1.0, 1.1e-5, 2.0], free=(0, 3), outer=6,
-                             spinup=SPINUP)
-    print("calibration history:", [(list(h[0][[0, 3]]), h[1]) for h in hist])
-    assert abs(got[0] - 180.0) < 1e-4 * 180.0, (got, hist)
-    assert abs(got[3] - 1.2e-5) < 1e-3 * 1.2e-5, (got, hist)
+    target, run = ca_target(DECK, 96, hidden, spinup=SPINUP)
+    try:
+        assert run.stats["events"] > 1000
+        got, hist = calibrate(run, target, [220.0, 0.4, 1.0, 0.9e-5, 2.0], free=(0, 3))
+    finally:
+        run.close()
+    assert abs(got[0] - 180.0) < 1e-4 * 180.0, (got, hist[-3:])
+    assert abs(got[3] - 1.2e-5) < 1e-4 * 1.2e-5, (got, hist[-3:])
