@@ -137,6 +137,8 @@ __global__ void kb_reset_c(CafeBatchArgs B) {
   if (threadIdx.x == 0) {
     R.D.ctr[CTR_SLOW] = 0;
     R.D.ctr[CTR_NPAIRS] = 0;
+    R.D.fill_seq[0] = 0;  // the event loop's fill hand-off (two blocks per realisation)
+    R.D.fill_seq[1] = 0;
   }
 }
 __global__ void kb_rows_prep(CafeBatchArgs B) {

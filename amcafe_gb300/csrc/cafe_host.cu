@@ -2355,6 +2355,7 @@ struct CafeBatchEngine {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   std::vector<cudaEvent_t> ev_plain;
   int share = 4, chunks = 1;      // launch shape in use
+  bool loop_pairs = false;        // two event-loop blocks per realisation (fill helper)
   bool tuned = false;
   int tune_steps = 6;             // batch steps timed per candidate
   std::vector<std::pair<std::pair<int, int>, double>> trials;  // ((share, chunks), ms per batch step)
@@ -2373,9 +2374,10 @@ const int kBatchThreads[BK_COUNT] = {32, 256, 256, 256, 256, 32, CAFE_DENSE_THRE
 
 // blocks of realisation s in a batched launch of `kind` (its plain graphed
 // step's grid, cafe_sim launch_melt / launch_voxels)
-long long batch_blocks(const cafe_sim *s, int kind) {
+long long batch_blocks(const cafe_sim *s, int kind, bool loop_pairs) {
   const long long g = s->gsm;
   switch (kind) {
+    case BK_LOOP: return loop_pairs ? 2 : 1;
     case BK_MELT: case BK_PBOX0: case BK_PBOX1: return g * 16;
     case BK_LIST: case BK_PREP: case BK_ORDER: case BK_FINAL: return g * 4;
     case BK_ACOUNT: case BK_ASCATTER: return std::max<long long>(1, std::min<long long>(s->nblk_act, g * 8));
@@ -2408,7 +2410,7 @@ int batch_capture(CafeBatchEngine *E) {
     long long acc = 0;
     for (int r = 0; r < n; ++r) {
       start[(size_t)k * (n + 1) + r] = (int)acc;
-      acc += batch_blocks(E->sims[r], k);
+      acc += batch_blocks(E->sims[r], k, E->loop_pairs);
     }
     if (acc > 0x7fffffffLL) return fail(CAFE_E_CAPACITY, "batch: too many blocks in one launch");
     start[(size_t)k * (n + 1) + n] = (int)acc;
@@ -2442,7 +2444,21 @@ int batch_capture(CafeBatchEngine *E) {
   kb_rows_prep<<<E->total[BK_PREP], T[BK_PREP], 0, st>>>(A);
   kb_rows_geo<<<E->total[BK_GEO], T[BK_GEO], 0, st>>>(A);
   kb_rows_order<<<E->total[BK_ORDER], T[BK_ORDER], 0, st>>>(A);
-  kb_event_loop<<<E->total[BK_LOOP], T[BK_LOOP], 0, st>>>(A);
+  if (E->loop_pairs) {
+    // every pair must be resident at once: a cooperative launch
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(E->total[BK_LOOP]);
+    cfg.blockDim = dim3(T[BK_LOOP]);
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, kb_event_loop, A);
+  } else {
+    kb_event_loop<<<E->total[BK_LOOP], T[BK_LOOP], 0, st>>>(A);
+  }
   kb_rows_finalize<<<E->total[BK_FINAL], T[BK_FINAL], 0, st>>>(A);
   kb_writeback<<<E->total[BK_WB], T[BK_WB], 0, st>>>(A);
   kb_mushy2solid<<<E->total[BK_M2S], T[BK_M2S], 0, st>>>(A);
@@ -2488,8 +2504,10 @@ int batch_tune_next(CafeBatchEngine *E, double ms) {
              i ? ", " : "", E->trials[i].first.first, E->trials[i].first.second, E->trials[i].second);
     s += buf;
   }
-  snprintf(buf, sizeof buf, "], \"chosen\": {\"grid_share_sms\": %d, \"compaction_chunks\": %d}, \"steps_each\": %d}",
-           E->trials[best].first.first, E->trials[best].first.second, E->tune_steps);
+  snprintf(buf, sizeof buf,
+           "], \"chosen\": {\"grid_share_sms\": %d, \"compaction_chunks\": %d}, \"steps_each\": %d, "
+           "\"event_loop_blocks\": %d}",
+           E->trials[best].first.first, E->trials[best].first.second, E->tune_steps, E->loop_pairs ? 2 : 1);
   s += buf;
   E->log = s;
   E->tuned = true;
@@ -2539,6 +2557,16 @@ CafeBatchEngine *cafe_internal_batch_engine_create(cafe_sim *const *sims, int n,
   }
   E->hR.resize(n);
   E->hR_valid.assign(n, 0);
+  {
+    // event-loop pairs when every realisation has its helper on and all the
+    // pairs fit on the GPU at once
+    int per_sm = 0, coop = 0;
+    cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, E->device);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kb_event_loop, CAFE_LOOP_THREADS, 0);
+    bool all = true;
+    for (int r = 0; r < n; ++r) all = all && sims[r]->event_helper;
+    E->loop_pairs = all && coop && (long long)per_sm * E->nsm >= 2LL * n;
+  }
   // every realisation reads its step parameters from its slot of dP
   for (int r = 0; r < n; ++r) {
     cafe_sim *s = sims[r];
