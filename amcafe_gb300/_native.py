@@ -73,7 +73,8 @@ class CafeStats(ctypes.Structure):
                 ("launches", ctypes.c_ulonglong), ("exact_scan_steps", ctypes.c_ulonglong),
                 ("row_evaluations", ctypes.c_ulonglong), ("cycles_select", ctypes.c_ulonglong),
                 ("cycles_apply", ctypes.c_ulonglong), ("cycles_fill", ctypes.c_ulonglong),
-                ("graph_captures", ctypes.c_ulonglong), ("easm_integrals", ctypes.c_ulonglong)]
+                ("graph_captures", ctypes.c_ulonglong), ("easm_integrals", ctypes.c_ulonglong),
+                ("cycles_merge", ctypes.c_ulonglong)]
 
 
 _lib = None

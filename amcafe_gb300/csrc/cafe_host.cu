@@ -1683,6 +1683,7 @@ int cafe_sim_stats(cafe_sim *s, cafe_stats *st) {
   st->cycles_select = v[STAT_CYC_SELECT];
   st->cycles_apply = v[STAT_CYC_APPLY];
   st->cycles_fill = v[STAT_CYC_FILL];
+  st->cycles_merge = v[STAT_CYC_OTHER];
   st->graph_captures = (unsigned long long)s->graph_captures;
   st->easm_integrals = v[STAT_EASM_INTEGRALS];
 #ifdef CAFE_DETAIL_CYCLES

@@ -73,11 +73,13 @@ typedef struct {
   unsigned long long launches;     /* kernels launched by this handle since the last phase reset */
   unsigned long long exact_scan_steps; /* steps run with the full per-event scan */
   unsigned long long row_evaluations;  /* keyed-selection rounds that evaluated rows exactly */
-  unsigned long long cycles_select;    /* event-loop SM cycles in event selection */
+  unsigned long long cycles_select;    /* event-loop SM cycles taking this event's winner */
   unsigned long long cycles_apply;     /* ... applying the capture/nucleation */
-  unsigned long long cycles_fill;      /* ... neighbour bookkeeping and new frontier rows */
+  unsigned long long cycles_fill;      /* ... new frontier row and next selection, side by side */
   unsigned long long graph_captures;   /* step graphs captured (one per handle unless buffers move) */
   unsigned long long easm_integrals;   /* EASM: Utilities::Integral evaluations (25 nodes each) */
+  unsigned long long cycles_merge;     /* ... taking the next event's winner (the new row's
+                                          result included) */
 } cafe_stats;
 
 /* Grid::Grid (Grid.C:15-109, deck parse Grid.C:165-318) + Partition::
