@@ -32,7 +32,7 @@ NPHASE = 8
 class CafeOptions(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int), ("active_capacity", ctypes.c_longlong),
                 ("grain_capacity", ctypes.c_longlong), ("event_scan", ctypes.c_int),
-                ("event_single_block", ctypes.c_int)]
+                ("event_fill_helper", ctypes.c_int)]
 
 
 class CafeGrid(ctypes.Structure):

@@ -34,14 +34,14 @@ def _ptr(a, ct):
 
 class Simulation:
     def __init__(self, deck, device=0, active_capacity=0, grain_capacity=0, event_scan=0, _handle=None,
-                 event_single_block=0):
+                 event_fill_helper=0):
         self._lib = load()
         self._owned = _handle is None
         if _handle is not None:  # a realisation owned by a Batch
             self._h = ctypes.c_void_p(_handle)
         else:
             self._h = ctypes.c_void_p()
-            opt = CafeOptions(device, active_capacity, grain_capacity, event_scan, event_single_block)
+            opt = CafeOptions(device, active_capacity, grain_capacity, event_scan, event_fill_helper)
             check(self._lib.cafe_sim_create(str(deck).encode(), ctypes.byref(opt), ctypes.byref(self._h)))
         inf = self.info()
         self.shape = (inf["nz"], inf["ny"], inf["nx"])
@@ -254,11 +254,11 @@ class Batch:
     host threads. `sims[i]` reads realisation i like a Simulation."""
 
     def __init__(self, decks, device=0, threads=0, active_capacity=0, grain_capacity=0, event_scan=0,
-                 event_single_block=0):
+                 event_fill_helper=0):
         self._lib = load()
         self._h = ctypes.c_void_p()
         arr = (ctypes.c_char_p * len(decks))(*[str(d).encode() for d in decks])
-        opt = CafeOptions(device, active_capacity, grain_capacity, event_scan, event_single_block)
+        opt = CafeOptions(device, active_capacity, grain_capacity, event_scan, event_fill_helper)
         check(self._lib.cafe_batch_create(arr, len(decks), ctypes.byref(opt), int(threads), ctypes.byref(self._h)))
         self.sims = [Simulation(None, _handle=self._lib.cafe_batch_sim(self._h, i)) for i in range(len(decks))]
 

@@ -422,7 +422,7 @@ struct cafe_sim {
   int prev_lo[3] = {0, 0, 0}, prev_hi[3] = {0, 0, 0};
   bool full_k2 = false;   // next solid->mushy pass must scan the whole box
   int event_scan = 0;     // 1: evaluate every frontier row at every event
-  bool event_helper = true;  // the event loop's new-row fills run in a second block
+  bool event_helper = false;  // the event loop's new-row fills run in a second block
   std::vector<void *> owned;
   int *h_pinned = nullptr;  // pinned host mirror of ctr + err
   // staging for host transfers (allocated on first use)
@@ -1053,7 +1053,7 @@ int cafe_sim_create(const char *deck_path, const cafe_options *opt, cafe_sim **o
   GridH &g = s->g;
   s->device = opt ? opt->device : 0;
   s->event_scan = opt ? opt->event_scan : 0;
-  s->event_helper = !(opt && opt->event_single_block);
+  s->event_helper = opt && opt->event_fill_helper;
   cudaError_t ce = cudaSetDevice(s->device);
   if (ce != cudaSuccess) {
     delete s;

@@ -36,9 +36,10 @@ typedef struct {
   long long grain_capacity;    /* initial grain-table capacity; 0 = automatic */
   int event_scan;              /* 0: keyed event selection (default); 1: evaluate every
                                   frontier cell at every event (the reference's scan) */
-  int event_single_block;      /* 0 (default): the event loop hands each new frontier row's
-                                  set-up to a second thread block on another SM; 1: one block
-                                  does everything (same results) */
+  int event_fill_helper;       /* 1: the event loop hands each new frontier row's set-up to a
+                                  second thread block on another SM (same results; measured
+                                  slower on this GPU: the selection, not the set-up, bounds an
+                                  event); 0 (default): one block does everything */
 } cafe_options;
 
 typedef struct {

@@ -22,8 +22,8 @@ def _final(sim):
     return st
 
 
-@pytest.mark.parametrize("threads", [0, 3])
-def test_batch_matches_plain_runs(tmp_path, threads):
+@pytest.mark.parametrize("threads,helper", [(0, 0), (3, 0), (0, 1)])
+def test_batch_matches_plain_runs(tmp_path, threads, helper):
     """Uneven realisations (sides 24-40 voxels, their own speeds and seeds)
     end in bit-identical states to their plain runs; with batched launches
     the autotuner tried its candidates during the run and reported them."""
@@ -38,7 +38,7 @@ def test_batch_matches_plain_runs(tmp_path, threads):
             sim.begin()
             sim.run()
             plain.append(_final(sim))
-    with Batch(decks, threads=threads) as b:
+    with Batch(decks, threads=threads, event_fill_helper=helper) as b:
         total = b.run()
         assert total > 0
         for i, want in enumerate(plain):
@@ -56,6 +56,7 @@ def test_batch_matches_plain_runs(tmp_path, threads):
             assert len(tun["candidates"]) == 6 and all(c["ms_per_batch_step"] > 0 for c in tun["candidates"])
             best = min(tun["candidates"], key=lambda c: c["ms_per_batch_step"])
             assert tun["chosen"]["grid_share_sms"] == best["grid_share_sms"]
+            assert tun["event_loop_blocks"] == (2 if helper else 1)
         else:
             assert rep["launches"] == 0 and rep["tuning"] is None
 

@@ -53,13 +53,13 @@ def test_graphed_and_ungraphed_steps_agree(tmp_path, outint):
 
 @pytest.mark.parametrize("deck,steps", [("layers_rot.in", 0), ("odd_dims.in", 0)])
 def test_fill_helper_block_changes_nothing(deck, steps):
-    """The event loop with its new-row fills handed to a second block (the
-    default) and with one block doing everything end in identical states."""
+    """The event loop with its new-row fills handed to a second block and
+    with one block doing everything (the default) end in identical states."""
     from amcafe_gb300 import Simulation
 
     out = []
-    for single in (0, 1):
-        with Simulation(os.path.join(DECKS, deck), event_single_block=single) as sim:
+    for helper in (1, 0):
+        with Simulation(os.path.join(DECKS, deck), event_fill_helper=helper) as sim:
             sim.InitializeVoxels()
             sim.begin()
             sim.run(steps)
