@@ -1086,13 +1086,33 @@ __device__ __forceinline__ int cafe_find_slot(const CafeDev &D, int q, int targe
 
 // Applies the logged growth of events row_m+1 .. min(upto, row_death). A
 // nucleation logs +0, which leaves an extent unchanged (extents are never -0).
-__device__ __forceinline__ void cafe_row_replay(const CafeDev &D, int r, int upto) {
+// The event loop keeps the first CAFE_EVD_SMEM entries of the growth log in
+// shared memory as well (evd): a replay reads them there instead of making a
+// round trip to L2 per replayed event (the log is written as the events
+// happen, so its lines are not in L1); evd may be null (global log only).
+#define CAFE_EVD_SMEM 2048
+__device__ __forceinline__ void cafe_row_replay(const CafeDev &D, int r, int upto, const double *evd = nullptr) {
   int m = D.row_m[r];
   int stop = min(upto, D.row_death[r]);
   if (stop <= m) return;
   double E = D.row_E[r];
-  for (int k = m + 1; k <= stop; ++k) {
-    E = E + D.ev_vd[k];
+  int k = m + 1;
+  if (evd) {
+    // four log entries loaded together, then the dependent additions
+    for (; k + 3 <= stop && k + 3 < CAFE_EVD_SMEM; k += 4) {
+      const double a = evd[k], b = evd[k + 1], c = evd[k + 2], d = evd[k + 3];
+      E = E + a;
+      E = cafe_is_neg(E) ? 0.0 : E;
+      E = E + b;
+      E = cafe_is_neg(E) ? 0.0 : E;
+      E = E + c;
+      E = cafe_is_neg(E) ? 0.0 : E;
+      E = E + d;
+      E = cafe_is_neg(E) ? 0.0 : E;
+    }
+  }
+  for (; k <= stop; ++k) {
+    E = E + ((evd && k < CAFE_EVD_SMEM) ? evd[k] : D.ev_vd[k]);
     E = cafe_is_neg(E) ? 0.0 : E;  // (E < 0.0) ? 0.0 : E
   }
   D.row_E[r] = E;
@@ -1102,12 +1122,12 @@ __device__ __forceinline__ void cafe_row_replay(const CafeDev &D, int r, int upt
 // Exact evaluation of row r (live slots `live`) for the iteration after `ev`
 // events at time T.
 __device__ __forceinline__ void cafe_row_eval_live(const CafeDev &D, const CafeConsts &K, int r, int ev,
-                                                   double T, uint32_t live) {
+                                                   double T, uint32_t live, const double *evd = nullptr) {
 #ifdef CAFE_DETAIL_CYCLES
   long long rp0 = clock64();
   int rm0 = D.row_m[r];
 #endif
-  cafe_row_replay(D, r, ev);
+  cafe_row_replay(D, r, ev, evd);
 #ifdef CAFE_DETAIL_CYCLES
   atomicAdd(&D.stat[STAT_DETAIL + 27], (unsigned long long)(D.row_m[r] - rm0 > 0 ? D.row_m[r] - rm0 : 0));
   atomicAdd(&D.stat[STAT_DETAIL + 28], 1ULL);
@@ -1137,8 +1157,8 @@ __device__ __forceinline__ void cafe_row_eval_live(const CafeDev &D, const CafeC
   D.row_key2[r] = k2 == CAFE_KEY_NONE ? key : cafe_key(T + cafe_unkey(k2));
 }
 __device__ __forceinline__ void cafe_row_eval(const CafeDev &D, const CafeConsts &K, int r, int ev,
-                                              double T) {
-  cafe_row_eval_live(D, K, r, ev, T, D.row_live[r]);
+                                              double T, const double *evd = nullptr) {
+  cafe_row_eval_live(D, K, r, ev, T, D.row_live[r], evd);
 }
 
 // Frontier rows of the step, in three passes so that the capture geometry,
@@ -1273,7 +1293,7 @@ __device__ __forceinline__ void cafe_bar_n(int id, int n) { asm volatile("bar.sy
 __device__ void cafe_select_keyed(const CafeDev &D, const CafeConsts &K, int ev, double T, int nrows, int gtid,
                                   int gn, int bar, unsigned long long &my_min, bool &my_forced,
                                   unsigned char *dirty, unsigned char *forced, CafeSelShared &S, double gmax,
-                                  double emax, double dsum, double V) {
+                                  double emax, double dsum, double V, const double *evd) {
   const int lane = gtid & 31, gw = gtid >> 5, ngw = gn >> 5;
 #ifdef CAFE_DETAIL_CYCLES
   long long sc0 = cafe_clock_ordered();
@@ -1422,7 +1442,7 @@ __device__ void cafe_select_keyed(const CafeDev &D, const CafeConsts &K, int ev,
 #ifdef CAFE_DETAIL_CYCLES
             long long ev0 = cafe_clock_ordered();
 #endif
-            cafe_row_eval(D, K, r, ev, T);
+            cafe_row_eval(D, K, r, ev, T, evd);
 #ifdef CAFE_DETAIL_CYCLES
             eval_cyc += cafe_clock_ordered() - ev0;
 #endif
@@ -1621,6 +1641,7 @@ __device__ __forceinline__ void d_event_loop(const CafeDev &D, const CafeConsts 
   }
   const bool use_helper = cafe_nblk == 2;
   __shared__ int s_post, s_seq;  // this event's fill went to the helper; requests posted
+  __shared__ double s_evd[CAFE_EVD_SMEM];  // the growth log's first entries (cafe_row_replay)
   const double V = K.vhat_cls[1];
   unsigned long long my_min = CAFE_KEY_NONE;  // smallest key of this selecting thread's rows
   bool my_forced = false;                     // one of them is stamped -1
@@ -1661,6 +1682,7 @@ __device__ __forceinline__ void d_event_loop(const CafeDev &D, const CafeConsts 
     s_seq = 0;
     s_cyc[0] = s_cyc[1] = s_cyc[2] = s_cyc[3] = 0;
     D.ev_vd[0] = 0.0;
+    s_evd[0] = 0.0;
     D.ev_vs[0] = 0.0;
     s_slow = !allow_fast || D.ctr[CTR_SLOW] != 0;
     s_done = (*D.err != 0) || (s_na > D.act_cap) || (s_nvs2 > D.vs2_cap) || (s_nrows > D.row_cap);
@@ -1710,7 +1732,7 @@ __device__ __forceinline__ void d_event_loop(const CafeDev &D, const CafeConsts 
     // selection of the first event
     if (hid >= 0)
       cafe_select_keyed(D, K, 0, 0.0, s_nrows, hid, NSEL, 2, my_min, my_forced, s_dirty, s_forced, s_sel, s_gmax,
-                        s_emax, s_dsum, V);
+                        s_emax, s_dsum, V, s_evd);
     __syncthreads();
     if (tid == 0) s_best = s_sel.red[0];
     __syncthreads();
@@ -1744,6 +1766,7 @@ __device__ __forceinline__ void d_event_loop(const CafeDev &D, const CafeConsts 
             // log this event's growth of the rows (VoxelsCA.C:514)
             s_vd = s_nuc ? 0.0 : V * s_dt;
             D.ev_vd[s_ev] = s_vd;
+            if (s_ev < CAFE_EVD_SMEM) s_evd[s_ev] = s_vd;
             s_vs = s_vs + s_vd;
             D.ev_vs[s_ev] = s_vs;
             s_dsum += fabs(s_dt);
@@ -1949,7 +1972,7 @@ __device__ __forceinline__ void d_event_loop(const CafeDev &D, const CafeConsts 
         }
       } else {
         cafe_select_keyed(D, K, e, s_tinc, nrows_ev, hid, NSEL, 2, my_min, my_forced, s_dirty, s_forced, s_sel,
-                          s_gmax, s_emax, s_dsum, V);
+                          s_gmax, s_emax, s_dsum, V, s_evd);
       }
       __syncthreads();
       CAFE_DCYC(2);
@@ -2009,7 +2032,7 @@ __device__ __forceinline__ void d_event_loop(const CafeDev &D, const CafeConsts 
       // a capturing cell with another growth velocity: bring every row up to
       // date and continue with the exact per-event scan
       for (int r = tid; r < s_nrows; r += nthr) {
-        cafe_row_replay(D, r, s_ev);
+        cafe_row_replay(D, r, s_ev, s_evd);
         D.row_m[r] = CAFE_M_DONE;
       }
       __syncthreads();
