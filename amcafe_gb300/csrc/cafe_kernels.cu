@@ -999,6 +999,7 @@ __device__ __forceinline__ void cafe_row_best_live(const CafeDev &D, const CafeC
   bool mono = vb > 0 && vb < CRM_BITS_INF;  // 0 < v < inf
   const double *g = D.row_g + r * CAFE_NSLOT;
   const uint8_t *ord = D.row_ord + r * CAFE_NSLOT;
+  const int32_t *nbr = D.a_nbr + (long long)p * CAFE_NSLOT;
   int nn = D.a_nn[p];
   int jrow = D.row_j[r];
   double ruq_p = D.a_ruq[p];
@@ -1007,22 +1008,19 @@ __device__ __forceinline__ void cafe_row_best_live(const CafeDev &D, const CafeC
   // with k2out (best enters empty): the smallest time key of the candidates
   // other than the best one; in g order the slot that ends the visit has it
   unsigned long long k2 = CAFE_KEY_NONE;
-  for (int k = 0; k < nn; ++k) {
-    int s = mono ? ord[k] : k;
-    if (!(live >> s & 1u)) continue;
-    double dr = g[s] - E;
+  // visits slot s of order position k with numerator gs and neighbour q:
+  // 0 go on, 1 the visit ends
+  auto visit = [&](int k, int s, double gs, int q) -> int {
+    if (!(live >> s & 1u)) return 0;
+    double dr = gs - E;
     double t = dr / v;
-    if (cafe_is_nan(t)) continue;
+    if (cafe_is_nan(t)) return 0;
     unsigned long long tk = cafe_key_canon(t);
-    if (bounded && !(tk <= CAFE_KEY_1E6)) {
-      if (mono) break;
-      continue;
-    }
+    if (bounded && !(tk <= CAFE_KEY_1E6)) return mono ? 1 : 0;
     if (mono && have && tk > tfirst) {
       k2 = min(k2, tk);
-      break;
+      return 1;
     }
-    int q = D.a_nbr[(long long)p * CAFE_NSLOT + s];
     CafeCand c;
     c.t = t;
     c.tk = tk;
@@ -1043,6 +1041,26 @@ __device__ __forceinline__ void cafe_row_best_live(const CafeDev &D, const CafeC
       have = true;
       tfirst = tk;
     }
+    return 0;
+  };
+  // the first four slots of the visiting order with their numerators and
+  // neighbours, loaded together (a visit usually ends within them)
+  int s4[4], q4[4];
+  double g4[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) s4[i] = i < nn ? (mono ? (int)ord[i] : i) : 0;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    g4[i] = i < nn ? g[s4[i]] : 0.0;
+    q4[i] = i < nn ? nbr[s4[i]] : 0;
+  }
+  bool ended = false;
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+    if (!ended && i < nn) ended = visit(i, s4[i], g4[i], q4[i]) != 0;
+  for (int k = 4; k < nn && !ended; ++k) {
+    int s = mono ? ord[k] : k;
+    ended = visit(k, s, g[s], nbr[s]) != 0;
   }
   if (k2out) *k2out = k2;
 }
@@ -1086,33 +1104,13 @@ __device__ __forceinline__ int cafe_find_slot(const CafeDev &D, int q, int targe
 
 // Applies the logged growth of events row_m+1 .. min(upto, row_death). A
 // nucleation logs +0, which leaves an extent unchanged (extents are never -0).
-// The event loop keeps the first CAFE_EVD_SMEM entries of the growth log in
-// shared memory as well (evd): a replay reads them there instead of making a
-// round trip to L2 per replayed event (the log is written as the events
-// happen, so its lines are not in L1); evd may be null (global log only).
-#define CAFE_EVD_SMEM 2048
-__device__ __forceinline__ void cafe_row_replay(const CafeDev &D, int r, int upto, const double *evd = nullptr) {
+__device__ __forceinline__ void cafe_row_replay(const CafeDev &D, int r, int upto) {
   int m = D.row_m[r];
   int stop = min(upto, D.row_death[r]);
   if (stop <= m) return;
   double E = D.row_E[r];
-  int k = m + 1;
-  if (evd) {
-    // four log entries loaded together, then the dependent additions
-    for (; k + 3 <= stop && k + 3 < CAFE_EVD_SMEM; k += 4) {
-      const double a = evd[k], b = evd[k + 1], c = evd[k + 2], d = evd[k + 3];
-      E = E + a;
-      E = cafe_is_neg(E) ? 0.0 : E;
-      E = E + b;
-      E = cafe_is_neg(E) ? 0.0 : E;
-      E = E + c;
-      E = cafe_is_neg(E) ? 0.0 : E;
-      E = E + d;
-      E = cafe_is_neg(E) ? 0.0 : E;
-    }
-  }
-  for (; k <= stop; ++k) {
-    E = E + ((evd && k < CAFE_EVD_SMEM) ? evd[k] : D.ev_vd[k]);
+  for (int k = m + 1; k <= stop; ++k) {
+    E = E + D.ev_vd[k];
     E = cafe_is_neg(E) ? 0.0 : E;  // (E < 0.0) ? 0.0 : E
   }
   D.row_E[r] = E;
@@ -1122,12 +1120,12 @@ __device__ __forceinline__ void cafe_row_replay(const CafeDev &D, int r, int upt
 // Exact evaluation of row r (live slots `live`) for the iteration after `ev`
 // events at time T.
 __device__ __forceinline__ void cafe_row_eval_live(const CafeDev &D, const CafeConsts &K, int r, int ev,
-                                                   double T, uint32_t live, const double *evd = nullptr) {
+                                                   double T, uint32_t live) {
 #ifdef CAFE_DETAIL_CYCLES
   long long rp0 = clock64();
   int rm0 = D.row_m[r];
 #endif
-  cafe_row_replay(D, r, ev, evd);
+  cafe_row_replay(D, r, ev);
 #ifdef CAFE_DETAIL_CYCLES
   atomicAdd(&D.stat[STAT_DETAIL + 27], (unsigned long long)(D.row_m[r] - rm0 > 0 ? D.row_m[r] - rm0 : 0));
   atomicAdd(&D.stat[STAT_DETAIL + 28], 1ULL);
@@ -1157,8 +1155,8 @@ __device__ __forceinline__ void cafe_row_eval_live(const CafeDev &D, const CafeC
   D.row_key2[r] = k2 == CAFE_KEY_NONE ? key : cafe_key(T + cafe_unkey(k2));
 }
 __device__ __forceinline__ void cafe_row_eval(const CafeDev &D, const CafeConsts &K, int r, int ev,
-                                              double T, const double *evd = nullptr) {
-  cafe_row_eval_live(D, K, r, ev, T, D.row_live[r], evd);
+                                              double T) {
+  cafe_row_eval_live(D, K, r, ev, T, D.row_live[r]);
 }
 
 // Frontier rows of the step, in three passes so that the capture geometry,
@@ -1293,7 +1291,7 @@ __device__ __forceinline__ void cafe_bar_n(int id, int n) { asm volatile("bar.sy
 __device__ void cafe_select_keyed(const CafeDev &D, const CafeConsts &K, int ev, double T, int nrows, int gtid,
                                   int gn, int bar, unsigned long long &my_min, bool &my_forced,
                                   unsigned char *dirty, unsigned char *forced, CafeSelShared &S, double gmax,
-                                  double emax, double dsum, double V, const double *evd) {
+                                  double emax, double dsum, double V) {
   const int lane = gtid & 31, gw = gtid >> 5, ngw = gn >> 5;
 #ifdef CAFE_DETAIL_CYCLES
   long long sc0 = cafe_clock_ordered();
@@ -1442,7 +1440,7 @@ __device__ void cafe_select_keyed(const CafeDev &D, const CafeConsts &K, int ev,
 #ifdef CAFE_DETAIL_CYCLES
             long long ev0 = cafe_clock_ordered();
 #endif
-            cafe_row_eval(D, K, r, ev, T, evd);
+            cafe_row_eval(D, K, r, ev, T);
 #ifdef CAFE_DETAIL_CYCLES
             eval_cyc += cafe_clock_ordered() - ev0;
 #endif
@@ -1641,7 +1639,6 @@ __device__ __forceinline__ void d_event_loop(const CafeDev &D, const CafeConsts 
   }
   const bool use_helper = cafe_nblk == 2;
   __shared__ int s_post, s_seq;  // this event's fill went to the helper; requests posted
-  __shared__ double s_evd[CAFE_EVD_SMEM];  // the growth log's first entries (cafe_row_replay)
   const double V = K.vhat_cls[1];
   unsigned long long my_min = CAFE_KEY_NONE;  // smallest key of this selecting thread's rows
   bool my_forced = false;                     // one of them is stamped -1
@@ -1682,7 +1679,6 @@ __device__ __forceinline__ void d_event_loop(const CafeDev &D, const CafeConsts 
     s_seq = 0;
     s_cyc[0] = s_cyc[1] = s_cyc[2] = s_cyc[3] = 0;
     D.ev_vd[0] = 0.0;
-    s_evd[0] = 0.0;
     D.ev_vs[0] = 0.0;
     s_slow = !allow_fast || D.ctr[CTR_SLOW] != 0;
     s_done = (*D.err != 0) || (s_na > D.act_cap) || (s_nvs2 > D.vs2_cap) || (s_nrows > D.row_cap);
@@ -1732,7 +1728,7 @@ __device__ __forceinline__ void d_event_loop(const CafeDev &D, const CafeConsts 
     // selection of the first event
     if (hid >= 0)
       cafe_select_keyed(D, K, 0, 0.0, s_nrows, hid, NSEL, 2, my_min, my_forced, s_dirty, s_forced, s_sel, s_gmax,
-                        s_emax, s_dsum, V, s_evd);
+                        s_emax, s_dsum, V);
     __syncthreads();
     if (tid == 0) s_best = s_sel.red[0];
     __syncthreads();
@@ -1766,7 +1762,6 @@ __device__ __forceinline__ void d_event_loop(const CafeDev &D, const CafeConsts 
             // log this event's growth of the rows (VoxelsCA.C:514)
             s_vd = s_nuc ? 0.0 : V * s_dt;
             D.ev_vd[s_ev] = s_vd;
-            if (s_ev < CAFE_EVD_SMEM) s_evd[s_ev] = s_vd;
             s_vs = s_vs + s_vd;
             D.ev_vs[s_ev] = s_vs;
             s_dsum += fabs(s_dt);
@@ -1972,7 +1967,7 @@ __device__ __forceinline__ void d_event_loop(const CafeDev &D, const CafeConsts 
         }
       } else {
         cafe_select_keyed(D, K, e, s_tinc, nrows_ev, hid, NSEL, 2, my_min, my_forced, s_dirty, s_forced, s_sel,
-                          s_gmax, s_emax, s_dsum, V, s_evd);
+                          s_gmax, s_emax, s_dsum, V);
       }
       __syncthreads();
       CAFE_DCYC(2);
@@ -2032,7 +2027,7 @@ __device__ __forceinline__ void d_event_loop(const CafeDev &D, const CafeConsts 
       // a capturing cell with another growth velocity: bring every row up to
       // date and continue with the exact per-event scan
       for (int r = tid; r < s_nrows; r += nthr) {
-        cafe_row_replay(D, r, s_ev, s_evd);
+        cafe_row_replay(D, r, s_ev);
         D.row_m[r] = CAFE_M_DONE;
       }
       __syncthreads();
