@@ -68,7 +68,9 @@ def test_config1_window_across_the_first_layer_change(tmp_path):
     from amcafe_gb300 import Simulation
 
     chunk = 3000
-    ck = str(tmp_path / "c1.ckpt")
+    # the checkpoint (0.7 GB) in memory where the machine offers it
+    ckdir = "/dev/shm" if os.path.isdir("/dev/shm") and os.access("/dev/shm", os.W_OK) else str(tmp_path)
+    ck = os.path.join(ckdir, "cafe_c1_window_%d.ckpt" % os.getpid())
     sim = Simulation(C1, device=0)
     sim.InitializeVoxels()
     sim.begin()
@@ -98,3 +100,4 @@ def test_config1_window_across_the_first_layer_change(tmp_path):
     assert info["indlayer"] == layer0 + 1
     assert info["nGrain"] != ng0
     sim.close()
+    os.unlink(ck)
