@@ -527,8 +527,11 @@ def run_ensemble(args, ws, rank, local):
     digests_b = [_final_digest(s) for s in b.sims]
     nvox = [s.ncell for s in b.sims]
     steps_each = [s.info()["steps"] for s in b.sims]
-    launches = sum(s.stats()["launches"] for s in b.sims)
-    threads = min(args.threads or 1, n)  # as cafe_batch_create picks
+    report = b.report()
+    # the realisations' own launches (initialisation, layer work, plain steps)
+    # and the batched launches (one per step kernel for all realisations)
+    launches = sum(s.stats()["launches"] for s in b.sims) + report["launches"]
+    threads = min(args.threads, n) if args.threads > 0 else 0  # 0: batched launches
     b.close()
     # ---- sequential plain runs of the same realisations (bounded by --seq-seconds)
     seq_s, seq_done, same = 0.0, 0, True
@@ -589,6 +592,8 @@ def run_ensemble(args, ws, rank, local):
             "cpu_baseline": cpu,
             "clocks": clk,
             "gpu_launches": int(launches),
+            "batched": {"batch_steps": report["batch_steps"], "launches": report["launches"],
+                        "autotuner": report["tuning"]},
             "wall_s_timed": batch_s,
         }
         print(json.dumps(out))
