@@ -1289,7 +1289,7 @@ __device__ __forceinline__ void cafe_bar_n(int id, int n) { asm volatile("bar.sy
 // in S.red[0] (valid after the group's next barrier; every group thread has
 // passed the last barrier when this returns).
 __device__ void cafe_select_keyed(const CafeDev &D, const CafeConsts &K, int ev, double T, int nrows, int gtid,
-                                  int gn, int bar, unsigned long long &my_min, bool &my_forced,
+                                  int gn, int bar, unsigned long long &my_min, int &my_hot, bool &my_forced,
                                   unsigned char *dirty, unsigned char *forced, CafeSelShared &S, double gmax,
                                   double emax, double dsum, double V) {
   const int lane = gtid & 31, gw = gtid >> 5, ngw = gn >> 5;
@@ -1303,6 +1303,7 @@ __device__ void cafe_select_keyed(const CafeDev &D, const CafeConsts &K, int ev,
   if (dirty[gtid]) {
     dirty[gtid] = 0;
     unsigned long long m = CAFE_KEY_NONE;
+    int mr = -1;
     // batches of eight loads in flight together
     for (int r0 = gtid; r0 < nrows; r0 += 8 * gn) {
       unsigned long long kk[8];
@@ -1312,9 +1313,14 @@ __device__ void cafe_select_keyed(const CafeDev &D, const CafeConsts &K, int ev,
         kk[i] = r < nrows ? D.row_key[r] : CAFE_KEY_NONE;
       }
 #pragma unroll
-      for (int i = 0; i < 8; ++i) m = min(m, kk[i]);
+      for (int i = 0; i < 8; ++i)
+        if (kk[i] < m) {
+          m = kk[i];
+          mr = r0 + i * gn;
+        }
     }
     my_min = m;
+    my_hot = mr;
   }
   CafeCand best;
   // this thread's last scan in this selection: marked rows, smallest key of
@@ -1322,6 +1328,7 @@ __device__ void cafe_select_keyed(const CafeDev &D, const CafeConsts &K, int ev,
   bool sc_have = false;
   uint32_t sc_mark = 0;
   unsigned long long sc_u = CAFE_KEY_NONE;
+  int sc_ur = -1;
 #ifdef CAFE_DETAIL_CYCLES
   long long sc1 = cafe_clock_ordered();
   if (gtid == 0) S.cyc[0] += sc1 - sc0;  // dirty rescan
@@ -1375,6 +1382,7 @@ __device__ void cafe_select_keyed(const CafeDev &D, const CafeConsts &K, int ev,
     best = cafe_cand_none();
     if (kthr != CAFE_KEY_NONE && (my_min <= kthr || my_forced)) {
       unsigned long long m = CAFE_KEY_NONE;
+      int mr = -1;
       // this thread's rows r = r0 + i gn, 32 at a time: first their keys,
       // loaded together, mark the rows at or below the threshold (and, when
       // forced, the rows stamped -1); then only the marked rows are visited.
@@ -1388,6 +1396,7 @@ __device__ void cafe_select_keyed(const CafeDev &D, const CafeConsts &K, int ev,
         if (one_chunk && sc_have && !my_forced && sc_u > kthr) {
           mark = sc_mark;
           m = sc_u;
+          mr = sc_ur;
         } else {
 #ifdef CAFE_DETAIL_CYCLES
           long long pa0 = cafe_clock_ordered();
@@ -1414,10 +1423,12 @@ __device__ void cafe_select_keyed(const CafeDev &D, const CafeConsts &K, int ev,
 #pragma unroll
             for (int i = 0; i < 8; ++i) {
               // a visited row's key enters the minimum after its visit
-              if (kk[i] <= kthr || (fm >> i & 1u))
+              if (kk[i] <= kthr || (fm >> i & 1u)) {
                 mark |= 1u << (b + i);
-              else
-                m = min(m, kk[i]);
+              } else if (kk[i] < m) {
+                m = kk[i];
+                mr = r0 + (b + i) * gn;
+              }
             }
           }
 #ifdef CAFE_DETAIL_CYCLES
@@ -1428,6 +1439,7 @@ __device__ void cafe_select_keyed(const CafeDev &D, const CafeConsts &K, int ev,
             sc_have = true;
             sc_mark = mark;
             sc_u = m;
+            sc_ur = mr;
           }
         }
         while (mark) {
@@ -1460,10 +1472,14 @@ __device__ void cafe_select_keyed(const CafeDev &D, const CafeConsts &K, int ev,
             c.q = D.row_bq[r];
             if (cafe_cand_better(c, best)) best = c;
           }
-          m = min(m, k);
+          if (k < m) {
+            m = k;
+            mr = r;
+          }
         }
       }
       my_min = m;
+      my_hot = mr;
       my_forced = false;
     }
 #ifdef CAFE_DETAIL_CYCLES
@@ -1641,6 +1657,7 @@ __device__ __forceinline__ void d_event_loop(const CafeDev &D, const CafeConsts 
   __shared__ int s_post, s_seq;  // this event's fill went to the helper; requests posted
   const double V = K.vhat_cls[1];
   unsigned long long my_min = CAFE_KEY_NONE;  // smallest key of this selecting thread's rows
+  int my_hot = -1;                            // ... and its row
   bool my_forced = false;                     // one of them is stamped -1
   if (hid >= 0) {
     s_dirty[hid] = 1;
@@ -1727,7 +1744,7 @@ __device__ __forceinline__ void d_event_loop(const CafeDev &D, const CafeConsts 
     }
     // selection of the first event
     if (hid >= 0)
-      cafe_select_keyed(D, K, 0, 0.0, s_nrows, hid, NSEL, 2, my_min, my_forced, s_dirty, s_forced, s_sel, s_gmax,
+      cafe_select_keyed(D, K, 0, 0.0, s_nrows, hid, NSEL, 2, my_min, my_hot, my_forced, s_dirty, s_forced, s_sel, s_gmax,
                         s_emax, s_dsum, V);
     __syncthreads();
     if (tid == 0) s_best = s_sel.red[0];
@@ -1893,23 +1910,32 @@ __device__ __forceinline__ void d_event_loop(const CafeDev &D, const CafeConsts 
         st.x = s_rng;
         s_unext = cafe_uniform_next(&st);
         s_rng_next = st.x;
-      } else if (hid >= 0 && !s_nuc && cafe_is_neg(s_dt)) {
-        // a negative event may clamp a small extent at zero (VoxelsCA.C:515),
-        // which breaks the key bound of that row: mark the rows whose
-        // extrapolated extent comes near zero for re-evaluation
-        const double vd = s_vd;
-        const double margin = (double)(e + 16) * 0x1p-48 * (s_emax + s_gmax + V * s_dsum + 1e-300);
-        const double vs_prev = D.ev_vs[e - 1];
-        for (int r = hid; r < nrows_ev; r += NSEL) {
-          if (D.row_death[r] < e) continue;
-          int m = D.row_m[r];
-          if (m >= e) continue;
-          double elb = D.row_E[r] + (vs_prev - D.ev_vs[m]);
-          if (elb + vd < margin) {
-            D.row_stamp[r] = -1;
-            s_forced[r % NSEL] = 1;
+      } else if (hid >= 0) {
+        if (!s_nuc && cafe_is_neg(s_dt)) {
+          // a negative event may clamp a small extent at zero (VoxelsCA.C:515),
+          // which breaks the key bound of that row: mark the rows whose
+          // extrapolated extent comes near zero for re-evaluation
+          const double vd = s_vd;
+          const double margin = (double)(e + 16) * 0x1p-48 * (s_emax + s_gmax + V * s_dsum + 1e-300);
+          const double vs_prev = D.ev_vs[e - 1];
+          for (int r = hid; r < nrows_ev; r += NSEL) {
+            if (D.row_death[r] < e) continue;
+            int m = D.row_m[r];
+            if (m >= e) continue;
+            double elb = D.row_E[r] + (vs_prev - D.ev_vs[m]);
+            if (elb + vd < margin) {
+              D.row_stamp[r] = -1;
+              s_forced[r % NSEL] = 1;
+            }
           }
         }
+        // this thread's smallest-key row is the one an exact evaluation of
+        // the next selection most likely needs: its growth is replayed up to
+        // this event now, while the capture is applied, so that evaluation
+        // replays (almost) nothing; the same additions in the same order as
+        // the lazy replay, only earlier (after the clamp check above, which
+        // reads the state before this event)
+        if (my_hot >= 0 && my_hot < nrows_ev) cafe_row_replay(D, my_hot, e);
       }
       __syncthreads();
       CAFE_DCYC(1);
@@ -1966,7 +1992,7 @@ __device__ __forceinline__ void d_event_loop(const CafeDev &D, const CafeConsts 
           }
         }
       } else {
-        cafe_select_keyed(D, K, e, s_tinc, nrows_ev, hid, NSEL, 2, my_min, my_forced, s_dirty, s_forced, s_sel,
+        cafe_select_keyed(D, K, e, s_tinc, nrows_ev, hid, NSEL, 2, my_min, my_hot, my_forced, s_dirty, s_forced, s_sel,
                           s_gmax, s_emax, s_dsum, V);
       }
       __syncthreads();
