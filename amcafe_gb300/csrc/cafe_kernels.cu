@@ -1658,6 +1658,9 @@ __device__ __forceinline__ void d_event_loop(const CafeDev &D, const CafeConsts 
   const double V = K.vhat_cls[1];
   unsigned long long my_min = CAFE_KEY_NONE;  // smallest key of this selecting thread's rows
   int my_hot = -1;                            // ... and its row
+  int hot_r = -1;                             // the row whose extent this thread keeps current
+  bool hot_ok = false;                        // hot_E is its extent after event e - 1
+  double hot_E = 0.0;
   bool my_forced = false;                     // one of them is stamped -1
   if (hid >= 0) {
     s_dirty[hid] = 1;
@@ -1930,12 +1933,33 @@ __device__ __forceinline__ void d_event_loop(const CafeDev &D, const CafeConsts 
           }
         }
         // this thread's smallest-key row is the one an exact evaluation of
-        // the next selection most likely needs: its growth is replayed up to
-        // this event now, while the capture is applied, so that evaluation
-        // replays (almost) nothing; the same additions in the same order as
-        // the lazy replay, only earlier (after the clamp check above, which
-        // reads the state before this event)
-        if (my_hot >= 0 && my_hot < nrows_ev) cafe_row_replay(D, my_hot, e);
+        // the next selection most likely needs. Once its extent is current
+        // (after that evaluation's replay) it is kept current, one addition
+        // per event with the logged growth, held in registers and written
+        // through, so that the next evaluation replays nothing: the same
+        // additions in the same order as the lazy replay, only earlier (and
+        // after the clamp check above, which reads the state before this
+        // event). Only this thread writes its rows' extents in the keyed loop;
+        // a row that dies marks its owner dirty, whose rescan moves my_hot.
+        if (my_hot >= 0 && my_hot < nrows_ev) {
+          if (hot_r != my_hot) {
+            hot_r = my_hot;
+            hot_ok = false;
+          }
+          if (!hot_ok && D.row_m[hot_r] == e - 1 && D.row_death[hot_r] >= e) {
+            hot_E = D.row_E[hot_r];
+            hot_ok = true;
+          }
+          if (hot_ok) {
+            hot_E = hot_E + s_vd;
+            hot_E = cafe_is_neg(hot_E) ? 0.0 : hot_E;  // (E < 0.0) ? 0.0 : E
+            D.row_E[hot_r] = hot_E;
+            D.row_m[hot_r] = e;
+          }
+        } else {
+          hot_r = -1;
+          hot_ok = false;
+        }
       }
       __syncthreads();
       CAFE_DCYC(1);

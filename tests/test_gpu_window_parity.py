@@ -67,7 +67,7 @@ def test_config1_window_across_the_first_layer_change(tmp_path):
     step of the change is found by running in chunks from checkpoints."""
     from amcafe_gb300 import Simulation
 
-    chunk = 3000
+    chunk = 1000
     # the checkpoint (0.7 GB) in memory where the machine offers it
     ckdir = "/dev/shm" if os.path.isdir("/dev/shm") and os.access("/dev/shm", os.W_OK) else str(tmp_path)
     ck = os.path.join(ckdir, "cafe_c1_window_%d.ckpt" % os.getpid())
