@@ -1280,18 +1280,38 @@ __device__ __forceinline__ int cafe_bar_or(int id, int n, int v) {
 }
 __device__ __forceinline__ void cafe_bar_n(int id, int n) { asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory"); }
 
+// Smallest and second smallest key (and rows) of a sequence of rows: row r
+// with key k enters.
+__device__ __forceinline__ void cafe_top2(unsigned long long k, int r, unsigned long long &m, int &mr,
+                                          unsigned long long &m2, int &r2) {
+  if (k < m) {
+    m2 = m;
+    r2 = mr;
+    m = k;
+    mr = r;
+  } else if (k < m2) {
+    m2 = k;
+    r2 = r;
+  }
+}
+
 // Keyed selection of the best capture among rows [0, nrows) for the iteration
 // after `ev` events at time T (VoxelsCA.C:386-480 restricted to the rows that
 // can hold the minimum), by the group of gn threads (gtid = 0..gn-1) that
 // shares named barrier `bar`. Thread gtid owns rows r = gtid (mod gn) and keeps
-// the smallest key among them in my_min, rescanned when dirty[gtid] is set; a
-// forced[gtid] flag makes it evaluate its rows stamped -1. The result is left
+// the smallest key among them in my_min, with its row in my_hot, and the
+// smallest key of its other rows in my_u2, with its row in my_r2 (-1 none; -2
+// not known), all rescanned when dirty[gtid] is set; a forced[gtid] flag makes
+// it evaluate its rows stamped -1. Every key change made elsewhere (a row's
+// key raised, a row's death, a new row) sets dirty, so between rescans the
+// thread's own evaluations are the only changes. The result is left
 // in S.red[0] (valid after the group's next barrier; every group thread has
 // passed the last barrier when this returns).
 __device__ void cafe_select_keyed(const CafeDev &D, const CafeConsts &K, int ev, double T, int nrows, int gtid,
-                                  int gn, int bar, unsigned long long &my_min, int &my_hot, bool &my_forced,
-                                  unsigned char *dirty, unsigned char *forced, CafeSelShared &S, double gmax,
-                                  double emax, double dsum, double V) {
+                                  int gn, int bar, unsigned long long &my_min, int &my_hot,
+                                  unsigned long long &my_u2, int &my_r2, bool &my_forced, unsigned char *dirty,
+                                  unsigned char *forced, CafeSelShared &S, double gmax, double emax, double dsum,
+                                  double V) {
   const int lane = gtid & 31, gw = gtid >> 5, ngw = gn >> 5;
 #ifdef CAFE_DETAIL_CYCLES
   long long sc0 = cafe_clock_ordered();
@@ -1302,8 +1322,8 @@ __device__ void cafe_select_keyed(const CafeDev &D, const CafeConsts &K, int ev,
   }
   if (dirty[gtid]) {
     dirty[gtid] = 0;
-    unsigned long long m = CAFE_KEY_NONE;
-    int mr = -1;
+    unsigned long long m = CAFE_KEY_NONE, m2 = CAFE_KEY_NONE;
+    int mr = -1, r2 = -1;
     // batches of eight loads in flight together
     for (int r0 = gtid; r0 < nrows; r0 += 8 * gn) {
       unsigned long long kk[8];
@@ -1313,22 +1333,20 @@ __device__ void cafe_select_keyed(const CafeDev &D, const CafeConsts &K, int ev,
         kk[i] = r < nrows ? D.row_key[r] : CAFE_KEY_NONE;
       }
 #pragma unroll
-      for (int i = 0; i < 8; ++i)
-        if (kk[i] < m) {
-          m = kk[i];
-          mr = r0 + i * gn;
-        }
+      for (int i = 0; i < 8; ++i) cafe_top2(kk[i], r0 + i * gn, m, mr, m2, r2);
     }
     my_min = m;
     my_hot = mr;
+    my_u2 = m2;
+    my_r2 = r2;
   }
   CafeCand best;
-  // this thread's last scan in this selection: marked rows, smallest key of
-  // the others
+  // this thread's last scan in this selection: marked rows, the two smallest
+  // keys of the others
   bool sc_have = false;
   uint32_t sc_mark = 0;
-  unsigned long long sc_u = CAFE_KEY_NONE;
-  int sc_ur = -1;
+  unsigned long long sc_u = CAFE_KEY_NONE, sc_u2 = CAFE_KEY_NONE;
+  int sc_ur = -1, sc_r2 = -1;
 #ifdef CAFE_DETAIL_CYCLES
   long long sc1 = cafe_clock_ordered();
   if (gtid == 0) S.cyc[0] += sc1 - sc0;  // dirty rescan
@@ -1381,106 +1399,130 @@ __device__ void cafe_select_keyed(const CafeDev &D, const CafeConsts &K, int ev,
 #endif
     best = cafe_cand_none();
     if (kthr != CAFE_KEY_NONE && (my_min <= kthr || my_forced)) {
-      unsigned long long m = CAFE_KEY_NONE;
-      int mr = -1;
-      // this thread's rows r = r0 + i gn, 32 at a time: first their keys,
-      // loaded together, mark the rows at or below the threshold (and, when
-      // forced, the rows stamped -1); then only the marked rows are visited.
-      // Within one selection only this thread changes its rows, and only
-      // marked ones: with its rows in one chunk, a later round whose
-      // threshold lies below the smallest unmarked key of the last scan
-      // visits the same marked rows again without loading the other keys.
-      const bool one_chunk = nrows <= 32 * gn;
-      for (int r0 = gtid; r0 < nrows; r0 += 32 * gn) {
-        uint32_t mark = 0;
-        if (one_chunk && sc_have && !my_forced && sc_u > kthr) {
-          mark = sc_mark;
-          m = sc_u;
-          mr = sc_ur;
-        } else {
+      // visits row r: evaluates it when its key may be the minimum and was not
+      // evaluated for this iteration (or when it is forced), takes its best
+      // candidate when its key is at or below the threshold, returns the key
+      auto visit = [&](int r) -> unsigned long long {
+        unsigned long long k = D.row_key[r];
+        int stamp = D.row_stamp[r];
+        // stamp -1: forced after a possible clamp of the row's extent
+        if ((k <= kthr && stamp != ev + 1) || (stamp == -1 && D.row_alive[r])) {
 #ifdef CAFE_DETAIL_CYCLES
-          long long pa0 = cafe_clock_ordered();
+          long long ev0 = cafe_clock_ordered();
 #endif
-          // (branch-free batches of eight loads, so that they are in flight
-          // together)
+          cafe_row_eval(D, K, r, ev, T);
+#ifdef CAFE_DETAIL_CYCLES
+          eval_cyc += cafe_clock_ordered() - ev0;
+#endif
+          k = D.row_key[r];
+          again = 1;
+        }
+        if (k <= kthr) {
+          CafeCand c;
+          c.t = D.row_bt[r];
+          c.ruqs = D.row_bruq[r];
+          c.tk = cafe_key_canon(c.t);
+          c.rk = cafe_key_canon(c.ruqs);
+          c.j = D.row_j[r];
+          c.s = D.row_bslot[r];
+          c.r = r;
+          c.p = D.row_pos[r];
+          c.q = D.row_bq[r];
+          if (cafe_cand_better(c, best)) best = c;
+        }
+        return k;
+      };
+      if (!my_forced && my_r2 != -2 && my_u2 > kthr && my_hot >= 0) {
+        // every other row of this thread has a key above the threshold: only
+        // the smallest-key row is visited and no other key is loaded
+#ifdef CAFE_DETAIL_CYCLES
+        n_mark += 1;
+#endif
+        const unsigned long long k = visit(my_hot);
+        if (k <= my_u2) {
+          my_min = k;
+        } else {
+          // the second row is now the smallest; the next one is not known
+          my_min = my_u2;
+          my_hot = my_r2;
+          my_r2 = -2;
+        }
+      } else {
+        unsigned long long m = CAFE_KEY_NONE, m2 = CAFE_KEY_NONE;
+        int mr = -1, r2 = -1;
+        // this thread's rows r = r0 + i gn, 32 at a time: first their keys,
+        // loaded together, mark the rows at or below the threshold (and, when
+        // forced, the rows stamped -1); then only the marked rows are visited.
+        // Within one selection only this thread changes its rows, and only
+        // marked ones: with its rows in one chunk, a later round whose
+        // threshold lies below the smallest unmarked key of the last scan
+        // visits the same marked rows again without loading the other keys.
+        const bool one_chunk = nrows <= 32 * gn;
+        for (int r0 = gtid; r0 < nrows; r0 += 32 * gn) {
+          uint32_t mark = 0;
+          if (one_chunk && sc_have && !my_forced && sc_u > kthr) {
+            mark = sc_mark;
+            m = sc_u;
+            mr = sc_ur;
+            m2 = sc_u2;
+            r2 = sc_r2;
+          } else {
+#ifdef CAFE_DETAIL_CYCLES
+            long long pa0 = cafe_clock_ordered();
+#endif
+            // (branch-free batches of eight loads, so that they are in flight
+            // together)
 #pragma unroll
-          for (int b = 0; b < 32; b += 8) {
-            if (r0 + b * gn >= nrows) break;
-            unsigned long long kk[8];
-#pragma unroll
-            for (int i = 0; i < 8; ++i) {
-              const int r = r0 + (b + i) * gn;
-              kk[i] = r < nrows ? D.row_key[r] : CAFE_KEY_NONE;
-            }
-            uint32_t fm = 0;  // rows stamped -1, visited whatever their key
-            if (my_forced) {
+            for (int b = 0; b < 32; b += 8) {
+              if (r0 + b * gn >= nrows) break;
+              unsigned long long kk[8];
 #pragma unroll
               for (int i = 0; i < 8; ++i) {
                 const int r = r0 + (b + i) * gn;
-                fm |= (r < nrows && D.row_stamp[r] == -1) ? 1u << i : 0u;
+                kk[i] = r < nrows ? D.row_key[r] : CAFE_KEY_NONE;
               }
-            }
+              uint32_t fm = 0;  // rows stamped -1, visited whatever their key
+              if (my_forced) {
 #pragma unroll
-            for (int i = 0; i < 8; ++i) {
-              // a visited row's key enters the minimum after its visit
-              if (kk[i] <= kthr || (fm >> i & 1u)) {
-                mark |= 1u << (b + i);
-              } else if (kk[i] < m) {
-                m = kk[i];
-                mr = r0 + (b + i) * gn;
+                for (int i = 0; i < 8; ++i) {
+                  const int r = r0 + (b + i) * gn;
+                  fm |= (r < nrows && D.row_stamp[r] == -1) ? 1u << i : 0u;
+                }
+              }
+#pragma unroll
+              for (int i = 0; i < 8; ++i) {
+                // a visited row's key enters the two smallest after its visit
+                if (kk[i] <= kthr || (fm >> i & 1u))
+                  mark |= 1u << (b + i);
+                else
+                  cafe_top2(kk[i], r0 + (b + i) * gn, m, mr, m2, r2);
               }
             }
-          }
 #ifdef CAFE_DETAIL_CYCLES
-          phase_a += cafe_clock_ordered() - pa0;
-          n_mark += __popc(mark);
+            phase_a += cafe_clock_ordered() - pa0;
+            n_mark += __popc(mark);
 #endif
-          if (one_chunk) {
-            sc_have = true;
-            sc_mark = mark;
-            sc_u = m;
-            sc_ur = mr;
+            if (one_chunk) {
+              sc_have = true;
+              sc_mark = mark;
+              sc_u = m;
+              sc_ur = mr;
+              sc_u2 = m2;
+              sc_r2 = r2;
+            }
+          }
+          while (mark) {
+            const int r = r0 + (__ffs(mark) - 1) * gn;
+            mark &= mark - 1;
+            cafe_top2(visit(r), r, m, mr, m2, r2);
           }
         }
-        while (mark) {
-          const int r = r0 + (__ffs(mark) - 1) * gn;
-          mark &= mark - 1;
-          unsigned long long k = D.row_key[r];
-          int stamp = D.row_stamp[r];
-          // stamp -1: forced after a possible clamp of the row's extent
-          if ((k <= kthr && stamp != ev + 1) || (stamp == -1 && D.row_alive[r])) {
-#ifdef CAFE_DETAIL_CYCLES
-            long long ev0 = cafe_clock_ordered();
-#endif
-            cafe_row_eval(D, K, r, ev, T);
-#ifdef CAFE_DETAIL_CYCLES
-            eval_cyc += cafe_clock_ordered() - ev0;
-#endif
-            k = D.row_key[r];
-            again = 1;
-          }
-          if (k <= kthr) {
-            CafeCand c;
-            c.t = D.row_bt[r];
-            c.ruqs = D.row_bruq[r];
-            c.tk = cafe_key_canon(c.t);
-            c.rk = cafe_key_canon(c.ruqs);
-            c.j = D.row_j[r];
-            c.s = D.row_bslot[r];
-            c.r = r;
-            c.p = D.row_pos[r];
-            c.q = D.row_bq[r];
-            if (cafe_cand_better(c, best)) best = c;
-          }
-          if (k < m) {
-            m = k;
-            mr = r;
-          }
-        }
+        my_min = m;
+        my_hot = mr;
+        my_u2 = m2;
+        my_r2 = r2;
+        my_forced = false;
       }
-      my_min = m;
-      my_hot = mr;
-      my_forced = false;
     }
 #ifdef CAFE_DETAIL_CYCLES
     if (again) {
@@ -1658,6 +1700,8 @@ __device__ __forceinline__ void d_event_loop(const CafeDev &D, const CafeConsts 
   const double V = K.vhat_cls[1];
   unsigned long long my_min = CAFE_KEY_NONE;  // smallest key of this selecting thread's rows
   int my_hot = -1;                            // ... and its row
+  unsigned long long my_u2 = CAFE_KEY_NONE;   // smallest key of its other rows
+  int my_r2 = -2;                             // ... and its row (-1 none, -2 not known)
   int hot_r = -1;                             // the row whose extent this thread keeps current
   bool hot_ok = false;                        // hot_E is its extent after event e - 1
   double hot_E = 0.0;
@@ -1747,8 +1791,8 @@ __device__ __forceinline__ void d_event_loop(const CafeDev &D, const CafeConsts 
     }
     // selection of the first event
     if (hid >= 0)
-      cafe_select_keyed(D, K, 0, 0.0, s_nrows, hid, NSEL, 2, my_min, my_hot, my_forced, s_dirty, s_forced, s_sel, s_gmax,
-                        s_emax, s_dsum, V);
+      cafe_select_keyed(D, K, 0, 0.0, s_nrows, hid, NSEL, 2, my_min, my_hot, my_u2, my_r2, my_forced, s_dirty,
+                        s_forced, s_sel, s_gmax, s_emax, s_dsum, V);
     __syncthreads();
     if (tid == 0) s_best = s_sel.red[0];
     __syncthreads();
@@ -2016,8 +2060,8 @@ __device__ __forceinline__ void d_event_loop(const CafeDev &D, const CafeConsts 
           }
         }
       } else {
-        cafe_select_keyed(D, K, e, s_tinc, nrows_ev, hid, NSEL, 2, my_min, my_hot, my_forced, s_dirty, s_forced, s_sel,
-                          s_gmax, s_emax, s_dsum, V);
+        cafe_select_keyed(D, K, e, s_tinc, nrows_ev, hid, NSEL, 2, my_min, my_hot, my_u2, my_r2, my_forced, s_dirty,
+                          s_forced, s_sel, s_gmax, s_emax, s_dsum, V);
       }
       __syncthreads();
       CAFE_DCYC(2);
