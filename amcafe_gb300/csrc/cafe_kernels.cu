@@ -255,6 +255,50 @@ __device__ __forceinline__ void cafe_active_range(const CafeDev &D, const CafeCo
   r1 = (long long)(zhi + 1) * K.nxy;
 }
 
+// Activity flags of the eight cells i0..i0+7 of row (j, k), i0 and nx multiples
+// of 8: cafe_is_active for each, from the states of the 3 x 3 rows around the
+// chunk over i0-1..i0+8 (an aligned 64-bit word and two bytes per row) and the
+// classes of their liquid cells, all loaded before any test, so that no load
+// waits on another's outcome. A neighbour "emits" when it is mushy or liquid
+// below the liquidus; a cell at or above the liquidus is active when an
+// emitter lies among its 26 neighbours, i.e. in the three-wide window of the
+// nine rows' emitter masks (the cell itself never emits: it is at or above
+// the liquidus and, being tested at all, not mushy).
+__device__ __forceinline__ uint32_t cafe_chunk_active_rows(const CafeDev &D, const CafeConsts &K,
+                                                           const CafeStepParams &P, int i0, int j, int k) {
+  const uint32_t hotmask = (K.hot_cls[0] ? 1u : 0u) | (K.hot_cls[1] ? 2u : 0u) | (K.hot_cls[2] ? 4u : 0u);
+  uint32_t win = 0;               // bit x: an emitter at x - 1..x + 1 (x = 0..9 for i0 - 1 + x) in some row
+  uint32_t own_hot = 0, own_s1 = 0, own_s2 = 0;  // bit c: cell i0 + c at/above the liquidus, liquid, mushy
+#pragma unroll
+  for (int r = 0; r < 9; ++r) {
+    const int y = j + r % 3 - 1, z = k + r / 3 - 1;
+    const bool rowin = y >= 0 && y < K.ny && z >= 0 && z < K.nz;
+    const long long rb = (long long)K.nxy * (rowin ? z : 0) + (long long)K.nx * (rowin ? y : 0);
+    const unsigned long long w = rowin ? *(const unsigned long long *)(D.state + rb + i0) : 0ULL;
+    const unsigned int sl = (rowin && i0 > 0) ? D.state[rb + i0 - 1] : 0u;
+    const unsigned int sr = (rowin && i0 + 8 < K.nx) ? D.state[rb + i0 + 8] : 0u;
+    uint32_t e = 0;
+#pragma unroll
+    for (int x = 0; x < 10; ++x) {
+      const unsigned int s = x == 0 ? sl : (x == 9 ? sr : (unsigned int)(w >> (8 * (x - 1))) & 0xffu);
+      const bool own = r == 4 && x >= 1 && x <= 8;
+      // the class of a liquid neighbour, and of every cell of the chunk
+      const int c = (s == 1u || own) ? cafe_cls(D, P, i0 - 1 + x, y, z) : 1;
+      const bool hot = (hotmask >> c) & 1u;
+      e |= (s == 2u || (s == 1u && !hot)) ? 1u << x : 0u;
+      if (own) {
+        own_hot |= hot ? 1u << (x - 1) : 0u;
+        own_s1 |= s == 1u ? 1u << (x - 1) : 0u;
+        own_s2 |= s == 2u ? 1u << (x - 1) : 0u;
+      }
+    }
+    win |= e | (e << 1) | (e >> 1);
+  }
+  // cell i0 + c is bit c + 1 of the window
+  const uint32_t nb = (win >> 1) & 0xffu;
+  return (own_s2 | (own_hot & nb) | (~own_hot & own_s1)) & 0xffu;
+}
+
 // Activity flags of the CAFE_CELLS_PER_THREAD (8) cells from `base` (bit c
 // for cell base + c). A cell that cannot be at or above the liquidus (outside
 // the pool box, or not below the laser plane) is active exactly when it is
@@ -282,6 +326,7 @@ __device__ __forceinline__ uint32_t cafe_chunk_active(const CafeDev &D, const Ca
       }
       return flags;
     }
+    if (j0 == j1 && k0 == k1 && (K.nx & 7) == 0) return cafe_chunk_active_rows(D, K, P, i0, j0, k0);
   }
   for (int c = 0; c < CAFE_CELLS_PER_THREAD; ++c) {
     long long idx = base + c;
