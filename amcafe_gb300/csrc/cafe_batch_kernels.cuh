@@ -108,7 +108,7 @@ __global__ void kb_active_count(CafeBatchArgs B) {
   CAFE_BATCH_BLOCK(BK_ACOUNT);
   d_active_count(R.D, R.K, R.D.Pd, R.act_chunks, R.nblk_act, b, nb);
 }
-__global__ void kb_scan_blocks(CafeBatchArgs B) {
+__global__ void __launch_bounds__(1024) kb_scan_blocks(CafeBatchArgs B) {
   CAFE_BATCH_BLOCK(BK_SCAN);
   d_scan_blocks(R.D.blk, R.nblk_act, R.D.ctr + CTR_NA, b, nb);
 }
@@ -124,7 +124,7 @@ __global__ void kb_lists_count(CafeBatchArgs B) {
   CAFE_BATCH_BLOCK(BK_LCOUNT);
   d_lists_count(R.D, b, nb);
 }
-__global__ void kb_scan_pairs(CafeBatchArgs B) {
+__global__ void __launch_bounds__(1024) kb_scan_pairs(CafeBatchArgs B) {
   CAFE_BATCH_BLOCK(BK_SCANP);
   d_scan_pairs(R.D.blk, R.nblk_pos, R.D.ctr + CTR_NA, R.D.ctr + CTR_NVS2, R.D.ctr + CTR_NROWS, b, nb);
 }

@@ -255,20 +255,42 @@ __device__ __forceinline__ void cafe_active_range(const CafeDev &D, const CafeCo
   r1 = (long long)(zhi + 1) * K.nxy;
 }
 
+// Flags of the eight state bytes of w (bit c for byte c): the byte is 1
+// (liquid) or 2 (mushy). Bit arithmetic on the word: a byte is 1 or 2 when
+// it is below 4 and its two low bits differ; the eight results, one per
+// byte's lowest bit, are gathered into the top byte by one multiplication.
+__device__ __forceinline__ uint32_t cafe_liq_or_mushy8(unsigned long long w) {
+  const unsigned long long t = w & 0xFCFCFCFCFCFCFCFCULL;
+  const unsigned long long u = (t | (t >> 2) | (t >> 4)) & 0x0C0C0C0C0C0C0C0CULL;
+  const unsigned long long ge4 = (u | (u >> 1)) & 0x0404040404040404ULL;  // bit 2: the byte is >= 4
+  const unsigned long long a = (w ^ (w >> 1)) & ~(ge4 >> 2) & 0x0101010101010101ULL;
+  return (uint32_t)((a * 0x0102040810204080ULL) >> 56);
+}
+
 // Activity flags of the eight cells i0..i0+7 of row (j, k), i0 and nx multiples
-// of 8: cafe_is_active for each, from the states of the 3 x 3 rows around the
-// chunk over i0-1..i0+8 (an aligned 64-bit word and two bytes per row) and the
-// classes of their liquid cells, all loaded before any test, so that no load
-// waits on another's outcome. A neighbour "emits" when it is mushy or liquid
-// below the liquidus; a cell at or above the liquidus is active when an
+// of 8: cafe_is_active for each. The chunk's own classes come first: when no
+// cell of the chunk is at or above the liquidus, each is active exactly when
+// liquid or mushy. Otherwise the states of the 3 x 3 rows around the chunk over
+// i0-1..i0+8 (an aligned 64-bit word and two bytes per row) and the classes of
+// their liquid cells are loaded, all before any test, so that no load waits on
+// another's outcome. A neighbour "emits" when it is mushy or liquid below the
+// liquidus; a cell at or above the liquidus is active when mushy or when an
 // emitter lies among its 26 neighbours, i.e. in the three-wide window of the
-// nine rows' emitter masks (the cell itself never emits: it is at or above
-// the liquidus and, being tested at all, not mushy).
+// nine rows' emitter masks (the cell itself, at or above the liquidus, emits
+// only if mushy, and then it is active anyway).
 __device__ __forceinline__ uint32_t cafe_chunk_active_rows(const CafeDev &D, const CafeConsts &K,
                                                            const CafeStepParams &P, int i0, int j, int k) {
   const uint32_t hotmask = (K.hot_cls[0] ? 1u : 0u) | (K.hot_cls[1] ? 2u : 0u) | (K.hot_cls[2] ? 4u : 0u);
-  uint32_t win = 0;               // bit x: an emitter at x - 1..x + 1 (x = 0..9 for i0 - 1 + x) in some row
-  uint32_t own_hot = 0, own_s1 = 0, own_s2 = 0;  // bit c: cell i0 + c at/above the liquidus, liquid, mushy
+  const unsigned long long wown = *(const unsigned long long *)(D.state + (long long)K.nxy * k + (long long)K.nx * j + i0);
+  uint32_t own_hot = 0;  // bit c: cell i0 + c at or above the liquidus
+#pragma unroll
+  for (int c = 0; c < 8; ++c) own_hot |= ((hotmask >> cafe_cls(D, P, i0 + c, j, k)) & 1u) << c;
+  const uint32_t own_lm = cafe_liq_or_mushy8(wown);
+  if (own_hot == 0) return own_lm;
+  uint32_t own_mushy = 0;
+#pragma unroll
+  for (int c = 0; c < 8; ++c) own_mushy |= (((wown >> (8 * c)) & 0xffu) == 2u ? 1u : 0u) << c;
+  uint32_t win = 0;  // bit x: an emitter at x - 1..x + 1 (x = 0..9 for i0 - 1 + x) in some row
 #pragma unroll
   for (int r = 0; r < 9; ++r) {
     const int y = j + r % 3 - 1, z = k + r / 3 - 1;
@@ -281,30 +303,36 @@ __device__ __forceinline__ uint32_t cafe_chunk_active_rows(const CafeDev &D, con
 #pragma unroll
     for (int x = 0; x < 10; ++x) {
       const unsigned int s = x == 0 ? sl : (x == 9 ? sr : (unsigned int)(w >> (8 * (x - 1))) & 0xffu);
-      const bool own = r == 4 && x >= 1 && x <= 8;
-      // the class of a liquid neighbour, and of every cell of the chunk
-      const int c = (s == 1u || own) ? cafe_cls(D, P, i0 - 1 + x, y, z) : 1;
+      // the class of a liquid neighbour
+      const int c = s == 1u ? cafe_cls(D, P, i0 - 1 + x, y, z) : 1;
       const bool hot = (hotmask >> c) & 1u;
       e |= (s == 2u || (s == 1u && !hot)) ? 1u << x : 0u;
-      if (own) {
-        own_hot |= hot ? 1u << (x - 1) : 0u;
-        own_s1 |= s == 1u ? 1u << (x - 1) : 0u;
-        own_s2 |= s == 2u ? 1u << (x - 1) : 0u;
-      }
     }
     win |= e | (e << 1) | (e >> 1);
   }
   // cell i0 + c is bit c + 1 of the window
   const uint32_t nb = (win >> 1) & 0xffu;
-  return (own_s2 | (own_hot & nb) | (~own_hot & own_s1)) & 0xffu;
+  return ((~own_hot & own_lm) | (own_hot & (own_mushy | nb))) & 0xffu;
+}
+
+// Activity flags of the 8-cell chunk i0..i0+7 of row (j0, k0) (bit c for
+// cell i0 + c). A cell that cannot be at or above the liquidus (outside the
+// pool box, or not below the laser plane) is active exactly when it is liquid
+// or mushy, so a chunk outside the hot region is decided from its state bytes,
+// loaded as one 64-bit word; other chunks take the 3 x 3-row test.
+__device__ __forceinline__ uint32_t cafe_chunk_active_row(const CafeDev &D, const CafeConsts &K,
+                                                          const CafeStepParams &P, long long base, int i0,
+                                                          int j0, int k0) {
+  // (with any_hot_full, T0 or tS reaches the liquidus and no class is cold)
+  const bool cold = !P.any_hot_full && (k0 >= P.kabove || k0 < P.lo[2] || k0 >= P.hi[2] || j0 < P.lo[1] ||
+                                        j0 >= P.hi[1] || i0 + 7 < P.lo[0] || i0 >= P.hi[0]);
+  if (cold) return cafe_liq_or_mushy8(*(const unsigned long long *)(D.state + base));
+  return cafe_chunk_active_rows(D, K, P, i0, j0, k0);
 }
 
 // Activity flags of the CAFE_CELLS_PER_THREAD (8) cells from `base` (bit c
-// for cell base + c). A cell that cannot be at or above the liquidus (outside
-// the pool box, or not below the laser plane) is active exactly when it is
-// liquid or mushy, so a chunk lying in one row outside the hot region is
-// decided from its state bytes, loaded as one 64-bit word; other chunks take
-// the cell-by-cell test.
+// for cell base + c) for any grid: a chunk lying in one row is decided as in
+// cafe_chunk_active_row, others cell by cell.
 __device__ __forceinline__ uint32_t cafe_chunk_active(const CafeDev &D, const CafeConsts &K,
                                                       const CafeStepParams &P, long long base) {
   static_assert(CAFE_CELLS_PER_THREAD == 8, "one 64-bit word of states per thread");
@@ -313,20 +341,12 @@ __device__ __forceinline__ uint32_t cafe_chunk_active(const CafeDev &D, const Ca
     int i0, j0, k0, i1, j1, k1;
     cafe_cell_xyz(K, base, i0, j0, k0);
     cafe_cell_xyz(K, base + 7, i1, j1, k1);
+    if (j0 == j1 && k0 == k1 && (K.nx & 7) == 0) return cafe_chunk_active_row(D, K, P, base, i0, j0, k0);
     bool cold = false;
-    // (with any_hot_full, T0 or tS reaches the liquidus and no class is cold)
     if (!P.any_hot_full && j0 == j1 && k0 == k1)
       cold = k0 >= P.kabove || k0 < P.lo[2] || k0 >= P.hi[2] || j0 < P.lo[1] || j0 >= P.hi[1] || i1 < P.lo[0] ||
              i0 >= P.hi[0];
-    if (cold) {
-      unsigned long long w = *(const unsigned long long *)(D.state + base);
-      for (int c = 0; c < 8; ++c) {
-        unsigned int b = (unsigned int)(w >> (8 * c)) & 0xffu;
-        flags |= (b - 1u < 2u ? 1u : 0u) << c;
-      }
-      return flags;
-    }
-    if (j0 == j1 && k0 == k1 && (K.nx & 7) == 0) return cafe_chunk_active_rows(D, K, P, i0, j0, k0);
+    if (cold && (base & 7) == 0) return cafe_liq_or_mushy8(*(const unsigned long long *)(D.state + base));
   }
   for (int c = 0; c < CAFE_CELLS_PER_THREAD; ++c) {
     long long idx = base + c;
@@ -336,18 +356,39 @@ __device__ __forceinline__ uint32_t cafe_chunk_active(const CafeDev &D, const Ca
 }
 
 // Activity flags of this thread's `chunks` chunks (bit 8 c + j for cell
-// base + 8 c + j).
+// base + 8 c + j), base a multiple of 8. With nx a multiple of 8 every chunk
+// lies in one row: the cell coordinates are formed once and stepped from
+// chunk to chunk.
 __device__ __forceinline__ uint32_t cafe_thread_active(const CafeDev &D, const CafeConsts &K,
                                                        const CafeStepParams &P, long long base, int chunks,
                                                        long long r0, long long r1) {
   uint32_t f = 0;
   if (base >= r1 || base + 8LL * chunks <= r0) return 0;  // no plane that can hold active cells
+  if ((K.nx & 7) == 0 && base + 8LL * chunks <= K.N) {
+    int i, j, k;
+    cafe_cell_xyz(K, base, i, j, k);
 #pragma unroll
-  for (int c = 0; c < CAFE_ACT_MAX_CHUNKS; ++c)
-    if (c < chunks) f |= cafe_chunk_active(D, K, P, base + 8 * c) << (8 * c);
-  // cells of the range's edge chunks that lie outside it
-  for (int c = 0; c < 8 * chunks; ++c)
-    if (base + c < r0 || base + c >= r1) f &= ~(1u << c);
+    for (int c = 0; c < CAFE_ACT_MAX_CHUNKS; ++c)
+      if (c < chunks) {
+        f |= cafe_chunk_active_row(D, K, P, base + 8 * c, i, j, k) << (8 * c);
+        i += 8;
+        if (i == K.nx) {
+          i = 0;
+          if (++j == K.ny) {
+            j = 0;
+            ++k;
+          }
+        }
+      }
+  } else {
+#pragma unroll
+    for (int c = 0; c < CAFE_ACT_MAX_CHUNKS; ++c)
+      if (c < chunks) f |= cafe_chunk_active(D, K, P, base + 8 * c) << (8 * c);
+  }
+  // cells of the range's edge chunks that lie outside it: keep [r0 - base, r1 - base)
+  const long long lo = r0 - base, hi = r1 - base;
+  if (lo > 0) f &= lo >= 32 ? 0u : ~((1u << lo) - 1u);
+  if (hi < 32) f &= hi <= 0 ? 0u : (1u << hi) - 1u;
   return f;
 }
 
@@ -386,34 +427,93 @@ __global__ void k_active_count(CafeDev D, CafeConsts K, const CafeStepParams *__
   d_active_count(D, K, Pp, chunks, nvb, blockIdx.x, gridDim.x);
 }
 
+// Exclusive scan over the block of one value per thread (blockDim.x a multiple
+// of 32, at most 1024; every thread must call it): returns this thread's
+// prefix and leaves the block total in tot. ws: 33 shared words.
+__device__ __forceinline__ long long cafe_block_excl_scan(long long v, long long *ws, long long &tot) {
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  long long incl = v;
+  for (int o = 1; o < 32; o <<= 1) {
+    const long long t = __shfl_up_sync(FULL, incl, o);
+    if (lane >= o) incl += t;
+  }
+  if (lane == 31) ws[w] = incl;
+  __syncthreads();
+  if (w == 0) {
+    const long long x = lane < nw ? ws[lane] : 0;
+    long long xi = x;
+    for (int o = 1; o < 32; o <<= 1) {
+      const long long t = __shfl_up_sync(FULL, xi, o);
+      if (lane >= o) xi += t;
+    }
+    if (lane < nw) ws[lane] = xi - x;
+    if (lane == 31) ws[32] = xi;
+  }
+  __syncthreads();
+  tot = ws[32];
+  return ws[w] + incl - v;
+}
+
 // Exclusive scan of n block counts in place; writes the total to *total.
 __device__ __forceinline__ void d_scan_blocks(int32_t *blk, long long n, int *total, const int cafe_bid, const int cafe_nblk) {
-  __shared__ long long part[1024];
-  long long per = (n + blockDim.x - 1) / blockDim.x;
+  __shared__ long long ws[33];
+  // each thread's segment is a multiple of four counts, so that its groups of
+  // four are aligned 16-byte loads and stores (a warp's lanes read segments
+  // apart, and one vector access serves four counts)
+  const long long per = ((n + blockDim.x - 1) / blockDim.x + 3) & ~3LL;
   long long b0 = threadIdx.x * per, b1 = b0 + per < n ? b0 + per : n;
+  if (b0 > n) b0 = n;
   long long s = 0;
-#pragma unroll 8
-  for (long long b = b0; b < b1; ++b) s += blk[b];
-  part[threadIdx.x] = s;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    long long acc = 0;
-    for (int t = 0; t < (int)blockDim.x; ++t) {
-      long long v = part[t];
-      part[t] = acc;
-      acc += v;
+  for (long long b = b0; b < b1; b += 16) {
+    int4 v[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const long long g = b + 4 * i;
+      if (g + 4 <= b1)
+        v[i] = *(const int4 *)(blk + g);
+      else
+        v[i] = make_int4(g < b1 ? blk[g] : 0, g + 1 < b1 ? blk[g + 1] : 0, g + 2 < b1 ? blk[g + 2] : 0, 0);
     }
-    *total = (int)acc;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) s += (long long)v[i].x + v[i].y + v[i].z + v[i].w;
   }
-  __syncthreads();
-  long long acc = part[threadIdx.x];
-  for (long long b = b0; b < b1; ++b) {
-    long long v = blk[b];
-    blk[b] = (int32_t)acc;
-    acc += v;
+  long long tot;
+  long long acc = cafe_block_excl_scan(s, ws, tot);
+  if (threadIdx.x == 0) *total = (int)tot;
+  for (long long b = b0; b < b1; b += 16) {
+    int4 v[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const long long g = b + 4 * i;
+      if (g + 4 <= b1)
+        v[i] = *(const int4 *)(blk + g);
+      else
+        v[i] = make_int4(g < b1 ? blk[g] : 0, g + 1 < b1 ? blk[g + 1] : 0, g + 2 < b1 ? blk[g + 2] : 0, 0);
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const long long g = b + 4 * i;
+      int4 o;
+      o.x = (int32_t)acc;
+      acc += v[i].x;
+      o.y = (int32_t)acc;
+      acc += v[i].y;
+      o.z = (int32_t)acc;
+      acc += v[i].z;
+      o.w = (int32_t)acc;
+      acc += v[i].w;
+      if (g + 4 <= b1) {
+        *(int4 *)(blk + g) = o;
+      } else {
+        if (g < b1) blk[g] = o.x;
+        if (g + 1 < b1) blk[g + 1] = o.y;
+        if (g + 2 < b1) blk[g + 2] = o.z;
+      }
+    }
   }
 }
-__global__ void k_scan_blocks(int32_t *blk, long long n, int *total) {
+__global__ void __launch_bounds__(1024) k_scan_blocks(int32_t *blk, long long n, int *total) {
   d_scan_blocks(blk, n, total, blockIdx.x, gridDim.x);
 }
 
@@ -567,45 +667,47 @@ __global__ void k_lists_count(CafeDev D) {
 // Exclusive scan of the (mushy, frontier) count pairs of the position blocks
 // that hold active positions (na from *na_ptr); totals to *tot0, *tot1.
 __device__ __forceinline__ void d_scan_pairs(int32_t *blk, long long n, const int *na_ptr, int *tot0, int *tot1, const int cafe_bid, const int cafe_nblk) {
-  __shared__ long long part[2][1024];
+  __shared__ long long ws[2][33];
   {
     long long used = ((long long)*na_ptr + CAFE_CELLS_PER_BLOCK - 1) / CAFE_CELLS_PER_BLOCK;
     if (used < n) n = used;
   }
   long long per = (n + blockDim.x - 1) / blockDim.x;
   long long b0 = threadIdx.x * per, b1 = b0 + per < n ? b0 + per : n;
+  const int2 *p2 = (const int2 *)blk;  // (count 0, count 1) of block b
   long long s0 = 0, s1 = 0;
-#pragma unroll 8
-  for (long long b = b0; b < b1; ++b) {
-    s0 += blk[2 * b];
-    s1 += blk[2 * b + 1];
-  }
-  part[0][threadIdx.x] = s0;
-  part[1][threadIdx.x] = s1;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    long long a0 = 0, a1 = 0;
-    for (int t = 0; t < (int)blockDim.x; ++t) {
-      long long v0 = part[0][t], v1 = part[1][t];
-      part[0][t] = a0;
-      part[1][t] = a1;
-      a0 += v0;
-      a1 += v1;
+  for (long long b = b0; b < b1; b += 8) {
+    int2 v[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) v[i] = b + i < b1 ? p2[b + i] : make_int2(0, 0);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      s0 += v[i].x;
+      s1 += v[i].y;
     }
-    *tot0 = (int)a0;
-    *tot1 = (int)a1;
   }
-  __syncthreads();
-  long long a0 = part[0][threadIdx.x], a1 = part[1][threadIdx.x];
-  for (long long b = b0; b < b1; ++b) {
-    long long v0 = blk[2 * b], v1 = blk[2 * b + 1];
-    blk[2 * b] = (int32_t)a0;
-    blk[2 * b + 1] = (int32_t)a1;
-    a0 += v0;
-    a1 += v1;
+  long long t0, t1;
+  long long a0 = cafe_block_excl_scan(s0, ws[0], t0);
+  long long a1 = cafe_block_excl_scan(s1, ws[1], t1);
+  if (threadIdx.x == 0) {
+    *tot0 = (int)t0;
+    *tot1 = (int)t1;
+  }
+  int2 *q2 = (int2 *)blk;
+  for (long long b = b0; b < b1; b += 8) {
+    int2 v[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) v[i] = b + i < b1 ? q2[b + i] : make_int2(0, 0);
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+      if (b + i < b1) {
+        q2[b + i] = make_int2((int32_t)a0, (int32_t)a1);
+        a0 += v[i].x;
+        a1 += v[i].y;
+      }
   }
 }
-__global__ void k_scan_pairs(int32_t *blk, long long n, const int *na_ptr, int *tot0, int *tot1) {
+__global__ void __launch_bounds__(1024) k_scan_pairs(int32_t *blk, long long n, const int *na_ptr, int *tot0, int *tot1) {
   d_scan_pairs(blk, n, na_ptr, tot0, tot1, blockIdx.x, gridDim.x);
 }
 

@@ -15,9 +15,10 @@ Printed keys beyond the common contract:
   e2e        the same metric through the C ABI with host buffers: the state is
              uploaded from pinned host memory before the steps and downloaded
              after, and every step reads its summary (nGrain, flags) back to the
-             host; up to E2E_REWIND_MAX cells the run is first restored from a
-             checkpoint taken at the start of the timed window, so that the
-             end-to-end steps are the timed steps;
+             host; the run is first restored from a checkpoint taken at the
+             start of the timed window (in a temporary directory or /dev/shm,
+             wherever it fits), so that the end-to-end steps are the timed
+             steps;
   roofline   for the phase with the largest device time in the timed region,
              its algorithmic bytes per launch over its mean launch time
              (CUDA events on the engine's stream), against the measured HBM
@@ -63,7 +64,10 @@ FALLBACK_HBM_GBS = 6800.0
 # the end-to-end run repeats the timed window from a checkpoint up to this
 # many cells (config 1: 16.8 M, a 0.7 GB checkpoint); larger boxes time the
 # steps that follow the timed window instead
-E2E_REWIND_MAX = 64 << 20
+E2E_REWIND_MAX = 1 << 31  # cells (the engine's limit)
+# checkpoint file size per cell (gID 4, state 1, extent and centre 32, build
+# flags 2, rounded up)
+CKPT_BYTES_PER_CELL = 40
 # host memory of one copy of the CPU restatement per cell (about 58 B measured
 # on config 1)
 REF_BYTES_PER_CELL = 64
@@ -646,8 +650,9 @@ def main():
     info0 = sim.info()
     nvox = info0["nx"] * info0["ny"] * info0["nz"]
     # the state at the start of the timed window, in pinned host memory (the
-    # end-to-end run uploads it) and, up to E2E_REWIND_MAX cells, a checkpoint
-    # there, so that the end-to-end run repeats the timed window's steps
+    # end-to-end run uploads it), and a checkpoint there (in a temporary
+    # directory or /dev/shm, wherever it fits), so that the end-to-end run
+    # repeats the timed window's steps
     st_host = cth_host = ckpt = None
     if not args.no_e2e or (rank == 0 and not args.no_cpu):
         import torch
@@ -661,15 +666,15 @@ def main():
                                      centroid=pinned(3 * ncell, torch.float64),
                                      buildj=pinned(ncell, torch.int32)))
         cth_host = sim.ctheta()
-    if not args.no_e2e and nvox <= E2E_REWIND_MAX:
-        fd, ckpt = tempfile.mkstemp(suffix=".ckpt")
-        os.close(fd)
+    ckpt_dir = _state_dir(CKPT_BYTES_PER_CELL * nvox) if not args.no_e2e and nvox <= E2E_REWIND_MAX else None
+    if ckpt_dir is not None:
+        ckpt = os.path.join(ckpt_dir, "window.ckpt")
         try:
             sim.checkpoint(ckpt)
         except Exception as exc:  # e.g. no room for the file: time the following steps instead
             print("bench: no checkpoint for the end-to-end run (%s)" % exc, file=sys.stderr)
-            os.unlink(ckpt)
-            ckpt = None
+            shutil.rmtree(ckpt_dir, ignore_errors=True)
+            ckpt = ckpt_dir = None
     snapshot = None
     if rank == 0 and not args.no_cpu:
         snapshot = (info0, st_host, cth_host)
@@ -806,8 +811,8 @@ def main():
                else "the steps after the timed and phase-timing steps",
                "events_per_step": (sim.stats()["events"] - ev_e0) / max(1, n_e)}
         del out_state, inf
-    if ckpt is not None and os.path.exists(ckpt):
-        os.unlink(ckpt)
+    if ckpt_dir is not None:
+        shutil.rmtree(ckpt_dir, ignore_errors=True)
     if rank == 0:
         ev = stats1["events"] - stats0["events"]
         out = {
