@@ -23,6 +23,8 @@ Printed keys beyond the common contract:
              its algorithmic bytes per launch over its mean launch time
              (CUDA events on the engine's stream), against the measured HBM
              copy bandwidth;
+  event_cycles  SM cycles per capture/nucleation event of the timed steps,
+             by section of the event loop (its own clock64 counters);
   cpu_baseline  the CPU oracle (a single-threaded restatement of the
              reference) resumed from the GPU state at the start of the timed
              window, for a bounded wall-clock sample.
@@ -838,6 +840,11 @@ def main():
             "clocks": clk,
             "gpu_launches": launches,
             "events_per_step": ev / max(1, k),
+            # the event loop's own clock (thread 0 of its block), SM cycles per
+            # capture/nucleation event in the timed steps, by section
+            "event_cycles": {sec: round((stats1["cycles_" + key] - stats0["cycles_" + key]) / max(1, ev))
+                             for sec, key in (("winner", "select"), ("capture", "apply"),
+                                              ("fill_and_next_selection", "fill"), ("merge", "merge"))},
             "phase_ms": {p: round(v[0], 3) for p, v in phases.items()},
             "wall_s_timed": wall,
             "setup_s": setup_s,
