@@ -1248,6 +1248,9 @@ __device__ __forceinline__ int cafe_find_slot(const CafeDev &D, int q, int targe
 // the step (k_rows_finalize).
 #define CAFE_ALIVE 0x7fffffff   // row_death of a row that is still alive
 #define CAFE_M_DONE 0x7fffffff  // row_m of a row whose extent is kept current
+#ifndef CAFE_CATCHUP
+#define CAFE_CATCHUP 2  // logged events a selecting thread replays per event for its second row
+#endif
 
 // Applies the logged growth of events row_m+1 .. min(upto, row_death). A
 // nucleation logs +0, which leaves an extent unchanged (extents are never -0).
@@ -1852,6 +1855,9 @@ __device__ __forceinline__ void d_event_loop(const CafeDev &D, const CafeConsts 
   int hot_r = -1;                             // the row whose extent this thread keeps current
   bool hot_ok = false;                        // hot_E is its extent after event e - 1
   double hot_E = 0.0;
+  int sec_r = -1;                             // likewise its second-smallest-key row
+  bool sec_ok = false;
+  double sec_E = 0.0;
   bool my_forced = false;                     // one of them is stamped -1
   if (hid >= 0) {
     s_dirty[hid] = 1;
@@ -2150,6 +2156,52 @@ __device__ __forceinline__ void d_event_loop(const CafeDev &D, const CafeConsts 
         } else {
           hot_r = -1;
           hot_ok = false;
+        }
+        // The second-smallest-key row becomes the smallest when the smallest
+        // one's key rises (its best candidate captured elsewhere). It is kept
+        // current the same way; as it is rarely evaluated, it is first brought
+        // up to date by a replay of at most CAFE_CATCHUP logged events per
+        // event, in this section where the selecting threads are otherwise
+        // idle. A row of this thread that dies marks it dirty, whose rescan
+        // moves my_r2.
+        if (my_r2 >= 0 && my_r2 < nrows_ev && my_r2 != hot_r) {
+          if (sec_r != my_r2) {
+            sec_r = my_r2;
+            sec_ok = false;
+          }
+          if (!sec_ok) {
+            // one level of loads: the row's death, watermark and extent, then
+            // the logged growths (independent of the running extent)
+            const int death = D.row_death[sec_r], m0 = D.row_m[sec_r];
+            double E = D.row_E[sec_r];
+            if (death >= e && m0 <= e - 1) {
+              const int stop = min(e - 1, m0 + CAFE_CATCHUP);
+#pragma unroll
+              for (int i = 1; i <= CAFE_CATCHUP; ++i) {
+                const int k = m0 + i;
+                if (k <= stop) {
+                  E = E + D.ev_vd[k];
+                  E = cafe_is_neg(E) ? 0.0 : E;  // (E < 0.0) ? 0.0 : E
+                }
+              }
+              if (stop == e - 1) {
+                sec_E = E;
+                sec_ok = true;
+              } else {
+                D.row_E[sec_r] = E;
+                D.row_m[sec_r] = stop;
+              }
+            }
+          }
+          if (sec_ok) {
+            sec_E = sec_E + s_vd;
+            sec_E = cafe_is_neg(sec_E) ? 0.0 : sec_E;  // (E < 0.0) ? 0.0 : E
+            D.row_E[sec_r] = sec_E;
+            D.row_m[sec_r] = e;
+          }
+        } else {
+          sec_r = -1;
+          sec_ok = false;
         }
       }
       __syncthreads();

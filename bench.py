@@ -667,7 +667,11 @@ def main():
                                      extents=pinned(ncell, torch.float64),
                                      centroid=pinned(3 * ncell, torch.float64),
                                      buildj=pinned(ncell, torch.int32)))
-        cth_host = sim.ctheta()
+        # the grain table too, in pinned memory (a pageable host buffer makes
+        # the driver stage the copy and block)
+        cth = sim.ctheta()
+        cth_host = pinned(len(cth), torch.float64)
+        cth_host[:] = cth
     ckpt_dir = _state_dir(CKPT_BYTES_PER_CELL * nvox) if not args.no_e2e and nvox <= E2E_REWIND_MAX else None
     if ckpt_dir is not None:
         ckpt = os.path.join(ckpt_dir, "window.ckpt")
@@ -784,7 +788,9 @@ def main():
             # too large to checkpoint here: the steps after the timed ones,
             # from the state reached there
             st_host = sim.state(out=st_host)
-            cth_host = sim.ctheta()
+            cth = sim.ctheta()
+            cth_host = pinned(len(cth), torch.float64)
+            cth_host[:] = cth
         h2d = sum(a.nbytes for a in (st_host["gID"], st_host["vState"], st_host["extents"], st_host["centroid"])) \
             + cth_host.nbytes
         d2h = h2d - cth_host.nbytes + st_host["buildj"].nbytes
@@ -795,6 +801,7 @@ def main():
         barrier(dist)
         te0 = time.time()
         sim.upload_state(st_host["gID"], st_host["vState"], st_host["extents"], st_host["centroid"], cth_host)
+        te1 = time.time()  # (the upload returns after its copies completed)
         n_e, done_e = 0, False
         per_step_d2h = 0
         while n_e < ke and not done_e:
@@ -802,8 +809,12 @@ def main():
             inf = sim.info()  # per-step result read back to the host
             per_step_d2h += 8
             n_e += 1
+        sim.synchronize()
+        te2 = time.time()
         out_state = sim.state(out=st_host)
         te = time.time() - te0
+        te_parts = {"upload_s": round(te1 - te0, 4), "steps_s": round(te2 - te1, 4),
+                    "download_s": round(te0 + te - te2, 4)}
         te = reduce_max(dist, te)
         e2e = {"value": ws * nvox * n_e / te, "unit": "voxel-updates/s",
                "h2d_bytes_per_step": int(h2d / max(1, n_e)),
@@ -811,7 +822,7 @@ def main():
                "steps": n_e, "window_start_step": e2e_start,
                "window": "the timed window again (restored from a checkpoint)" if rewound
                else "the steps after the timed and phase-timing steps",
-               "events_per_step": (sim.stats()["events"] - ev_e0) / max(1, n_e)}
+               "events_per_step": (sim.stats()["events"] - ev_e0) / max(1, n_e), "wall": te_parts}
         del out_state, inf
     if ckpt_dir is not None:
         shutil.rmtree(ckpt_dir, ignore_errors=True)
