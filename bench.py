@@ -15,10 +15,11 @@ Printed keys beyond the common contract:
   e2e        the same metric through the C ABI with host buffers: the state is
              uploaded from pinned host memory before the steps and downloaded
              after, and every step reads its summary (nGrain, flags) back to the
-             host; the run is first restored from a checkpoint taken at the
-             start of the timed window (in a temporary directory or /dev/shm,
-             wherever it fits), so that the end-to-end steps are the timed
-             steps;
+             host; it runs the timed window's steps first, then the engine
+             is restored from a checkpoint taken one step before the window
+             (in a temporary directory or /dev/shm, wherever it fits) and
+             steps once, untimed, to the window's start for the device-timed
+             steps; `wall` splits its time into upload, steps and download;
   roofline   for the phase with the largest device time in the timed region,
              its algorithmic bytes per launch over its mean launch time
              (CUDA events on the engine's stream), against the measured HBM
@@ -645,17 +646,30 @@ def main():
     sim.begin()
     if spinup > 0:
         sim.run(spinup)
-    for _ in range(args.warmup):
+    nvox = sim.ncell
+    # a checkpoint one step before the timed window (before the last warm-up
+    # step), in a temporary directory or /dev/shm, wherever it fits: the
+    # end-to-end leg runs the window first, then the engine is rewound there
+    # and that one step, whose full passes a restore entails, stays untimed
+    ckpt = None
+    ckpt_dir = _state_dir(CKPT_BYTES_PER_CELL * nvox) if not args.no_e2e and nvox <= E2E_REWIND_MAX else None
+    for i in range(args.warmup):
+        if i == args.warmup - 1 and ckpt_dir is not None:
+            sim.synchronize()
+            ckpt = os.path.join(ckpt_dir, "window.ckpt")
+            try:
+                sim.checkpoint(ckpt)
+            except Exception as exc:  # e.g. no room for the file: time the following steps instead
+                print("bench: no checkpoint for the end-to-end run (%s)" % exc, file=sys.stderr)
+                shutil.rmtree(ckpt_dir, ignore_errors=True)
+                ckpt = ckpt_dir = None
         sim.step()
     sim.synchronize()
     setup_s = time.time() - t_setup
     info0 = sim.info()
-    nvox = info0["nx"] * info0["ny"] * info0["nz"]
     # the state at the start of the timed window, in pinned host memory (the
-    # end-to-end run uploads it), and a checkpoint there (in a temporary
-    # directory or /dev/shm, wherever it fits), so that the end-to-end run
-    # repeats the timed window's steps
-    st_host = cth_host = ckpt = None
+    # end-to-end run uploads it)
+    st_host = cth_host = None
     if not args.no_e2e or (rank == 0 and not args.no_cpu):
         import torch
 
@@ -672,15 +686,58 @@ def main():
         cth = sim.ctheta()
         cth_host = pinned(len(cth), torch.float64)
         cth_host[:] = cth
-    ckpt_dir = _state_dir(CKPT_BYTES_PER_CELL * nvox) if not args.no_e2e and nvox <= E2E_REWIND_MAX else None
-    if ckpt_dir is not None:
-        ckpt = os.path.join(ckpt_dir, "window.ckpt")
-        try:
-            sim.checkpoint(ckpt)
-        except Exception as exc:  # e.g. no room for the file: time the following steps instead
-            print("bench: no checkpoint for the end-to-end run (%s)" % exc, file=sys.stderr)
-            shutil.rmtree(ckpt_dir, ignore_errors=True)
-            ckpt = ckpt_dir = None
+
+    def run_e2e(window):
+        """The end-to-end leg through the C ABI with host buffers: upload of
+        st_host, args.steps steps with each step's summary read back, download
+        into st_host; wall clock."""
+        h2d = sum(a.nbytes for a in (st_host["gID"], st_host["vState"], st_host["extents"], st_host["centroid"])) \
+            + cth_host.nbytes
+        d2h = h2d - cth_host.nbytes + st_host["buildj"].nbytes
+        ke = args.steps
+        sim.synchronize()
+        e2e_start = sim.info()["steps"]
+        ev_e0 = sim.stats()["events"]
+        barrier(dist)
+        te0 = time.time()
+        sim.upload_state(st_host["gID"], st_host["vState"], st_host["extents"], st_host["centroid"], cth_host)
+        te1 = time.time()  # (the upload returns after its copies completed)
+        n_e, done_e = 0, False
+        per_step_d2h = 0
+        while n_e < ke and not done_e:
+            done_e = sim.step()
+            sim.info()  # per-step result read back to the host
+            per_step_d2h += 8
+            n_e += 1
+        sim.synchronize()
+        te2 = time.time()
+        sim.state(out=st_host)
+        te = time.time() - te0
+        te_parts = {"upload_s": round(te1 - te0, 4), "steps_s": round(te2 - te1, 4),
+                    "download_s": round(te0 + te - te2, 4)}
+        te = reduce_max(dist, te)
+        return {"value": ws * nvox * n_e / te, "unit": "voxel-updates/s",
+                "h2d_bytes_per_step": int(h2d / max(1, n_e)),
+                "d2h_bytes_per_step": int(d2h / max(1, n_e) + per_step_d2h / max(1, n_e)),
+                "steps": n_e, "window_start_step": e2e_start, "window": window,
+                "events_per_step": (sim.stats()["events"] - ev_e0) / max(1, n_e), "wall": te_parts}
+
+    # ---- end to end first, from the window's start (host-to-device copies on
+    # the box run slowly for a while after a restore or a large host copy),
+    # then back to the step before the window (restore) and one untimed step
+    # to the window's start for the device-timed steps
+    e2e = None
+    if ckpt is not None:
+        e2e = run_e2e("the timed window, run before it (then rewound from a checkpoint)")
+        sim.restore(ckpt)
+        os.unlink(ckpt)
+        ckpt = None
+        sim.step()  # to the window's start again, untimed
+        sim.synchronize()
+        if sim.info()["steps"] != info0["steps"]:
+            raise RuntimeError("bench: the rewind did not reach the window's start")
+        st_host = sim.state(out=st_host)  # the window's start (the CPU baseline's input)
+        sim.synchronize()
     snapshot = None
     if rank == 0 and not args.no_cpu:
         snapshot = (info0, st_host, cth_host)
@@ -776,54 +833,14 @@ def main():
     if snapshot is not None:
         cpu = cpu_baseline(deck, snapshot[0], snapshot[1], snapshot[2], nvox, args.cpu_seconds)
 
-    # ---- end to end through the C ABI with host buffers
-    e2e = None
-    if not args.no_e2e and (ckpt is not None or not done):
-        rewound = ckpt is not None
-        if rewound:
-            # back to the start of the timed window (untimed): the same steps
-            sim.restore(ckpt)
-            os.unlink(ckpt)
-        else:
-            # too large to checkpoint here: the steps after the timed ones,
-            # from the state reached there
-            st_host = sim.state(out=st_host)
-            cth = sim.ctheta()
-            cth_host = pinned(len(cth), torch.float64)
-            cth_host[:] = cth
-        h2d = sum(a.nbytes for a in (st_host["gID"], st_host["vState"], st_host["extents"], st_host["centroid"])) \
-            + cth_host.nbytes
-        d2h = h2d - cth_host.nbytes + st_host["buildj"].nbytes
-        ke = args.steps
-        sim.synchronize()
-        e2e_start = sim.info()["steps"]
-        ev_e0 = sim.stats()["events"]
-        barrier(dist)
-        te0 = time.time()
-        sim.upload_state(st_host["gID"], st_host["vState"], st_host["extents"], st_host["centroid"], cth_host)
-        te1 = time.time()  # (the upload returns after its copies completed)
-        n_e, done_e = 0, False
-        per_step_d2h = 0
-        while n_e < ke and not done_e:
-            done_e = sim.step()
-            inf = sim.info()  # per-step result read back to the host
-            per_step_d2h += 8
-            n_e += 1
-        sim.synchronize()
-        te2 = time.time()
-        out_state = sim.state(out=st_host)
-        te = time.time() - te0
-        te_parts = {"upload_s": round(te1 - te0, 4), "steps_s": round(te2 - te1, 4),
-                    "download_s": round(te0 + te - te2, 4)}
-        te = reduce_max(dist, te)
-        e2e = {"value": ws * nvox * n_e / te, "unit": "voxel-updates/s",
-               "h2d_bytes_per_step": int(h2d / max(1, n_e)),
-               "d2h_bytes_per_step": int(d2h / max(1, n_e) + per_step_d2h / max(1, n_e)),
-               "steps": n_e, "window_start_step": e2e_start,
-               "window": "the timed window again (restored from a checkpoint)" if rewound
-               else "the steps after the timed and phase-timing steps",
-               "events_per_step": (sim.stats()["events"] - ev_e0) / max(1, n_e), "wall": te_parts}
-        del out_state, inf
+    # ---- end to end without a checkpoint: the steps after the timed ones,
+    # from the state reached there
+    if e2e is None and not args.no_e2e and not done:
+        st_host = sim.state(out=st_host)
+        cth = sim.ctheta()
+        cth_host = pinned(len(cth), torch.float64)
+        cth_host[:] = cth
+        e2e = run_e2e("the steps after the timed and phase-timing steps")
     if ckpt_dir is not None:
         shutil.rmtree(ckpt_dir, ignore_errors=True)
     if rank == 0:
